@@ -1,0 +1,181 @@
+/*
+ * vdr.h -- C ABI of libvdr.so, the GB300 (sm_103a) element-by-element HEX8
+ * directional-residual (DR) solve of the Vanadis transport model.
+ *
+ * Two families of entry points:
+ *
+ * 1. kernel_dbcg_simple_ -- the reference's own solve entry point, same
+ *    symbol, same arguments, same meaning.  It replaces
+ *      src_v2026_2_1/cudatest.cu:301-305
+ *      (= src_v2026_2_1/cudatest_coloring_gtx1060_optimized.cu:434-438),
+ *    which the Fortran driver calls at src_v2026_2_1/VANADIS.FOR:809-810 as
+ *      CALL kernel_dbcg_simple(NON,FMV3,TNW2,TOL,IL_I,ITER,ERR,BB,
+ *                              ISS,DIAG,NAX,NAY,NAZ,bc_dirichlet)
+ *    through an implicit interface (every argument by reference, trailing
+ *    underscore).  The driver links against libvdr.so unchanged.
+ *
+ * 2. vdr_* -- a handle API that keeps the mesh, the per-element fields and
+ *    the operator resident on the GPU across time steps and recomputes the
+ *    DR element terms on the device (no host-assembled BB).  Its arrays use
+ *    the reference driver's layouts: node coordinates xx/yy/zz[N]
+ *    (siatka, vanadis_full_DR_OpenMP_timing.for:201-219), connectivity
+ *    iss(E,8) column-major 1-based (w_el, :221-251), face codes kod(E,6)
+ *    (kod_el_dr, :253-295), velocity (E,3) column-major and per-element
+ *    scalars (the values atmosfera, :163-199, returns per element), the
+ *    Dirichlet node mask bc_dirichlet[N] (build_bc_nodes, :1719-1810).
+ *
+ * All host pointers are caller-owned and only read during the call unless
+ * documented as outputs.  "_device" variants take device pointers and run
+ * on the handle's stream (vdr_stream), returning before the GPU finishes
+ * unless stated.  No entry point ever calls exit(); errors come back as
+ * status codes and vdr_last_error() describes the latest one.
+ * A handle is not thread-safe; distinct handles may be used from distinct
+ * host threads.
+ */
+#ifndef VDR_H
+#define VDR_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define VDR_OK 0
+#define VDR_NOT_CONVERGED 1
+#define VDR_BREAKDOWN 2
+#define VDR_CUDA_ERROR 3
+#define VDR_BAD_ARGUMENT 4
+#define VDR_TIMEOUT 5
+
+/* ---- DR variants (gauss_point_hex8DR) ----
+ * VDR_DR_OT: vanadis_full_DR_OpenMP_timing.for:1567-1716 (axis lengths,
+ *            exp-based coth; NaN for element Peclet > 709.78, as there)
+ * VDR_DR_GP: src_updates/gauss_point_hex8DR.for:1-174
+ * VDR_DR_VF: src_v2026_2_1/VANADIS.FOR:1868-2023 (numerically safe) */
+#define VDR_DR_OT 0
+#define VDR_DR_GP 1
+#define VDR_DR_VF 2
+
+/* ---- scatter of element results to nodes ---- */
+#define VDR_SCATTER_AUTO 0   /* measured choice: atomic */
+#define VDR_SCATTER_ATOMIC 1 /* fp64 atomics, elements in natural order */
+#define VDR_SCATTER_COLOR 2  /* colour by colour, no atomics, deterministic */
+
+/* ---- operator apply ---- */
+#define VDR_APPLY_AUTO 0        /* measured choice: stored */
+#define VDR_APPLY_STORED 1      /* element matrices built on the GPU by the
+                                   DR recompute kernel, kept in HBM */
+#define VDR_APPLY_MATRIX_FREE 2 /* DR terms recomputed at every apply */
+
+/* ---- Krylov method ---- */
+#define VDR_SOLVER_BICGSTAB 0 /* Jacobi right-preconditioned BiCGStab */
+#define VDR_SOLVER_BICG 1     /* Jacobi BiCG, the reference's dbcg_simple */
+
+typedef struct vdr_options {
+  int dr_variant;      /* VDR_DR_* (default VDR_DR_VF) */
+  int scatter;         /* VDR_SCATTER_* */
+  int apply_mode;      /* VDR_APPLY_* */
+  int solver;          /* VDR_SOLVER_* */
+  int iters_per_graph; /* iterations per CUDA-graph launch (0 -> 8) */
+  int device;          /* CUDA device ordinal */
+  int reserved[10];
+} vdr_options;
+
+typedef struct vdr_handle vdr_handle;
+
+/* Fills *opt with the defaults. */
+int vdr_default_options(vdr_options *opt);
+
+/* Creates a handle for a HEX8 mesh.  iss is iss(E,8), column-major,
+ * 1-based; kod is kod(E,6) column-major or NULL (then no element carries
+ * the face-3 Robin term).  opt may be NULL (defaults). */
+int vdr_create(vdr_handle **h, int nnode, int nelem, const double *xx,
+               const double *yy, const double *zz, const int *iss,
+               const int *kod, const vdr_options *opt);
+
+/* Per-element fields: vel (E,3) column-major, lam[E] isotropic
+ * diffusivity, pdec[E] decay rate (NULL = 0), q[E] source in kg/s
+ * (NULL = 0), robin_alpha the face-3 transfer coefficient (licz_alfa). */
+int vdr_set_fields(vdr_handle *h, const double *vel, const double *lam,
+                   const double *pdec, const double *q, double robin_alpha);
+
+/* Homogeneous Dirichlet node mask, bc[N] (1 = Dirichlet).  The operator
+ * returns 0 on these rows and ignores these columns (matvec_0,
+ * vanadis_full_DR_OpenMP_timing.for:1837-1881). */
+int vdr_set_dirichlet(vdr_handle *h, const int *bc);
+
+/* Selects the system matrix A = aH*H + aM*M (H = diffusion + DR advection
+ * + decay*M + Robin, M = int W N).  Steady problems: (1, 0).  The
+ * reference's theta-scheme: (2, 3/dt) (przest3d, :691-716). */
+int vdr_set_operator(vdr_handle *h, double aH, double aM);
+
+/* y = P A P x (transpose = 0) or y = P A^T P x, host arrays of length N. */
+int vdr_apply(vdr_handle *h, const double *x, double *y, int transpose);
+int vdr_apply_device(vdr_handle *h, const double *d_x, double *d_y,
+                     int transpose);
+
+/* Right-hand side b = cf*f - (H - rM*M) T_old, assembled on the GPU, with
+ * b = 0 on Dirichlet nodes (przest3d :691-716, :766-772).  t_old may be
+ * NULL (steady: b = cf*f).  Host arrays of length N. */
+int vdr_assemble_rhs(vdr_handle *h, double cf, double rM, const double *t_old,
+                     double *b);
+int vdr_assemble_rhs_device(vdr_handle *h, double cf, double rM,
+                            const double *d_t_old, double *d_b);
+
+/* Jacobi diagonal of the current operator (1 on Dirichlet nodes). */
+int vdr_get_diag(vdr_handle *h, double *diag);
+
+/* Solves A x = b.  x holds the initial guess on entry (Dirichlet entries
+ * are zeroed, as the reference does) and the solution on exit.  Stops when
+ * ||r||_2/||b||_2 <= tol (recursively updated residual, as dbcg_simple) or
+ * after itmax iterations.  Returns VDR_OK, VDR_NOT_CONVERGED,
+ * VDR_BREAKDOWN or an error.  *iter = iterations done (0 if x already met
+ * tol), *err = final relative residual. */
+int vdr_solve(vdr_handle *h, const double *b, double *x, double tol,
+              int itmax, int *iter, double *err);
+int vdr_solve_device(vdr_handle *h, const double *d_b, double *d_x,
+                     double tol, int itmax, int *iter, double *err);
+
+/* True relative residual ||b - A x||/||b|| computed on the GPU in FP64. */
+int vdr_true_residual_device(vdr_handle *h, const double *d_b,
+                             const double *d_x, double *rel);
+
+/* Total mass int c dOmega, 2x2x2 Gauss (integrate_mass_hex8,
+ * vanadis_full_DR_OpenMP_timing.for:2181-2285). */
+int vdr_mass(vdr_handle *h, const double *c, double *mass);
+int vdr_mass_device(vdr_handle *h, const double *d_c, double *mass);
+
+/* Host only, no GPU needed: the element colouring used by
+ * VDR_SCATTER_COLOR.  On the reference's structured numbering (w_el) it is
+ * the parity colouring of cudatest_coloring_gtx1060_optimized.cu:50-74,
+ * (i&1) + 2(j&1) + 4(k&1); otherwise first-fit greedy in element order.
+ * colors[nelem] out.  Returns the number of colours, or -VDR_BAD_ARGUMENT. */
+int vdr_color_elements(int nnode, int nelem, const int *iss, int *colors);
+
+/* The handle's CUDA stream (cudaStream_t). */
+void *vdr_stream(vdr_handle *h);
+
+int vdr_destroy(vdr_handle *h);
+
+/* Message of the most recent failure in this thread ("" if none). */
+const char *vdr_last_error(void);
+
+/* Drop-in for src_v2026_2_1/cudatest.cu:301-305.  N: number of unknowns;
+ * B[N] right-hand side; X[N] initial guess in, solution out; TOL, ITMAX;
+ * ITER out; ERR out (||r||/||b||); BB[64*E] element matrices as sklad_wd
+ * lays them out (BB[64e+8i+j] = A_e(i,j)); ISS(E,8) column-major 1-based;
+ * DIAG[N] Jacobi diagonal; NAX,NAY,NAZ node counts, E =
+ * (NAX-1)(NAY-1)(NAZ-1); bc_dirichlet[N].  Jacobi BiCG as dbcg_simple.
+ * Like the reference it returns nothing; on a CUDA failure ERR is set to
+ * +Inf (so the caller's ERR > TOL test reports it) and vdr_last_error()
+ * holds the message.  Device buffers persist between calls and are reused
+ * while the sizes fit. */
+void kernel_dbcg_simple_(int *N, double *B, double *X, double *TOL,
+                         int *ITMAX, int *ITER, double *ERR, double *BB,
+                         int *ISS, double *DIAG, int *NAX, int *NAY, int *NAZ,
+                         int *bc_dirichlet);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VDR_H */

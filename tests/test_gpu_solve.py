@@ -1,0 +1,159 @@
+"""GPU solve parity through the C ABI: BiCGStab and BiCG solutions against
+the oracle (1e-9 relative L2 when both converge tightly), the reference's
+recorded 20-step run through both the handle API and the drop-in
+kernel_dbcg_simple_, and the solver's edge cases."""
+import numpy as np
+import pytest
+
+from helpers import kat_problem, load_kat, rel_l2, run_kat_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def systems(vdr, oracle):
+    from oracle.system import reference_system
+    P = vdr.problems
+    out = {}
+    for name, prob in (("const_adv_OT", P.constant_advection(16, 16, 8, seed=21)),
+                       ("rotation_VF", P.rotation_shear(16, 16, 8, seed=22))):
+        out[name] = (prob, reference_system(prob, tol=1e-13))
+    return out
+
+
+@pytest.mark.parametrize("name", ["const_adv_OT", "rotation_VF"])
+@pytest.mark.parametrize("solver", ["bicgstab", "bicg"])
+@pytest.mark.parametrize("mode,scatter", [("stored", "atomic"),
+                                          ("stored", "color"),
+                                          ("matrix_free", "atomic")])
+def test_solution_parity(vdr, gpu_lib, systems, name, solver, mode, scatter):
+    prob, ref = systems[name]
+    assert ref["status"] == 0
+    opts = vdr.Options(solver=solver, apply_mode=mode, scatter=scatter)
+    with vdr.Solver(prob, opts) as s:
+        x, it, err, st = s.solve(ref["b"], tol=1e-13, itmax=20000)
+    assert st == 0, (st, it, err)
+    assert err <= 1e-13
+    assert rel_l2(x, ref["x_solution"]) < 1e-9
+
+
+def test_iteration_count_matches_oracle_bicgstab(vdr, gpu_lib, systems):
+    prob, ref = systems["const_adv_OT"]
+    with vdr.Solver(prob, vdr.Options(solver="bicgstab")) as s:
+        _, it, _, st = s.solve(ref["b"], tol=1e-13, itmax=20000)
+    assert st == 0
+    assert abs(it - ref["iterations"]) <= max(3, 0.05 * ref["iterations"])
+
+
+def test_kat_run_handle_api(vdr, oracle, gpu_lib):
+    """The recorded 7x20x20, 20-step run with assembly on the GPU
+    (vdr_assemble_rhs) and BiCG on the GPU."""
+    k = load_kat()
+    prob = kat_problem(vdr)
+    dt = float(k["dt"])
+    m = prob.mesh
+    t = np.zeros(m.nnode)
+    its, masses = [], []
+    with vdr.Solver(prob, vdr.Options(solver="bicg"), aH=2.0, aM=3.0 / dt) as s:
+        for step in range(k["steps"]):
+            b = s.assemble_rhs(3.0, 3.0 / dt, t)
+            t, it, err, st = s.solve(b, t, tol=k["tol"], itmax=k["itmax"])
+            assert st == 0
+            its.append(it)
+            masses.append(s.mass(t))
+    ref_its = k["log"]["iterations"]
+    assert all(abs(a - b) <= 2 for a, b in zip(its, ref_its)), its
+    ref_m = np.array(k["log"]["masses"])
+    assert np.max(np.abs(np.array(masses) - ref_m) / ref_m) < 1e-6
+
+
+def test_kat_run_dropin_kernel_dbcg_simple(vdr, oracle, gpu_lib):
+    """Same run through the reference's own entry point with the oracle's
+    host-assembled BB, exactly as VANADIS.FOR:793-810 calls it."""
+    k = load_kat()
+    prob = kat_problem(vdr)
+    m = prob.mesh
+    dt = float(k["dt"])
+    t = np.zeros(m.nnode)
+    its, masses = [], []
+    for step in range(k["steps"]):
+        bb, b, diag = oracle.assemble(prob.variant, m.xx, m.yy, m.zz, m.iss,
+                                      prob.vel, prob.lam, prob.pdec, prob.q,
+                                      kod=m.kod, robin_alpha=prob.robin_alpha,
+                                      aH=2.0, aM=3.0 / dt, cf=3.0,
+                                      rM=3.0 / dt, t_old=t)
+        bc = prob.bc
+        b[bc == 1] = 0.0
+        diag[bc == 1] = 1.0
+        t[bc == 1] = 0.0
+        t, it, err = vdr.kernel_dbcg_simple(m.nnode, b, t, k["tol"], k["itmax"],
+                                            bb, m.iss, diag, m.nax, m.nay,
+                                            m.naz, bc)
+        assert err <= k["tol"]
+        its.append(it)
+        masses.append(oracle.integrate_mass(m.iss, m.xx, m.yy, m.zz, t))
+    assert all(abs(a - b) <= 2 for a, b in zip(its, k["log"]["iterations"])), its
+    ref_m = np.array(k["log"]["masses"])
+    assert np.max(np.abs(np.array(masses) - ref_m) / ref_m) < 1e-6
+
+
+def test_dropin_matches_oracle_dbcg(vdr, oracle, gpu_lib):
+    prob = kat_problem(vdr)
+    m = prob.mesh
+    bb, b, diag = oracle.assemble(prob.variant, m.xx, m.yy, m.zz, m.iss,
+                                  prob.vel, prob.lam, prob.pdec, prob.q,
+                                  kod=m.kod, robin_alpha=prob.robin_alpha,
+                                  aH=2.0, aM=0.03, cf=3.0, rM=0.03)
+    b[prob.bc == 1] = 0.0
+    diag[prob.bc == 1] = 1.0
+    x0 = np.zeros(m.nnode)
+    xr, itr, er, _ = oracle.dbcg(b, x0, bb, m.iss, diag, prob.bc, 1e-13, 5000)
+    x, it, err = vdr.kernel_dbcg_simple(m.nnode, b, x0, 1e-13, 5000, bb, m.iss,
+                                        diag, m.nax, m.nay, m.naz, prob.bc)
+    assert err <= 1e-13
+    assert rel_l2(x, xr) < 1e-9
+    assert abs(it - itr) <= 3
+
+
+def test_zero_rhs_gives_zero(vdr, gpu_lib):
+    prob = vdr.problems.rotation_shear(6, 6, 4, seed=3)
+    with vdr.Solver(prob) as s:
+        x, it, err, st = s.solve(np.zeros(prob.mesh.nnode),
+                                 np.ones(prob.mesh.nnode))
+    assert st == 0 and it == 0 and np.all(x == 0.0)
+
+
+def test_converged_initial_guess_takes_no_iteration(vdr, gpu_lib, systems):
+    prob, ref = systems["rotation_VF"]
+    with vdr.Solver(prob) as s:
+        x, it, err, st = s.solve(ref["b"], ref["x_solution"], tol=1e-8)
+    assert st == 0 and it == 0 and err <= 1e-8
+
+
+def test_itmax_reports_not_converged(vdr, gpu_lib, systems):
+    prob, ref = systems["rotation_VF"]
+    for solver in ("bicgstab", "bicg"):
+        with vdr.Solver(prob, vdr.Options(solver=solver)) as s:
+            x, it, err, st = s.solve(ref["b"], tol=1e-14, itmax=5)
+        assert st == 1 and it == 5 and err > 1e-14
+
+
+def test_dirichlet_entries_of_solution_are_zero(vdr, gpu_lib, systems):
+    prob, ref = systems["const_adv_OT"]
+    x0 = np.random.default_rng(9).standard_normal(prob.mesh.nnode)
+    with vdr.Solver(prob) as s:
+        x, it, err, st = s.solve(ref["b"], x0, tol=1e-10)
+    assert st == 0 and np.all(x[prob.bc == 1] == 0.0)
+
+
+def test_true_residual_device(vdr, gpu_lib, systems):
+    torch = pytest.importorskip("torch")
+    prob, ref = systems["rotation_VF"]
+    with vdr.Solver(prob) as s:
+        b = torch.tensor(ref["b"], device="cuda")
+        x = torch.zeros_like(b)
+        torch.cuda.synchronize()  # the handle runs on its own stream
+        it, err, st = s.solve_device(b, x, tol=1e-10)
+        torch.cuda.synchronize()
+        rel = s.true_residual_device(b, x)
+    assert st == 0 and rel < 1e-9

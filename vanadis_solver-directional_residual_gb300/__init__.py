@@ -1,0 +1,16 @@
+"""GB300 (sm_103a) element-by-element HEX8 directional-residual solve.
+
+A drop-in for the solve path of the Vanadis transport model: the reference
+driver's ``kernel_dbcg_simple_`` entry point, plus a handle API that keeps
+mesh, fields and operator resident on the GPU and recomputes the DR element
+terms there.  The compute lives in ``lib/libvdr.so`` (hand-written CUDA for
+sm_103a + C++ host runtime, C ABI in ``include/vdr.h``); this package is its
+Python host binding.
+"""
+from . import problems
+from ._lib import (VdrError, build_library, last_error, library_path,
+                   load_library)
+from .solver import Options, Solver, kernel_dbcg_simple
+
+__all__ = ["problems", "Options", "Solver", "kernel_dbcg_simple", "VdrError",
+           "build_library", "load_library", "library_path", "last_error"]

@@ -1,0 +1,103 @@
+"""ctypes binding of libvdr.so (the C ABI declared in include/vdr.h).
+
+The library is the only compute path: if it is missing or cannot load, the
+package raises instead of falling back to anything else."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+_lib = None
+
+OK, NOT_CONVERGED, BREAKDOWN, CUDA_ERROR, BAD_ARGUMENT, TIMEOUT = range(6)
+STATUS_NAMES = {0: "ok", 1: "not converged", 2: "breakdown",
+                3: "cuda error", 4: "bad argument", 5: "timeout"}
+
+DR_OT, DR_GP, DR_VF = 0, 1, 2
+SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOR = 0, 1, 2
+APPLY_AUTO, APPLY_STORED, APPLY_MATRIX_FREE = 0, 1, 2
+SOLVER_BICGSTAB, SOLVER_BICG = 0, 1
+
+
+class VdrOptions(ctypes.Structure):
+    _fields_ = [("dr_variant", ctypes.c_int), ("scatter", ctypes.c_int),
+                ("apply_mode", ctypes.c_int), ("solver", ctypes.c_int),
+                ("iters_per_graph", ctypes.c_int), ("device", ctypes.c_int),
+                ("reserved", ctypes.c_int * 10)]
+
+
+# Every symbol include/vdr.h declares, with its ctypes signature.
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_i = ctypes.c_int
+_d = ctypes.c_double
+SIGNATURES = {
+    "vdr_default_options": (_i, [ctypes.POINTER(VdrOptions)]),
+    "vdr_create": (_i, [ctypes.POINTER(_P), _i, _i, _D, _D, _D, _I, _I,
+                        ctypes.POINTER(VdrOptions)]),
+    "vdr_set_fields": (_i, [_P, _D, _D, _D, _D, _d]),
+    "vdr_set_dirichlet": (_i, [_P, _I]),
+    "vdr_set_operator": (_i, [_P, _d, _d]),
+    "vdr_apply": (_i, [_P, _D, _D, _i]),
+    "vdr_apply_device": (_i, [_P, _P, _P, _i]),
+    "vdr_assemble_rhs": (_i, [_P, _d, _d, _D, _D]),
+    "vdr_assemble_rhs_device": (_i, [_P, _d, _d, _P, _P]),
+    "vdr_get_diag": (_i, [_P, _D]),
+    "vdr_solve": (_i, [_P, _D, _D, _d, _i, _I, _D]),
+    "vdr_solve_device": (_i, [_P, _P, _P, _d, _i, _I, _D]),
+    "vdr_true_residual_device": (_i, [_P, _P, _P, _D]),
+    "vdr_mass": (_i, [_P, _D, _D]),
+    "vdr_mass_device": (_i, [_P, _P, _D]),
+    "vdr_color_elements": (_i, [_i, _i, _I, _I]),
+    "vdr_stream": (_P, [_P]),
+    "vdr_destroy": (_i, [_P]),
+    "vdr_last_error": (ctypes.c_char_p, []),
+    "kernel_dbcg_simple_": (None, [_I, _D, _D, _D, _I, _I, _D, _D, _I, _D,
+                                   _I, _I, _I, _I]),
+}
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def build_library(force: bool = False) -> str:
+    return _build.build(force=force)
+
+
+def load_library():
+    """Load libvdr.so (it must have been built; raises otherwise)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(
+            "libvdr.so not built (%s); run __graft_entry__.build()" % path)
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return load_library().vdr_last_error().decode(errors="replace")
+
+
+class VdrError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__("%s: %s (%s)" % (where, STATUS_NAMES.get(status, status),
+                                          last_error()))
+
+
+def check(status: int, where: str, allow=(OK,)) -> int:
+    if status not in allow:
+        raise VdrError(status, where)
+    return status

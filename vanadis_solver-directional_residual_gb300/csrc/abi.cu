@@ -1,0 +1,759 @@
+// abi.cu -- the extern "C" surface of libvdr.so (include/vdr.h): handle
+// lifetime, host-side mesh preparation (structured-numbering detection,
+// element colouring, storage permutation), uploads, and the drop-in
+// kernel_dbcg_simple_ entry point of the reference
+// (src_v2026_2_1/cudatest.cu:301-602).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "vdr.h"
+#include "vdr_internal.h"
+
+struct vdr_handle {
+  vdr::Handle h;
+  // host-API staging buffers on the device
+  double *io = nullptr;  // [3][N]: x, y / b, scratch
+  double *mass_partials = nullptr;
+  double *mass_out = nullptr;
+};
+
+namespace vdr {
+
+int true_residual_device(Handle &h, const double *b, const double *x, double *rel);
+
+namespace {
+thread_local std::string g_err;
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t n) {
+  if (*p) return cudaSuccess;
+  return cudaMalloc((void **)p, sizeof(T) * std::max<size_t>(n, 1));
+}
+void dfree(void *p) {
+  if (p) cudaFree(p);
+}
+
+// The reference driver's numbering (w_el): returns true and the node
+// counts when iss is exactly the canonical structured connectivity.
+bool detect_structured(int N, int E, const int *iss, int *nax, int *nay,
+                       int *naz) {
+  if (E < 1) return false;
+  const long a = (long)iss[3L * E] - iss[0];
+  if (a < 2) return false;
+  const long ab = (long)iss[4L * E] - iss[0];
+  if (ab % a) return false;
+  const long b = ab / a;
+  if (b < 2 || (long)N % (a * b)) return false;
+  const long c = (long)N / (a * b);
+  if (c < 2 || (a - 1) * (b - 1) * (c - 1) != (long)E) return false;
+  const long ex = a - 1, ey = b - 1;
+  const long pl = a * b;
+  const long offs[8] = {0, 1, 1 + a, a, pl, 1 + pl, 1 + pl + a, pl + a};
+  for (long e = 0; e < E; e++) {
+    const long i = e % ex, j = (e / ex) % ey, k = e / (ex * ey);
+    const long base = i + a * j + pl * k + 1;
+    for (int s = 0; s < 8; s++)
+      if ((long)iss[(long)s * E + e] != base + offs[s]) return false;
+  }
+  *nax = (int)a;
+  *nay = (int)b;
+  *naz = (int)c;
+  return true;
+}
+
+// Colours: the reference's parity colouring on its structured numbering
+// (cudatest_coloring_gtx1060_optimized.cu:50-74), first-fit greedy in
+// element order otherwise (which reproduces the parity colouring on the
+// structured numbering).  Host only.
+int element_colors(int N, int E, int nax, int nay, const int *iss,
+                   std::vector<int> &color) {
+  color.assign(E, 0);
+  if (nax > 0) {
+    const long ex = nax - 1, ey = nay - 1;
+    for (long e = 0; e < E; e++) {
+      const long i = e % ex, j = (e / ex) % ey, k = e / (ex * ey);
+      color[e] = (int)((i & 1) + 2 * (j & 1) + 4 * (k & 1));
+    }
+    return 8;
+  }
+  std::vector<uint32_t> used(N, 0u);
+  int nc = 0;
+  for (long e = 0; e < E; e++) {
+    uint32_t m = 0;
+    for (int s = 0; s < 8; s++) m |= used[iss[(long)s * E + e] - 1];
+    if (m == 0xffffffffu) return -1;
+    int c = 0;
+    while (m & (1u << c)) c++;
+    color[e] = c;
+    nc = std::max(nc, c + 1);
+    for (int s = 0; s < 8; s++) used[iss[(long)s * E + e] - 1] |= (1u << c);
+  }
+  return nc;
+}
+
+template <typename T>
+void permute_cols(const T *src, T *dst, long E, int ncols,
+                  const std::vector<int> &perm) {
+  for (int c = 0; c < ncols; c++)
+    for (long p = 0; p < E; p++) dst[(long)c * E + p] = src[(long)c * E + perm[p]];
+}
+
+int check_handle(vdr_handle *H) {
+  if (!H) {
+    set_error("null handle");
+    return VDR_BAD_ARGUMENT;
+  }
+  cudaError_t e = cudaSetDevice(H->h.device);
+  if (e) return cuda_fail(e, "cudaSetDevice");
+  return VDR_OK;
+}
+
+int ensure_operator(Handle &h) {
+  if (!h.fields_set) {
+    set_error("fields not set (vdr_set_fields)");
+    return VDR_BAD_ARGUMENT;
+  }
+  cudaError_t e;
+  if (h.op64_valid && h.diag_valid) return VDR_OK;
+  if ((e = dalloc(&h.diag, h.N))) return cuda_fail(e, "alloc diag");
+  const bool stored = h.apply_mode == VDR_APPLY_STORED;
+  if (stored && (e = dalloc(&h.A64, (size_t)h.E * 32))) return cuda_fail(e, "alloc element matrices");
+  if ((e = cudaMemsetAsync(h.diag, 0, sizeof(double) * h.N, h.stream)))
+    return cuda_fail(e, "memset diag");
+  OpArgs a = op_args(h);
+  if ((e = launch_build_stored(a, h.aH, h.aM, stored ? h.A64 : nullptr, nullptr,
+                               h.diag, h.stream)))
+    return cuda_fail(e, "element matrices");
+  if ((e = launch_diag_fix(h.diag, h.mask, h.N, h.stream))) return cuda_fail(e, "diag");
+  h.op64_valid = true;
+  h.diag_valid = true;
+  return VDR_OK;
+}
+
+void invalidate(Handle &h) {
+  h.op64_valid = h.op32_valid = h.diag_valid = false;
+}
+
+int upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+  if (e) return cuda_fail(e, "upload");
+  return VDR_OK;
+}
+
+void free_handle(Handle &h) {
+  dfree(h.xx); dfree(h.yy); dfree(h.zz);
+  dfree(h.xx32); dfree(h.yy32); dfree(h.zz32);
+  dfree(h.conn); dfree(h.mask);
+  dfree(h.vel); dfree(h.lam); dfree(h.pdec); dfree(h.q);
+  dfree(h.vel32); dfree(h.lam32); dfree(h.pdec32); dfree(h.robin);
+  dfree(h.A64); dfree(h.A32); dfree(h.diag);
+  dfree(h.work); dfree(h.st); dfree(h.partials);
+  if (h.h_st) cudaFreeHost(h.h_st);
+  for (int k = 0; k < 4; k++)
+    if (h.graph_exec[k]) cudaGraphExecDestroy(h.graph_exec[k]);
+  for (int k = 0; k < 2; k++)
+    if (h.ev[k]) cudaEventDestroy(h.ev[k]);
+  if (h.stream) cudaStreamDestroy(h.stream);
+  h = Handle();
+}
+
+}  // namespace
+
+void set_error(const std::string &msg) { g_err = msg; }
+
+int cuda_fail(cudaError_t e, const char *what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return VDR_CUDA_ERROR;
+}
+
+OpArgs op_args(const Handle &h) {
+  OpArgs a;
+  a.E = h.E;
+  a.N = h.N;
+  a.variant = h.opt.dr_variant;
+  a.conn = h.conn;
+  a.xx = h.xx;
+  a.yy = h.yy;
+  a.zz = h.zz;
+  a.xx32 = h.xx32;
+  a.yy32 = h.yy32;
+  a.zz32 = h.zz32;
+  a.f.vel = h.vel;
+  a.f.lam = h.lam;
+  a.f.pdec = h.pdec;
+  a.f.q = h.q;
+  a.f.robin = h.robin;
+  a.f.robin_alpha = h.robin_alpha;
+  a.vel32 = h.vel32;
+  a.lam32 = h.lam32;
+  a.pdec32 = h.pdec32;
+  a.aH = h.aH;
+  a.aM = h.aM;
+  return a;
+}
+
+}  // namespace vdr
+
+using namespace vdr;
+
+extern "C" {
+
+const char *vdr_last_error(void) { return g_err.c_str(); }
+
+int vdr_default_options(vdr_options *o) {
+  if (!o) return VDR_BAD_ARGUMENT;
+  std::memset(o, 0, sizeof(*o));
+  o->dr_variant = VDR_DR_VF;
+  o->scatter = VDR_SCATTER_AUTO;
+  o->apply_mode = VDR_APPLY_AUTO;
+  o->solver = VDR_SOLVER_BICGSTAB;
+  o->iters_per_graph = 8;
+  o->device = 0;
+  return VDR_OK;
+}
+
+int vdr_create(vdr_handle **out, int nnode, int nelem, const double *xx,
+               const double *yy, const double *zz, const int *iss,
+               const int *kod, const vdr_options *opt) {
+  if (!out || !xx || !yy || !zz || !iss || nnode < 8 || nelem < 1) {
+    set_error("vdr_create: null pointer or empty mesh");
+    return VDR_BAD_ARGUMENT;
+  }
+  *out = nullptr;
+  const long E = nelem;
+  for (long t = 0; t < 8 * E; t++) {
+    if (iss[t] < 1 || iss[t] > nnode) {
+      char buf[128];
+      std::snprintf(buf, sizeof buf,
+                    "vdr_create: iss entry %ld = %d outside 1..%d", t, iss[t], nnode);
+      set_error(buf);
+      return VDR_BAD_ARGUMENT;
+    }
+  }
+  vdr_options o;
+  if (opt) o = *opt; else vdr_default_options(&o);
+  if (o.dr_variant < VDR_DR_OT || o.dr_variant > VDR_DR_VF) {
+    set_error("vdr_create: unknown dr_variant");
+    return VDR_BAD_ARGUMENT;
+  }
+  vdr_handle *H = new vdr_handle();
+  Handle &h = H->h;
+  h.N = nnode;
+  h.E = nelem;
+  h.opt = o;
+  h.device = o.device;
+  h.scatter = (o.scatter == VDR_SCATTER_COLOR) ? VDR_SCATTER_COLOR : VDR_SCATTER_ATOMIC;
+  h.apply_mode = (o.apply_mode == VDR_APPLY_MATRIX_FREE) ? VDR_APPLY_MATRIX_FREE
+                                                         : VDR_APPLY_STORED;
+  cudaError_t e;
+  int st = VDR_OK;
+  if ((e = cudaSetDevice(h.device)) ||
+      (e = cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking))) {
+    st = cuda_fail(e, "vdr_create: device/stream");
+    delete H;
+    return st;
+  }
+  detect_structured(nnode, nelem, iss, &h.nax, &h.nay, &h.naz);
+
+  // storage order
+  h.perm.resize(E);
+  std::iota(h.perm.begin(), h.perm.end(), 0);
+  h.color_off.assign(2, 0);
+  h.color_off[1] = nelem;
+  h.ncolors = 1;
+  if (h.scatter == VDR_SCATTER_COLOR) {
+    std::vector<int> color;
+    const int nc = element_colors(h.N, h.E, h.nax, h.nay, iss, color);
+    if (nc < 1) {
+      set_error("vdr_create: colouring needs more than 32 colours");
+      free_handle(h);
+      delete H;
+      return VDR_BAD_ARGUMENT;
+    }
+    h.ncolors = nc;
+    h.color_off.assign(nc + 1, 0);
+    for (long e2 = 0; e2 < E; e2++) h.color_off[color[e2] + 1]++;
+    for (int c = 0; c < nc; c++) h.color_off[c + 1] += h.color_off[c];
+    std::vector<int> cursor(h.color_off.begin(), h.color_off.end() - 1);
+    for (long e2 = 0; e2 < E; e2++) h.perm[cursor[color[e2]]++] = (int)e2;
+  }
+
+  std::vector<int> conn(8 * E);
+  for (int s = 0; s < 8; s++)
+    for (long p = 0; p < E; p++) conn[s * E + p] = iss[s * E + h.perm[p]] - 1;
+  std::vector<float> c32(nnode);
+  std::vector<unsigned char> robin(E, 0);
+  bool any_robin = false;
+  if (kod)
+    for (long p = 0; p < E; p++) {
+      robin[p] = kod[2 * E + h.perm[p]] == 3;
+      any_robin |= robin[p] != 0;
+    }
+  do {
+    if ((e = dalloc(&h.xx, nnode)) || (e = dalloc(&h.yy, nnode)) ||
+        (e = dalloc(&h.zz, nnode)) || (e = dalloc(&h.xx32, nnode)) ||
+        (e = dalloc(&h.yy32, nnode)) || (e = dalloc(&h.zz32, nnode)) ||
+        (e = dalloc(&h.conn, 8 * E)) || (e = dalloc(&h.mask, nnode))) {
+      st = cuda_fail(e, "vdr_create: alloc");
+      break;
+    }
+    if ((st = upload(h.xx, xx, sizeof(double) * nnode, h.stream)) ||
+        (st = upload(h.yy, yy, sizeof(double) * nnode, h.stream)) ||
+        (st = upload(h.zz, zz, sizeof(double) * nnode, h.stream)) ||
+        (st = upload(h.conn, conn.data(), sizeof(int) * 8 * E, h.stream)))
+      break;
+    const double *src[3] = {xx, yy, zz};
+    float *dst[3] = {h.xx32, h.yy32, h.zz32};
+    for (int k = 0; k < 3 && !st; k++) {
+      for (long i = 0; i < nnode; i++) c32[i] = (float)src[k][i];
+      st = upload(dst[k], c32.data(), sizeof(float) * nnode, h.stream);
+      if (!st && (e = cudaStreamSynchronize(h.stream))) st = cuda_fail(e, "sync");
+    }
+    if (st) break;
+    if ((e = cudaMemsetAsync(h.mask, 0, nnode, h.stream))) {
+      st = cuda_fail(e, "memset");
+      break;
+    }
+    if (any_robin) {
+      if ((e = dalloc(&h.robin, E))) {
+        st = cuda_fail(e, "alloc");
+        break;
+      }
+      if ((st = upload(h.robin, robin.data(), E, h.stream))) break;
+    }
+    if ((e = cudaStreamSynchronize(h.stream))) st = cuda_fail(e, "vdr_create");
+  } while (0);
+  if (st) {
+    free_handle(h);
+    delete H;
+    return st;
+  }
+  *out = H;
+  return VDR_OK;
+}
+
+int vdr_set_fields(vdr_handle *H, const double *vel, const double *lam,
+                   const double *pdec, const double *q, double robin_alpha) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!vel || !lam) {
+    set_error("vdr_set_fields: vel and lam are required");
+    return VDR_BAD_ARGUMENT;
+  }
+  const long E = h.E;
+  cudaError_t e;
+  if ((e = dalloc(&h.vel, 3 * E)) || (e = dalloc(&h.lam, E)) ||
+      (e = dalloc(&h.pdec, E)) || (e = dalloc(&h.q, E)) ||
+      (e = dalloc(&h.vel32, 3 * E)) || (e = dalloc(&h.lam32, E)) ||
+      (e = dalloc(&h.pdec32, E)))
+    return cuda_fail(e, "vdr_set_fields: alloc");
+  std::vector<double> buf(3 * E);
+  std::vector<float> buf32(3 * E);
+  auto put = [&](const double *src, int ncols, double *d64, float *d32) -> int {
+    if (src) {
+      permute_cols(src, buf.data(), E, ncols, h.perm);
+    } else {
+      std::fill(buf.begin(), buf.begin() + ncols * E, 0.0);
+    }
+    int s2 = upload(d64, buf.data(), sizeof(double) * ncols * E, h.stream);
+    if (s2) return s2;
+    if (d32) {
+      for (long i = 0; i < ncols * E; i++) buf32[i] = (float)buf[i];
+      s2 = upload(d32, buf32.data(), sizeof(float) * ncols * E, h.stream);
+      if (s2) return s2;
+    }
+    cudaError_t e3 = cudaStreamSynchronize(h.stream);  // buf is reused
+    return e3 ? cuda_fail(e3, "vdr_set_fields") : VDR_OK;
+  };
+  if ((st = put(vel, 3, h.vel, h.vel32)) || (st = put(lam, 1, h.lam, h.lam32)) ||
+      (st = put(pdec, 1, h.pdec, h.pdec32)) || (st = put(q, 1, h.q, nullptr)))
+    return st;
+  h.robin_alpha = robin_alpha;
+  h.fields_set = true;
+  invalidate(h);
+  return VDR_OK;
+}
+
+int vdr_set_dirichlet(vdr_handle *H, const int *bc) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  cudaError_t e;
+  std::vector<unsigned char> m(h.N, 0);
+  if (bc)
+    for (long i = 0; i < h.N; i++) m[i] = bc[i] == 1;
+  if ((st = upload(h.mask, m.data(), h.N, h.stream))) return st;
+  if ((e = launch_mask_conn(h.conn, h.E, h.mask, h.stream)))
+    return cuda_fail(e, "mask");
+  if ((e = cudaStreamSynchronize(h.stream))) return cuda_fail(e, "mask");
+  h.mask_set = true;
+  invalidate(h);
+  return VDR_OK;
+}
+
+int vdr_set_operator(vdr_handle *H, double aH, double aM) {
+  int st = check_handle(H);
+  if (st) return st;
+  H->h.aH = aH;
+  H->h.aM = aM;
+  invalidate(H->h);
+  return VDR_OK;
+}
+
+static int ensure_io(vdr_handle *H) {
+  cudaError_t e = dalloc(&H->io, 3 * (size_t)H->h.N);
+  return e ? cuda_fail(e, "alloc io") : VDR_OK;
+}
+
+int vdr_apply_device(vdr_handle *H, const double *x, double *y, int transpose) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!x || !y) {
+    set_error("vdr_apply_device: null vector");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator(h))) return st;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(y, 0, sizeof(double) * h.N, h.stream)))
+    return cuda_fail(e, "memset");
+  if ((e = launch_apply(h, transpose != 0, x, y, nullptr, nullptr, h.stream)))
+    return cuda_fail(e, "apply");
+  return VDR_OK;
+}
+
+int vdr_apply(vdr_handle *H, const double *x, double *y, int transpose) {
+  int st = check_handle(H);
+  if (st) return st;
+  if ((st = ensure_io(H))) return st;
+  Handle &h = H->h;
+  double *dx = H->io, *dy = H->io + h.N;
+  if ((st = upload(dx, x, sizeof(double) * h.N, h.stream))) return st;
+  if ((st = vdr_apply_device(H, dx, dy, transpose))) return st;
+  cudaError_t e = cudaMemcpyAsync(y, dy, sizeof(double) * h.N,
+                                  cudaMemcpyDeviceToHost, h.stream);
+  if (!e) e = cudaStreamSynchronize(h.stream);
+  return e ? cuda_fail(e, "vdr_apply") : VDR_OK;
+}
+
+int vdr_assemble_rhs_device(vdr_handle *H, double cf, double rM,
+                            const double *t_old, double *b) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!h.fields_set) {
+    set_error("fields not set");
+    return VDR_BAD_ARGUMENT;
+  }
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(b, 0, sizeof(double) * h.N, h.stream)))
+    return cuda_fail(e, "memset");
+  if ((e = launch_rhs(op_args(h), cf, rM, t_old, b, h.stream)))
+    return cuda_fail(e, "rhs");
+  return VDR_OK;
+}
+
+int vdr_assemble_rhs(vdr_handle *H, double cf, double rM, const double *t_old,
+                     double *b) {
+  int st = check_handle(H);
+  if (st) return st;
+  if ((st = ensure_io(H))) return st;
+  Handle &h = H->h;
+  double *dt = nullptr, *db = H->io + h.N;
+  if (t_old) {
+    dt = H->io;
+    if ((st = upload(dt, t_old, sizeof(double) * h.N, h.stream))) return st;
+  }
+  if ((st = vdr_assemble_rhs_device(H, cf, rM, dt, db))) return st;
+  cudaError_t e = cudaMemcpyAsync(b, db, sizeof(double) * h.N,
+                                  cudaMemcpyDeviceToHost, h.stream);
+  if (!e) e = cudaStreamSynchronize(h.stream);
+  return e ? cuda_fail(e, "vdr_assemble_rhs") : VDR_OK;
+}
+
+int vdr_get_diag(vdr_handle *H, double *diag) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if ((st = ensure_operator(h))) return st;
+  cudaError_t e = cudaMemcpyAsync(diag, h.diag, sizeof(double) * h.N,
+                                  cudaMemcpyDeviceToHost, h.stream);
+  if (!e) e = cudaStreamSynchronize(h.stream);
+  return e ? cuda_fail(e, "vdr_get_diag") : VDR_OK;
+}
+
+int vdr_solve_device(vdr_handle *H, const double *b, double *x, double tol,
+                     int itmax, int *iter, double *err) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!b || !x || !(tol >= 0.0)) {
+    set_error("vdr_solve_device: bad arguments");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator(h))) return st;
+  if ((st = ensure_io(H))) return st;
+  // Homogeneous Dirichlet rows of b are imposed (b = 0 there), as przest3d
+  // does before the solve (vanadis_full_DR_OpenMP_timing.for:766-772).
+  double *bm = H->io + 2 * (size_t)h.N;
+  cudaError_t e = cudaMemcpyAsync(bm, b, sizeof(double) * h.N,
+                                  cudaMemcpyDeviceToDevice, h.stream);
+  if (!e) e = launch_mask_vec(bm, h.mask, h.N, h.stream);
+  if (e) return cuda_fail(e, "rhs copy");
+  const int method = h.opt.solver == VDR_SOLVER_BICG ? VDR_SOLVER_BICG
+                                                     : VDR_SOLVER_BICGSTAB;
+  return solve_device(h, method, bm, x, tol, itmax, iter, err);
+}
+
+int vdr_solve(vdr_handle *H, const double *b, double *x, double tol,
+              int itmax, int *iter, double *err) {
+  int st = check_handle(H);
+  if (st) return st;
+  if ((st = ensure_io(H))) return st;
+  Handle &h = H->h;
+  double *db = H->io, *dx = H->io + h.N;
+  if ((st = upload(db, b, sizeof(double) * h.N, h.stream)) ||
+      (st = upload(dx, x, sizeof(double) * h.N, h.stream)))
+    return st;
+  st = vdr_solve_device(H, db, dx, tol, itmax, iter, err);
+  if (st == VDR_CUDA_ERROR || st == VDR_BAD_ARGUMENT) return st;
+  cudaError_t e = cudaMemcpyAsync(x, dx, sizeof(double) * h.N,
+                                  cudaMemcpyDeviceToHost, h.stream);
+  if (!e) e = cudaStreamSynchronize(h.stream);
+  return e ? cuda_fail(e, "vdr_solve") : st;
+}
+
+int vdr_true_residual_device(vdr_handle *H, const double *b, const double *x,
+                             double *rel) {
+  int st = check_handle(H);
+  if (st) return st;
+  if ((st = ensure_operator(H->h))) return st;
+  return true_residual_device(H->h, b, x, rel);
+}
+
+int vdr_mass_device(vdr_handle *H, const double *c, double *mass) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  cudaError_t e;
+  if ((e = dalloc(&H->mass_partials, 8192)) || (e = dalloc(&H->mass_out, 1)))
+    return cuda_fail(e, "alloc");
+  if ((e = launch_mass(h, c, H->mass_partials, H->mass_out, h.stream)))
+    return cuda_fail(e, "mass");
+  e = cudaMemcpyAsync(mass, H->mass_out, sizeof(double), cudaMemcpyDeviceToHost,
+                      h.stream);
+  if (!e) e = cudaStreamSynchronize(h.stream);
+  return e ? cuda_fail(e, "mass") : VDR_OK;
+}
+
+int vdr_mass(vdr_handle *H, const double *c, double *mass) {
+  int st = check_handle(H);
+  if (st) return st;
+  if ((st = ensure_io(H))) return st;
+  if ((st = upload(H->io, c, sizeof(double) * H->h.N, H->h.stream))) return st;
+  return vdr_mass_device(H, H->io, mass);
+}
+
+int vdr_color_elements(int nnode, int nelem, const int *iss, int *colors) {
+  if (!iss || !colors || nnode < 1 || nelem < 1) {
+    set_error("vdr_color_elements: bad arguments");
+    return -VDR_BAD_ARGUMENT;
+  }
+  for (long t = 0; t < 8L * nelem; t++)
+    if (iss[t] < 1 || iss[t] > nnode) {
+      set_error("vdr_color_elements: iss entry outside 1..nnode");
+      return -VDR_BAD_ARGUMENT;
+    }
+  int nax = 0, nay = 0, naz = 0;
+  detect_structured(nnode, nelem, iss, &nax, &nay, &naz);
+  std::vector<int> color;
+  const int nc = element_colors(nnode, nelem, nax, nay, iss, color);
+  if (nc < 1) {
+    set_error("vdr_color_elements: more than 32 colours needed");
+    return -VDR_BAD_ARGUMENT;
+  }
+  std::memcpy(colors, color.data(), sizeof(int) * (size_t)nelem);
+  return nc;
+}
+
+void *vdr_stream(vdr_handle *H) { return H ? (void *)H->h.stream : nullptr; }
+
+int vdr_destroy(vdr_handle *H) {
+  if (!H) return VDR_OK;
+  cudaSetDevice(H->h.device);
+  if (H->h.stream) cudaStreamSynchronize(H->h.stream);
+  dfree(H->io);
+  dfree(H->mass_partials);
+  dfree(H->mass_out);
+  free_handle(H->h);
+  delete H;
+  return VDR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Drop-in: kernel_dbcg_simple_ (src_v2026_2_1/cudatest.cu:301-602).
+// Device buffers persist in a process-wide context and grow as needed, so a
+// time loop pays for cudaMalloc once, not per step as the reference does
+// (cudatest.cu:408-432, 576-601).
+// ---------------------------------------------------------------------------
+namespace {
+struct Legacy {
+  std::mutex mu;
+  Handle h;
+  int capN = 0, capE = 0;
+  double *bb = nullptr, *b = nullptr, *x = nullptr;
+  int *iss = nullptr, *bc = nullptr, *bad = nullptr;
+};
+Legacy &legacy() {
+  static Legacy L;
+  return L;
+}
+
+int legacy_prepare(Legacy &L, int N, int E) {
+  Handle &h = L.h;
+  cudaError_t e;
+  if (!h.stream) {
+    vdr_default_options(&h.opt);
+    h.opt.solver = VDR_SOLVER_BICG;
+    if ((e = cudaGetDevice(&h.device))) return cuda_fail(e, "device");
+    if ((e = cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking)))
+      return cuda_fail(e, "stream");
+    h.scatter = VDR_SCATTER_ATOMIC;
+    h.apply_mode = VDR_APPLY_STORED;
+  }
+  if (N > L.capN || E > L.capE) {
+    dfree(h.A64); h.A64 = nullptr;
+    dfree(h.conn); h.conn = nullptr;
+    dfree(h.diag); h.diag = nullptr;
+    dfree(h.mask); h.mask = nullptr;
+    dfree(L.bb); L.bb = nullptr;
+    dfree(L.b); L.b = nullptr;
+    dfree(L.x); L.x = nullptr;
+    dfree(L.iss); L.iss = nullptr;
+    dfree(L.bc); L.bc = nullptr;
+    dfree(h.work); h.work = nullptr; h.nwork = 0;
+    dfree(h.partials); h.partials = nullptr;
+    dfree(h.st); h.st = nullptr;
+    if (h.h_st) cudaFreeHost(h.h_st);
+    h.h_st = nullptr;
+    for (int k = 0; k < 4; k++) {
+      if (h.graph_exec[k]) cudaGraphExecDestroy(h.graph_exec[k]);
+      h.graph_exec[k] = nullptr;
+      h.graph_key[k] = nullptr;
+    }
+    for (int k = 0; k < 2; k++) {
+      if (h.ev[k]) cudaEventDestroy(h.ev[k]);
+      h.ev[k] = nullptr;
+    }
+    const size_t cN = std::max(N, L.capN), cE = std::max(E, L.capE);
+    if ((e = dalloc(&h.A64, cE * 32)) || (e = dalloc(&h.conn, cE * 8)) ||
+        (e = dalloc(&h.diag, cN)) || (e = dalloc(&h.mask, cN)) ||
+        (e = dalloc(&L.bb, cE * 64)) || (e = dalloc(&L.b, cN)) ||
+        (e = dalloc(&L.x, cN)) || (e = dalloc(&L.iss, cE * 8)) ||
+        (e = dalloc(&L.bc, cN)) || (e = dalloc(&L.bad, 1))) {
+      L.capN = L.capE = 0;
+      return cuda_fail(e, "kernel_dbcg_simple_: alloc");
+    }
+    L.capN = (int)cN;
+    L.capE = (int)cE;
+  }
+  return VDR_OK;
+}
+}  // namespace
+
+void kernel_dbcg_simple_(int *Np, double *B, double *X, double *TOLp,
+                         int *ITMAXp, int *ITERp, double *ERRp, double *BB,
+                         int *ISS, double *DIAG, int *NAXp, int *NAYp,
+                         int *NAZp, int *bc_dirichlet) {
+  const double inf = std::numeric_limits<double>::infinity();
+  if (!Np || !B || !X || !TOLp || !ITMAXp || !ITERp || !ERRp || !BB || !ISS ||
+      !DIAG || !NAXp || !NAYp || !NAZp) {
+    set_error("kernel_dbcg_simple_: null argument");
+    if (ERRp) *ERRp = inf;
+    return;
+  }
+  const int N = *Np;
+  const long nax = *NAXp, nay = *NAYp, naz = *NAZp;
+  const long E = (nax - 1) * (nay - 1) * (naz - 1);
+  if (N < 1 || nax < 2 || nay < 2 || naz < 2 || nax * nay * naz != N ||
+      E > 0x7fffffffL / 64) {
+    set_error("kernel_dbcg_simple_: N must equal NAX*NAY*NAZ");
+    *ERRp = inf;
+    return;
+  }
+  Legacy &L = legacy();
+  std::lock_guard<std::mutex> lock(L.mu);
+  Handle &h = L.h;
+  int st = legacy_prepare(L, N, (int)E);
+  if (st) {
+    *ERRp = inf;
+    return;
+  }
+  h.N = N;
+  h.E = (int)E;
+  cudaStream_t s = h.stream;
+  cudaError_t e;
+  int bad = 0;
+  do {
+    if ((e = cudaMemcpyAsync(L.b, B, sizeof(double) * N, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(L.x, X, sizeof(double) * N, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(L.bb, BB, sizeof(double) * 64 * E, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(L.iss, ISS, sizeof(int) * 8 * E, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(h.diag, DIAG, sizeof(double) * N, cudaMemcpyHostToDevice, s)))
+      break;
+    if (bc_dirichlet) {
+      if ((e = cudaMemcpyAsync(L.bc, bc_dirichlet, sizeof(int) * N, cudaMemcpyHostToDevice, s)) ||
+          (e = launch_bc_to_mask(L.bc, h.mask, N, s)))
+        break;
+    } else if ((e = cudaMemsetAsync(h.mask, 0, N, s))) {
+      break;
+    }
+    if ((e = cudaMemsetAsync(L.bad, 0, sizeof(int), s)) ||
+        (e = launch_legacy_conn(L.iss, (int)E, N, bc_dirichlet ? L.bc : nullptr,
+                                h.conn, L.bad, s)) ||
+        (e = launch_legacy_bb(L.bb, (int)E, h.A64, s)) ||
+        (e = cudaMemcpyAsync(&bad, L.bad, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+      break;
+  } while (0);
+  if (e) {
+    cuda_fail(e, "kernel_dbcg_simple_: upload");
+    *ERRp = inf;
+    return;
+  }
+  if (bad) {
+    set_error("kernel_dbcg_simple_: ISS entry outside 1..N");
+    *ERRp = inf;
+    return;
+  }
+  h.op64_valid = h.diag_valid = true;
+  h.fields_set = true;
+  int iter = 0;
+  double err = inf;
+  st = solve_device(h, VDR_SOLVER_BICG, L.b, L.x, *TOLp, *ITMAXp, &iter, &err);
+  if (st == VDR_CUDA_ERROR || st == VDR_BAD_ARGUMENT) {
+    *ERRp = inf;
+    return;
+  }
+  e = cudaMemcpyAsync(X, L.x, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+  if (!e) e = cudaStreamSynchronize(s);
+  if (e) {
+    cuda_fail(e, "kernel_dbcg_simple_: download");
+    *ERRp = inf;
+    return;
+  }
+  *ITERp = iter;
+  *ERRp = err;
+}
+
+}  // extern "C"

@@ -1,0 +1,295 @@
+// apply.cu -- element-by-element operator apply over the HBM-resident
+// element matrices, plus the small conversion kernels around it.
+//
+// y = P A P x with A = sum_e A_e (never assembled): one thread per element
+// gathers x at its 8 nodes (Dirichlet columns read as 0 through the sign
+// bit of the connectivity), multiplies by the element's 8x8 block and adds
+// the 8 results into y.  Same operation as matvec_0 / mttvec_0
+// (vanadis_full_DR_OpenMP_timing.for:1837-1933) and MATVEC_C_cu /
+// MTTVEC_C_cu (src_v2026_2_1/cudatest.cu:184-227).
+//
+// Layout of the element-matrix store (GB300-first, not the reference's BB):
+// entry (i,j) of element p sits at pair index 4*i + j/2 of a double2 array
+// with stride E, i.e. A64[(4i + j/2)*E + p] -> every warp load is 32
+// consecutive elements' same entry pair: 512 contiguous bytes, streamed
+// once per apply with the evict-first (.cs) cache hint so that x and y
+// stay in the 129 MB L2.  FP32 copy: float4 A32[(2i + j/4)*E + p].
+//
+// Scatter: VDR_SCATTER_ATOMIC uses fp64 atomics (red.global.add.f64) in
+// natural element order; VDR_SCATTER_COLOR runs one pass per colour over a
+// colour-major element order, with plain read-modify-writes (no two elements
+// of a colour share a node, cudatest_coloring_gtx1060_optimized.cu:50-74).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "vdr_internal.h"
+
+namespace vdr {
+namespace {
+
+int sm_count2() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+template <bool TRANS, bool ATOMIC>
+__global__ void __launch_bounds__(256) stored_apply_f64(
+    const double2 *__restrict__ A, const int *__restrict__ conn, int E, int p0,
+    int p1, const double *__restrict__ x, double *__restrict__ y,
+    const int *skip, const int *skip2) {
+  if (skip && *(volatile const int *)skip) return;
+  if (skip2 && *(volatile const int *)skip2) return;
+  for (long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x; p < p1;
+       p += (long)gridDim.x * blockDim.x) {
+    int c[8];
+    double xv[8];
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      c[s] = __ldg(conn + (size_t)s * E + p);
+      xv[s] = c[s] < 0 ? 0.0 : __ldg(x + c[s]);
+    }
+    double acc[8];
+    if (!TRANS) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const double2 a0 = __ldcs(A + (size_t)(4 * i + 0) * E + p);
+        const double2 a1 = __ldcs(A + (size_t)(4 * i + 1) * E + p);
+        const double2 a2 = __ldcs(A + (size_t)(4 * i + 2) * E + p);
+        const double2 a3 = __ldcs(A + (size_t)(4 * i + 3) * E + p);
+        acc[i] = a0.x * xv[0] + a0.y * xv[1] + a1.x * xv[2] + a1.y * xv[3] +
+                 a2.x * xv[4] + a2.y * xv[5] + a3.x * xv[6] + a3.y * xv[7];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[j] = 0.0;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++) {
+          const double2 a = __ldcs(A + (size_t)(4 * i + jj) * E + p);
+          acc[2 * jj] += a.x * xv[i];
+          acc[2 * jj + 1] += a.y * xv[i];
+        }
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      if (c[s] >= 0) {
+        if (ATOMIC)
+          atomicAdd(y + c[s], acc[s]);
+        else
+          y[c[s]] += acc[s];
+      }
+    }
+  }
+}
+
+template <bool TRANS, bool ATOMIC>
+__global__ void __launch_bounds__(256) stored_apply_f32(
+    const float4 *__restrict__ A, const int *__restrict__ conn, int E, int p0,
+    int p1, const double *__restrict__ x, double *__restrict__ y,
+    const int *skip, const int *skip2) {
+  if (skip && *(volatile const int *)skip) return;
+  if (skip2 && *(volatile const int *)skip2) return;
+  for (long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x; p < p1;
+       p += (long)gridDim.x * blockDim.x) {
+    int c[8];
+    float xv[8];
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      c[s] = __ldg(conn + (size_t)s * E + p);
+      xv[s] = c[s] < 0 ? 0.f : (float)__ldg(x + c[s]);
+    }
+    float acc[8];
+    if (!TRANS) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float4 a0 = __ldcs(A + (size_t)(2 * i) * E + p);
+        const float4 a1 = __ldcs(A + (size_t)(2 * i + 1) * E + p);
+        acc[i] = a0.x * xv[0] + a0.y * xv[1] + a0.z * xv[2] + a0.w * xv[3] +
+                 a1.x * xv[4] + a1.y * xv[5] + a1.z * xv[6] + a1.w * xv[7];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[j] = 0.f;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float4 a0 = __ldcs(A + (size_t)(2 * i) * E + p);
+        const float4 a1 = __ldcs(A + (size_t)(2 * i + 1) * E + p);
+        acc[0] += a0.x * xv[i];
+        acc[1] += a0.y * xv[i];
+        acc[2] += a0.z * xv[i];
+        acc[3] += a0.w * xv[i];
+        acc[4] += a1.x * xv[i];
+        acc[5] += a1.y * xv[i];
+        acc[6] += a1.z * xv[i];
+        acc[7] += a1.w * xv[i];
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      if (c[s] >= 0) {
+        if (ATOMIC)
+          atomicAdd(y + c[s], (double)acc[s]);
+        else
+          y[c[s]] += (double)acc[s];
+      }
+    }
+  }
+}
+
+// Reference BB (BB[64e + 8i + j], sklad_wd) -> pair store A64[(4i+j/2)*E+e];
+// reference ISS (iss(E,8) column-major, 1-based) -> masked 0-based conn.
+__global__ void legacy_convert_kernel(const double2 *__restrict__ bb, int E,
+                                      double2 *__restrict__ A) {
+  const long total = (long)E * 32;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long)gridDim.x * blockDim.x) {
+    const long e = t >> 5;
+    const int k = (int)(t & 31);
+    A[(size_t)k * E + e] = bb[t];
+  }
+}
+
+__global__ void legacy_conn_kernel(const int *__restrict__ iss, int E, int N,
+                                   const int *__restrict__ bc,
+                                   int *__restrict__ conn, int *bad) {
+  const long total = (long)E * 8;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long)gridDim.x * blockDim.x) {
+    const int n = iss[t] - 1;
+    if (n < 0 || n >= N) {
+      atomicExch(bad, 1);
+      conn[t] = MASK_BIT;  // node 0, masked: never read or written
+      continue;
+    }
+    conn[t] = (bc && bc[n] == 1) ? (n | MASK_BIT) : n;
+  }
+}
+
+__global__ void mask_conn_kernel(int *__restrict__ conn, long total,
+                                 const unsigned char *__restrict__ mask) {
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long)gridDim.x * blockDim.x) {
+    const int n = conn[t] & NODE_BITS;
+    conn[t] = mask[n] ? (n | MASK_BIT) : n;
+  }
+}
+
+__global__ void diag_fix_kernel(double *__restrict__ d,
+                                const unsigned char *__restrict__ m, int N) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (long)gridDim.x * blockDim.x)
+    if (m[i]) d[i] = 1.0;
+}
+
+__global__ void mask_vec_kernel(double *__restrict__ v,
+                                const unsigned char *__restrict__ m, int N) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (long)gridDim.x * blockDim.x)
+    if (m[i]) v[i] = 0.0;
+}
+
+__global__ void bc_to_mask_kernel(const int *__restrict__ bc,
+                                  unsigned char *__restrict__ m, int N) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (long)gridDim.x * blockDim.x)
+    m[i] = bc[i] == 1 ? 1 : 0;
+}
+
+int grid_for(long n, int threads, int per_sm) {
+  const long need = (n + threads - 1) / threads;
+  return (int)std::max<long>(1, std::min<long>(need, (long)sm_count2() * per_sm));
+}
+
+}  // namespace
+
+cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
+                                const double *x, double *y, const int *skip,
+                                const int *skip2, cudaStream_t s) {
+  const bool color = h.scatter == VDR_SCATTER_COLOR;
+  const int nranges = color ? h.ncolors : 1;
+  for (int r = 0; r < nranges; r++) {
+    const int p0 = color ? h.color_off[r] : 0;
+    const int p1 = color ? h.color_off[r + 1] : h.E;
+    if (p1 <= p0) continue;
+    const int grid = grid_for(p1 - p0, 256, 8);
+#define VDR_LAUNCH(K, AP)                                                     \
+  K<<<grid, 256, 0, s>>>(AP, h.conn, h.E, p0, p1, x, y, skip, skip2)
+    if (!fp32) {
+      if (transpose) {
+        if (color) VDR_LAUNCH((stored_apply_f64<true, false>), h.A64);
+        else VDR_LAUNCH((stored_apply_f64<true, true>), h.A64);
+      } else {
+        if (color) VDR_LAUNCH((stored_apply_f64<false, false>), h.A64);
+        else VDR_LAUNCH((stored_apply_f64<false, true>), h.A64);
+      }
+    } else {
+      if (transpose) {
+        if (color) VDR_LAUNCH((stored_apply_f32<true, false>), h.A32);
+        else VDR_LAUNCH((stored_apply_f32<true, true>), h.A32);
+      } else {
+        if (color) VDR_LAUNCH((stored_apply_f32<false, false>), h.A32);
+        else VDR_LAUNCH((stored_apply_f32<false, true>), h.A32);
+      }
+    }
+#undef VDR_LAUNCH
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_legacy_bb(const double *bb_ref, int E, double2 *A64,
+                             cudaStream_t s) {
+  legacy_convert_kernel<<<grid_for((long)E * 32, 256, 16), 256, 0, s>>>(
+      reinterpret_cast<const double2 *>(bb_ref), E, A64);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_legacy_conn(const int *iss_ref, int E, int N, const int *bc,
+                               int *conn, int *bad, cudaStream_t s) {
+  legacy_conn_kernel<<<grid_for((long)E * 8, 256, 16), 256, 0, s>>>(
+      iss_ref, E, N, bc, conn, bad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mask_conn(int *conn, int E, const unsigned char *mask,
+                             cudaStream_t s) {
+  mask_conn_kernel<<<grid_for((long)E * 8, 256, 16), 256, 0, s>>>(
+      conn, (long)E * 8, mask);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diag_fix(double *diag, const unsigned char *mask, int N,
+                            cudaStream_t s) {
+  diag_fix_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(diag, mask, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mask_vec(double *v, const unsigned char *mask, int N,
+                            cudaStream_t s) {
+  mask_vec_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(v, mask, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bc_to_mask(const int *bc, unsigned char *mask, int N,
+                              cudaStream_t s) {
+  bc_to_mask_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(bc, mask, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply(const Handle &h, bool transpose, const double *x,
+                         double *y, const int *skip, const int *skip2,
+                         cudaStream_t s) {
+  if (h.apply_mode == VDR_APPLY_MATRIX_FREE)
+    return launch_mf_apply(op_args(h), false, transpose, x, y, skip, skip2, s);
+  return launch_stored_apply(h, false, transpose, x, y, skip, skip2, s);
+}
+
+}  // namespace vdr

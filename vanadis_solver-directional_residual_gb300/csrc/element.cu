@@ -1,0 +1,460 @@
+// element.cu -- per-element DR recompute kernels.
+//
+// Every kernel here maps one element onto 8 consecutive lanes; lane q
+// evaluates Gauss point q (the reference's point order: the node-sign
+// pattern of par_3d times 0.577350269189626) so the geometry, Jacobian
+// inverse and DR weight of the 8 points are computed in parallel in
+// registers.  What differs is what is done with them:
+//
+//   elem_rows_kernel<T,STORE>  C = c1*H + c2*M, row i kept by lane i, written
+//                              to the HBM-resident element-matrix store and
+//                              its diagonal scattered into the Jacobi diag
+//                              (el3d + sklad_wd + diag assembly,
+//                              vanadis_full_DR_OpenMP_timing.for:431-610,
+//                              691-737, 880-904)
+//   elem_rows_kernel<T,RHS>    b += cf*f - C . T_old   (przest3d :691-716)
+//   mf_apply_kernel<T,TRANS>   y += C x or C^T x without forming C: lane q
+//                              forms its point's contribution to all 8
+//                              outputs, then a 3-step shuffle reduce-scatter
+//                              leaves output i in lane i (matrix-free apply)
+//   mass_kernel                int c dOmega (integrate_mass_hex8 :2181-2285)
+//
+// with H = int lambda gradN.gradN + int W (v.gradN) + P int W N
+//          + alpha int_{face 3} W N,  M = int W N,  f = (Q/vol) int W.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "dr_device.cuh"
+#include "vdr_internal.h"
+
+namespace vdr {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <typename T>
+struct Src;
+template <>
+struct Src<double> {
+  static __device__ __forceinline__ const double *xx(const OpArgs &a) { return a.xx; }
+  static __device__ __forceinline__ const double *yy(const OpArgs &a) { return a.yy; }
+  static __device__ __forceinline__ const double *zz(const OpArgs &a) { return a.zz; }
+  static __device__ __forceinline__ const double *vel(const OpArgs &a) { return a.f.vel; }
+  static __device__ __forceinline__ const double *lam(const OpArgs &a) { return a.f.lam; }
+  static __device__ __forceinline__ const double *pdec(const OpArgs &a) { return a.f.pdec; }
+};
+template <>
+struct Src<float> {
+  static __device__ __forceinline__ const float *xx(const OpArgs &a) { return a.xx32; }
+  static __device__ __forceinline__ const float *yy(const OpArgs &a) { return a.yy32; }
+  static __device__ __forceinline__ const float *zz(const OpArgs &a) { return a.zz32; }
+  static __device__ __forceinline__ const float *vel(const OpArgs &a) { return a.vel32; }
+  static __device__ __forceinline__ const float *lam(const OpArgs &a) { return a.lam32; }
+  static __device__ __forceinline__ const float *pdec(const OpArgs &a) { return a.pdec32; }
+};
+
+template <typename T>
+struct Elem {
+  T xe[8], ye[8], ze[8];
+  int c[8];  // connectivity entries (node | MASK_BIT)
+  T vx, vy, vz, lam, pdec;
+  bool robin;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_elem(const OpArgs &a, long p, Elem<T> &e) {
+  const T *X = Src<T>::xx(a), *Y = Src<T>::yy(a), *Z = Src<T>::zz(a);
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    e.c[s] = __ldg(a.conn + (size_t)s * a.E + p);
+    const int n = e.c[s] & NODE_BITS;
+    e.xe[s] = __ldg(X + n);
+    e.ye[s] = __ldg(Y + n);
+    e.ze[s] = __ldg(Z + n);
+  }
+  const T *V = Src<T>::vel(a);
+  e.vx = __ldg(V + p);
+  e.vy = __ldg(V + a.E + p);
+  e.vz = __ldg(V + 2 * (size_t)a.E + p);
+  e.lam = __ldg(Src<T>::lam(a) + p);
+  const T *P = Src<T>::pdec(a);
+  e.pdec = P ? __ldg(P + p) : T(0);
+  e.robin = a.f.robin ? (__ldg(a.f.robin + p) != 0) : false;
+}
+
+template <typename T>
+__device__ __forceinline__ T gauss_coord(int q, int axis) {
+  const T c = T(VDR_GAUSS_C);
+  const float sg = axis == 0 ? node_sx(q) : (axis == 1 ? node_sy(q) : node_sz(q));
+  return sg > 0 ? c : -c;
+}
+
+// Sum over the 8 lanes of one element (butterfly, same order in all lanes).
+template <typename T>
+__device__ __forceinline__ T group8_sum(T v) {
+  v += __shfl_xor_sync(FULL, v, 1);
+  v += __shfl_xor_sync(FULL, v, 2);
+  v += __shfl_xor_sync(FULL, v, 4);
+  return v;
+}
+
+// Reduce-scatter over the 8 lanes of one element: lane t returns
+// sum over lanes of v[t].
+template <typename T>
+__device__ __forceinline__ T group8_reduce_scatter(const T (&v)[8], int lane8) {
+  const bool b2 = lane8 & 4, b1 = lane8 & 2, b0 = lane8 & 1;
+  T h[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const T send = b2 ? v[k] : v[k + 4];
+    const T keep = b2 ? v[k + 4] : v[k];
+    h[k] = keep + __shfl_xor_sync(FULL, send, 4);
+  }
+  T g[2];
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const T send = b1 ? h[k] : h[k + 2];
+    const T keep = b1 ? h[k + 2] : h[k];
+    g[k] = keep + __shfl_xor_sync(FULL, send, 2);
+  }
+  const T send = b0 ? g[0] : g[1];
+  const T keep = b0 ? g[1] : g[0];
+  return keep + __shfl_xor_sync(FULL, send, 1);
+}
+
+constexpr int ROWS_EPB = 8;  // elements per 64-thread block
+
+template <typename T>
+struct RowSmem {
+  T g[ROWS_EPB][8][5][8];  // per element, per Gauss point: gx, gy, gz, s, w
+  T d[ROWS_EPB][8][2];     // detJ, c1*lambda*detJ
+  T fnw[ROWS_EPB][4][2][8];  // face points: N, W
+  T fd[ROWS_EPB][4];       // c1*alpha*detJs
+};
+
+// MODE 0: store C rows (+ diag); MODE 1: rhs.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(64) elem_rows_kernel(
+    OpArgs a, T c1, T c2, double2 *__restrict__ A64, float4 *__restrict__ A32,
+    double *__restrict__ diag, double cf, const double *__restrict__ told,
+    double *__restrict__ b) {
+  __shared__ RowSmem<T> sm;
+  const int lane8 = threadIdx.x & 7;
+  const int le = threadIdx.x >> 3;
+  const long E = a.E;
+  for (long base = (long)blockIdx.x * ROWS_EPB; base < E;
+       base += (long)gridDim.x * ROWS_EPB) {
+    const long pe = base + le;
+    const bool valid = pe < E;
+    const long p = valid ? pe : E - 1;
+    Elem<T> el;
+    load_elem<T>(a, p, el);
+    GPData<T> o;
+    gp_eval<T>(a.variant, gauss_coord<T>(lane8, 0), gauss_coord<T>(lane8, 1),
+               gauss_coord<T>(lane8, 2), el.xe, el.ye, el.ze, el.lam, el.vx,
+               el.vy, el.vz, o);
+    const T vol = group8_sum<T>(o.detj);
+    const T cm = c1 * el.pdec + c2;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      sm.g[le][lane8][0][j] = o.gx[j];
+      sm.g[le][lane8][1][j] = o.gy[j];
+      sm.g[le][lane8][2][j] = o.gz[j];
+      sm.g[le][lane8][3][j] =
+          c1 * (el.vx * o.gx[j] + el.vy * o.gy[j] + el.vz * o.gz[j]) + cm * o.n[j];
+      sm.g[le][lane8][4][j] = o.w[j];
+    }
+    sm.d[le][lane8][0] = o.detj;
+    sm.d[le][lane8][1] = c1 * el.lam * o.detj;
+    if (el.robin && lane8 < 4) {
+      const T gc = T(VDR_GAUSS_C);
+      const T r = (lane8 & 2) ? gc : -gc;
+      const T s = (lane8 & 1) ? gc : -gc;
+      const T djs = face3_detjs<T>(el.xe, el.ye, el.ze, r, s);
+      gp_eval<T>(a.variant, T(-1), r, s, el.xe, el.ye, el.ze, el.lam, el.vx,
+                 el.vy, el.vz, o);
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        sm.fnw[le][lane8][0][j] = o.n[j];
+        sm.fnw[le][lane8][1][j] = o.w[j];
+      }
+      sm.fd[le][lane8] = c1 * T(a.f.robin_alpha) * djs;
+    }
+    __syncwarp();
+    const int i = lane8;
+    T acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[j] = T(0);
+    T fw = T(0);
+#pragma unroll 2
+    for (int q = 0; q < 8; q++) {
+      const T dj = sm.d[le][q][0];
+      const T dl = sm.d[le][q][1];
+      const T gxi = sm.g[le][q][0][i], gyi = sm.g[le][q][1][i],
+              gzi = sm.g[le][q][2][i];
+      const T wi = sm.g[le][q][4][i];
+      const T wd = wi * dj;
+      fw += wd;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const T gg = gxi * sm.g[le][q][0][j] + gyi * sm.g[le][q][1][j] +
+                     gzi * sm.g[le][q][2][j];
+        acc[j] += dl * gg + wd * sm.g[le][q][3][j];
+      }
+    }
+    if (el.robin) {
+#pragma unroll
+      for (int f = 0; f < 4; f++) {
+        const T aw = sm.fd[le][f] * sm.fnw[le][f][1][i];
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[j] += aw * sm.fnw[le][f][0][j];
+      }
+    }
+    __syncwarp();
+    if (valid) {
+      const int ci = el.c[i];
+      if (MODE == 0) {
+        if (A64) {
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++)
+            A64[(size_t)(4 * i + jj) * E + p] =
+                make_double2((double)acc[2 * jj], (double)acc[2 * jj + 1]);
+        }
+        if (A32) {
+#pragma unroll
+          for (int h = 0; h < 2; h++)
+            A32[(size_t)(2 * i + h) * E + p] =
+                make_float4((float)acc[4 * h], (float)acc[4 * h + 1],
+                            (float)acc[4 * h + 2], (float)acc[4 * h + 3]);
+        }
+        if (diag && ci >= 0) atomicAdd(diag + ci, (double)acc[i]);
+      } else {
+        if (ci >= 0) {
+          const double q = a.f.q ? __ldg(a.f.q + p) : 0.0;
+          double val = cf * ((q / (double)vol) * (double)fw);
+          if (told) {
+            double ft = 0.0;
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+              ft += (double)acc[j] * __ldg(told + (el.c[j] & NODE_BITS));
+            val -= ft;
+          }
+          atomicAdd(b + ci, val);
+        }
+      }
+    }
+  }
+}
+
+template <typename T, bool TRANS>
+__global__ void __launch_bounds__(256) mf_apply_kernel(
+    OpArgs a, T c1, T c2, const double *__restrict__ x, double *__restrict__ y,
+    const int *skip, const int *skip2) {
+  if (skip && *(volatile const int *)skip) return;
+  if (skip2 && *(volatile const int *)skip2) return;
+  const int lane8 = threadIdx.x & 7;
+  const long E = a.E;
+  const long groups_per_block = blockDim.x >> 3;
+  for (long base = (long)blockIdx.x * groups_per_block; base < E;
+       base += (long)gridDim.x * groups_per_block) {
+    const long pe = base + (threadIdx.x >> 3);
+    const bool valid = pe < E;
+    const long p = valid ? pe : E - 1;
+    Elem<T> el;
+    load_elem<T>(a, p, el);
+    T xv[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      xv[j] = el.c[j] < 0 ? T(0) : (T)__ldg(x + el.c[j]);
+    GPData<T> o;
+    gp_eval<T>(a.variant, gauss_coord<T>(lane8, 0), gauss_coord<T>(lane8, 1),
+               gauss_coord<T>(lane8, 2), el.xe, el.ye, el.ze, el.lam, el.vx,
+               el.vy, el.vz, o);
+    const T cm = c1 * el.pdec + c2;
+    const T dl = c1 * el.lam * o.detj;
+    T con[8];
+    if (!TRANS) {
+      T u = 0, gu = 0, hu = 0, ku = 0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        u += o.n[j] * xv[j];
+        gu += o.gx[j] * xv[j];
+        hu += o.gy[j] * xv[j];
+        ku += o.gz[j] * xv[j];
+      }
+      const T t = o.detj * (c1 * (el.vx * gu + el.vy * hu + el.vz * ku) + cm * u);
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        con[i] = dl * (o.gx[i] * gu + o.gy[i] * hu + o.gz[i] * ku) + o.w[i] * t;
+    } else {
+      T ws = 0, gu = 0, hu = 0, ku = 0;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        ws += o.w[i] * xv[i];
+        gu += o.gx[i] * xv[i];
+        hu += o.gy[i] * xv[i];
+        ku += o.gz[i] * xv[i];
+      }
+      const T dw = o.detj * ws;
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+        con[j] = dl * (o.gx[j] * gu + o.gy[j] * hu + o.gz[j] * ku) +
+                 dw * (c1 * (el.vx * o.gx[j] + el.vy * o.gy[j] + el.vz * o.gz[j]) +
+                       cm * o.n[j]);
+    }
+    if (el.robin && lane8 < 4) {
+      const T gc = T(VDR_GAUSS_C);
+      const T r = (lane8 & 2) ? gc : -gc;
+      const T s = (lane8 & 1) ? gc : -gc;
+      const T ca = c1 * T(a.f.robin_alpha) * face3_detjs<T>(el.xe, el.ye, el.ze, r, s);
+      gp_eval<T>(a.variant, T(-1), r, s, el.xe, el.ye, el.ze, el.lam, el.vx,
+                 el.vy, el.vz, o);
+      if (!TRANS) {
+        T uf = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) uf += o.n[j] * xv[j];
+#pragma unroll
+        for (int i = 0; i < 8; i++) con[i] += ca * o.w[i] * uf;
+      } else {
+        T wf = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) wf += o.w[i] * xv[i];
+#pragma unroll
+        for (int j = 0; j < 8; j++) con[j] += ca * o.n[j] * wf;
+      }
+    }
+    const T mine = group8_reduce_scatter<T>(con, lane8);
+    const int cme = el.c[lane8];
+    if (valid && cme >= 0) atomicAdd(y + cme, (double)mine);
+  }
+}
+
+// integrate_mass_hex8: one thread per element, 2x2x2 Gauss with
+// abscissa 1/sqrt(3); block partials summed in fixed order by the host
+// launcher's second kernel.
+__global__ void __launch_bounds__(256) mass_kernel(
+    const int *__restrict__ conn, int E, const double *__restrict__ xx,
+    const double *__restrict__ yy, const double *__restrict__ zz,
+    const double *__restrict__ c, double *__restrict__ partials) {
+  const double g = 1.0 / sqrt(3.0);
+  double acc = 0.0;
+  for (long p = (long)blockIdx.x * blockDim.x + threadIdx.x; p < E;
+       p += (long)gridDim.x * blockDim.x) {
+    double xe[8], ye[8], ze[8], ce[8];
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      const int n = __ldg(conn + (size_t)s * E + p) & NODE_BITS;
+      xe[s] = __ldg(xx + n);
+      ye[s] = __ldg(yy + n);
+      ze[s] = __ldg(zz + n);
+      ce[s] = __ldg(c + n);
+    }
+#pragma unroll 1
+    for (int q = 0; q < 8; q++) {
+      GPData<double> o;
+      const double xi = ((q >> 2) & 1) ? g : -g;
+      const double eta = ((q >> 1) & 1) ? g : -g;
+      const double zeta = (q & 1) ? g : -g;
+      // DR weights are not needed: zero velocity keeps W = N.
+      gp_eval<double>(VDR_DR_VF, xi, eta, zeta, xe, ye, ze, 1.0, 0.0, 0.0, 0.0, o);
+      double cv = 0.0;
+#pragma unroll
+      for (int s = 0; s < 8; s++) cv += o.n[s] * ce[s];
+      acc += cv * o.detj;
+    }
+  }
+  __shared__ double sm[256];
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = 128; off > 0; off >>= 1) {
+    if (threadIdx.x < off) sm[threadIdx.x] += sm[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = sm[0];
+}
+
+__global__ void sum_partials_kernel(const double *__restrict__ partials, int n,
+                                    double *__restrict__ out) {
+  __shared__ double sm[256];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += partials[i];
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = 128; off > 0; off >>= 1) {
+    if (threadIdx.x < off) sm[threadIdx.x] += sm[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sm[0];
+}
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+}  // namespace
+
+cudaError_t launch_build_stored(const OpArgs &a, double c1, double c2,
+                                double2 *A64, float4 *A32, double *diag,
+                                cudaStream_t s) {
+  if (a.E <= 0) return cudaSuccess;
+  const long blocks_needed = ((long)a.E + ROWS_EPB - 1) / ROWS_EPB;
+  const int grid = (int)std::min<long>(blocks_needed, (long)sm_count() * 32);
+  if (A32 && !A64 && !diag) {
+    elem_rows_kernel<float, 0><<<grid, 64, 0, s>>>(a, (float)c1, (float)c2,
+                                                   nullptr, A32, nullptr, 0.0,
+                                                   nullptr, nullptr);
+  } else {
+    elem_rows_kernel<double, 0><<<grid, 64, 0, s>>>(a, c1, c2, A64, A32, diag,
+                                                    0.0, nullptr, nullptr);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rhs(const OpArgs &a, double cf, double rM,
+                       const double *t_old, double *b, cudaStream_t s) {
+  if (a.E <= 0) return cudaSuccess;
+  const long blocks_needed = ((long)a.E + ROWS_EPB - 1) / ROWS_EPB;
+  const int grid = (int)std::min<long>(blocks_needed, (long)sm_count() * 32);
+  elem_rows_kernel<double, 1><<<grid, 64, 0, s>>>(a, 1.0, -rM, nullptr, nullptr,
+                                                  nullptr, cf, t_old, b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
+                            const double *x, double *y, const int *skip,
+                            const int *skip2, cudaStream_t s) {
+  if (a.E <= 0) return cudaSuccess;
+  const long blocks_needed = ((long)a.E + 31) / 32;
+  const int grid = (int)std::min<long>(blocks_needed, (long)sm_count() * 8);
+  if (fp32) {
+    if (transpose)
+      mf_apply_kernel<float, true><<<grid, 256, 0, s>>>(a, (float)a.aH, (float)a.aM, x, y, skip, skip2);
+    else
+      mf_apply_kernel<float, false><<<grid, 256, 0, s>>>(a, (float)a.aH, (float)a.aM, x, y, skip, skip2);
+  } else {
+    if (transpose)
+      mf_apply_kernel<double, true><<<grid, 256, 0, s>>>(a, a.aH, a.aM, x, y, skip, skip2);
+    else
+      mf_apply_kernel<double, false><<<grid, 256, 0, s>>>(a, a.aH, a.aM, x, y, skip, skip2);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mass(const Handle &h, const double *c, double *partials,
+                        double *out, cudaStream_t s) {
+  const int grid = std::max(1, std::min((h.E + 255) / 256, sm_count() * 4));
+  mass_kernel<<<grid, 256, 0, s>>>(h.conn, h.E, h.xx, h.yy, h.zz, c, partials);
+  sum_partials_kernel<<<1, 256, 0, s>>>(partials, grid, out);
+  return cudaGetLastError();
+}
+
+}  // namespace vdr

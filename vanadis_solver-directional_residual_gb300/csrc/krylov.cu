@@ -1,0 +1,570 @@
+// krylov.cu -- Jacobi-preconditioned BiCG (the reference's dbcg_simple,
+// vanadis_full_DR_OpenMP_timing.for:906-984 / kernel_dbcg_simple_,
+// src_v2026_2_1/cudatest.cu:301-602) and BiCGStab on the GPU.
+//
+// GB300 design:
+//  * Every Krylov scalar (rho, alpha, omega, beta, norms, the iteration
+//    count, convergence and breakdown flags) lives in a device struct
+//    (KState).  Dot products are fused into the vector update that produces
+//    their operands; each kernel's blocks write partial sums and the last
+//    block to finish (ticketed with one atomic) adds the partials in a fixed
+//    order and updates the scalars.  Reductions are therefore deterministic
+//    for a fixed grid, and no spin-wait exists anywhere.
+//  * The Jacobi preconditioner is fused into the vector updates (z = r/d is
+//    never stored for BiCG).
+//  * One iteration is a fixed chain of launches that read their scalars
+//    from KState, so `iters_per_graph` iterations are captured once into a
+//    CUDA graph and replayed; once `done` is set every kernel returns at
+//    entry.  The host reads KState back asynchronously once per graph
+//    launch, one launch behind, so the GPU never waits for the host.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "vdr_internal.h"
+
+namespace vdr {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+int sm_count3() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+template <int NQ>
+__device__ __forceinline__ void block_sum(double (&v)[NQ]) {
+  __shared__ double sm[RED_THREADS / 32][MAXQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      v[q] += __shfl_xor_sync(FULL, v[q], off);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) sm[w][q] = v[q];
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      v[q] = (l < (int)(blockDim.x >> 5)) ? sm[l][q] : 0.0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+        v[q] += __shfl_xor_sync(FULL, v[q], off);
+    }
+  }
+}
+
+// Grid-wide sum of NQ values.  Returns true in thread 0 of the last block
+// to arrive, with the totals in `out`.
+template <int NQ>
+__device__ __forceinline__ bool grid_sum(double (&v)[NQ], double *partials,
+                                         unsigned int *ticket,
+                                         double (&out)[NQ]) {
+  __shared__ bool last;
+  block_sum<NQ>(v);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; q++) partials[q * gridDim.x + blockIdx.x] = v[q];
+    __threadfence();
+    const unsigned t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double w[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    w[q] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+      w[q] += __ldcg(partials + q * gridDim.x + b);
+  }
+  block_sum<NQ>(w);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; q++) out[q] = w[q];
+    *ticket = 0u;
+    return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ bool finite(double x) { return isfinite(x); }
+
+struct Vec {
+  int n;
+  KState *st;
+  double *partials;
+  const double *b, *d;
+  const unsigned char *m;
+  double *x, *r, *rh, *p, *v, *ph, *s, *sh, *t;  // BiCGStab
+  double *rr, *pp, *z, *zz;                      // BiCG (r, p, x shared)
+};
+
+#define GRID_LOOP(i) \
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (long)gridDim.x * blockDim.x)
+
+// -------- shared start: r = b - r (r holds A x0), residual norms --------
+// BiCGStab: rh = r, rho = (rh, r).  BiCG: rr = r, bknum = (r/d, rr).
+template <bool BICG>
+__global__ void __launch_bounds__(RED_THREADS) k_start(Vec a) {
+  double v[3] = {0.0, 0.0, 0.0};
+  GRID_LOOP(i) {
+    const double bi = a.b[i];
+    const double ri = bi - a.r[i];
+    a.r[i] = ri;
+    if (BICG) {
+      a.rr[i] = ri;
+      v[2] += (ri / a.d[i]) * ri;
+    } else {
+      a.rh[i] = ri;
+    }
+    v[0] += bi * bi;
+    v[1] += ri * ri;
+  }
+  double o[3];
+  if (grid_sum<3>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    st->bnrm2 = o[0];
+    st->iter = 0;
+    st->sconv = 0;
+    st->status = VDR_NOT_CONVERGED;
+    st->done = 0;
+    st->rho = o[1];
+    st->rho_old = 1.0;
+    st->alpha = 1.0;
+    st->omega = 1.0;
+    st->bknum = o[2];
+    st->bkden = 1.0;
+    if (o[0] == 0.0) {  // b = 0: the solution is x = 0
+      st->err = 0.0;
+      st->status = VDR_OK;
+      st->done = 2;  // tells the host to zero x
+      return;
+    }
+    st->err = sqrt(o[1]) / sqrt(o[0]);
+    if (!(st->err == st->err)) {
+      st->status = VDR_BREAKDOWN;
+      st->done = 1;
+    } else if (st->err <= st->tol) {
+      st->status = VDR_OK;
+      st->done = 1;
+    } else if (st->itmax <= 0) {
+      st->done = 1;
+    }
+  }
+}
+
+// ---------------------------- BiCGStab ----------------------------------
+// p = r + beta (p - omega v); ph = M^-1 p (0 on Dirichlet); v = 0.
+__global__ void __launch_bounds__(RED_THREADS) bs_p(Vec a) {
+  const KState *st = a.st;
+  if (st->done) return;
+  const bool first = st->iter == 0;
+  const double beta = first ? 0.0 : (st->rho / st->rho_old) * (st->alpha / st->omega);
+  const double om = st->omega;
+  GRID_LOOP(i) {
+    const double pi = first ? a.r[i] : a.r[i] + beta * (a.p[i] - om * a.v[i]);
+    a.p[i] = pi;
+    a.ph[i] = a.m[i] ? 0.0 : pi / a.d[i];
+    a.v[i] = 0.0;
+  }
+}
+
+// alpha = rho / (rh, v)
+__global__ void __launch_bounds__(RED_THREADS) bs_alpha(Vec a) {
+  if (a.st->done) return;
+  double v[1] = {0.0};
+  GRID_LOOP(i) v[0] += a.rh[i] * a.v[i];
+  double o[1];
+  if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    if (o[0] == 0.0 || !finite(o[0])) {
+      st->status = VDR_BREAKDOWN;
+      st->done = 1;
+    } else {
+      st->alpha = st->rho / o[0];
+    }
+  }
+}
+
+// s = r - alpha v; sh = M^-1 s; t = 0; ||s||.
+__global__ void __launch_bounds__(RED_THREADS) bs_s(Vec a) {
+  if (a.st->done) return;
+  const double al = a.st->alpha;
+  double v[1] = {0.0};
+  GRID_LOOP(i) {
+    const double si = a.r[i] - al * a.v[i];
+    a.s[i] = si;
+    a.sh[i] = a.m[i] ? 0.0 : si / a.d[i];
+    a.t[i] = 0.0;
+    v[0] += si * si;
+  }
+  double o[1];
+  if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    st->snrm = sqrt(o[0]) / sqrt(st->bnrm2);
+    if (st->snrm <= st->tol) st->sconv = 1;
+  }
+}
+
+// omega = (t, s) / (t, t)
+__global__ void __launch_bounds__(RED_THREADS) bs_omega(Vec a) {
+  if (a.st->done || a.st->sconv) return;
+  double v[2] = {0.0, 0.0};
+  GRID_LOOP(i) {
+    const double ti = a.t[i];
+    v[0] += ti * a.s[i];
+    v[1] += ti * ti;
+  }
+  double o[2];
+  if (grid_sum<2>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    if (o[1] == 0.0 || !finite(o[1]) || !finite(o[0])) {
+      st->status = VDR_BREAKDOWN;
+      st->done = 1;
+    } else {
+      st->omega = o[0] / o[1];
+    }
+  }
+}
+
+// x += alpha ph + omega sh; r = s - omega t; rho_new = (rh, r); ||r||.
+__global__ void __launch_bounds__(RED_THREADS) bs_xr(Vec a) {
+  KState *stc = a.st;
+  if (stc->done) return;
+  const double al = stc->alpha;
+  if (stc->sconv) {
+    double v[1] = {0.0};
+    GRID_LOOP(i) {
+      a.x[i] += al * a.ph[i];
+      a.r[i] = a.s[i];
+    }
+    double o[1];
+    if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
+      KState *st = a.st;
+      st->iter += 1;
+      st->err = st->snrm;
+      st->status = VDR_OK;
+      st->done = 1;
+    }
+    return;
+  }
+  const double om = stc->omega;
+  double v[2] = {0.0, 0.0};
+  GRID_LOOP(i) {
+    a.x[i] += al * a.ph[i] + om * a.sh[i];
+    const double ri = a.s[i] - om * a.t[i];
+    a.r[i] = ri;
+    v[0] += ri * ri;
+    v[1] += a.rh[i] * ri;
+  }
+  double o[2];
+  if (grid_sum<2>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    st->iter += 1;
+    st->rho_old = st->rho;
+    st->rho = o[1];
+    st->err = sqrt(o[0]) / sqrt(st->bnrm2);
+    if (!(st->err == st->err) || !finite(o[1])) {
+      st->status = VDR_BREAKDOWN;
+      st->done = 1;
+    } else if (st->err <= st->tol) {
+      st->status = VDR_OK;
+      st->done = 1;
+    } else if (o[1] == 0.0 || om == 0.0) {
+      st->status = VDR_BREAKDOWN;
+      st->done = 1;
+    } else if (st->iter >= st->itmax) {
+      st->status = VDR_NOT_CONVERGED;
+      st->done = 1;
+    }
+  }
+}
+
+// ------------------------------ BiCG -------------------------------------
+// p = z + bk p, pp = zz + bk pp with z = r/d, zz = rr/d (masked in place as
+// matvec_0 masks its input); clears the two apply outputs.
+__global__ void __launch_bounds__(RED_THREADS) bc_p(Vec a) {
+  const KState *st = a.st;
+  if (st->done) return;
+  const bool first = st->iter == 0;
+  const double bk = first ? 0.0 : st->bknum / st->bkden;
+  GRID_LOOP(i) {
+    const double di = a.d[i];
+    const double zi = a.r[i] / di, zzi = a.rr[i] / di;
+    const bool mi = a.m[i];
+    a.p[i] = mi ? 0.0 : (first ? zi : zi + bk * a.p[i]);
+    a.pp[i] = mi ? 0.0 : (first ? zzi : zzi + bk * a.pp[i]);
+    a.z[i] = 0.0;
+    a.zz[i] = 0.0;
+  }
+}
+
+// ak = bknum / (z, pp)
+__global__ void __launch_bounds__(RED_THREADS) bc_ak(Vec a) {
+  if (a.st->done) return;
+  double v[1] = {0.0};
+  GRID_LOOP(i) v[0] += a.z[i] * a.pp[i];
+  double o[1];
+  if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    st->ak = st->bknum / o[0];
+    if (!finite(st->ak)) {
+      st->status = VDR_BREAKDOWN;
+      st->done = 1;
+    }
+  }
+}
+
+// x += ak p; r -= ak z; rr -= ak zz; err = ||r||/||b||; bknum' = (r/d, rr).
+__global__ void __launch_bounds__(RED_THREADS) bc_upd(Vec a) {
+  if (a.st->done) return;
+  const double ak = a.st->ak;
+  double v[2] = {0.0, 0.0};
+  GRID_LOOP(i) {
+    a.x[i] += ak * a.p[i];
+    const double ri = a.r[i] - ak * a.z[i];
+    const double rri = a.rr[i] - ak * a.zz[i];
+    a.r[i] = ri;
+    a.rr[i] = rri;
+    v[0] += ri * ri;
+    v[1] += (ri / a.d[i]) * rri;
+  }
+  double o[2];
+  if (grid_sum<2>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    st->iter += 1;
+    st->err = sqrt(o[0]) / sqrt(st->bnrm2);
+    st->bkden = st->bknum;
+    st->bknum = o[1];
+    if (!(st->err == st->err)) {
+      st->status = VDR_BREAKDOWN;
+      st->done = 1;
+    } else if (st->err <= st->tol) {
+      st->status = VDR_OK;
+      st->done = 1;
+    } else if (st->iter >= st->itmax) {
+      st->status = VDR_NOT_CONVERGED;
+      st->done = 1;
+    }
+  }
+}
+
+__global__ void k_true_residual(Vec a, const double *ax, double *partials,
+                                unsigned int *ticket, double *out) {
+  double v[2] = {0.0, 0.0};
+  GRID_LOOP(i) {
+    const double bi = a.b[i];
+    const double ri = bi - ax[i];
+    v[0] += ri * ri;
+    v[1] += bi * bi;
+  }
+  double o[2];
+  if (grid_sum<2>(v, partials, ticket, o)) *out = sqrt(o[0]) / sqrt(o[1]);
+}
+
+int red_grid(int n) {
+  const long need = ((long)n + RED_THREADS - 1) / RED_THREADS;
+  return (int)std::max<long>(1, std::min<long>(need, (long)sm_count3() * 8));
+}
+
+Vec make_vec(Handle &h, const double *b, double *x) {
+  Vec a{};
+  a.n = h.N;
+  a.st = h.st;
+  a.partials = h.partials;
+  a.b = b;
+  a.d = h.diag;
+  a.m = h.mask;
+  a.x = x;
+  double *w = h.work;
+  const size_t N = h.N;
+  a.r = w + 0 * N;
+  a.rh = w + 1 * N;
+  a.p = w + 2 * N;
+  a.v = w + 3 * N;
+  a.ph = w + 4 * N;
+  a.s = w + 5 * N;
+  a.sh = w + 6 * N;
+  a.t = w + 7 * N;
+  // BiCG reuses the same slots: rr = rh, pp = ph, z = v, zz = t.
+  a.rr = a.rh;
+  a.pp = a.ph;
+  a.z = a.v;
+  a.zz = a.t;
+  return a;
+}
+
+cudaError_t launch_iteration(Handle &h, int method, const Vec &a) {
+  const int g = red_grid(h.N);
+  cudaStream_t s = h.stream;
+  cudaError_t e;
+  if (method == VDR_SOLVER_BICGSTAB) {
+    bs_p<<<g, RED_THREADS, 0, s>>>(a);
+    if ((e = launch_apply(h, false, a.ph, a.v, &h.st->done, nullptr, s))) return e;
+    bs_alpha<<<g, RED_THREADS, 0, s>>>(a);
+    bs_s<<<g, RED_THREADS, 0, s>>>(a);
+    if ((e = launch_apply(h, false, a.sh, a.t, &h.st->done, &h.st->sconv, s))) return e;
+    bs_omega<<<g, RED_THREADS, 0, s>>>(a);
+    bs_xr<<<g, RED_THREADS, 0, s>>>(a);
+  } else {
+    bc_p<<<g, RED_THREADS, 0, s>>>(a);
+    if ((e = launch_apply(h, false, a.p, a.z, &h.st->done, nullptr, s))) return e;
+    if ((e = launch_apply(h, true, a.pp, a.zz, &h.st->done, nullptr, s))) return e;
+    bc_ak<<<g, RED_THREADS, 0, s>>>(a);
+    bc_upd<<<g, RED_THREADS, 0, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t ensure_solver_workspace(Handle &h, int nvec) {
+  cudaError_t e;
+  if (h.nwork < nvec) {
+    if (h.work) cudaFree(h.work);
+    h.work = nullptr;
+    h.nwork = 0;
+    if ((e = cudaMalloc(&h.work, sizeof(double) * (size_t)h.N * nvec))) return e;
+    h.nwork = nvec;
+    for (int k = 0; k < 4; k++) {
+      if (h.graph_exec[k]) cudaGraphExecDestroy(h.graph_exec[k]);
+      h.graph_exec[k] = nullptr;
+      h.graph_key[k] = nullptr;
+    }
+  }
+  if (!h.st) {
+    if ((e = cudaMalloc(&h.st, sizeof(KState)))) return e;
+    if ((e = cudaMemset(h.st, 0, sizeof(KState)))) return e;
+    if ((e = cudaMallocHost(&h.h_st, 2 * sizeof(KState)))) return e;
+    const int g = red_grid(h.N);
+    h.red_blocks = g;
+    if ((e = cudaMalloc(&h.partials, sizeof(double) * MAXQ * (size_t)std::max(g, 4096))))
+      return e;
+    for (int k = 0; k < 2; k++)
+      if ((e = cudaEventCreateWithFlags(&h.ev[k], cudaEventDisableTiming))) return e;
+  }
+  return cudaSuccess;
+}
+
+// Solves A x = b on device arrays b (length N) and x (in/out).
+int solve_device(Handle &h, int method, const double *b, double *x,
+                 double tol, int itmax, int *iter, double *err) {
+  cudaError_t e = ensure_solver_workspace(h, 8);
+  if (e) return cuda_fail(e, "solver workspace");
+  cudaStream_t s = h.stream;
+  Vec a = make_vec(h, b, x);
+  const int g = red_grid(h.N);
+
+  // KState scalars the kernels read: tol, itmax (ticket stays 0 between uses).
+  KState init{};
+  init.tol = tol;
+  init.itmax = itmax;
+  std::memcpy(&h.h_st[0], &init, sizeof(KState));
+  if ((e = cudaMemcpyAsync(h.st, &h.h_st[0], sizeof(KState),
+                           cudaMemcpyHostToDevice, s)))
+    return cuda_fail(e, "state upload");
+
+  // x on Dirichlet nodes is zeroed in place, as matvec_0 does to its input.
+  if ((e = launch_mask_vec(x, h.mask, h.N, s))) return cuda_fail(e, "mask x");
+  if ((e = cudaMemsetAsync(a.r, 0, sizeof(double) * h.N, s)))
+    return cuda_fail(e, "memset");
+  if ((e = launch_apply(h, false, x, a.r, nullptr, nullptr, s)))
+    return cuda_fail(e, "initial apply");
+  if (method == VDR_SOLVER_BICGSTAB)
+    k_start<false><<<g, RED_THREADS, 0, s>>>(a);
+  else
+    k_start<true><<<g, RED_THREADS, 0, s>>>(a);
+  if ((e = cudaGetLastError())) return cuda_fail(e, "start kernel");
+
+  // One graph per (method); its kernels only see handle-owned buffers plus
+  // b and x, which are part of the key.
+  const int K = h.opt.iters_per_graph > 0 ? h.opt.iters_per_graph : 8;
+  const int slot = method & 1;
+  const void *key = (const void *)((uintptr_t)b ^ ((uintptr_t)x << 1) ^
+                                   ((uintptr_t)h.work << 2) ^ (uintptr_t)K ^
+                                   ((uintptr_t)h.apply_mode << 8) ^
+                                   ((uintptr_t)h.scatter << 12));
+  if (!h.graph_exec[slot] || h.graph_key[slot] != key) {
+    if (h.graph_exec[slot]) cudaGraphExecDestroy(h.graph_exec[slot]);
+    h.graph_exec[slot] = nullptr;
+    cudaGraph_t graph;
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)))
+      return cuda_fail(e, "begin capture");
+    for (int k = 0; k < K; k++) {
+      e = launch_iteration(h, method, a);
+      if (e) break;
+    }
+    cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (e) return cuda_fail(e, "capture");
+    if (e2) return cuda_fail(e2, "end capture");
+    e = cudaGraphInstantiate(&h.graph_exec[slot], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e) return cuda_fail(e, "graph instantiate");
+    h.graph_key[slot] = key;
+  }
+
+  const int max_launches = (itmax + K - 1) / K + 1;
+  int launched = 0;
+  bool finished = false;
+  for (int c = 0; c < max_launches && !finished; c++) {
+    if ((e = cudaGraphLaunch(h.graph_exec[slot], s))) return cuda_fail(e, "graph launch");
+    if ((e = cudaMemcpyAsync(&h.h_st[c & 1], h.st, sizeof(KState),
+                             cudaMemcpyDeviceToHost, s)))
+      return cuda_fail(e, "state readback");
+    if ((e = cudaEventRecord(h.ev[c & 1], s))) return cuda_fail(e, "event");
+    launched++;
+    if (c > 0) {
+      if ((e = cudaEventSynchronize(h.ev[(c - 1) & 1]))) return cuda_fail(e, "sync");
+      if (h.h_st[(c - 1) & 1].done) finished = true;
+    }
+  }
+  if ((e = cudaStreamSynchronize(s))) return cuda_fail(e, "solve");
+  KState fin;
+  if ((e = cudaMemcpy(&fin, h.st, sizeof(KState), cudaMemcpyDeviceToHost)))
+    return cuda_fail(e, "final state");
+  (void)launched;
+  if (fin.done == 2) {  // b == 0
+    if ((e = cudaMemsetAsync(x, 0, sizeof(double) * h.N, s))) return cuda_fail(e, "zero x");
+    cudaStreamSynchronize(s);
+  }
+  if (iter) *iter = fin.iter;
+  if (err) *err = fin.err;
+  if (!fin.done) return VDR_NOT_CONVERGED;
+  return fin.status;
+}
+
+// Relative true residual ||b - A x|| / ||b|| (FP64, device).
+int true_residual_device(Handle &h, const double *b, const double *x,
+                         double *rel) {
+  cudaError_t e = ensure_solver_workspace(h, 8);
+  if (e) return cuda_fail(e, "solver workspace");
+  cudaStream_t s = h.stream;
+  Vec a = make_vec(h, b, const_cast<double *>(x));
+  double *ax = a.t;
+  double *out = a.sh;  // scalar scratch
+  if ((e = cudaMemsetAsync(ax, 0, sizeof(double) * h.N, s))) return cuda_fail(e, "memset");
+  if ((e = launch_apply(h, false, x, ax, nullptr, nullptr, s))) return cuda_fail(e, "apply");
+  const int g = red_grid(h.N);
+  k_true_residual<<<g, RED_THREADS, 0, s>>>(a, ax, h.partials, &h.st->ticket, out);
+  if ((e = cudaGetLastError())) return cuda_fail(e, "residual");
+  if ((e = cudaMemcpyAsync(rel, out, sizeof(double), cudaMemcpyDeviceToHost, s)))
+    return cuda_fail(e, "readback");
+  if ((e = cudaStreamSynchronize(s))) return cuda_fail(e, "sync");
+  return VDR_OK;
+}
+
+}  // namespace vdr

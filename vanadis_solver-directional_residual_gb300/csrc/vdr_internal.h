@@ -1,0 +1,150 @@
+// vdr_internal.h -- host-side internals shared by the translation units of
+// libvdr.so.  Not installed; the public surface is include/vdr.h.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "vdr.h"
+
+namespace vdr {
+
+// A Dirichlet node is stored in the connectivity with this bit set, so the
+// operator applies mask their inputs and outputs without extra loads.
+constexpr int MASK_BIT = (int)0x80000000u;
+constexpr int NODE_BITS = 0x7fffffff;
+
+// Reduction scratch: per-block partial sums of up to MAXQ quantities.
+constexpr int MAXQ = 4;
+constexpr int RED_THREADS = 256;
+
+// Device-resident Krylov state.  Scalars live here so that a captured
+// iteration never needs the host; `done` gates every kernel of the graph.
+struct KState {
+  double bnrm2, err, snrm;
+  double rho, rho_old, alpha, omega;       // BiCGStab
+  double bknum, bkden, ak;                 // BiCG
+  double tol;
+  int iter, itmax, done, sconv, status, pad;
+  unsigned int ticket;
+  unsigned int pad2;
+};
+
+struct DeviceOp;  // forward
+
+// Element-wise fields, device pointers in storage order.
+struct Fields {
+  const double *vel = nullptr;   // [3][E]
+  const double *lam = nullptr;   // [E]
+  const double *pdec = nullptr;  // [E] (nullable -> 0)
+  const double *q = nullptr;     // [E] (nullable -> 0)
+  const unsigned char *robin = nullptr;  // [E] (nullable -> none)
+  double robin_alpha = 0.0;
+};
+
+// Everything an operator kernel needs, by value.
+struct OpArgs {
+  int E = 0, N = 0, variant = VDR_DR_VF;
+  const int *conn = nullptr;  // [8][E]
+  const double *xx = nullptr, *yy = nullptr, *zz = nullptr;
+  const float *xx32 = nullptr, *yy32 = nullptr, *zz32 = nullptr;
+  Fields f;
+  const float *vel32 = nullptr, *lam32 = nullptr, *pdec32 = nullptr;
+  double aH = 1.0, aM = 0.0;
+};
+
+struct Handle {
+  int N = 0, E = 0;
+  int nax = 0, nay = 0, naz = 0;  // > 0 when the mesh is the canonical structured numbering
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  vdr_options opt{};
+  int scatter = VDR_SCATTER_ATOMIC;
+  int apply_mode = VDR_APPLY_STORED;
+
+  // geometry / topology (device, storage order)
+  double *xx = nullptr, *yy = nullptr, *zz = nullptr;
+  float *xx32 = nullptr, *yy32 = nullptr, *zz32 = nullptr;
+  int *conn = nullptr;               // [8][E] 0-based | MASK_BIT
+  std::vector<int> perm;             // storage position -> element id
+  std::vector<int> color_off;        // colour c occupies [off[c], off[c+1])
+  int ncolors = 0;
+  unsigned char *mask = nullptr;     // [N] 1 = Dirichlet
+  bool mask_set = false;
+
+  // fields (device, storage order)
+  double *vel = nullptr, *lam = nullptr, *pdec = nullptr, *q = nullptr;
+  float *vel32 = nullptr, *lam32 = nullptr, *pdec32 = nullptr;
+  unsigned char *robin = nullptr;
+  double robin_alpha = 0.0;
+  bool fields_set = false;
+
+  // operator state
+  double aH = 1.0, aM = 0.0;
+  bool op64_valid = false, op32_valid = false, diag_valid = false;
+  double2 *A64 = nullptr;  // [32][E] stored element matrices (row-major pairs)
+  float4 *A32 = nullptr;   // [16][E]
+  double *diag = nullptr;  // [N] assembled diagonal, 1 on Dirichlet nodes
+
+  // solver workspace
+  double *work = nullptr;
+  int nwork = 0;
+  KState *st = nullptr;
+  KState *h_st = nullptr;  // pinned mirror
+  double *partials = nullptr;
+  int red_blocks = 0;
+  cudaGraphExec_t graph_exec[4] = {nullptr, nullptr, nullptr, nullptr};
+  const void *graph_key[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+
+  // host staging
+  double *h_stage = nullptr;
+  size_t h_stage_bytes = 0;
+};
+
+OpArgs op_args(const Handle &h);
+
+// ---- launchers (element.cu) ----
+cudaError_t launch_build_stored(const OpArgs &a, double c1, double c2,
+                                double2 *A64, float4 *A32, double *diag,
+                                cudaStream_t s);
+cudaError_t launch_rhs(const OpArgs &a, double cf, double rM,
+                       const double *t_old, double *b, cudaStream_t s);
+cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
+                            const double *x, double *y, const int *skip,
+                            const int *skip2, cudaStream_t s);
+cudaError_t launch_mass(const Handle &h, const double *c, double *partials,
+                        double *out, cudaStream_t s);
+
+// ---- launchers (apply.cu) ----
+cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
+                                const double *x, double *y, const int *skip,
+                                const int *skip2, cudaStream_t s);
+cudaError_t launch_apply(const Handle &h, bool transpose, const double *x,
+                         double *y, const int *skip, const int *skip2,
+                         cudaStream_t s);
+cudaError_t launch_mask_conn(int *conn, int E, const unsigned char *mask,
+                             cudaStream_t s);
+cudaError_t launch_legacy_bb(const double *bb_ref, int E, double2 *A64,
+                             cudaStream_t s);
+cudaError_t launch_legacy_conn(const int *iss_ref, int E, int N, const int *bc,
+                               int *conn, int *bad, cudaStream_t s);
+cudaError_t launch_diag_fix(double *diag, const unsigned char *mask, int N,
+                            cudaStream_t s);
+cudaError_t launch_mask_vec(double *v, const unsigned char *mask, int N,
+                            cudaStream_t s);
+cudaError_t launch_bc_to_mask(const int *bc, unsigned char *mask, int N,
+                              cudaStream_t s);
+
+// ---- solvers (krylov.cu) ----
+int solve_device(Handle &h, int method, const double *b, double *x,
+                 double tol, int itmax, int *iter, double *err);
+cudaError_t ensure_solver_workspace(Handle &h, int nvec);
+
+// ---- errors ----
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+}  // namespace vdr

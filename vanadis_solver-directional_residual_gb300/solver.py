@@ -1,0 +1,230 @@
+"""Host-side mirror of the reference's solve interface over libvdr.so.
+
+* ``kernel_dbcg_simple(...)`` -- the reference's entry point
+  (src_v2026_2_1/cudatest.cu:301-305, called from VANADIS.FOR:809-810) with
+  its argument meaning: stored element matrices BB, ISS(E,8), DIAG, node
+  counts and the Dirichlet mask in; X, ITER, ERR out.
+* ``Solver`` -- the handle API: mesh and per-element fields stay resident
+  on the GPU, the DR element terms are recomputed there, and the solve,
+  apply, right-hand-side assembly and mass integral run on device.
+
+Host arrays are numpy; device arrays may be any object exposing
+``data_ptr()`` (torch CUDA tensors), which the ``*_device`` methods use
+without copies.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(_I)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(int(t.data_ptr()))
+
+
+_VARIANTS = {"ot": L.DR_OT, "gp": L.DR_GP, "vf": L.DR_VF}
+_SCATTER = {"auto": L.SCATTER_AUTO, "atomic": L.SCATTER_ATOMIC,
+            "color": L.SCATTER_COLOR, "colour": L.SCATTER_COLOR}
+_APPLY = {"auto": L.APPLY_AUTO, "stored": L.APPLY_STORED,
+          "matrix_free": L.APPLY_MATRIX_FREE}
+_SOLVER = {"bicgstab": L.SOLVER_BICGSTAB, "bicg": L.SOLVER_BICG}
+
+
+@dataclass
+class Options:
+    dr_variant: object = None  # None -> the problem's; or "ot"/"gp"/"vf"/int
+    scatter: str = "auto"
+    apply_mode: str = "auto"
+    solver: str = "bicgstab"
+    iters_per_graph: int = 8
+    device: int = 0
+
+    def to_c(self, default_variant: int) -> L.VdrOptions:
+        o = L.VdrOptions()
+        L.load_library().vdr_default_options(ctypes.byref(o))
+        v = self.dr_variant
+        if v is None:
+            v = default_variant
+        o.dr_variant = _VARIANTS[v] if isinstance(v, str) else int(v)
+        o.scatter = _SCATTER[self.scatter]
+        o.apply_mode = _APPLY[self.apply_mode]
+        o.solver = _SOLVER[self.solver]
+        o.iters_per_graph = int(self.iters_per_graph)
+        o.device = int(self.device)
+        return o
+
+
+class Solver:
+    """GPU-resident EBE DR operator and Krylov solver for one mesh."""
+
+    def __init__(self, problem, options: Options | None = None,
+                 aH: float = 1.0, aM: float = 0.0):
+        self.lib = L.load_library()
+        self.problem = problem
+        self.options = options or Options()
+        m = problem.mesh
+        self.N, self.E = m.nnode, m.nelem
+        self._keep = [_f64(m.xx), _f64(m.yy), _f64(m.zz), _i32(m.iss),
+                      _i32(m.kod)]
+        xx, yy, zz, iss, kod = self._keep
+        h = ctypes.c_void_p()
+        opt = self.options.to_c(problem.variant)
+        L.check(self.lib.vdr_create(ctypes.byref(h), self.N, self.E, _dp(xx),
+                                    _dp(yy), _dp(zz), _ip(iss), _ip(kod),
+                                    ctypes.byref(opt)), "vdr_create")
+        self.h = h
+        self.set_fields(problem.vel, problem.lam, problem.pdec, problem.q,
+                        problem.robin_alpha)
+        self.set_dirichlet(problem.bc)
+        self.set_operator(aH, aM)
+
+    # -- configuration -------------------------------------------------
+    def set_fields(self, vel, lam, pdec=None, q=None, robin_alpha=0.0):
+        L.check(self.lib.vdr_set_fields(self.h, _dp(_f64(vel)), _dp(_f64(lam)),
+                                        _dp(_f64(pdec)), _dp(_f64(q)),
+                                        float(robin_alpha)), "vdr_set_fields")
+
+    def set_dirichlet(self, bc):
+        L.check(self.lib.vdr_set_dirichlet(self.h, _ip(_i32(bc))),
+                "vdr_set_dirichlet")
+
+    def set_operator(self, aH: float, aM: float):
+        L.check(self.lib.vdr_set_operator(self.h, float(aH), float(aM)),
+                "vdr_set_operator")
+
+    # -- host-array calls ---------------------------------------------
+    def apply(self, x, transpose=False):
+        x = _f64(x)
+        y = np.empty(self.N)
+        L.check(self.lib.vdr_apply(self.h, _dp(x), _dp(y), int(transpose)),
+                "vdr_apply")
+        return y
+
+    def assemble_rhs(self, cf=1.0, rM=0.0, t_old=None):
+        b = np.empty(self.N)
+        L.check(self.lib.vdr_assemble_rhs(self.h, float(cf), float(rM),
+                                          _dp(_f64(t_old)), _dp(b)),
+                "vdr_assemble_rhs")
+        return b
+
+    def diag(self):
+        d = np.empty(self.N)
+        L.check(self.lib.vdr_get_diag(self.h, _dp(d)), "vdr_get_diag")
+        return d
+
+    def solve(self, b, x0=None, tol=None, itmax=1000):
+        """Returns (x, iterations, relative residual, status)."""
+        b = _f64(b)
+        x = np.zeros(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        it, err = ctypes.c_int(0), ctypes.c_double(0.0)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve(self.h, _dp(b), _dp(x), float(tol), int(itmax),
+                                ctypes.byref(it), ctypes.byref(err))
+        L.check(st, "vdr_solve", allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return x, it.value, err.value, st
+
+    def mass(self, c):
+        m = ctypes.c_double()
+        L.check(self.lib.vdr_mass(self.h, _dp(_f64(c)), ctypes.byref(m)),
+                "vdr_mass")
+        return m.value
+
+    # -- device-array calls (torch CUDA tensors or anything with data_ptr)
+    def apply_device(self, x, y, transpose=False):
+        L.check(self.lib.vdr_apply_device(self.h, _ptr(x), _ptr(y),
+                                          int(transpose)), "vdr_apply_device")
+
+    def assemble_rhs_device(self, b, cf=1.0, rM=0.0, t_old=None):
+        L.check(self.lib.vdr_assemble_rhs_device(self.h, float(cf), float(rM),
+                                                 _ptr(t_old), _ptr(b)),
+                "vdr_assemble_rhs_device")
+
+    def solve_device(self, b, x, tol=None, itmax=1000):
+        it, err = ctypes.c_int(0), ctypes.c_double(0.0)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve_device(self.h, _ptr(b), _ptr(x), float(tol),
+                                       int(itmax), ctypes.byref(it),
+                                       ctypes.byref(err))
+        L.check(st, "vdr_solve_device",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return it.value, err.value, st
+
+    def true_residual_device(self, b, x):
+        r = ctypes.c_double()
+        L.check(self.lib.vdr_true_residual_device(self.h, _ptr(b), _ptr(x),
+                                                  ctypes.byref(r)),
+                "vdr_true_residual_device")
+        return r.value
+
+    def mass_device(self, c):
+        m = ctypes.c_double()
+        L.check(self.lib.vdr_mass_device(self.h, _ptr(c), ctypes.byref(m)),
+                "vdr_mass_device")
+        return m.value
+
+    def stream(self) -> int:
+        return int(self.lib.vdr_stream(self.h) or 0)
+
+    # -- lifetime ------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vdr_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def kernel_dbcg_simple(N, B, X, TOL, ITMAX, BB, ISS, DIAG, NAX, NAY, NAZ,
+                       bc_dirichlet):
+    """The reference's solve call.  Returns (X, ITER, ERR); X is a new array
+    holding the solution (the C symbol itself writes X in place)."""
+    lib = L.load_library()
+    n = ctypes.c_int(int(N))
+    b = _f64(B)
+    x = np.array(X, dtype=np.float64, copy=True)
+    tol = ctypes.c_double(float(TOL))
+    itmax = ctypes.c_int(int(ITMAX))
+    it = ctypes.c_int(0)
+    err = ctypes.c_double(0.0)
+    bb, iss, dg = _f64(BB), _i32(ISS), _f64(DIAG)
+    nax, nay, naz = (ctypes.c_int(int(v)) for v in (NAX, NAY, NAZ))
+    bc = _i32(bc_dirichlet)
+    lib.kernel_dbcg_simple_(ctypes.byref(n), _dp(b), _dp(x), ctypes.byref(tol),
+                            ctypes.byref(itmax), ctypes.byref(it),
+                            ctypes.byref(err), _dp(bb), _ip(iss), _dp(dg),
+                            ctypes.byref(nax), ctypes.byref(nay),
+                            ctypes.byref(naz), _ip(bc))
+    return x, it.value, err.value
