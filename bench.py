@@ -1,0 +1,395 @@
+#!/usr/bin/env python3
+"""Benchmark: one implicit step of the Vanadis DR transport model on the
+large synthetic mesh, solved on one GB300 by libvdr.so.
+
+Workload (one "step"): rotation + shear flow on a 256x256x128-element
+jittered HEX8 mesh (8,388,608 elements, 8,520,321 nodes), lognormal
+per-element diffusivity, two Gaussian sources, zero Dirichlet on inflow
+faces, VF DR variant; the reference's theta-scheme system
+A = 2H + (3/dt)M, b = 3f - (H - (3/dt)M) T_old with T_old = 0, at Courant
+number |u|max dt/h = 10 (the reference's recorded run has |v| dt/h = 10
+along its flow); FP64 Jacobi-BiCGStab from x = 0 to ||r||/||b|| <= 1e-8.
+A step does what one pass of the reference's przest3d does on the GPU:
+element matrices + Jacobi diagonal (DR recompute), right-hand side, solve.
+
+  value     seconds per step with mesh and fields resident in HBM (CUDA
+            events on the library's stream)
+  e2e       the same step through the C ABI with host arrays: fields
+            uploaded, right-hand side downloaded, solution downloaded
+  roofline  the dominant kernel, the stored-matrix EBE apply, timed alone
+  --impl reference   the reference's CPU algorithm (the C oracle port of
+            vanadis_full_DR_OpenMP_timing.for) on this host's cores
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("solve time to rel. residual 1e-8: learned+FP32 vs plain FP64; "
+          "matvec HBM GB/s")
+COURANT = 10.0
+TOL = 1e-8
+
+
+def args_parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--nex", type=int, default=256)
+    ap.add_argument("--ney", type=int, default=256)
+    ap.add_argument("--nez", type=int, default=128)
+    ap.add_argument("--scatter", default="atomic", choices=["atomic", "color"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-iters", type=int, default=4,
+                    help="BiCGStab iterations timed in the CPU sample")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_config(a, prob):
+    return {
+        "workload": "rotation_shear %dx%dx%d, theta-step at Courant %g, FP64 "
+                    "Jacobi-BiCGStab to 1e-8 (VF DR variant)"
+                    % (a.nex, a.ney, a.nez, COURANT),
+        "elements": prob.mesh.nelem, "nodes": prob.mesh.nnode,
+        "dirichlet_nodes": int(prob.bc.sum()),
+        "apply": "stored element matrices (built on GPU each step)",
+        "scatter": a.scatter, "solver": "bicgstab", "precision": "fp64",
+        "l2": "inputs larger than L2 (element matrices 4.3 GB per apply)",
+    }
+
+
+def make_problem(a):
+    import __graft_entry__
+    P = __graft_entry__.package().problems
+    prob = P.rotation_shear(a.nex, a.ney, a.nez, seed=1002)
+    h = 1.0 / max(a.nex, a.ney, a.nez)
+    dt = COURANT * h  # max |u| = 1
+    return prob, dt
+
+
+# --------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                maxs.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxs),
+                "samples": len(sms), "reasons": sorted(reasons)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (a line 'traffic_bytes_per_launch: <number>')."""
+    path = os.path.join(ROOT, "profiles", "stored_apply_f64_rotation_shear.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+# --------------------------------------------------------------- CPU legs
+def cpu_solve_sample(prob, dt, iters, full=False):
+    """The oracle port on the host cores: OpenMP assembly of the whole
+    system + `iters` BiCGStab iterations with the OpenMP colour-parallel
+    apply (or a full solve).  Returns timings."""
+    import numpy as np
+    import oracle as O
+    threads = os.cpu_count() or 1
+    m = prob.mesh
+    t0 = time.perf_counter()
+    bb, b, d = O.assemble(prob.variant, m.xx, m.yy, m.zz, m.iss, prob.vel,
+                          prob.lam, prob.pdec, prob.q, kod=m.kod,
+                          robin_alpha=prob.robin_alpha, aH=2.0, aM=3.0 / dt,
+                          cf=3.0, rM=3.0 / dt, nthreads=threads)
+    b[prob.bc == 1] = 0.0
+    d[prob.bc == 1] = 1.0
+    t_asm = time.perf_counter() - t0
+    c, nc = O.greedy_colors(m.iss, m.nnode)
+    ce, co = O.color_lists(c, nc)
+    t0 = time.perf_counter()
+    x, it, err, st = O.bicgstab(b, np.zeros(m.nnode), bb, m.iss, d, prob.bc,
+                                TOL, 100000 if full else iters,
+                                colors=(ce, co), nthreads=threads)
+    t_sol = time.perf_counter() - t0
+    return {"t_asm": t_asm, "t_solve": t_sol, "iters": it, "err": err,
+            "status": st, "threads": threads}
+
+
+def run_reference(a):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    prob, dt = make_problem(a)
+    # the oracle's own iteration count, from one full CPU solve
+    full = cpu_solve_sample(prob, dt, 0, full=True)
+    n_it = full["iters"]
+    vals = []
+    for k in range(a.warmup + a.steps):
+        s = cpu_solve_sample(prob, dt, a.cpu_iters)
+        proj = s["t_asm"] + n_it * s["t_solve"] / max(1, s["iters"])
+        if k >= a.warmup:
+            vals.append(proj)
+    v = statistics.mean(vals)
+    sample = ("per step: full-system OpenMP assembly + %d BiCGStab iterations "
+              "(OpenMP colour-parallel apply) on %d threads, projected to the "
+              "%d iterations of one full CPU solve (that solve: %.1f s)"
+              % (a.cpu_iters, full["threads"], n_it,
+                 full["t_asm"] + full["t_solve"]))
+    line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": v * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": workload_config(a, prob),
+            "cpu_baseline": {"value": v, "unit": "s",
+                             "cores": full["threads"], "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "reference_iterations": n_it}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------- GPU arm
+def run_native(a):
+    import numpy as np
+    import torch
+    import __graft_entry__
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    vdr = __graft_entry__.package()
+    vdr.load_library()
+    prob, dt = make_problem(a)
+    N, E = prob.mesh.nnode, prob.mesh.nelem
+    aH, aM, cf, rM = 2.0, 3.0 / dt, 3.0, 3.0 / dt
+    opts = vdr.Options(apply_mode="stored", scatter=a.scatter,
+                       solver="bicgstab", device=local)
+    s = vdr.Solver(prob, opts, aH=aH, aM=aM)
+    stream = torch.cuda.ExternalStream(s.stream())
+    b = torch.zeros(N, dtype=torch.float64, device="cuda")
+    x = torch.zeros_like(b)
+    torch.cuda.synchronize()
+
+    def step():
+        with torch.cuda.stream(stream):
+            x.zero_()
+        s.set_operator(aH, aM)          # element matrices rebuilt this step
+        s.assemble_rhs_device(b, cf, rM, None)
+        it, err, st = s.solve_device(b, x, tol=TOL, itmax=20000)
+        return it, err, st
+
+    for _ in range(a.warmup):
+        it, err, st = step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = vdr.kernel_launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    iters = []
+    for _ in range(a.steps):
+        it, err, st = step()
+        iters.append(it)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    launches = vdr.kernel_launch_count() - launches0
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    rel_true = s.true_residual_device(b, x)
+    stats = s.stats()
+
+    # ---- breakdown: element matrices vs Krylov (one extra step) ----
+    e_a, e_b, e_c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    with torch.cuda.stream(stream):
+        x.zero_()
+    s.set_operator(aH, aM)
+    e_a.record(stream)
+    s.assemble_rhs_device(b, cf, rM, None)
+    y = torch.zeros_like(b)
+    s.apply_accumulate_device(x, y)     # triggers the element-matrix build
+    e_b.record(stream)
+    s.solve_device(b, x, tol=TOL, itmax=20000)
+    e_c.record(stream)
+    torch.cuda.synchronize()
+    t_build = e_a.elapsed_time(e_b)
+    t_krylov = e_b.elapsed_time(e_c)
+
+    # ---- roofline of the dominant kernel: stored EBE apply ----
+    xr = torch.randn(N, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    reps = 20
+    for _ in range(3):
+        s.apply_accumulate_device(xr, y)
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    for _ in range(reps):
+        s.apply_accumulate_device(xr, y)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    t_apply_ms = r0.elapsed_time(r1) / reps
+    alg_bytes = 544.0 * E + 24.0 * N
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / (t_apply_ms * 1e-3) / 1e9
+    traffic = profile_traffic()
+
+    # ---- e2e through the C ABI with host buffers ----
+    vel, lam, pdec, q = prob.vel, prob.lam, prob.pdec, prob.q
+    h2d = 8 * (vel.size + lam.size + pdec.size + q.size) + 8 * N + 8 * N
+    d2h = 8 * N + 8 * N
+    e2e_times = []
+    xh = np.zeros(N)
+    for k in range(2 + a.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.set_fields(vel, lam, pdec, q, prob.robin_alpha)   # H2D fields
+        s.set_operator(aH, aM)
+        bh = s.assemble_rhs(cf, rM, None)                    # D2H b
+        xh[:] = 0.0
+        xh2, it2, err2, st2 = s.solve(bh, xh, tol=TOL, itmax=20000)  # H2D b,x; D2H x
+        e2e_times.append(time.perf_counter() - t0)
+    e2e = statistics.mean(e2e_times[2:])
+
+    # ---- CPU baseline (oracle port on the host cores, bounded sample) ----
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        smp = cpu_solve_sample(prob, dt, a.cpu_iters)
+        proj = smp["t_asm"] + iters[-1] * smp["t_solve"] / max(1, smp["iters"])
+        cpu = {"value": proj, "unit": "s", "cores": smp["threads"],
+               "kind": "port",
+               "sample": "full-system OpenMP assembly (%.2f s) + %d BiCGStab "
+                         "iterations (%.3f s each, OpenMP colour-parallel "
+                         "apply) projected to the GPU run's %d iterations"
+                         % (smp["t_asm"], smp["iters"],
+                            smp["t_solve"] / max(1, smp["iters"]), iters[-1])}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms,
+            "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(a, prob),
+            "iterations": iters[-1], "final_err": err,
+            "true_rel_residual": rel_true, "status": st,
+            "breakdown_ms": {"element_matrices_and_rhs": t_build,
+                             "krylov": t_krylov,
+                             "per_iteration": t_krylov / max(1, iters[-1])},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic,
+                         "kernel": "stored_apply_f64 (EBE apply, atomic scatter)",
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "launch_ms": t_apply_ms, "peak_kind": peak_kind},
+            "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "solve_stats": stats,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    a = args_parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_native(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -113,6 +113,10 @@ int vdr_set_operator(vdr_handle *h, double aH, double aM);
 int vdr_apply(vdr_handle *h, const double *x, double *y, int transpose);
 int vdr_apply_device(vdr_handle *h, const double *d_x, double *d_y,
                      int transpose);
+/* d_y += P A P d_x (or the transpose) without clearing d_y first; Dirichlet
+ * rows of d_y are left as they are. */
+int vdr_apply_accumulate_device(vdr_handle *h, const double *d_x, double *d_y,
+                                int transpose);
 
 /* Right-hand side b = cf*f - (H - rM*M) T_old, assembled on the GPU, with
  * b = 0 on Dirichlet nodes (przest3d :691-716, :766-772).  t_old may be
@@ -135,6 +139,22 @@ int vdr_solve(vdr_handle *h, const double *b, double *x, double tol,
               int itmax, int *iter, double *err);
 int vdr_solve_device(vdr_handle *h, const double *d_b, double *d_x,
                      double tol, int itmax, int *iter, double *err);
+
+/* Statistics of the handle's most recent solve. */
+typedef struct vdr_solve_stats {
+  int iterations;      /* Krylov iterations done */
+  int status;          /* VDR_* status of that solve */
+  int graph_launches;  /* CUDA-graph launches (iters_per_graph iterations each) */
+  int kernel_launches; /* kernels launched by the solve, graph nodes included */
+  int breakdown;       /* 0, or which quantity vanished: 1 (r0,r) 2 (r0,v)
+                          3 (t,t) 4 omega 5 non-finite residual */
+  int reserved[3];
+} vdr_solve_stats;
+int vdr_last_solve_stats(vdr_handle *h, vdr_solve_stats *stats);
+
+/* Number of CUDA kernels this library has launched in the process so far
+ * (graph nodes counted per graph launch). */
+long long vdr_kernel_launch_count(void);
 
 /* True relative residual ||b - A x||/||b|| computed on the GPU in FP64. */
 int vdr_true_residual_device(vdr_handle *h, const double *d_b,

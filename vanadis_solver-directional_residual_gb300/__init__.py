@@ -10,7 +10,8 @@ Python host binding.
 from . import problems
 from ._lib import (VdrError, build_library, last_error, library_path,
                    load_library)
-from .solver import Options, Solver, kernel_dbcg_simple
+from .solver import Options, Solver, kernel_dbcg_simple, kernel_launch_count
 
-__all__ = ["problems", "Options", "Solver", "kernel_dbcg_simple", "VdrError",
+__all__ = ["problems", "Options", "Solver", "kernel_dbcg_simple",
+           "kernel_launch_count", "VdrError",
            "build_library", "load_library", "library_path", "last_error"]

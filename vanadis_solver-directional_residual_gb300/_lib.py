@@ -28,6 +28,13 @@ class VdrOptions(ctypes.Structure):
                 ("reserved", ctypes.c_int * 10)]
 
 
+class VdrSolveStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("status", ctypes.c_int),
+                ("graph_launches", ctypes.c_int),
+                ("kernel_launches", ctypes.c_int), ("breakdown", ctypes.c_int),
+                ("reserved", ctypes.c_int * 3)]
+
+
 # Every symbol include/vdr.h declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _D = ctypes.POINTER(ctypes.c_double)
@@ -43,6 +50,7 @@ SIGNATURES = {
     "vdr_set_operator": (_i, [_P, _d, _d]),
     "vdr_apply": (_i, [_P, _D, _D, _i]),
     "vdr_apply_device": (_i, [_P, _P, _P, _i]),
+    "vdr_apply_accumulate_device": (_i, [_P, _P, _P, _i]),
     "vdr_assemble_rhs": (_i, [_P, _d, _d, _D, _D]),
     "vdr_assemble_rhs_device": (_i, [_P, _d, _d, _P, _P]),
     "vdr_get_diag": (_i, [_P, _D]),
@@ -52,6 +60,8 @@ SIGNATURES = {
     "vdr_mass": (_i, [_P, _D, _D]),
     "vdr_mass_device": (_i, [_P, _P, _D]),
     "vdr_color_elements": (_i, [_i, _i, _I, _I]),
+    "vdr_last_solve_stats": (_i, [_P, ctypes.POINTER(VdrSolveStats)]),
+    "vdr_kernel_launch_count": (ctypes.c_longlong, []),
     "vdr_stream": (_P, [_P]),
     "vdr_destroy": (_i, [_P]),
     "vdr_last_error": (ctypes.c_char_p, []),

@@ -7,6 +7,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <limits>
@@ -169,6 +170,12 @@ void free_handle(Handle &h) {
 }  // namespace
 
 void set_error(const std::string &msg) { g_err = msg; }
+
+namespace {
+std::atomic<long long> g_launches{0};
+}
+void count_launches(long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 int cuda_fail(cudaError_t e, const char *what) {
   set_error(std::string(what) + ": " + cudaGetErrorString(e));
@@ -432,6 +439,20 @@ int vdr_apply_device(vdr_handle *H, const double *x, double *y, int transpose) {
   return VDR_OK;
 }
 
+int vdr_apply_accumulate_device(vdr_handle *H, const double *x, double *y,
+                                int transpose) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!x || !y) {
+    set_error("vdr_apply_accumulate_device: null vector");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator(h))) return st;
+  cudaError_t e = launch_apply(h, transpose != 0, x, y, nullptr, nullptr, h.stream);
+  return e ? cuda_fail(e, "apply") : VDR_OK;
+}
+
 int vdr_apply(vdr_handle *H, const double *x, double *y, int transpose) {
   int st = check_handle(H);
   if (st) return st;
@@ -585,6 +606,17 @@ int vdr_color_elements(int nnode, int nelem, const int *iss, int *colors) {
   std::memcpy(colors, color.data(), sizeof(int) * (size_t)nelem);
   return nc;
 }
+
+int vdr_last_solve_stats(vdr_handle *H, vdr_solve_stats *stats) {
+  if (!H || !stats) {
+    set_error("vdr_last_solve_stats: null argument");
+    return VDR_BAD_ARGUMENT;
+  }
+  *stats = H->h.last;
+  return VDR_OK;
+}
+
+long long vdr_kernel_launch_count(void) { return launches_so_far(); }
 
 void *vdr_stream(vdr_handle *H) { return H ? (void *)H->h.stream : nullptr; }
 

@@ -211,6 +211,14 @@ int grid_for(long n, int threads, int per_sm) {
 
 }  // namespace
 
+int apply_launches(const Handle &h) {
+  if (h.apply_mode == VDR_APPLY_MATRIX_FREE || h.scatter != VDR_SCATTER_COLOR)
+    return 1;
+  int n = 0;
+  for (int r = 0; r < h.ncolors; r++) n += h.color_off[r + 1] > h.color_off[r];
+  return n;
+}
+
 cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
                                 const double *x, double *y, const int *skip,
                                 const int *skip2, cudaStream_t s) {
@@ -241,6 +249,7 @@ cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
       }
     }
 #undef VDR_LAUNCH
+    count_launches(1);
   }
   return cudaGetLastError();
 }
@@ -249,6 +258,7 @@ cudaError_t launch_legacy_bb(const double *bb_ref, int E, double2 *A64,
                              cudaStream_t s) {
   legacy_convert_kernel<<<grid_for((long)E * 32, 256, 16), 256, 0, s>>>(
       reinterpret_cast<const double2 *>(bb_ref), E, A64);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -256,6 +266,7 @@ cudaError_t launch_legacy_conn(const int *iss_ref, int E, int N, const int *bc,
                                int *conn, int *bad, cudaStream_t s) {
   legacy_conn_kernel<<<grid_for((long)E * 8, 256, 16), 256, 0, s>>>(
       iss_ref, E, N, bc, conn, bad);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -263,24 +274,28 @@ cudaError_t launch_mask_conn(int *conn, int E, const unsigned char *mask,
                              cudaStream_t s) {
   mask_conn_kernel<<<grid_for((long)E * 8, 256, 16), 256, 0, s>>>(
       conn, (long)E * 8, mask);
+  count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_diag_fix(double *diag, const unsigned char *mask, int N,
                             cudaStream_t s) {
   diag_fix_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(diag, mask, N);
+  count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mask_vec(double *v, const unsigned char *mask, int N,
                             cudaStream_t s) {
   mask_vec_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(v, mask, N);
+  count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_bc_to_mask(const int *bc, unsigned char *mask, int N,
                               cudaStream_t s) {
   bc_to_mask_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(bc, mask, N);
+  count_launches(1);
   return cudaGetLastError();
 }
 

@@ -416,6 +416,7 @@ cudaError_t launch_build_stored(const OpArgs &a, double c1, double c2,
     elem_rows_kernel<double, 0><<<grid, 64, 0, s>>>(a, c1, c2, A64, A32, diag,
                                                     0.0, nullptr, nullptr);
   }
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -426,6 +427,7 @@ cudaError_t launch_rhs(const OpArgs &a, double cf, double rM,
   const int grid = (int)std::min<long>(blocks_needed, (long)sm_count() * 32);
   elem_rows_kernel<double, 1><<<grid, 64, 0, s>>>(a, 1.0, -rM, nullptr, nullptr,
                                                   nullptr, cf, t_old, b);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -446,6 +448,7 @@ cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
     else
       mf_apply_kernel<double, false><<<grid, 256, 0, s>>>(a, a.aH, a.aM, x, y, skip, skip2);
   }
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -454,6 +457,7 @@ cudaError_t launch_mass(const Handle &h, const double *c, double *partials,
   const int grid = std::max(1, std::min((h.E + 255) / 256, sm_count() * 4));
   mass_kernel<<<grid, 256, 0, s>>>(h.conn, h.E, h.xx, h.yy, h.zz, c, partials);
   sum_partials_kernel<<<1, 256, 0, s>>>(partials, grid, out);
+  count_launches(2);
   return cudaGetLastError();
 }
 

@@ -155,8 +155,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_start(Vec a) {
       return;
     }
     st->err = sqrt(o[1]) / sqrt(o[0]);
+    st->reason = 0;
     if (!(st->err == st->err)) {
       st->status = VDR_BREAKDOWN;
+      st->reason = 5;
       st->done = 1;
     } else if (st->err <= st->tol) {
       st->status = VDR_OK;
@@ -193,6 +195,7 @@ __global__ void __launch_bounds__(RED_THREADS) bs_alpha(Vec a) {
     KState *st = a.st;
     if (o[0] == 0.0 || !finite(o[0])) {
       st->status = VDR_BREAKDOWN;
+      st->reason = 2;
       st->done = 1;
     } else {
       st->alpha = st->rho / o[0];
@@ -234,6 +237,7 @@ __global__ void __launch_bounds__(RED_THREADS) bs_omega(Vec a) {
     KState *st = a.st;
     if (o[1] == 0.0 || !finite(o[1]) || !finite(o[0])) {
       st->status = VDR_BREAKDOWN;
+      st->reason = 3;
       st->done = 1;
     } else {
       st->omega = o[0] / o[1];
@@ -280,12 +284,14 @@ __global__ void __launch_bounds__(RED_THREADS) bs_xr(Vec a) {
     st->err = sqrt(o[0]) / sqrt(st->bnrm2);
     if (!(st->err == st->err) || !finite(o[1])) {
       st->status = VDR_BREAKDOWN;
+      st->reason = 5;
       st->done = 1;
     } else if (st->err <= st->tol) {
       st->status = VDR_OK;
       st->done = 1;
     } else if (o[1] == 0.0 || om == 0.0) {
       st->status = VDR_BREAKDOWN;
+      st->reason = o[1] == 0.0 ? 1 : 4;
       st->done = 1;
     } else if (st->iter >= st->itmax) {
       st->status = VDR_NOT_CONVERGED;
@@ -324,6 +330,7 @@ __global__ void __launch_bounds__(RED_THREADS) bc_ak(Vec a) {
     st->ak = st->bknum / o[0];
     if (!finite(st->ak)) {
       st->status = VDR_BREAKDOWN;
+      st->reason = 2;
       st->done = 1;
     }
   }
@@ -352,6 +359,7 @@ __global__ void __launch_bounds__(RED_THREADS) bc_upd(Vec a) {
     st->bknum = o[1];
     if (!(st->err == st->err)) {
       st->status = VDR_BREAKDOWN;
+      st->reason = 5;
       st->done = 1;
     } else if (st->err <= st->tol) {
       st->status = VDR_OK;
@@ -468,6 +476,8 @@ int solve_device(Handle &h, int method, const double *b, double *x,
   cudaStream_t s = h.stream;
   Vec a = make_vec(h, b, x);
   const int g = red_grid(h.N);
+  const long long launches0 = launches_so_far();
+  h.last = vdr_solve_stats{};
 
   // KState scalars the kernels read: tol, itmax (ticket stays 0 between uses).
   KState init{};
@@ -488,9 +498,10 @@ int solve_device(Handle &h, int method, const double *b, double *x,
     k_start<false><<<g, RED_THREADS, 0, s>>>(a);
   else
     k_start<true><<<g, RED_THREADS, 0, s>>>(a);
+  count_launches(1);
   if ((e = cudaGetLastError())) return cuda_fail(e, "start kernel");
 
-  // One graph per (method); its kernels only see handle-owned buffers plus
+  // One graph per method; its kernels only see handle-owned buffers plus
   // b and x, which are part of the key.
   const int K = h.opt.iters_per_graph > 0 ? h.opt.iters_per_graph : 8;
   const int slot = method & 1;
@@ -504,10 +515,12 @@ int solve_device(Handle &h, int method, const double *b, double *x,
     cudaGraph_t graph;
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)))
       return cuda_fail(e, "begin capture");
+    const long long before = launches_so_far();
     for (int k = 0; k < K; k++) {
       e = launch_iteration(h, method, a);
       if (e) break;
     }
+    count_launches(before - launches_so_far());  // captured, not launched
     cudaError_t e2 = cudaStreamEndCapture(s, &graph);
     if (e) return cuda_fail(e, "capture");
     if (e2) return cuda_fail(e2, "end capture");
@@ -516,12 +529,14 @@ int solve_device(Handle &h, int method, const double *b, double *x,
     if (e) return cuda_fail(e, "graph instantiate");
     h.graph_key[slot] = key;
   }
+  const int per_iter = (method == VDR_SOLVER_BICGSTAB ? 5 : 3) + 2 * apply_launches(h);
 
   const int max_launches = (itmax + K - 1) / K + 1;
   int launched = 0;
   bool finished = false;
   for (int c = 0; c < max_launches && !finished; c++) {
     if ((e = cudaGraphLaunch(h.graph_exec[slot], s))) return cuda_fail(e, "graph launch");
+    count_launches((long)K * per_iter);
     if ((e = cudaMemcpyAsync(&h.h_st[c & 1], h.st, sizeof(KState),
                              cudaMemcpyDeviceToHost, s)))
       return cuda_fail(e, "state readback");
@@ -536,15 +551,19 @@ int solve_device(Handle &h, int method, const double *b, double *x,
   KState fin;
   if ((e = cudaMemcpy(&fin, h.st, sizeof(KState), cudaMemcpyDeviceToHost)))
     return cuda_fail(e, "final state");
-  (void)launched;
   if (fin.done == 2) {  // b == 0
     if ((e = cudaMemsetAsync(x, 0, sizeof(double) * h.N, s))) return cuda_fail(e, "zero x");
-    cudaStreamSynchronize(s);
+    if ((e = cudaStreamSynchronize(s))) return cuda_fail(e, "zero x");
   }
+  const int status = fin.done ? fin.status : VDR_NOT_CONVERGED;
+  h.last.iterations = fin.iter;
+  h.last.status = status;
+  h.last.graph_launches = launched;
+  h.last.kernel_launches = (int)(launches_so_far() - launches0);
+  h.last.breakdown = status == VDR_BREAKDOWN ? fin.reason : 0;
   if (iter) *iter = fin.iter;
   if (err) *err = fin.err;
-  if (!fin.done) return VDR_NOT_CONVERGED;
-  return fin.status;
+  return status;
 }
 
 // Relative true residual ||b - A x|| / ||b|| (FP64, device).
@@ -560,6 +579,7 @@ int true_residual_device(Handle &h, const double *b, const double *x,
   if ((e = launch_apply(h, false, x, ax, nullptr, nullptr, s))) return cuda_fail(e, "apply");
   const int g = red_grid(h.N);
   k_true_residual<<<g, RED_THREADS, 0, s>>>(a, ax, h.partials, &h.st->ticket, out);
+  count_launches(1);
   if ((e = cudaGetLastError())) return cuda_fail(e, "residual");
   if ((e = cudaMemcpyAsync(rel, out, sizeof(double), cudaMemcpyDeviceToHost, s)))
     return cuda_fail(e, "readback");

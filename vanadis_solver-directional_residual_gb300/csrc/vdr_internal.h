@@ -27,7 +27,7 @@ struct KState {
   double rho, rho_old, alpha, omega;       // BiCGStab
   double bknum, bkden, ak;                 // BiCG
   double tol;
-  int iter, itmax, done, sconv, status, pad;
+  int iter, itmax, done, sconv, status, reason;  // reason: see vdr_solve_stats
   unsigned int ticket;
   unsigned int pad2;
 };
@@ -102,7 +102,15 @@ struct Handle {
   // host staging
   double *h_stage = nullptr;
   size_t h_stage_bytes = 0;
+
+  vdr_solve_stats last{};
 };
+
+// Process-wide count of kernels launched by this library (graph nodes
+// included), for the benchmark's launch accounting.
+void count_launches(long n);
+long long launches_so_far();
+int apply_launches(const Handle &h);  // kernels per operator apply
 
 OpArgs op_args(const Handle &h);
 

@@ -157,6 +157,11 @@ class Solver:
         L.check(self.lib.vdr_apply_device(self.h, _ptr(x), _ptr(y),
                                           int(transpose)), "vdr_apply_device")
 
+    def apply_accumulate_device(self, x, y, transpose=False):
+        L.check(self.lib.vdr_apply_accumulate_device(self.h, _ptr(x), _ptr(y),
+                                                     int(transpose)),
+                "vdr_apply_accumulate_device")
+
     def assemble_rhs_device(self, b, cf=1.0, rM=0.0, t_old=None):
         L.check(self.lib.vdr_assemble_rhs_device(self.h, float(cf), float(rM),
                                                  _ptr(t_old), _ptr(b)),
@@ -185,6 +190,15 @@ class Solver:
                 "vdr_mass_device")
         return m.value
 
+    def stats(self) -> dict:
+        """Statistics of the most recent solve (vdr_last_solve_stats)."""
+        st = L.VdrSolveStats()
+        L.check(self.lib.vdr_last_solve_stats(self.h, ctypes.byref(st)),
+                "vdr_last_solve_stats")
+        return {k: getattr(st, k) for k in ("iterations", "status",
+                                            "graph_launches",
+                                            "kernel_launches", "breakdown")}
+
     def stream(self) -> int:
         return int(self.lib.vdr_stream(self.h) or 0)
 
@@ -205,6 +219,11 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+def kernel_launch_count() -> int:
+    """Kernels libvdr.so has launched in this process (vdr_kernel_launch_count)."""
+    return int(L.load_library().vdr_kernel_launch_count())
 
 
 def kernel_dbcg_simple(N, B, X, TOL, ITMAX, BB, ISS, DIAG, NAX, NAY, NAZ,
