@@ -118,27 +118,51 @@ int check_handle(vdr_handle *H) {
   return VDR_OK;
 }
 
-int ensure_operator(Handle &h) {
+// Builds the stored element matrices and the Jacobi diagonal if they are
+// stale; when `rhs` is given, the right-hand side is assembled in the same
+// element pass (or alone, if the operator is already valid).
+int build_operator(Handle &h, const BuildArgs *rhs) {
   if (!h.fields_set) {
     set_error("fields not set (vdr_set_fields)");
     return VDR_BAD_ARGUMENT;
   }
   cudaError_t e;
-  if (h.op64_valid && h.diag_valid) return VDR_OK;
-  if ((e = dalloc(&h.diag, h.N))) return cuda_fail(e, "alloc diag");
-  const bool stored = h.apply_mode == VDR_APPLY_STORED;
-  if (stored && (e = dalloc(&h.A64, (size_t)h.E * 32))) return cuda_fail(e, "alloc element matrices");
-  if ((e = cudaMemsetAsync(h.diag, 0, sizeof(double) * h.N, h.stream)))
-    return cuda_fail(e, "memset diag");
-  OpArgs a = op_args(h);
-  if ((e = launch_build_stored(a, h.aH, h.aM, stored ? h.A64 : nullptr, nullptr,
-                               h.diag, h.stream)))
+  const bool need_op = !(h.op64_valid && h.diag_valid);
+  if (!need_op && !rhs) return VDR_OK;
+  BuildArgs ba;
+  if (rhs) {
+    ba.cf = rhs->cf;
+    ba.rM = rhs->rM;
+    ba.told = rhs->told;
+    ba.b = rhs->b;
+    if ((e = cudaMemsetAsync(ba.b, 0, sizeof(double) * h.N, h.stream)))
+      return cuda_fail(e, "memset rhs");
+  }
+  if (need_op) {
+    if ((e = dalloc(&h.diag, h.N)) || (e = dalloc(&h.dinv, h.N)))
+      return cuda_fail(e, "alloc diag");
+    const bool stored = h.apply_mode == VDR_APPLY_STORED;
+    if (stored && (e = dalloc(&h.A64, (size_t)h.E * 32)))
+      return cuda_fail(e, "alloc element matrices");
+    if ((e = cudaMemsetAsync(h.diag, 0, sizeof(double) * h.N, h.stream)))
+      return cuda_fail(e, "memset diag");
+    ba.aH = h.aH;
+    ba.aM = h.aM;
+    ba.A64 = stored ? h.A64 : nullptr;
+    ba.diag = h.diag;
+  }
+  if ((e = launch_build(op_args(h), ba, false, h.stream)))
     return cuda_fail(e, "element matrices");
-  if ((e = launch_diag_fix(h.diag, h.mask, h.N, h.stream))) return cuda_fail(e, "diag");
-  h.op64_valid = true;
-  h.diag_valid = true;
+  if (need_op) {
+    if ((e = launch_diag_fix(h.diag, h.dinv, h.mask, h.N, h.stream)))
+      return cuda_fail(e, "diag");
+    h.op64_valid = true;
+    h.diag_valid = true;
+  }
   return VDR_OK;
 }
+
+int ensure_operator(Handle &h) { return build_operator(h, nullptr); }
 
 void invalidate(Handle &h) {
   h.op64_valid = h.op32_valid = h.diag_valid = false;
@@ -156,7 +180,7 @@ void free_handle(Handle &h) {
   dfree(h.conn); dfree(h.mask);
   dfree(h.vel); dfree(h.lam); dfree(h.pdec); dfree(h.q);
   dfree(h.vel32); dfree(h.lam32); dfree(h.pdec32); dfree(h.robin);
-  dfree(h.A64); dfree(h.A32); dfree(h.diag);
+  dfree(h.A64); dfree(h.A32); dfree(h.diag); dfree(h.dinv);
   dfree(h.work); dfree(h.st); dfree(h.partials);
   if (h.h_st) cudaFreeHost(h.h_st);
   for (int k = 0; k < 4; k++)
@@ -472,16 +496,16 @@ int vdr_assemble_rhs_device(vdr_handle *H, double cf, double rM,
   int st = check_handle(H);
   if (st) return st;
   Handle &h = H->h;
-  if (!h.fields_set) {
-    set_error("fields not set");
+  if (!b) {
+    set_error("vdr_assemble_rhs_device: null b");
     return VDR_BAD_ARGUMENT;
   }
-  cudaError_t e;
-  if ((e = cudaMemsetAsync(b, 0, sizeof(double) * h.N, h.stream)))
-    return cuda_fail(e, "memset");
-  if ((e = launch_rhs(op_args(h), cf, rM, t_old, b, h.stream)))
-    return cuda_fail(e, "rhs");
-  return VDR_OK;
+  BuildArgs rhs;
+  rhs.cf = cf;
+  rhs.rM = rM;
+  rhs.told = t_old;
+  rhs.b = b;
+  return build_operator(h, &rhs);
 }
 
 int vdr_assemble_rhs(vdr_handle *H, double cf, double rM, const double *t_old,
@@ -667,6 +691,7 @@ int legacy_prepare(Legacy &L, int N, int E) {
     dfree(h.A64); h.A64 = nullptr;
     dfree(h.conn); h.conn = nullptr;
     dfree(h.diag); h.diag = nullptr;
+    dfree(h.dinv); h.dinv = nullptr;
     dfree(h.mask); h.mask = nullptr;
     dfree(L.bb); L.bb = nullptr;
     dfree(L.b); L.b = nullptr;
@@ -689,7 +714,8 @@ int legacy_prepare(Legacy &L, int N, int E) {
     }
     const size_t cN = std::max(N, L.capN), cE = std::max(E, L.capE);
     if ((e = dalloc(&h.A64, cE * 32)) || (e = dalloc(&h.conn, cE * 8)) ||
-        (e = dalloc(&h.diag, cN)) || (e = dalloc(&h.mask, cN)) ||
+        (e = dalloc(&h.diag, cN)) || (e = dalloc(&h.dinv, cN)) ||
+        (e = dalloc(&h.mask, cN)) ||
         (e = dalloc(&L.bb, cE * 64)) || (e = dalloc(&L.b, cN)) ||
         (e = dalloc(&L.x, cN)) || (e = dalloc(&L.iss, cE * 8)) ||
         (e = dalloc(&L.bc, cN)) || (e = dalloc(&L.bad, 1))) {
@@ -754,6 +780,7 @@ void kernel_dbcg_simple_(int *Np, double *B, double *X, double *TOLp,
         (e = launch_legacy_conn(L.iss, (int)E, N, bc_dirichlet ? L.bc : nullptr,
                                 h.conn, L.bad, s)) ||
         (e = launch_legacy_bb(L.bb, (int)E, h.A64, s)) ||
+        (e = launch_diag_fix(h.diag, h.dinv, nullptr, N, s)) ||
         (e = cudaMemcpyAsync(&bad, L.bad, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
       break;

@@ -183,11 +183,17 @@ __global__ void mask_conn_kernel(int *__restrict__ conn, long total,
   }
 }
 
-__global__ void diag_fix_kernel(double *__restrict__ d,
+__global__ void diag_fix_kernel(double *__restrict__ d, double *__restrict__ dinv,
                                 const unsigned char *__restrict__ m, int N) {
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
-       i += (long)gridDim.x * blockDim.x)
-    if (m[i]) d[i] = 1.0;
+       i += (long)gridDim.x * blockDim.x) {
+    double di = d[i];
+    if (m && m[i]) {
+      di = 1.0;
+      d[i] = di;
+    }
+    dinv[i] = 1.0 / di;
+  }
 }
 
 __global__ void mask_vec_kernel(double *__restrict__ v,
@@ -278,9 +284,9 @@ cudaError_t launch_mask_conn(int *conn, int E, const unsigned char *mask,
   return cudaGetLastError();
 }
 
-cudaError_t launch_diag_fix(double *diag, const unsigned char *mask, int N,
-                            cudaStream_t s) {
-  diag_fix_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(diag, mask, N);
+cudaError_t launch_diag_fix(double *diag, double *dinv,
+                            const unsigned char *mask, int N, cudaStream_t s) {
+  diag_fix_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(diag, dinv, mask, N);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -83,28 +83,22 @@ struct GPData {
   T n[8], w[8], gx[8], gy[8], gz[8];
 };
 
-// Evaluates one Gauss (or face) point of element e.  xe/ye/ze hold the 8
-// node coordinates in local order; (vx,vy,vz), lam are the element's
-// velocity and isotropic diffusivity.
+// Shape functions and their reference-cube derivatives at one point
+// (shape_hex8DR, vanadis_full_DR_OpenMP_timing.for:1398-1474).
 template <typename T>
-__device__ __forceinline__ void gp_eval(const int variant, const T xi,
-                                        const T eta, const T zeta,
-                                        const T (&xe)[8], const T (&ye)[8],
-                                        const T (&ze)[8], const T lam,
-                                        const T vx, const T vy, const T vz,
-                                        GPData<T> &o) {
+__device__ __forceinline__ void shape_at(const T xi, const T eta, const T zeta,
+                                         T *n, T *d0, T *d1, T *d2) {
   const T xm = T(1) - xi, xp = T(1) + xi;
   const T ym = T(1) - eta, yp = T(1) + eta;
   const T zm = T(1) - zeta, zp = T(1) + zeta;
-  T d0[8], d1[8], d2[8];
-  o.n[0] = T(0.125) * xm * ym * zm;
-  o.n[1] = T(0.125) * xp * ym * zm;
-  o.n[2] = T(0.125) * xp * yp * zm;
-  o.n[3] = T(0.125) * xm * yp * zm;
-  o.n[4] = T(0.125) * xm * ym * zp;
-  o.n[5] = T(0.125) * xp * ym * zp;
-  o.n[6] = T(0.125) * xp * yp * zp;
-  o.n[7] = T(0.125) * xm * yp * zp;
+  n[0] = T(0.125) * xm * ym * zm;
+  n[1] = T(0.125) * xp * ym * zm;
+  n[2] = T(0.125) * xp * yp * zm;
+  n[3] = T(0.125) * xm * yp * zm;
+  n[4] = T(0.125) * xm * ym * zp;
+  n[5] = T(0.125) * xp * ym * zp;
+  n[6] = T(0.125) * xp * yp * zp;
+  n[7] = T(0.125) * xm * yp * zp;
   d0[0] = -(T(0.125) * ym * zm);
   d0[1] = T(0.125) * ym * zm;
   d0[2] = T(0.125) * yp * zm;
@@ -129,11 +123,23 @@ __device__ __forceinline__ void gp_eval(const int variant, const T xi,
   d2[5] = T(0.125) * xp * ym;
   d2[6] = T(0.125) * xp * yp;
   d2[7] = T(0.125) * xm * yp;
+}
 
+// Geometry and DR weight of one point given its shape data: detJ, grad N
+// (x,y,z) and W.  xe/ye/ze hold the 8 node coordinates in local order;
+// (vx,vy,vz), lam are the element's velocity and isotropic diffusivity.
+template <typename T>
+__device__ __forceinline__ void gp_core(const int variant, const T *nsh,
+                                        const T *d0, const T *d1, const T *d2,
+                                        const T (&xe)[8], const T (&ye)[8],
+                                        const T (&ze)[8], const T lam,
+                                        const T vx, const T vy, const T vz,
+                                        GPData<T> &o) {
   T j11 = 0, j12 = 0, j13 = 0, j21 = 0, j22 = 0, j23 = 0, j31 = 0, j32 = 0,
     j33 = 0;
 #pragma unroll
   for (int i = 0; i < 8; i++) {
+    o.n[i] = nsh[i];
     j11 += xe[i] * d0[i];
     j12 += xe[i] * d1[i];
     j13 += xe[i] * d2[i];
@@ -179,9 +185,10 @@ __device__ __forceinline__ void gp_eval(const int variant, const T xi,
   } else {
     T ex = 0, ey = 0, ez = 0;
     if (vmag > eps) {
-      ex = vx / vmag;
-      ey = vy / vmag;
-      ez = vz / vmag;
+      const T iv = T(1) / vmag;
+      ex = vx * iv;
+      ey = vy * iv;
+      ez = vz * iv;
     }
     const T gx = i11 * ex + i12 * ey + i13 * ez;
     const T gy = i21 * ex + i22 * ey + i23 * ez;
@@ -201,6 +208,20 @@ __device__ __forceinline__ void gp_eval(const int variant, const T xi,
   for (int i = 0; i < 8; i++)
     o.w[i] = o.n[i] + tau * (vx * o.gx[i] + vy * o.gy[i] + vz * o.gz[i]);
   o.detj = detj;
+}
+
+// Evaluates one Gauss (or face) point of an element: shape functions at
+// (xi,eta,zeta), then gp_core.
+template <typename T>
+__device__ __forceinline__ void gp_eval(const int variant, const T xi,
+                                        const T eta, const T zeta,
+                                        const T (&xe)[8], const T (&ye)[8],
+                                        const T (&ze)[8], const T lam,
+                                        const T vx, const T vy, const T vz,
+                                        GPData<T> &o) {
+  T n[8], d0[8], d1[8], d2[8];
+  shape_at<T>(xi, eta, zeta, n, d0, d1, d2);
+  gp_core<T>(variant, n, d0, d1, d2, xe, ye, ze, lam, vx, vy, vz, o);
 }
 
 // Surface Jacobian of the xi = -1 face (nodes 1,4,8,5 of the element) at

@@ -127,23 +127,54 @@ __device__ __forceinline__ T group8_reduce_scatter(const T (&v)[8], int lane8) {
 constexpr int ROWS_EPB = 8;  // elements per 64-thread block
 
 template <typename T>
-struct RowSmem {
-  T g[ROWS_EPB][8][5][8];  // per element, per Gauss point: gx, gy, gz, s, w
-  T d[ROWS_EPB][8][2];     // detJ, c1*lambda*detJ
-  T fnw[ROWS_EPB][4][2][8];  // face points: N, W
-  T fd[ROWS_EPB][4];       // c1*alpha*detJs
+struct BuildSmem {
+  T g[ROWS_EPB][8][6][8];    // per element, per Gauss point q, per node j:
+                             // dNj/dx, dNj/dy, dNj/dz, v.gradNj + P*Nj, Nj, Wj
+  T d[ROWS_EPB][8][2];       // detJ, lambda*detJ
+  T fnw[ROWS_EPB][4][2][8];  // face-3 points: N, W
+  T fd[ROWS_EPB][4];         // alpha*detJs
+  T tab[12][4][8];           // shape N, dN/dxi, dN/deta, dN/dzeta at the 8
+                             // volume points and the 4 face-3 points
 };
 
-// MODE 0: store C rows (+ diag); MODE 1: rhs.
-template <typename T, int MODE>
-__global__ void __launch_bounds__(64) elem_rows_kernel(
-    OpArgs a, T c1, T c2, double2 *__restrict__ A64, float4 *__restrict__ A32,
-    double *__restrict__ diag, double cf, const double *__restrict__ told,
-    double *__restrict__ b) {
-  __shared__ RowSmem<T> sm;
+// Fills the shape tables of the 12 evaluation points (same for every
+// element) once per block.
+template <typename T>
+__device__ __forceinline__ void fill_shape_tables(T (&tab)[12][4][8]) {
+  for (int t = threadIdx.x; t < 12; t += blockDim.x) {
+    T xi, eta, zeta;
+    if (t < 8) {
+      xi = gauss_coord<T>(t, 0);
+      eta = gauss_coord<T>(t, 1);
+      zeta = gauss_coord<T>(t, 2);
+    } else {
+      const T gc = T(VDR_GAUSS_C);
+      xi = T(-1);
+      eta = ((t - 8) & 2) ? gc : -gc;
+      zeta = ((t - 8) & 1) ? gc : -gc;
+    }
+    shape_at<T>(xi, eta, zeta, tab[t][0], tab[t][1], tab[t][2], tab[t][3]);
+  }
+  __syncthreads();
+}
+
+// One pass over the elements computing, per element, the rows of
+// H = int lambda gradN.gradN + int W (v.gradN + P N) + alpha int_face3 W N
+// and M = int W N (lane i keeps row i), then any of
+//   A_e = aH*H + aM*M  -> element-matrix store (FP64 pairs and/or FP32)
+//   diag += diag(A_e)
+//   b    += cf*f_e - (H - rM*M) . T_old|_e      (f = (Q/vol) int W)
+// so that the operator build and the right-hand side share the Gauss-point
+// work (przest3d's per-element loop, vanadis_full_DR_OpenMP_timing.for:
+// 676-740, in one kernel).
+template <typename T>
+__global__ void __launch_bounds__(64) elem_build_kernel(OpArgs a, BuildArgs ba) {
+  __shared__ BuildSmem<T> sm;
+  fill_shape_tables<T>(sm.tab);
   const int lane8 = threadIdx.x & 7;
   const int le = threadIdx.x >> 3;
   const long E = a.E;
+  const T aH = T(ba.aH), aM = T(ba.aM), rM = T(ba.rM);
   for (long base = (long)blockIdx.x * ROWS_EPB; base < E;
        base += (long)gridDim.x * ROWS_EPB) {
     const long pe = base + le;
@@ -152,41 +183,42 @@ __global__ void __launch_bounds__(64) elem_rows_kernel(
     Elem<T> el;
     load_elem<T>(a, p, el);
     GPData<T> o;
-    gp_eval<T>(a.variant, gauss_coord<T>(lane8, 0), gauss_coord<T>(lane8, 1),
-               gauss_coord<T>(lane8, 2), el.xe, el.ye, el.ze, el.lam, el.vx,
-               el.vy, el.vz, o);
+    gp_core<T>(a.variant, sm.tab[lane8][0], sm.tab[lane8][1], sm.tab[lane8][2],
+               sm.tab[lane8][3], el.xe, el.ye, el.ze, el.lam, el.vx, el.vy,
+               el.vz, o);
     const T vol = group8_sum<T>(o.detj);
-    const T cm = c1 * el.pdec + c2;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       sm.g[le][lane8][0][j] = o.gx[j];
       sm.g[le][lane8][1][j] = o.gy[j];
       sm.g[le][lane8][2][j] = o.gz[j];
       sm.g[le][lane8][3][j] =
-          c1 * (el.vx * o.gx[j] + el.vy * o.gy[j] + el.vz * o.gz[j]) + cm * o.n[j];
-      sm.g[le][lane8][4][j] = o.w[j];
+          (el.vx * o.gx[j] + el.vy * o.gy[j] + el.vz * o.gz[j]) + el.pdec * o.n[j];
+      sm.g[le][lane8][4][j] = o.n[j];
+      sm.g[le][lane8][5][j] = o.w[j];
     }
     sm.d[le][lane8][0] = o.detj;
-    sm.d[le][lane8][1] = c1 * el.lam * o.detj;
+    sm.d[le][lane8][1] = el.lam * o.detj;
     if (el.robin && lane8 < 4) {
       const T gc = T(VDR_GAUSS_C);
       const T r = (lane8 & 2) ? gc : -gc;
       const T s = (lane8 & 1) ? gc : -gc;
       const T djs = face3_detjs<T>(el.xe, el.ye, el.ze, r, s);
-      gp_eval<T>(a.variant, T(-1), r, s, el.xe, el.ye, el.ze, el.lam, el.vx,
-                 el.vy, el.vz, o);
+      gp_core<T>(a.variant, sm.tab[8 + lane8][0], sm.tab[8 + lane8][1],
+                 sm.tab[8 + lane8][2], sm.tab[8 + lane8][3], el.xe, el.ye,
+                 el.ze, el.lam, el.vx, el.vy, el.vz, o);
 #pragma unroll
       for (int j = 0; j < 8; j++) {
         sm.fnw[le][lane8][0][j] = o.n[j];
         sm.fnw[le][lane8][1][j] = o.w[j];
       }
-      sm.fd[le][lane8] = c1 * T(a.f.robin_alpha) * djs;
+      sm.fd[le][lane8] = T(a.f.robin_alpha) * djs;
     }
     __syncwarp();
     const int i = lane8;
-    T acc[8];
+    T accH[8], accM[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) acc[j] = T(0);
+    for (int j = 0; j < 8; j++) accH[j] = accM[j] = T(0);
     T fw = T(0);
 #pragma unroll 2
     for (int q = 0; q < 8; q++) {
@@ -194,14 +226,14 @@ __global__ void __launch_bounds__(64) elem_rows_kernel(
       const T dl = sm.d[le][q][1];
       const T gxi = sm.g[le][q][0][i], gyi = sm.g[le][q][1][i],
               gzi = sm.g[le][q][2][i];
-      const T wi = sm.g[le][q][4][i];
-      const T wd = wi * dj;
+      const T wd = sm.g[le][q][5][i] * dj;
       fw += wd;
 #pragma unroll
       for (int j = 0; j < 8; j++) {
         const T gg = gxi * sm.g[le][q][0][j] + gyi * sm.g[le][q][1][j] +
                      gzi * sm.g[le][q][2][j];
-        acc[j] += dl * gg + wd * sm.g[le][q][3][j];
+        accH[j] += dl * gg + wd * sm.g[le][q][3][j];
+        accM[j] += wd * sm.g[le][q][4][j];
       }
     }
     if (el.robin) {
@@ -209,41 +241,43 @@ __global__ void __launch_bounds__(64) elem_rows_kernel(
       for (int f = 0; f < 4; f++) {
         const T aw = sm.fd[le][f] * sm.fnw[le][f][1][i];
 #pragma unroll
-        for (int j = 0; j < 8; j++) acc[j] += aw * sm.fnw[le][f][0][j];
+        for (int j = 0; j < 8; j++) accH[j] += aw * sm.fnw[le][f][0][j];
       }
     }
     __syncwarp();
-    if (valid) {
-      const int ci = el.c[i];
-      if (MODE == 0) {
-        if (A64) {
+    if (!valid) continue;
+    const int ci = el.c[i];
+    if (ba.A64 || ba.A32 || ba.diag) {
+      T row[8];
 #pragma unroll
-          for (int jj = 0; jj < 4; jj++)
-            A64[(size_t)(4 * i + jj) * E + p] =
-                make_double2((double)acc[2 * jj], (double)acc[2 * jj + 1]);
-        }
-        if (A32) {
+      for (int j = 0; j < 8; j++) row[j] = aH * accH[j] + aM * accM[j];
+      if (ba.A64) {
 #pragma unroll
-          for (int h = 0; h < 2; h++)
-            A32[(size_t)(2 * i + h) * E + p] =
-                make_float4((float)acc[4 * h], (float)acc[4 * h + 1],
-                            (float)acc[4 * h + 2], (float)acc[4 * h + 3]);
-        }
-        if (diag && ci >= 0) atomicAdd(diag + ci, (double)acc[i]);
-      } else {
-        if (ci >= 0) {
-          const double q = a.f.q ? __ldg(a.f.q + p) : 0.0;
-          double val = cf * ((q / (double)vol) * (double)fw);
-          if (told) {
-            double ft = 0.0;
-#pragma unroll
-            for (int j = 0; j < 8; j++)
-              ft += (double)acc[j] * __ldg(told + (el.c[j] & NODE_BITS));
-            val -= ft;
-          }
-          atomicAdd(b + ci, val);
-        }
+        for (int jj = 0; jj < 4; jj++)
+          ba.A64[(size_t)(4 * i + jj) * E + p] =
+              make_double2((double)row[2 * jj], (double)row[2 * jj + 1]);
       }
+      if (ba.A32) {
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+          ba.A32[(size_t)(2 * i + h) * E + p] =
+              make_float4((float)row[4 * h], (float)row[4 * h + 1],
+                          (float)row[4 * h + 2], (float)row[4 * h + 3]);
+      }
+      if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, (double)row[i]);
+    }
+    if (ba.b && ci >= 0) {
+      const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
+      double val = ba.cf * ((qe / (double)vol) * (double)fw);
+      if (ba.told) {
+        double ft = 0.0;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+          ft += (double)(accH[j] - rM * accM[j]) *
+                __ldg(ba.told + (el.c[j] & NODE_BITS));
+        val -= ft;
+      }
+      atomicAdd(ba.b + ci, val);
     }
   }
 }
@@ -402,31 +436,15 @@ int sm_count() {
 
 }  // namespace
 
-cudaError_t launch_build_stored(const OpArgs &a, double c1, double c2,
-                                double2 *A64, float4 *A32, double *diag,
-                                cudaStream_t s) {
+cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
+                         cudaStream_t s) {
   if (a.E <= 0) return cudaSuccess;
   const long blocks_needed = ((long)a.E + ROWS_EPB - 1) / ROWS_EPB;
   const int grid = (int)std::min<long>(blocks_needed, (long)sm_count() * 32);
-  if (A32 && !A64 && !diag) {
-    elem_rows_kernel<float, 0><<<grid, 64, 0, s>>>(a, (float)c1, (float)c2,
-                                                   nullptr, A32, nullptr, 0.0,
-                                                   nullptr, nullptr);
-  } else {
-    elem_rows_kernel<double, 0><<<grid, 64, 0, s>>>(a, c1, c2, A64, A32, diag,
-                                                    0.0, nullptr, nullptr);
-  }
-  count_launches(1);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_rhs(const OpArgs &a, double cf, double rM,
-                       const double *t_old, double *b, cudaStream_t s) {
-  if (a.E <= 0) return cudaSuccess;
-  const long blocks_needed = ((long)a.E + ROWS_EPB - 1) / ROWS_EPB;
-  const int grid = (int)std::min<long>(blocks_needed, (long)sm_count() * 32);
-  elem_rows_kernel<double, 1><<<grid, 64, 0, s>>>(a, 1.0, -rM, nullptr, nullptr,
-                                                  nullptr, cf, t_old, b);
+  if (fp32)
+    elem_build_kernel<float><<<grid, 64, 0, s>>>(a, ba);
+  else
+    elem_build_kernel<double><<<grid, 64, 0, s>>>(a, ba);
   count_launches(1);
   return cudaGetLastError();
 }

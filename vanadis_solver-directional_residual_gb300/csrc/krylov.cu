@@ -107,33 +107,52 @@ struct Vec {
   int n;
   KState *st;
   double *partials;
-  const double *b, *d;
+  const double *b;
+  const double *dinv;  // 1/diag (diag is 1 on Dirichlet nodes)
   const unsigned char *m;
   double *x, *r, *rh, *p, *v, *ph, *s, *sh, *t;  // BiCGStab
   double *rr, *pp, *z, *zz;                      // BiCG (r, p, x shared)
 };
 
-#define GRID_LOOP(i) \
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (long)gridDim.x * blockDim.x)
+// Grid-stride loops unrolled U times with every load of the U elements
+// issued before any use, so each thread keeps U independent memory
+// requests in flight (these kernels are bound by HBM bandwidth).
+constexpr int U = 4;
+#define VLOOP(body_load, body_use)                                          \
+  {                                                                         \
+    const long stride_ = (long)gridDim.x * blockDim.x;                      \
+    for (long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x; i0 < a.n;   \
+         i0 += U * stride_) {                                               \
+      _Pragma("unroll") for (int u = 0; u < U; u++) {                       \
+        const long i = i0 + u * stride_;                                    \
+        const bool ok = i < a.n;                                            \
+        body_load                                                           \
+      }                                                                     \
+      _Pragma("unroll") for (int u = 0; u < U; u++) {                       \
+        const long i = i0 + u * stride_;                                    \
+        if (i < a.n) { body_use }                                           \
+      }                                                                     \
+    }                                                                       \
+  }
 
 // -------- shared start: r = b - r (r holds A x0), residual norms --------
 // BiCGStab: rh = r, rho = (rh, r).  BiCG: rr = r, bknum = (r/d, rr).
 template <bool BICG>
 __global__ void __launch_bounds__(RED_THREADS) k_start(Vec a) {
   double v[3] = {0.0, 0.0, 0.0};
-  GRID_LOOP(i) {
-    const double bi = a.b[i];
-    const double ri = bi - a.r[i];
-    a.r[i] = ri;
-    if (BICG) {
-      a.rr[i] = ri;
-      v[2] += (ri / a.d[i]) * ri;
-    } else {
-      a.rh[i] = ri;
-    }
-    v[0] += bi * bi;
-    v[1] += ri * ri;
-  }
+  double bv[U], rv[U], dv[U];
+  VLOOP(bv[u] = ok ? a.b[i] : 0.0; rv[u] = ok ? a.r[i] : 0.0;
+        dv[u] = (ok && BICG) ? a.dinv[i] : 0.0;,
+        const double ri = bv[u] - rv[u];
+        a.r[i] = ri;
+        if (BICG) {
+          a.rr[i] = ri;
+          v[2] += (ri * dv[u]) * ri;
+        } else {
+          a.rh[i] = ri;
+        }
+        v[0] += bv[u] * bv[u];
+        v[1] += ri * ri;)
   double o[3];
   if (grid_sum<3>(v, a.partials, &a.st->ticket, o)) {
     KState *st = a.st;
@@ -148,6 +167,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_start(Vec a) {
     st->omega = 1.0;
     st->bknum = o[2];
     st->bkden = 1.0;
+    st->reason = 0;
     if (o[0] == 0.0) {  // b = 0: the solution is x = 0
       st->err = 0.0;
       st->status = VDR_OK;
@@ -155,7 +175,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_start(Vec a) {
       return;
     }
     st->err = sqrt(o[1]) / sqrt(o[0]);
-    st->reason = 0;
     if (!(st->err == st->err)) {
       st->status = VDR_BREAKDOWN;
       st->reason = 5;
@@ -177,19 +196,24 @@ __global__ void __launch_bounds__(RED_THREADS) bs_p(Vec a) {
   const bool first = st->iter == 0;
   const double beta = first ? 0.0 : (st->rho / st->rho_old) * (st->alpha / st->omega);
   const double om = st->omega;
-  GRID_LOOP(i) {
-    const double pi = first ? a.r[i] : a.r[i] + beta * (a.p[i] - om * a.v[i]);
-    a.p[i] = pi;
-    a.ph[i] = a.m[i] ? 0.0 : pi / a.d[i];
-    a.v[i] = 0.0;
-  }
+  double rv[U], pv[U], vv[U], dv[U];
+  unsigned char mv[U];
+  VLOOP(rv[u] = ok ? a.r[i] : 0.0; pv[u] = (ok && !first) ? a.p[i] : 0.0;
+        vv[u] = (ok && !first) ? a.v[i] : 0.0; dv[u] = ok ? a.dinv[i] : 0.0;
+        mv[u] = ok ? a.m[i] : 1;,
+        const double pi = first ? rv[u] : rv[u] + beta * (pv[u] - om * vv[u]);
+        a.p[i] = pi;
+        a.ph[i] = mv[u] ? 0.0 : pi * dv[u];
+        a.v[i] = 0.0;)
 }
 
 // alpha = rho / (rh, v)
 __global__ void __launch_bounds__(RED_THREADS) bs_alpha(Vec a) {
   if (a.st->done) return;
   double v[1] = {0.0};
-  GRID_LOOP(i) v[0] += a.rh[i] * a.v[i];
+  double hv[U], vv[U];
+  VLOOP(hv[u] = ok ? a.rh[i] : 0.0; vv[u] = ok ? a.v[i] : 0.0;,
+        v[0] += hv[u] * vv[u];)
   double o[1];
   if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
     KState *st = a.st;
@@ -208,13 +232,15 @@ __global__ void __launch_bounds__(RED_THREADS) bs_s(Vec a) {
   if (a.st->done) return;
   const double al = a.st->alpha;
   double v[1] = {0.0};
-  GRID_LOOP(i) {
-    const double si = a.r[i] - al * a.v[i];
-    a.s[i] = si;
-    a.sh[i] = a.m[i] ? 0.0 : si / a.d[i];
-    a.t[i] = 0.0;
-    v[0] += si * si;
-  }
+  double rv[U], vv[U], dv[U];
+  unsigned char mv[U];
+  VLOOP(rv[u] = ok ? a.r[i] : 0.0; vv[u] = ok ? a.v[i] : 0.0;
+        dv[u] = ok ? a.dinv[i] : 0.0; mv[u] = ok ? a.m[i] : 1;,
+        const double si = rv[u] - al * vv[u];
+        a.s[i] = si;
+        a.sh[i] = mv[u] ? 0.0 : si * dv[u];
+        a.t[i] = 0.0;
+        v[0] += si * si;)
   double o[1];
   if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
     KState *st = a.st;
@@ -227,11 +253,10 @@ __global__ void __launch_bounds__(RED_THREADS) bs_s(Vec a) {
 __global__ void __launch_bounds__(RED_THREADS) bs_omega(Vec a) {
   if (a.st->done || a.st->sconv) return;
   double v[2] = {0.0, 0.0};
-  GRID_LOOP(i) {
-    const double ti = a.t[i];
-    v[0] += ti * a.s[i];
-    v[1] += ti * ti;
-  }
+  double tv[U], sv[U];
+  VLOOP(tv[u] = ok ? a.t[i] : 0.0; sv[u] = ok ? a.s[i] : 0.0;,
+        v[0] += tv[u] * sv[u];
+        v[1] += tv[u] * tv[u];)
   double o[2];
   if (grid_sum<2>(v, a.partials, &a.st->ticket, o)) {
     KState *st = a.st;
@@ -252,10 +277,11 @@ __global__ void __launch_bounds__(RED_THREADS) bs_xr(Vec a) {
   const double al = stc->alpha;
   if (stc->sconv) {
     double v[1] = {0.0};
-    GRID_LOOP(i) {
-      a.x[i] += al * a.ph[i];
-      a.r[i] = a.s[i];
-    }
+    double xv[U], pv[U], sv[U];
+    VLOOP(xv[u] = ok ? a.x[i] : 0.0; pv[u] = ok ? a.ph[i] : 0.0;
+          sv[u] = ok ? a.s[i] : 0.0;,
+          a.x[i] = xv[u] + al * pv[u];
+          a.r[i] = sv[u];)
     double o[1];
     if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
       KState *st = a.st;
@@ -268,13 +294,15 @@ __global__ void __launch_bounds__(RED_THREADS) bs_xr(Vec a) {
   }
   const double om = stc->omega;
   double v[2] = {0.0, 0.0};
-  GRID_LOOP(i) {
-    a.x[i] += al * a.ph[i] + om * a.sh[i];
-    const double ri = a.s[i] - om * a.t[i];
-    a.r[i] = ri;
-    v[0] += ri * ri;
-    v[1] += a.rh[i] * ri;
-  }
+  double xv[U], pv[U], shv[U], sv[U], tv[U], hv[U];
+  VLOOP(xv[u] = ok ? a.x[i] : 0.0; pv[u] = ok ? a.ph[i] : 0.0;
+        shv[u] = ok ? a.sh[i] : 0.0; sv[u] = ok ? a.s[i] : 0.0;
+        tv[u] = ok ? a.t[i] : 0.0; hv[u] = ok ? a.rh[i] : 0.0;,
+        a.x[i] = xv[u] + al * pv[u] + om * shv[u];
+        const double ri = sv[u] - om * tv[u];
+        a.r[i] = ri;
+        v[0] += ri * ri;
+        v[1] += hv[u] * ri;)
   double o[2];
   if (grid_sum<2>(v, a.partials, &a.st->ticket, o)) {
     KState *st = a.st;
@@ -308,22 +336,27 @@ __global__ void __launch_bounds__(RED_THREADS) bc_p(Vec a) {
   if (st->done) return;
   const bool first = st->iter == 0;
   const double bk = first ? 0.0 : st->bknum / st->bkden;
-  GRID_LOOP(i) {
-    const double di = a.d[i];
-    const double zi = a.r[i] / di, zzi = a.rr[i] / di;
-    const bool mi = a.m[i];
-    a.p[i] = mi ? 0.0 : (first ? zi : zi + bk * a.p[i]);
-    a.pp[i] = mi ? 0.0 : (first ? zzi : zzi + bk * a.pp[i]);
-    a.z[i] = 0.0;
-    a.zz[i] = 0.0;
-  }
+  double rv[U], rrv[U], dv[U], pv[U], ppv[U];
+  unsigned char mv[U];
+  VLOOP(rv[u] = ok ? a.r[i] : 0.0; rrv[u] = ok ? a.rr[i] : 0.0;
+        dv[u] = ok ? a.dinv[i] : 0.0; mv[u] = ok ? a.m[i] : 1;
+        pv[u] = (ok && !first) ? a.p[i] : 0.0;
+        ppv[u] = (ok && !first) ? a.pp[i] : 0.0;,
+        const double zi = rv[u] * dv[u];
+        const double zzi = rrv[u] * dv[u];
+        a.p[i] = mv[u] ? 0.0 : (first ? zi : zi + bk * pv[u]);
+        a.pp[i] = mv[u] ? 0.0 : (first ? zzi : zzi + bk * ppv[u]);
+        a.z[i] = 0.0;
+        a.zz[i] = 0.0;)
 }
 
 // ak = bknum / (z, pp)
 __global__ void __launch_bounds__(RED_THREADS) bc_ak(Vec a) {
   if (a.st->done) return;
   double v[1] = {0.0};
-  GRID_LOOP(i) v[0] += a.z[i] * a.pp[i];
+  double zv[U], pv[U];
+  VLOOP(zv[u] = ok ? a.z[i] : 0.0; pv[u] = ok ? a.pp[i] : 0.0;,
+        v[0] += zv[u] * pv[u];)
   double o[1];
   if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
     KState *st = a.st;
@@ -341,15 +374,18 @@ __global__ void __launch_bounds__(RED_THREADS) bc_upd(Vec a) {
   if (a.st->done) return;
   const double ak = a.st->ak;
   double v[2] = {0.0, 0.0};
-  GRID_LOOP(i) {
-    a.x[i] += ak * a.p[i];
-    const double ri = a.r[i] - ak * a.z[i];
-    const double rri = a.rr[i] - ak * a.zz[i];
-    a.r[i] = ri;
-    a.rr[i] = rri;
-    v[0] += ri * ri;
-    v[1] += (ri / a.d[i]) * rri;
-  }
+  double xv[U], pv[U], rv[U], zv[U], rrv[U], zzv[U], dv[U];
+  VLOOP(xv[u] = ok ? a.x[i] : 0.0; pv[u] = ok ? a.p[i] : 0.0;
+        rv[u] = ok ? a.r[i] : 0.0; zv[u] = ok ? a.z[i] : 0.0;
+        rrv[u] = ok ? a.rr[i] : 0.0; zzv[u] = ok ? a.zz[i] : 0.0;
+        dv[u] = ok ? a.dinv[i] : 0.0;,
+        a.x[i] = xv[u] + ak * pv[u];
+        const double ri = rv[u] - ak * zv[u];
+        const double rri = rrv[u] - ak * zzv[u];
+        a.r[i] = ri;
+        a.rr[i] = rri;
+        v[0] += ri * ri;
+        v[1] += (ri * dv[u]) * rri;)
   double o[2];
   if (grid_sum<2>(v, a.partials, &a.st->ticket, o)) {
     KState *st = a.st;
@@ -374,12 +410,11 @@ __global__ void __launch_bounds__(RED_THREADS) bc_upd(Vec a) {
 __global__ void k_true_residual(Vec a, const double *ax, double *partials,
                                 unsigned int *ticket, double *out) {
   double v[2] = {0.0, 0.0};
-  GRID_LOOP(i) {
-    const double bi = a.b[i];
-    const double ri = bi - ax[i];
-    v[0] += ri * ri;
-    v[1] += bi * bi;
-  }
+  double bv[U], av[U];
+  VLOOP(bv[u] = ok ? a.b[i] : 0.0; av[u] = ok ? ax[i] : 0.0;,
+        const double ri = bv[u] - av[u];
+        v[0] += ri * ri;
+        v[1] += bv[u] * bv[u];)
   double o[2];
   if (grid_sum<2>(v, partials, ticket, o)) *out = sqrt(o[0]) / sqrt(o[1]);
 }
@@ -395,7 +430,7 @@ Vec make_vec(Handle &h, const double *b, double *x) {
   a.st = h.st;
   a.partials = h.partials;
   a.b = b;
-  a.d = h.diag;
+  a.dinv = h.dinv;
   a.m = h.mask;
   a.x = x;
   double *w = h.work;

@@ -87,6 +87,7 @@ struct Handle {
   double2 *A64 = nullptr;  // [32][E] stored element matrices (row-major pairs)
   float4 *A32 = nullptr;   // [16][E]
   double *diag = nullptr;  // [N] assembled diagonal, 1 on Dirichlet nodes
+  double *dinv = nullptr;  // [N] 1/diag (the Jacobi preconditioner)
 
   // solver workspace
   double *work = nullptr;
@@ -114,12 +115,20 @@ int apply_launches(const Handle &h);  // kernels per operator apply
 
 OpArgs op_args(const Handle &h);
 
+// Outputs of one element-build pass (any pointer may be null).
+struct BuildArgs {
+  double aH = 1.0, aM = 0.0;     // A_e = aH*H + aM*M
+  double2 *A64 = nullptr;        // FP64 element-matrix store
+  float4 *A32 = nullptr;         // FP32 element-matrix store
+  double *diag = nullptr;        // += diag(A_e)
+  double cf = 1.0, rM = 0.0;     // b += cf*f - (H - rM*M) T_old
+  const double *told = nullptr;
+  double *b = nullptr;
+};
+
 // ---- launchers (element.cu) ----
-cudaError_t launch_build_stored(const OpArgs &a, double c1, double c2,
-                                double2 *A64, float4 *A32, double *diag,
-                                cudaStream_t s);
-cudaError_t launch_rhs(const OpArgs &a, double cf, double rM,
-                       const double *t_old, double *b, cudaStream_t s);
+cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
+                         cudaStream_t s);
 cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
                             const double *x, double *y, const int *skip,
                             const int *skip2, cudaStream_t s);
@@ -139,8 +148,9 @@ cudaError_t launch_legacy_bb(const double *bb_ref, int E, double2 *A64,
                              cudaStream_t s);
 cudaError_t launch_legacy_conn(const int *iss_ref, int E, int N, const int *bc,
                                int *conn, int *bad, cudaStream_t s);
-cudaError_t launch_diag_fix(double *diag, const unsigned char *mask, int N,
-                            cudaStream_t s);
+// diag = 1 on Dirichlet nodes (when mask != null); dinv = 1/diag.
+cudaError_t launch_diag_fix(double *diag, double *dinv,
+                            const unsigned char *mask, int N, cudaStream_t s);
 cudaError_t launch_mask_vec(double *v, const unsigned char *mask, int N,
                             cudaStream_t s);
 cudaError_t launch_bc_to_mask(const int *bc, unsigned char *mask, int N,
