@@ -37,12 +37,21 @@ def test_solution_parity(vdr, gpu_lib, systems, name, solver, mode, scatter):
     assert rel_l2(x, ref["x_solution"]) < 1e-9
 
 
-def test_iteration_count_matches_oracle_bicgstab(vdr, gpu_lib, systems):
+@pytest.mark.parametrize("solver", ["bicgstab", "bicg"])
+def test_iteration_count_matches_oracle(vdr, oracle, gpu_lib, systems, solver):
+    """Away from the rounding floor (tol 1e-10) the GPU and the oracle take
+    the same number of iterations up to a few (reductions sum in a
+    different order)."""
     prob, ref = systems["const_adv_OT"]
-    with vdr.Solver(prob, vdr.Options(solver="bicgstab")) as s:
-        _, it, _, st = s.solve(ref["b"], tol=1e-13, itmax=20000)
+    m = prob.mesh
+    fn = oracle.bicgstab if solver == "bicgstab" else oracle.dbcg
+    _, it_ref, _, st_ref = fn(ref["b"], np.zeros(m.nnode), ref["bb"], m.iss,
+                              ref["diag"], prob.bc, 1e-10, 20000)
+    assert st_ref == 0
+    with vdr.Solver(prob, vdr.Options(solver=solver)) as s:
+        _, it, _, st = s.solve(ref["b"], tol=1e-10, itmax=20000)
     assert st == 0
-    assert abs(it - ref["iterations"]) <= max(3, 0.05 * ref["iterations"])
+    assert abs(it - it_ref) <= max(3, 0.1 * it_ref), (it, it_ref)
 
 
 def test_kat_run_handle_api(vdr, oracle, gpu_lib):
