@@ -67,6 +67,8 @@ SIGNATURES = {
     "vdr_last_error": (ctypes.c_char_p, []),
     "kernel_dbcg_simple_": (None, [_I, _D, _D, _D, _I, _I, _D, _D, _I, _D,
                                    _I, _I, _I, _I]),
+    "vdr_bicg_noalloc_device": (_i, [_i, _i, _i, _i, _P, _P, _d, _i, _P, _P,
+                                     _P, _P, _P, _I, _D]),
 }
 
 
