@@ -153,6 +153,33 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def fp64_peak_tflops():
+    """Measured FP64 peak: cuBLAS DGEMM (torch.matmul, float64, 4096^3),
+    best of 3 -- the denominator for the FP64-pipe-bound element build."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+# FP64 operations per element of elem_build_kernel<double>, from its
+# operation census (FMA = 2 FLOP): per Gauss point ~500 FLOP of geometry and
+# DR weight, ~780 FLOP of H/M row accumulation, ~30 FLOP of output; x 8.
+BUILD_FLOP_PER_ELEMENT = 10400.0
+
+
 def profile_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu
     summary (a line 'traffic_bytes_per_launch: <number>')."""
@@ -322,6 +349,74 @@ def run_native(a):
     achieved = alg_bytes / (t_apply_ms * 1e-3) / 1e9
     traffic = profile_traffic()
 
+    # ---- FP64 element build: roofline against the measured FP64 peak ----
+    fp64_peak = fp64_peak_tflops()
+    build_tflops = BUILD_FLOP_PER_ELEMENT * E / (t_build * 1e-3) / 1e12
+
+    # ---- mixed precision (FP32 operator inside FP64 refinement) ----
+    xm = torch.zeros_like(b)
+    with torch.cuda.stream(stream):
+        x.zero_()
+    s.set_operator(aH, aM)
+    s.assemble_rhs_device(b, cf, rM, None)
+    s.solve_device(b, x, tol=TOL, itmax=20000)        # FP64 reference solution
+    torch.cuda.synchronize()
+    m_times = []
+    for k in range(3):
+        with torch.cuda.stream(stream):
+            xm.zero_()
+        s.set_operator(aH, aM)
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        m0.record(stream)
+        s.assemble_rhs_device(b, cf, rM, None)
+        mo, mi, merr, mst = s.solve_mixed_device(b, xm, tol=TOL, inner_tol=1e-5)
+        m1.record(stream)
+        torch.cuda.synchronize()
+        m_times.append(m0.elapsed_time(m1))
+    mixed = {"value": statistics.mean(m_times[1:]) / 1e3, "unit": "s",
+             "outer_corrections": mo, "inner_iterations": mi,
+             "fp64_rel_residual": merr, "status": mst,
+             "rel_l2_vs_fp64_solution": float(torch.linalg.norm(xm - x) /
+                                              torch.linalg.norm(x)),
+             "what": "FP32 operator (DR terms recomputed in FP32, FP32 element "
+                     "matrices) in BiCGStab to 1e-5 inside FP64 refinement"}
+
+    # ---- the colour-scatter variant of the same step ----
+    sc = vdr.Solver(prob, vdr.Options(apply_mode="stored", scatter="color",
+                                      solver="bicgstab", device=local),
+                    aH=aH, aM=aM)
+    cstream = torch.cuda.ExternalStream(sc.stream())
+    xc = torch.zeros_like(b)
+    c_times = []
+    for k in range(3):
+        with torch.cuda.stream(cstream):
+            xc.zero_()
+        sc.set_operator(aH, aM)
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(cstream)
+        sc.assemble_rhs_device(b, cf, rM, None)
+        cit, cerr, cst = sc.solve_device(b, xc, tol=TOL, itmax=20000)
+        c1.record(cstream)
+        torch.cuda.synchronize()
+        c_times.append(c0.elapsed_time(c1))
+    yc = torch.zeros_like(b)
+    for _ in range(3):
+        sc.apply_accumulate_device(xr, yc)
+    c2e, c3e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c2e.record(cstream)
+    for _ in range(reps):
+        sc.apply_accumulate_device(xr, yc)
+    c3e.record(cstream)
+    torch.cuda.synchronize()
+    scatter_variants = {
+        "atomic": {"step_s": ms / 1e3, "apply_ms": t_apply_ms,
+                   "apply_gbs": achieved},
+        "color": {"step_s": statistics.mean(c_times[1:]) / 1e3,
+                  "apply_ms": c2e.elapsed_time(c3e) / reps,
+                  "apply_gbs": alg_bytes / (c2e.elapsed_time(c3e) / reps * 1e-3) / 1e9,
+                  "iterations": cit, "status": cst}}
+    sc.close()
+
     # ---- e2e through the C ABI with host buffers ----
     vel, lam, pdec, q = prob.vel, prob.lam, prob.pdec, prob.q
     h2d = 8 * (vel.size + lam.size + pdec.size + q.size) + 8 * N + 8 * N
@@ -370,6 +465,15 @@ def run_native(a):
                          "kernel": "stored_apply_f64 (EBE apply, atomic scatter)",
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "launch_ms": t_apply_ms, "peak_kind": peak_kind},
+            "roofline_build": {"bound": "fp64", "achieved": build_tflops,
+                               "peak": fp64_peak, "unit": "TFLOP/s",
+                               "frac": build_tflops / fp64_peak,
+                               "kernel": "elem_build_kernel<double> (element "
+                                         "matrices + diag + RHS)",
+                               "flop_per_element": BUILD_FLOP_PER_ELEMENT,
+                               "peak_kind": "measured live: cuBLAS DGEMM 4096^3"},
+            "scatter_variants": scatter_variants,
+            "mixed_precision": mixed,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,

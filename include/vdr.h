@@ -118,6 +118,11 @@ int vdr_apply_device(vdr_handle *h, const double *d_x, double *d_y,
 int vdr_apply_accumulate_device(vdr_handle *h, const double *d_x, double *d_y,
                                 int transpose);
 
+/* y = P A32 P x with the FP32 operator (DR terms and element matrices
+ * computed in FP32; FP64 vectors, FP32 arithmetic inside the element). */
+int vdr_apply32_device(vdr_handle *h, const double *d_x, double *d_y,
+                       int transpose);
+
 /* Right-hand side b = cf*f - (H - rM*M) T_old, assembled on the GPU, with
  * b = 0 on Dirichlet nodes (przest3d :691-716, :766-772).  t_old may be
  * NULL (steady: b = cf*f).  Host arrays of length N. */
@@ -139,6 +144,17 @@ int vdr_solve(vdr_handle *h, const double *b, double *x, double tol,
               int itmax, int *iter, double *err);
 int vdr_solve_device(vdr_handle *h, const double *d_b, double *d_x,
                      double tol, int itmax, int *iter, double *err);
+
+/* Mixed precision: FP64 iterative refinement (residual b - A x and update
+ * x += d in FP64 with the FP64 operator) around inner solves A32 d = r with
+ * the FP32 operator (element Jacobians and DR terms recomputed in FP32, FP32
+ * element matrices), each to inner_tol relative to ||r||.  Stops when the
+ * FP64 true relative residual ||b - A x||/||b|| <= tol or after max_outer
+ * corrections; *err is that FP64 residual.  Device arrays. */
+int vdr_solve_mixed_device(vdr_handle *h, const double *d_b, double *d_x,
+                           double tol, double inner_tol, int max_outer,
+                           int inner_itmax, int *outer_iters, int *inner_iters,
+                           double *err);
 
 /* Statistics of the handle's most recent solve. */
 typedef struct vdr_solve_stats {

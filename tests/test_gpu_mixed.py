@@ -1,0 +1,77 @@
+"""Mixed precision: the FP32 operator (DR terms and element matrices
+recomputed in FP32) against the FP64 oracle, and FP64 iterative refinement
+around FP32 inner solves reaching the FP64 tolerance, with its error against
+the FP64 oracle solution reported and bounded."""
+import numpy as np
+import pytest
+
+from helpers import kat_problem, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FP32_APPLY_TOL = 2e-5  # FP32 recompute: ~1e-6 typical, bound with margin
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+def fp32_cases(vdr):
+    P = vdr.problems
+    return {"rotation_VF_64": P.rotation_shear(64, 64, 32, seed=31),
+            "const_adv_OT": P.constant_advection(16, 16, 8, seed=32),
+            "kat_VF_robin": kat_problem(vdr)}
+
+
+@pytest.mark.parametrize("name", ["rotation_VF_64", "const_adv_OT",
+                                  "kat_VF_robin"])
+@pytest.mark.parametrize("mode", ["stored", "matrix_free"])
+def test_fp32_operator_against_fp64_oracle(vdr, oracle, gpu_lib, torch, name,
+                                           mode):
+    prob = fp32_cases(vdr)[name]
+    m = prob.mesh
+    aH, aM = 2.0, 0.7
+    bb, _, _ = oracle.assemble(prob.variant, m.xx, m.yy, m.zz, m.iss, prob.vel,
+                               prob.lam, prob.pdec, prob.q, kod=m.kod,
+                               robin_alpha=prob.robin_alpha, aH=aH, aM=aM,
+                               want_b=False, want_diag=False, nthreads=8)
+    x = np.random.default_rng(8).standard_normal(m.nnode)
+    with vdr.Solver(prob, vdr.Options(apply_mode=mode), aH=aH, aM=aM) as s:
+        dx = torch.tensor(x, device="cuda")
+        dy = torch.empty_like(dx)
+        torch.cuda.synchronize()
+        for tr in (False, True):
+            s.apply32_device(dx, dy, transpose=tr)
+            torch.cuda.synchronize()
+            yref, _ = oracle.matvec0(m.iss, bb, prob.bc, x, transpose=tr)
+            err = rel_l2(dy.cpu().numpy(), yref)
+            assert err < FP32_APPLY_TOL, (name, mode, tr, err)
+            assert err > 1e-12  # really computed in FP32
+
+
+@pytest.mark.parametrize("solver", ["bicgstab", "bicg"])
+def test_mixed_refinement_reaches_fp64_tolerance(vdr, gpu_lib, torch, solver):
+    prob = vdr.problems.rotation_shear(32, 32, 16, seed=33)
+    dt = 10.0 / 32
+    aH, aM = 2.0, 3.0 / dt
+    opts = vdr.Options(solver=solver)
+    with vdr.Solver(prob, opts, aH=aH, aM=aM) as s:
+        b = torch.empty(prob.mesh.nnode, dtype=torch.float64, device="cuda")
+        s.assemble_rhs_device(b, 3.0, 3.0 / dt, None)
+        x64 = torch.zeros_like(b)
+        it, err64, st = s.solve_device(b, x64, tol=1e-12, itmax=5000)
+        assert st == 0
+        xm = torch.zeros_like(b)
+        torch.cuda.synchronize()
+        outer, inner, err, st = s.solve_mixed_device(b, xm, tol=1e-10,
+                                                     inner_tol=1e-5)
+        torch.cuda.synchronize()
+        assert st == 0, (outer, inner, err)
+        assert err <= 1e-10
+        assert 1 <= outer <= 4
+        true_rel = s.true_residual_device(b, xm)
+        assert true_rel <= 1.5e-10
+        # error against the FP64 solution (itself within 1e-12 of the oracle
+        # system): bounded by the residual times the conditioning seen here
+        assert rel_l2(xm.cpu().numpy(), x64.cpu().numpy()) < 1e-8

@@ -51,11 +51,13 @@ SIGNATURES = {
     "vdr_apply": (_i, [_P, _D, _D, _i]),
     "vdr_apply_device": (_i, [_P, _P, _P, _i]),
     "vdr_apply_accumulate_device": (_i, [_P, _P, _P, _i]),
+    "vdr_apply32_device": (_i, [_P, _P, _P, _i]),
     "vdr_assemble_rhs": (_i, [_P, _d, _d, _D, _D]),
     "vdr_assemble_rhs_device": (_i, [_P, _d, _d, _P, _P]),
     "vdr_get_diag": (_i, [_P, _D]),
     "vdr_solve": (_i, [_P, _D, _D, _d, _i, _I, _D]),
     "vdr_solve_device": (_i, [_P, _P, _P, _d, _i, _I, _D]),
+    "vdr_solve_mixed_device": (_i, [_P, _P, _P, _d, _d, _i, _i, _I, _I, _D]),
     "vdr_true_residual_device": (_i, [_P, _P, _P, _D]),
     "vdr_mass": (_i, [_P, _D, _D]),
     "vdr_mass_device": (_i, [_P, _P, _D]),

@@ -164,6 +164,26 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
 
 int ensure_operator(Handle &h) { return build_operator(h, nullptr); }
 
+// FP32 element matrices from the FP32 DR recompute (Jacobians and DR terms
+// evaluated in FP32), for the inner solves of the mixed-precision path.
+int ensure_operator32(Handle &h) {
+  if (h.op32_valid) return VDR_OK;
+  if (h.apply_mode != VDR_APPLY_STORED) {
+    h.op32_valid = true;  // matrix-free: recomputed in FP32 at each apply
+    return VDR_OK;
+  }
+  cudaError_t e;
+  if ((e = dalloc(&h.A32, (size_t)h.E * 16))) return cuda_fail(e, "alloc FP32 matrices");
+  BuildArgs ba;
+  ba.aH = h.aH;
+  ba.aM = h.aM;
+  ba.A32 = h.A32;
+  if ((e = launch_build(op_args(h), ba, true, h.stream)))
+    return cuda_fail(e, "FP32 element matrices");
+  h.op32_valid = true;
+  return VDR_OK;
+}
+
 void invalidate(Handle &h) {
   h.op64_valid = h.op32_valid = h.diag_valid = false;
 }
@@ -477,6 +497,28 @@ int vdr_apply_accumulate_device(vdr_handle *H, const double *x, double *y,
   return e ? cuda_fail(e, "apply") : VDR_OK;
 }
 
+int vdr_apply32_device(vdr_handle *H, const double *x, double *y,
+                       int transpose) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!x || !y) {
+    set_error("vdr_apply32_device: null vector");
+    return VDR_BAD_ARGUMENT;
+  }
+  if (!h.fields_set) {
+    set_error("fields not set (vdr_set_fields)");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator32(h))) return st;
+  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(double) * h.N, h.stream);
+  if (e) return cuda_fail(e, "memset");
+  h.apply_fp32 = true;
+  e = launch_apply(h, transpose != 0, x, y, nullptr, nullptr, h.stream);
+  h.apply_fp32 = false;
+  return e ? cuda_fail(e, "apply32") : VDR_OK;
+}
+
 int vdr_apply(vdr_handle *H, const double *x, double *y, int transpose) {
   int st = check_handle(H);
   if (st) return st;
@@ -558,6 +600,35 @@ int vdr_solve_device(vdr_handle *H, const double *b, double *x, double tol,
   const int method = h.opt.solver == VDR_SOLVER_BICG ? VDR_SOLVER_BICG
                                                      : VDR_SOLVER_BICGSTAB;
   return solve_device(h, method, bm, x, tol, itmax, iter, err);
+}
+
+int vdr_solve_mixed_device(vdr_handle *H, const double *b, double *x,
+                           double tol, double inner_tol, int max_outer,
+                           int inner_itmax, int *outer_iters, int *inner_iters,
+                           double *err) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!b || !x || !(tol >= 0.0) || !(inner_tol > 0.0) || max_outer < 0) {
+    set_error("vdr_solve_mixed_device: bad arguments");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator(h)) || (st = ensure_operator32(h))) return st;
+  if ((st = ensure_io(H))) return st;
+  double *bm = H->io + 2 * (size_t)h.N;
+  cudaError_t e = cudaMemcpyAsync(bm, b, sizeof(double) * h.N,
+                                  cudaMemcpyDeviceToDevice, h.stream);
+  if (!e) e = launch_mask_vec(bm, h.mask, h.N, h.stream);
+  if (e) return cuda_fail(e, "rhs copy");
+  const int method = h.opt.solver == VDR_SOLVER_BICG ? VDR_SOLVER_BICG
+                                                     : VDR_SOLVER_BICGSTAB;
+  MixedStats ms;
+  st = solve_mixed_device(h, method, bm, x, tol, inner_tol, max_outer,
+                          inner_itmax, &ms);
+  if (outer_iters) *outer_iters = ms.outer;
+  if (inner_iters) *inner_iters = ms.inner;
+  if (err) *err = ms.err;
+  return st;
 }
 
 int vdr_solve(vdr_handle *H, const double *b, double *x, double tol,

@@ -309,8 +309,8 @@ cudaError_t launch_apply(const Handle &h, bool transpose, const double *x,
                          double *y, const int *skip, const int *skip2,
                          cudaStream_t s) {
   if (h.apply_mode == VDR_APPLY_MATRIX_FREE)
-    return launch_mf_apply(op_args(h), false, transpose, x, y, skip, skip2, s);
-  return launch_stored_apply(h, false, transpose, x, y, skip, skip2, s);
+    return launch_mf_apply(op_args(h), h.apply_fp32, transpose, x, y, skip, skip2, s);
+  return launch_stored_apply(h, h.apply_fp32, transpose, x, y, skip, skip2, s);
 }
 
 }  // namespace vdr

@@ -38,18 +38,12 @@ template <typename T>
 struct Src;
 template <>
 struct Src<double> {
-  static __device__ __forceinline__ const double *xx(const OpArgs &a) { return a.xx; }
-  static __device__ __forceinline__ const double *yy(const OpArgs &a) { return a.yy; }
-  static __device__ __forceinline__ const double *zz(const OpArgs &a) { return a.zz; }
   static __device__ __forceinline__ const double *vel(const OpArgs &a) { return a.f.vel; }
   static __device__ __forceinline__ const double *lam(const OpArgs &a) { return a.f.lam; }
   static __device__ __forceinline__ const double *pdec(const OpArgs &a) { return a.f.pdec; }
 };
 template <>
 struct Src<float> {
-  static __device__ __forceinline__ const float *xx(const OpArgs &a) { return a.xx32; }
-  static __device__ __forceinline__ const float *yy(const OpArgs &a) { return a.yy32; }
-  static __device__ __forceinline__ const float *zz(const OpArgs &a) { return a.zz32; }
   static __device__ __forceinline__ const float *vel(const OpArgs &a) { return a.vel32; }
   static __device__ __forceinline__ const float *lam(const OpArgs &a) { return a.lam32; }
   static __device__ __forceinline__ const float *pdec(const OpArgs &a) { return a.pdec32; }
@@ -63,17 +57,45 @@ struct Elem {
   bool robin;
 };
 
+// FP64 kernels use the node coordinates as stored.  FP32 kernels use them
+// relative to local node 1, formed in FP64 and then rounded: the Jacobian,
+// streamline length and face Jacobian depend only on coordinate
+// differences, and rounding absolute coordinates (~1) to FP32 would cost
+// ~1e-5 relative accuracy on an element of size 1/256.
 template <typename T>
-__device__ __forceinline__ void load_elem(const OpArgs &a, long p, Elem<T> &e) {
-  const T *X = Src<T>::xx(a), *Y = Src<T>::yy(a), *Z = Src<T>::zz(a);
+__device__ __forceinline__ void load_coords(const OpArgs &a, long p, Elem<T> &e) {
 #pragma unroll
   for (int s = 0; s < 8; s++) {
     e.c[s] = __ldg(a.conn + (size_t)s * a.E + p);
     const int n = e.c[s] & NODE_BITS;
-    e.xe[s] = __ldg(X + n);
-    e.ye[s] = __ldg(Y + n);
-    e.ze[s] = __ldg(Z + n);
+    e.xe[s] = __ldg(a.xx + n);
+    e.ye[s] = __ldg(a.yy + n);
+    e.ze[s] = __ldg(a.zz + n);
   }
+}
+template <>
+__device__ __forceinline__ void load_coords<float>(const OpArgs &a, long p,
+                                                   Elem<float> &e) {
+  double x0 = 0.0, y0 = 0.0, z0 = 0.0;
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    e.c[s] = __ldg(a.conn + (size_t)s * a.E + p);
+    const int n = e.c[s] & NODE_BITS;
+    const double x = __ldg(a.xx + n), y = __ldg(a.yy + n), z = __ldg(a.zz + n);
+    if (s == 0) {
+      x0 = x;
+      y0 = y;
+      z0 = z;
+    }
+    e.xe[s] = (float)(x - x0);
+    e.ye[s] = (float)(y - y0);
+    e.ze[s] = (float)(z - z0);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void load_elem(const OpArgs &a, long p, Elem<T> &e) {
+  load_coords<T>(a, p, e);
   const T *V = Src<T>::vel(a);
   e.vx = __ldg(V + p);
   e.vy = __ldg(V + a.E + p);

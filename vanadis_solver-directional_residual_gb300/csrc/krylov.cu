@@ -539,7 +539,7 @@ int solve_device(Handle &h, int method, const double *b, double *x,
   // One graph per method; its kernels only see handle-owned buffers plus
   // b and x, which are part of the key.
   const int K = h.opt.iters_per_graph > 0 ? h.opt.iters_per_graph : 8;
-  const int slot = method & 1;
+  const int slot = (method & 1) | (h.apply_fp32 ? 2 : 0);
   const void *key = (const void *)((uintptr_t)b ^ ((uintptr_t)x << 1) ^
                                    ((uintptr_t)h.work << 2) ^ (uintptr_t)K ^
                                    ((uintptr_t)h.apply_mode << 8) ^
@@ -598,6 +598,88 @@ int solve_device(Handle &h, int method, const double *b, double *x,
   h.last.breakdown = status == VDR_BREAKDOWN ? fin.reason : 0;
   if (iter) *iter = fin.iter;
   if (err) *err = fin.err;
+  return status;
+}
+
+namespace {
+// r = b - r (r holds A x); out = ||r|| / ||b||.
+__global__ void __launch_bounds__(RED_THREADS) k_residual(Vec a, double *r,
+                                                          double *out) {
+  double v[2] = {0.0, 0.0};
+  double bv[U], av[U];
+  VLOOP(bv[u] = ok ? a.b[i] : 0.0; av[u] = ok ? r[i] : 0.0;,
+        const double ri = bv[u] - av[u];
+        r[i] = ri;
+        v[0] += ri * ri;
+        v[1] += bv[u] * bv[u];)
+  double o[2];
+  if (grid_sum<2>(v, a.partials, &a.st->ticket, o))
+    *out = o[1] > 0.0 ? sqrt(o[0]) / sqrt(o[1]) : 0.0;
+}
+
+// x += d
+__global__ void __launch_bounds__(RED_THREADS) k_axpy1(Vec a, const double *d) {
+  double xv[U], dv[U];
+  VLOOP(xv[u] = ok ? a.x[i] : 0.0; dv[u] = ok ? d[i] : 0.0;,
+        a.x[i] = xv[u] + dv[u];)
+}
+}  // namespace
+
+// Iterative refinement: the residual r = b - A x and the update x += d are
+// FP64 (FP64 operator); each correction d solves A32 d = r with the FP32
+// operator to inner_tol relative to ||r||.
+int solve_mixed_device(Handle &h, int method, const double *b, double *x,
+                       double tol, double inner_tol, int max_outer,
+                       int inner_itmax, MixedStats *ms) {
+  cudaError_t e = ensure_solver_workspace(h, 11);
+  if (e) return cuda_fail(e, "solver workspace");
+  cudaStream_t s = h.stream;
+  double *r = h.work + 8 * (size_t)h.N;
+  double *d = h.work + 9 * (size_t)h.N;
+  double *scal = h.work + 10 * (size_t)h.N;  // one double used
+  Vec a = make_vec(h, b, x);
+  const int g = red_grid(h.N);
+  MixedStats st;
+  int status = VDR_NOT_CONVERGED;
+  if ((e = launch_mask_vec(x, h.mask, h.N, s))) return cuda_fail(e, "mask x");
+  for (int outer = 0; outer <= max_outer; outer++) {
+    h.apply_fp32 = false;
+    if ((e = cudaMemsetAsync(r, 0, sizeof(double) * h.N, s)) ||
+        (e = launch_apply(h, false, x, r, nullptr, nullptr, s)))
+      return cuda_fail(e, "outer residual");
+    k_residual<<<g, RED_THREADS, 0, s>>>(a, r, scal);
+    count_launches(1);
+    double rel = 0.0;
+    if ((e = cudaMemcpyAsync(&rel, scal, sizeof(double), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+      return cuda_fail(e, "outer residual");
+    st.err = rel;
+    if (rel <= tol) {
+      status = VDR_OK;
+      break;
+    }
+    if (!(rel == rel)) {
+      status = VDR_BREAKDOWN;
+      break;
+    }
+    if (outer == max_outer) break;
+    st.outer = outer + 1;
+    if ((e = cudaMemsetAsync(d, 0, sizeof(double) * h.N, s)))
+      return cuda_fail(e, "memset");
+    h.apply_fp32 = true;
+    int it = 0;
+    double ierr = 0.0;
+    const int ist = solve_device(h, method, r, d, inner_tol, inner_itmax, &it, &ierr);
+    h.apply_fp32 = false;
+    if (ist == VDR_CUDA_ERROR || ist == VDR_BAD_ARGUMENT) return ist;
+    st.inner += it;
+    k_axpy1<<<g, RED_THREADS, 0, s>>>(a, d);
+    count_launches(1);
+    if ((e = cudaGetLastError())) return cuda_fail(e, "update");
+  }
+  if (ms) *ms = st;
+  h.last.iterations = st.inner;
+  h.last.status = status;
   return status;
 }
 

@@ -63,6 +63,7 @@ struct Handle {
   vdr_options opt{};
   int scatter = VDR_SCATTER_ATOMIC;
   int apply_mode = VDR_APPLY_STORED;
+  bool apply_fp32 = false;  // operator applies use the FP32 operator
 
   // geometry / topology (device, storage order)
   double *xx = nullptr, *yy = nullptr, *zz = nullptr;
@@ -159,6 +160,14 @@ cudaError_t launch_bc_to_mask(const int *bc, unsigned char *mask, int N,
 // ---- solvers (krylov.cu) ----
 int solve_device(Handle &h, int method, const double *b, double *x,
                  double tol, int itmax, int *iter, double *err);
+// FP64 iterative refinement around an inner solve with the FP32 operator.
+struct MixedStats {
+  int outer = 0, inner = 0;
+  double err = 0.0;
+};
+int solve_mixed_device(Handle &h, int method, const double *b, double *x,
+                       double tol, double inner_tol, int max_outer,
+                       int inner_itmax, MixedStats *ms);
 cudaError_t ensure_solver_workspace(Handle &h, int nvec);
 
 // ---- errors ----

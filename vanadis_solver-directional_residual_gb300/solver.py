@@ -162,6 +162,11 @@ class Solver:
                                                      int(transpose)),
                 "vdr_apply_accumulate_device")
 
+    def apply32_device(self, x, y, transpose=False):
+        """y = P A32 P x with the FP32 operator."""
+        L.check(self.lib.vdr_apply32_device(self.h, _ptr(x), _ptr(y),
+                                            int(transpose)), "vdr_apply32_device")
+
     def assemble_rhs_device(self, b, cf=1.0, rM=0.0, t_old=None):
         L.check(self.lib.vdr_assemble_rhs_device(self.h, float(cf), float(rM),
                                                  _ptr(t_old), _ptr(b)),
@@ -176,6 +181,22 @@ class Solver:
         L.check(st, "vdr_solve_device",
                 allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
         return it.value, err.value, st
+
+    def solve_mixed_device(self, b, x, tol=None, inner_tol=1e-5, max_outer=20,
+                           inner_itmax=1000):
+        """FP64 refinement around FP32-operator inner solves.  Returns
+        (outer corrections, inner iterations, FP64 relative residual,
+        status)."""
+        no, ni, err = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve_mixed_device(self.h, _ptr(b), _ptr(x),
+                                             float(tol), float(inner_tol),
+                                             int(max_outer), int(inner_itmax),
+                                             ctypes.byref(no), ctypes.byref(ni),
+                                             ctypes.byref(err))
+        L.check(st, "vdr_solve_mixed_device",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return no.value, ni.value, err.value, st
 
     def true_residual_device(self, b, x):
         r = ctypes.c_double()
