@@ -156,6 +156,20 @@ int vdr_solve_mixed_device(vdr_handle *h, const double *d_b, double *d_x,
                            int inner_itmax, int *outer_iters, int *inner_iters,
                            double *err);
 
+/* Device-resident time loop of the reference program (the do-while loop of
+ * VANADIS.FOR:71-86 / vanadis_full_DR_OpenMP_timing.for:59-74 around
+ * przest3d and integrate_mass_hex8): for k = 1..nsteps
+ *   b = cf*f - (H - rM*M) T      (GPU, Dirichlet rows zero)
+ *   T = A^-1 b                   (GPU solve, initial guess T, tolerance tol)
+ *   masses[k-1] = int T dOmega   (GPU, read back once at the end)
+ * with A the operator set by vdr_set_operator.  d_t holds T_0 on entry and
+ * T_nsteps on exit.  masses, iters, errs are host arrays of nsteps entries
+ * (each may be NULL).  Stops at the first solve that does not return
+ * VDR_OK and returns its status; *steps_done counts completed steps. */
+int vdr_time_steps(vdr_handle *h, int nsteps, double cf, double rM,
+                   double *d_t, double tol, int itmax, double *masses,
+                   int *iters, double *errs, int *steps_done);
+
 /* Statistics of the handle's most recent solve. */
 typedef struct vdr_solve_stats {
   int iterations;      /* Krylov iterations done */

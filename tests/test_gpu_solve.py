@@ -166,3 +166,22 @@ def test_true_residual_device(vdr, gpu_lib, systems):
         torch.cuda.synchronize()
         rel = s.true_residual_device(b, x)
     assert st == 0 and rel < 1e-9
+
+
+def test_kat_run_device_time_loop(vdr, gpu_lib):
+    """The recorded 20-step run in one call of the device-resident time loop
+    (assembly, solve and mass integral on the GPU)."""
+    torch = pytest.importorskip("torch")
+    k = load_kat()
+    prob = kat_problem(vdr)
+    dt = float(k["dt"])
+    with vdr.Solver(prob, vdr.Options(solver="bicg"), aH=2.0, aM=3.0 / dt) as s:
+        t = torch.zeros(prob.mesh.nnode, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        masses, its, errs, st, done = s.time_steps_device(
+            t, k["steps"], 3.0, 3.0 / dt, tol=k["tol"], itmax=k["itmax"])
+    assert st == 0 and done == k["steps"]
+    assert all(abs(a - b) <= 2 for a, b in zip(its, k["log"]["iterations"])), its
+    ref_m = np.array(k["log"]["masses"])
+    assert np.max(np.abs(masses - ref_m) / ref_m) < 1e-6
+    assert np.all(errs <= k["tol"])

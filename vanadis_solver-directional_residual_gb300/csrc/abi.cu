@@ -657,6 +657,68 @@ int vdr_true_residual_device(vdr_handle *H, const double *b, const double *x,
   return true_residual_device(H->h, b, x, rel);
 }
 
+int vdr_time_steps(vdr_handle *H, int nsteps, double cf, double rM,
+                   double *t, double tol, int itmax, double *masses,
+                   int *iters, double *errs, int *steps_done) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (steps_done) *steps_done = 0;
+  if (nsteps < 0 || !t || !(tol >= 0.0)) {
+    set_error("vdr_time_steps: bad arguments");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_io(H))) return st;
+  cudaError_t e;
+  double *b = H->io + (size_t)h.N;
+  double *dmass = nullptr;
+  if (masses && nsteps > 0) {
+    if ((e = cudaMalloc(&dmass, sizeof(double) * nsteps)))
+      return cuda_fail(e, "vdr_time_steps: alloc");
+  }
+  if ((e = dalloc(&H->mass_partials, 8192))) {
+    if (dmass) cudaFree(dmass);
+    return cuda_fail(e, "alloc");
+  }
+  const int method = h.opt.solver == VDR_SOLVER_BICG ? VDR_SOLVER_BICG
+                                                     : VDR_SOLVER_BICGSTAB;
+  int status = VDR_OK, done = 0;
+  for (int k = 0; k < nsteps; k++) {
+    BuildArgs rhs;
+    rhs.cf = cf;
+    rhs.rM = rM;
+    rhs.told = t;
+    rhs.b = b;
+    if ((st = build_operator(h, &rhs))) {
+      status = st;
+      break;
+    }
+    int it = 0;
+    double err = 0.0;
+    st = solve_device(h, method, b, t, tol, itmax, &it, &err);
+    if (iters) iters[k] = it;
+    if (errs) errs[k] = err;
+    if (dmass && (e = launch_mass(h, t, H->mass_partials, dmass + k, h.stream))) {
+      status = cuda_fail(e, "mass");
+      break;
+    }
+    if (st != VDR_OK) {
+      status = st;
+      break;
+    }
+    done = k + 1;
+  }
+  if (dmass) {
+    e = cudaMemcpyAsync(masses, dmass, sizeof(double) * nsteps,
+                        cudaMemcpyDeviceToHost, h.stream);
+    if (!e) e = cudaStreamSynchronize(h.stream);
+    cudaFree(dmass);
+    if (e && status == VDR_OK) status = cuda_fail(e, "masses");
+  }
+  if (steps_done) *steps_done = done;
+  return status;
+}
+
 int vdr_mass_device(vdr_handle *H, const double *c, double *mass) {
   int st = check_handle(H);
   if (st) return st;

@@ -198,6 +198,23 @@ class Solver:
                 allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
         return no.value, ni.value, err.value, st
 
+    def time_steps_device(self, t, nsteps, cf, rM, tol=None, itmax=1000):
+        """The reference's time loop on the device (vdr_time_steps): t (device
+        array) holds T_0 and returns T_nsteps.  Returns (masses, iterations,
+        residuals, status, steps_done)."""
+        masses = np.zeros(nsteps)
+        iters = np.zeros(nsteps, dtype=np.int32)
+        errs = np.zeros(nsteps)
+        done = ctypes.c_int(0)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_time_steps(self.h, int(nsteps), float(cf), float(rM),
+                                     _ptr(t), float(tol), int(itmax),
+                                     _dp(masses), _ip(iters), _dp(errs),
+                                     ctypes.byref(done))
+        L.check(st, "vdr_time_steps",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return masses, iters, errs, st, done.value
+
     def true_residual_device(self, b, x):
         r = ctypes.c_double()
         L.check(self.lib.vdr_true_residual_device(self.h, _ptr(b), _ptr(x),
