@@ -67,6 +67,15 @@ extern "C" {
                                    DR recompute kernel, kept in HBM */
 #define VDR_APPLY_MATRIX_FREE 2 /* DR terms recomputed at every apply */
 
+/* ---- element-matrix store (VDR_APPLY_STORED) ---- */
+#define VDR_STORE_AUTO 0 /* measured choice: double-float */
+#define VDR_STORE_FP64 1 /* FP64 entries, FP64 8x8 contraction */
+#define VDR_STORE_DF 2   /* each FP64 entry as an FP32 pair hi + lo (48-bit
+                            significand, same 8 bytes); the contraction runs
+                            on the FP32 pipe in double-float arithmetic.
+                            Falls back to FP64 when an entry or an input lies
+                            outside the FP32 exponent range. */
+
 /* ---- Krylov method ---- */
 #define VDR_SOLVER_BICGSTAB 0 /* Jacobi right-preconditioned BiCGStab */
 #define VDR_SOLVER_BICG 1     /* Jacobi BiCG, the reference's dbcg_simple */
@@ -78,7 +87,8 @@ typedef struct vdr_options {
   int solver;          /* VDR_SOLVER_* */
   int iters_per_graph; /* iterations per CUDA-graph launch (0 -> 8) */
   int device;          /* CUDA device ordinal */
-  int reserved[10];
+  int matrix_storage;  /* VDR_STORE_* */
+  int reserved[9];
 } vdr_options;
 
 typedef struct vdr_handle vdr_handle;

@@ -38,8 +38,9 @@ def problems(vdr):
 
 CASE_NAMES = ["const_adv_OT", "rotation_VF", "rotation_GP", "kat_VF_robin",
               "one_element", "ragged_2x1x3", "rotation_decay_robin"]
-MODES = [("stored", "atomic"), ("stored", "color"), ("matrix_free", "atomic"),
-         ("matrix_free", "color")]
+MODES = [("stored", "atomic", "df"), ("stored", "color", "df"),
+         ("stored", "atomic", "fp64"), ("stored", "color", "fp64"),
+         ("matrix_free", "atomic", "auto"), ("matrix_free", "color", "auto")]
 
 
 def oracle_bb(oracle, prob, aH, aM):
@@ -52,13 +53,14 @@ def oracle_bb(oracle, prob, aH, aM):
 
 
 @pytest.mark.parametrize("name", CASE_NAMES)
-@pytest.mark.parametrize("mode,scatter", MODES)
-def test_apply_parity(vdr, oracle, gpu_lib, problems, name, mode, scatter):
+@pytest.mark.parametrize("mode,scatter,store", MODES)
+def test_apply_parity(vdr, oracle, gpu_lib, problems, name, mode, scatter,
+                      store):
     prob = problems[name]
     aH, aM = 2.0, 0.37
     bb = oracle_bb(oracle, prob, aH, aM)
     x = np.random.default_rng(5).standard_normal(prob.mesh.nnode)
-    opts = vdr.Options(apply_mode=mode, scatter=scatter)
+    opts = vdr.Options(apply_mode=mode, scatter=scatter, matrix_storage=store)
     with vdr.Solver(prob, opts, aH=aH, aM=aM) as s:
         for tr in (False, True):
             yref, _ = oracle.matvec0(prob.mesh.iss, bb, prob.bc, x, transpose=tr)
@@ -123,3 +125,33 @@ def test_bad_connectivity_rejected_on_host(vdr, gpu_lib):
     with pytest.raises(vdr.VdrError) as ei:
         vdr.Solver(prob)
     assert ei.value.status == 4
+
+
+@pytest.mark.parametrize("scale", [1e-300, 1e-200, 1e-40, 1.0, 1e40, 1e200])
+def test_double_float_apply_any_input_scale(vdr, oracle, gpu_lib, problems,
+                                            scale):
+    """The double-float store scales each element's inputs by a power of two,
+    so the apply keeps FP64 accuracy for vectors of any magnitude, including
+    ones outside the FP32 range and mixed scales."""
+    prob = problems["rotation_VF"]
+    bb = oracle_bb(oracle, prob, 1.0, 0.0)
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal(prob.mesh.nnode) * scale
+    x[::7] *= 1e-30  # entries far below their neighbours
+    with vdr.Solver(prob, vdr.Options(matrix_storage="df")) as s:
+        for tr in (False, True):
+            yref, _ = oracle.matvec0(prob.mesh.iss, bb, prob.bc, x, transpose=tr)
+            assert rel_l2(s.apply(x, transpose=tr), yref) < TOL, (scale, tr)
+
+
+def test_double_float_store_falls_back_outside_range(vdr, oracle, gpu_lib):
+    """Operator entries beyond the pair store's exponent window (here
+    diffusivity 1e45) send the operator to the FP64 store; results still
+    match the oracle."""
+    prob = vdr.problems.rotation_shear(4, 4, 3, seed=17)
+    prob.lam[:] = 1e45
+    bb = oracle_bb(oracle, prob, 1.0, 0.0)
+    x = np.random.default_rng(7).standard_normal(prob.mesh.nnode)
+    with vdr.Solver(prob, vdr.Options(matrix_storage="df")) as s:
+        yref, _ = oracle.matvec0(prob.mesh.iss, bb, prob.bc, x)
+        assert rel_l2(s.apply(x), yref) < TOL

@@ -23,13 +23,16 @@ def systems(vdr, oracle):
 
 @pytest.mark.parametrize("name", ["const_adv_OT", "rotation_VF"])
 @pytest.mark.parametrize("solver", ["bicgstab", "bicg"])
-@pytest.mark.parametrize("mode,scatter", [("stored", "atomic"),
-                                          ("stored", "color"),
-                                          ("matrix_free", "atomic")])
-def test_solution_parity(vdr, gpu_lib, systems, name, solver, mode, scatter):
+@pytest.mark.parametrize("mode,scatter,store", [("stored", "atomic", "df"),
+                                                ("stored", "color", "df"),
+                                                ("stored", "atomic", "fp64"),
+                                                ("matrix_free", "atomic", "auto")])
+def test_solution_parity(vdr, gpu_lib, systems, name, solver, mode, scatter,
+                         store):
     prob, ref = systems[name]
     assert ref["status"] == 0
-    opts = vdr.Options(solver=solver, apply_mode=mode, scatter=scatter)
+    opts = vdr.Options(solver=solver, apply_mode=mode, scatter=scatter,
+                       matrix_storage=store)
     with vdr.Solver(prob, opts) as s:
         x, it, err, st = s.solve(ref["b"], tol=1e-13, itmax=20000)
     assert st == 0, (st, it, err)

@@ -19,13 +19,15 @@ DR_OT, DR_GP, DR_VF = 0, 1, 2
 SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOR = 0, 1, 2
 APPLY_AUTO, APPLY_STORED, APPLY_MATRIX_FREE = 0, 1, 2
 SOLVER_BICGSTAB, SOLVER_BICG = 0, 1
+STORE_AUTO, STORE_FP64, STORE_DF = 0, 1, 2
 
 
 class VdrOptions(ctypes.Structure):
     _fields_ = [("dr_variant", ctypes.c_int), ("scatter", ctypes.c_int),
                 ("apply_mode", ctypes.c_int), ("solver", ctypes.c_int),
                 ("iters_per_graph", ctypes.c_int), ("device", ctypes.c_int),
-                ("reserved", ctypes.c_int * 10)]
+                ("matrix_storage", ctypes.c_int),
+                ("reserved", ctypes.c_int * 9)]
 
 
 class VdrSolveStats(ctypes.Structure):

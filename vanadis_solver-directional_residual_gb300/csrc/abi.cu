@@ -138,21 +138,49 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
     if ((e = cudaMemsetAsync(ba.b, 0, sizeof(double) * h.N, h.stream)))
       return cuda_fail(e, "memset rhs");
   }
+  const bool stored = h.apply_mode == VDR_APPLY_STORED;
+  const bool df = stored && h.storage == VDR_STORE_DF;
   if (need_op) {
     if ((e = dalloc(&h.diag, h.N)) || (e = dalloc(&h.dinv, h.N)))
       return cuda_fail(e, "alloc diag");
-    const bool stored = h.apply_mode == VDR_APPLY_STORED;
-    if (stored && (e = dalloc(&h.A64, (size_t)h.E * 32)))
+    if (stored && !df && (e = dalloc(&h.A64, (size_t)h.E * 32)))
+      return cuda_fail(e, "alloc element matrices");
+    if (df && ((e = dalloc(&h.Ahi, (size_t)h.E * 16)) ||
+               (e = dalloc(&h.Alo, (size_t)h.E * 16)) || (e = dalloc(&h.flag, 1))))
       return cuda_fail(e, "alloc element matrices");
     if ((e = cudaMemsetAsync(h.diag, 0, sizeof(double) * h.N, h.stream)))
       return cuda_fail(e, "memset diag");
+    if (df && (e = cudaMemsetAsync(h.flag, 0, sizeof(int), h.stream)))
+      return cuda_fail(e, "memset flag");
     ba.aH = h.aH;
     ba.aM = h.aM;
-    ba.A64 = stored ? h.A64 : nullptr;
+    ba.A64 = (stored && !df) ? h.A64 : nullptr;
+    ba.Ahi = df ? h.Ahi : nullptr;
+    ba.Alo = df ? h.Alo : nullptr;
+    ba.bad = df ? h.flag : nullptr;
     ba.diag = h.diag;
   }
   if ((e = launch_build(op_args(h), ba, false, h.stream)))
     return cuda_fail(e, "element matrices");
+  if (need_op && df) {
+    // An entry outside the FP32 exponent range cannot be held as a pair:
+    // rebuild this operator as FP64 and keep the FP64 store for the handle.
+    int bad = 0;
+    if ((e = cudaMemcpyAsync(&bad, h.flag, sizeof(int), cudaMemcpyDeviceToHost,
+                             h.stream)) ||
+        (e = cudaStreamSynchronize(h.stream)))
+      return cuda_fail(e, "flag");
+    if (bad) {
+      h.storage = VDR_STORE_FP64;
+      if ((e = dalloc(&h.A64, (size_t)h.E * 32))) return cuda_fail(e, "alloc");
+      BuildArgs b64;
+      b64.aH = h.aH;
+      b64.aM = h.aM;
+      b64.A64 = h.A64;
+      if ((e = launch_build(op_args(h), b64, false, h.stream)))
+        return cuda_fail(e, "element matrices");
+    }
+  }
   if (need_op) {
     if ((e = launch_diag_fix(h.diag, h.dinv, h.mask, h.N, h.stream)))
       return cuda_fail(e, "diag");
@@ -201,6 +229,7 @@ void free_handle(Handle &h) {
   dfree(h.vel); dfree(h.lam); dfree(h.pdec); dfree(h.q);
   dfree(h.vel32); dfree(h.lam32); dfree(h.pdec32); dfree(h.robin);
   dfree(h.A64); dfree(h.A32); dfree(h.diag); dfree(h.dinv);
+  dfree(h.Ahi); dfree(h.Alo); dfree(h.flag);
   dfree(h.work); dfree(h.st); dfree(h.partials);
   if (h.h_st) cudaFreeHost(h.h_st);
   for (int k = 0; k < 4; k++)
@@ -305,6 +334,7 @@ int vdr_create(vdr_handle **out, int nnode, int nelem, const double *xx,
   h.scatter = (o.scatter == VDR_SCATTER_COLOR) ? VDR_SCATTER_COLOR : VDR_SCATTER_ATOMIC;
   h.apply_mode = (o.apply_mode == VDR_APPLY_MATRIX_FREE) ? VDR_APPLY_MATRIX_FREE
                                                          : VDR_APPLY_STORED;
+  h.storage = (o.matrix_storage == VDR_STORE_FP64) ? VDR_STORE_FP64 : VDR_STORE_DF;
   cudaError_t e;
   int st = VDR_OK;
   if ((e = cudaSetDevice(h.device)) ||
@@ -819,6 +849,7 @@ int legacy_prepare(Legacy &L, int N, int E) {
       return cuda_fail(e, "stream");
     h.scatter = VDR_SCATTER_ATOMIC;
     h.apply_mode = VDR_APPLY_STORED;
+    h.storage = VDR_STORE_FP64;
   }
   if (N > L.capN || E > L.capE) {
     dfree(h.A64); h.A64 = nullptr;

@@ -23,6 +23,7 @@
 
 #include <algorithm>
 
+#include "dfloat.cuh"
 #include "vdr_internal.h"
 
 namespace vdr {
@@ -145,6 +146,131 @@ __global__ void __launch_bounds__(256) stored_apply_f32(
   }
 }
 
+// Double-float store: entry (i,j) = hi + lo with hi in Ahi, lo in Alo, both
+// float4 [(2i + j/4)*E + p].  x is split into FP32 pairs with integer bit
+// operations; the 64-term contraction is FP32 two-products + TwoSum; each
+// output is merged to FP64 with one FP64 add.  FP64-pipe work per element
+// drops from 64 FMA to 8 adds, so the kernel is bound by HBM.
+// Elements whose gathered x leaves the FP32 exponent range (|x| >= 2^128)
+// are redone here in FP64 from the merged pairs, gather and scatter included.
+__device__ __noinline__ void df_element_fallback(
+    const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
+    const int *__restrict__ conn, int E, long p, bool trans, bool atomic,
+    const double *__restrict__ x, double *__restrict__ y) {
+  int c[8];
+  double xv[8], out[8];
+  for (int s = 0; s < 8; s++) {
+    c[s] = conn[(size_t)s * E + p];
+    xv[s] = c[s] < 0 ? 0.0 : x[c[s]];
+    out[s] = 0.0;
+  }
+  for (int i = 0; i < 8; i++)
+    for (int h = 0; h < 2; h++) {
+      const float4 vh = Ahi[(size_t)(2 * i + h) * E + p];
+      const float4 vl = Alo[(size_t)(2 * i + h) * E + p];
+      const double a[4] = {df_to_double(vh.x, vl.x), df_to_double(vh.y, vl.y),
+                           df_to_double(vh.z, vl.z), df_to_double(vh.w, vl.w)};
+      for (int k = 0; k < 4; k++) {
+        const int j = 4 * h + k;
+        if (trans)
+          out[j] += a[k] * xv[i];
+        else
+          out[i] += a[k] * xv[j];
+      }
+    }
+  for (int s = 0; s < 8; s++)
+    if (c[s] >= 0) {
+      if (atomic)
+        atomicAdd(y + c[s], out[s]);
+      else
+        y[c[s]] += out[s];
+    }
+}
+
+template <bool TRANS, bool ATOMIC>
+__global__ void __launch_bounds__(256) stored_apply_df(
+    const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
+    const int *__restrict__ conn, int E, int p0, int p1,
+    const double *__restrict__ x, double *__restrict__ y, const int *skip,
+    const int *skip2) {
+  if (skip && *(volatile const int *)skip) return;
+  if (skip2 && *(volatile const int *)skip2) return;
+  for (long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x; p < p1;
+       p += (long)gridDim.x * blockDim.x) {
+    int c[8];
+    double xv[8];
+    float xh[8], xl[8];
+    bool bad = false;
+    int emax = 0;
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      c[s] = __ldg(conn + (size_t)s * E + p);
+      xv[s] = c[s] < 0 ? 0.0 : __ldg(x + c[s]);
+      emax = max(emax, df_exp(xv[s]));
+    }
+    // x is scaled per element by 2^-shift so that its largest entry lies in
+    // [1,2); entries 2^126 below it are dropped (relative 1e-38).
+    const int shift = emax - 1023;
+#pragma unroll
+    for (int s = 0; s < 8; s++) df_split(xv[s], xh[s], xl[s], bad, shift);
+    if (bad) {
+      df_element_fallback(Ahi, Alo, conn, E, p, TRANS, ATOMIC, x, y);
+      continue;
+    }
+    double out[8];
+    if (!TRANS) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float4 h0 = __ldcs(Ahi + (size_t)(2 * i) * E + p);
+        const float4 h1 = __ldcs(Ahi + (size_t)(2 * i + 1) * E + p);
+        const float4 l0 = __ldcs(Alo + (size_t)(2 * i) * E + p);
+        const float4 l1 = __ldcs(Alo + (size_t)(2 * i + 1) * E + p);
+        DfAcc acc{0.0f, 0.0f};
+        df_fma_acc(acc, h0.x, l0.x, xh[0], xl[0]);
+        df_fma_acc(acc, h0.y, l0.y, xh[1], xl[1]);
+        df_fma_acc(acc, h0.z, l0.z, xh[2], xl[2]);
+        df_fma_acc(acc, h0.w, l0.w, xh[3], xl[3]);
+        df_fma_acc(acc, h1.x, l1.x, xh[4], xl[4]);
+        df_fma_acc(acc, h1.y, l1.y, xh[5], xl[5]);
+        df_fma_acc(acc, h1.z, l1.z, xh[6], xl[6]);
+        df_fma_acc(acc, h1.w, l1.w, xh[7], xl[7]);
+        out[i] = df_to_double(acc.s, acc.c);
+      }
+    } else {
+      DfAcc acc[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[j] = DfAcc{0.0f, 0.0f};
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float4 h0 = __ldcs(Ahi + (size_t)(2 * i) * E + p);
+        const float4 h1 = __ldcs(Ahi + (size_t)(2 * i + 1) * E + p);
+        const float4 l0 = __ldcs(Alo + (size_t)(2 * i) * E + p);
+        const float4 l1 = __ldcs(Alo + (size_t)(2 * i + 1) * E + p);
+        df_fma_acc(acc[0], h0.x, l0.x, xh[i], xl[i]);
+        df_fma_acc(acc[1], h0.y, l0.y, xh[i], xl[i]);
+        df_fma_acc(acc[2], h0.z, l0.z, xh[i], xl[i]);
+        df_fma_acc(acc[3], h0.w, l0.w, xh[i], xl[i]);
+        df_fma_acc(acc[4], h1.x, l1.x, xh[i], xl[i]);
+        df_fma_acc(acc[5], h1.y, l1.y, xh[i], xl[i]);
+        df_fma_acc(acc[6], h1.z, l1.z, xh[i], xl[i]);
+        df_fma_acc(acc[7], h1.w, l1.w, xh[i], xl[i]);
+      }
+#pragma unroll
+      for (int j = 0; j < 8; j++) out[j] = df_to_double(acc[j].s, acc[j].c);
+    }
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      if (!df_scale(out[s], shift)) out[s] = ldexp(out[s], shift);
+      if (c[s] >= 0) {
+        if (ATOMIC)
+          atomicAdd(y + c[s], out[s]);
+        else
+          y[c[s]] += out[s];
+      }
+    }
+  }
+}
+
 // Reference BB (BB[64e + 8i + j], sklad_wd) -> pair store A64[(4i+j/2)*E+e];
 // reference ISS (iss(E,8) column-major, 1-based) -> masked 0-based conn.
 __global__ void legacy_convert_kernel(const double2 *__restrict__ bb, int E,
@@ -237,7 +363,18 @@ cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
     const int grid = grid_for(p1 - p0, 256, 8);
 #define VDR_LAUNCH(K, AP)                                                     \
   K<<<grid, 256, 0, s>>>(AP, h.conn, h.E, p0, p1, x, y, skip, skip2)
-    if (!fp32) {
+    if (!fp32 && h.storage == VDR_STORE_DF) {
+#define VDR_LAUNCH_DF(K)                                                      \
+  K<<<grid, 256, 0, s>>>(h.Ahi, h.Alo, h.conn, h.E, p0, p1, x, y, skip, skip2)
+      if (transpose) {
+        if (color) VDR_LAUNCH_DF((stored_apply_df<true, false>));
+        else VDR_LAUNCH_DF((stored_apply_df<true, true>));
+      } else {
+        if (color) VDR_LAUNCH_DF((stored_apply_df<false, false>));
+        else VDR_LAUNCH_DF((stored_apply_df<false, true>));
+      }
+#undef VDR_LAUNCH_DF
+    } else if (!fp32) {
       if (transpose) {
         if (color) VDR_LAUNCH((stored_apply_f64<true, false>), h.A64);
         else VDR_LAUNCH((stored_apply_f64<true, true>), h.A64);

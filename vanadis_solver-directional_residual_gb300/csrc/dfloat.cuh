@@ -1,0 +1,115 @@
+// dfloat.cuh -- double-float (FP32 pair) arithmetic for GB300, whose FP64
+// pipe runs at 1/58 of the FP32 rate and also executes every float<->double
+// conversion.  A value is held as hi + lo with |lo| <= ulp(hi): ~48
+// significant bits (relative error <= 2^-47).  Splitting and merging use
+// integer bit operations only, never the FP64 pipe.
+//
+// Products are exact through the FMA two-product (p = a*b, e = fma(a,b,-p));
+// sums use Knuth's TwoSum (6 FP32 operations, no branch).  Published
+// algorithms: T. J. Dekker, "A floating-point technique for extending the
+// available precision", Numer. Math. 18 (1971); D. E. Knuth, TAOCP vol. 2,
+// section 4.2.2 (TwoSum).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vdr {
+
+// Biased FP64 exponent field of d (0 for zero/subnormal, 2047 inf/NaN).
+__device__ __forceinline__ int df_exp(double d) {
+  return (int)(((unsigned long long)__double_as_longlong(d) >> 52) & 0x7ffu);
+}
+
+// d * 2^-shift -> (hi, lo): hi = the scaled value truncated to 24
+// significant bits, lo = the remainder truncated to 24 bits (scaling by a
+// power of two is exact).  Scaled magnitudes below 2^-126 map to 0; at or
+// above 2^128 (and inf/NaN) set *bad and map to 0.
+__device__ __forceinline__ void df_split(double d, float &hi, float &lo,
+                                         bool &bad, int shift = 0) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ffu);
+  if (e == 2047) {
+    bad = true;
+    hi = lo = 0.0f;
+    return;
+  }
+  if (e == 0) {  // zero or subnormal: 0 (never rescaled into range)
+    hi = lo = 0.0f;
+    return;
+  }
+  const int ef = e - 896 - shift;  // float biased exponent after scaling
+  if (ef <= 0) {
+    hi = 0.0f;
+    lo = 0.0f;
+    return;
+  }
+  if (ef >= 255) {
+    bad = true;
+    hi = 0.0f;
+    lo = 0.0f;
+    return;
+  }
+  const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  hi = __uint_as_float(sign | ((unsigned)ef << 23) | (unsigned)(mant >> 29));
+  const unsigned tail = (unsigned)(mant & 0x1FFFFFFFull);  // 29 bits
+  const int msb = 31 - __clz(tail | 1u);
+  const int elo = msb + e - 948 - shift;  // biased exponent, leading tail bit
+  if (tail == 0u || elo <= 0) {
+    lo = 0.0f;
+    return;
+  }
+  const unsigned m = (msb >= 23) ? (tail >> (msb - 23)) : (tail << (23 - msb));
+  lo = __uint_as_float(sign | ((unsigned)elo << 23) | (m & 0x7fffffu));
+}
+
+// Exact float -> double by bits (zero and subnormal floats -> signed zero,
+// inf/NaN kept).
+__device__ __forceinline__ double df_f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u;
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned m = u & 0x7fffffu;
+  const unsigned ed = (e == 0u) ? 0u : ((e == 255u) ? 2047u : e + 896u);
+  const unsigned mm = (e == 0u) ? 0u : m;
+  return __hiloint2double((int)(sign | (ed << 20) | (mm >> 3)), (int)(mm << 29));
+}
+
+// d * 2^shift by exponent arithmetic; false if the result would leave the
+// normal FP64 range (the caller then uses ldexp).
+__device__ __forceinline__ bool df_scale(double &d, int shift) {
+  const long long b = __double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0) return (b & 0x7fffffffffffffffLL) == 0;  // zero: done; subnormal: ldexp
+  const int en = e + shift;
+  if (en < 1 || en > 2046) return false;
+  d = __longlong_as_double((b & ~(0x7ffLL << 52)) | ((long long)en << 52));
+  return true;
+}
+
+// hi + lo as one double: two exact conversions and one FP64 add.
+__device__ __forceinline__ double df_to_double(float hi, float lo) {
+  return df_f2d(hi) + df_f2d(lo);
+}
+
+// Accumulator s + c += (ah + al) * (xh + xl), dropping al*xl (2^-48).
+// Every operation is an explicit round-to-nearest intrinsic so that the
+// compiler cannot contract them into FMAs (that would break TwoSum).
+struct DfAcc {
+  float s, c;
+};
+__device__ __forceinline__ void df_fma_acc(DfAcc &acc, float ah, float al,
+                                           float xh, float xl) {
+  const float p = __fmul_rn(ah, xh);
+  float e = __fmaf_rn(ah, xh, -p);  // exact: ah*xh = p + e
+  e = __fmaf_rn(ah, xl, e);
+  e = __fmaf_rn(al, xh, e);
+  const float t = __fadd_rn(acc.s, p);
+  const float bp = __fsub_rn(t, acc.s);
+  const float err = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(t, bp)),
+                              __fsub_rn(p, bp));
+  acc.s = t;
+  acc.c = __fadd_rn(acc.c, __fadd_rn(err, e));
+}
+
+}  // namespace vdr

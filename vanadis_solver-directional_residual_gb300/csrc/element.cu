@@ -25,6 +25,7 @@
 
 #include <algorithm>
 
+#include "dfloat.cuh"
 #include "dr_device.cuh"
 #include "vdr_internal.h"
 
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(64) elem_build_kernel(OpArgs a, BuildArgs ba) 
     __syncwarp();
     if (!valid) continue;
     const int ci = el.c[i];
-    if (ba.A64 || ba.A32 || ba.diag) {
+    if (ba.A64 || ba.A32 || ba.Ahi || ba.diag) {
       T row[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) row[j] = aH * accH[j] + aM * accM[j];
@@ -285,6 +286,27 @@ __global__ void __launch_bounds__(64) elem_build_kernel(OpArgs a, BuildArgs ba) 
           ba.A32[(size_t)(2 * i + h) * E + p] =
               make_float4((float)row[4 * h], (float)row[4 * h + 1],
                           (float)row[4 * h + 2], (float)row[4 * h + 3]);
+      }
+      if (ba.Ahi) {
+        // The pair store holds nonzero entries in [2^-100, 2^120]; anything
+        // else sends the operator to the FP64 store.
+        bool bad = false;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int ej = df_exp((double)row[j]);
+          if (ej != 0 && (ej < 1023 - 100 || ej > 1023 + 120)) bad = true;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          float4 vh, vl;
+          df_split((double)row[4 * h], vh.x, vl.x, bad);
+          df_split((double)row[4 * h + 1], vh.y, vl.y, bad);
+          df_split((double)row[4 * h + 2], vh.z, vl.z, bad);
+          df_split((double)row[4 * h + 3], vh.w, vl.w, bad);
+          ba.Ahi[(size_t)(2 * i + h) * E + p] = vh;
+          ba.Alo[(size_t)(2 * i + h) * E + p] = vl;
+        }
+        if (bad) atomicOr(ba.bad, 1);
       }
       if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, (double)row[i]);
     }

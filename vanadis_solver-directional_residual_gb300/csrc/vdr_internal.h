@@ -64,6 +64,7 @@ struct Handle {
   int scatter = VDR_SCATTER_ATOMIC;
   int apply_mode = VDR_APPLY_STORED;
   bool apply_fp32 = false;  // operator applies use the FP32 operator
+  int storage = VDR_STORE_DF;  // element-matrix store (resolved, never AUTO)
 
   // geometry / topology (device, storage order)
   double *xx = nullptr, *yy = nullptr, *zz = nullptr;
@@ -87,6 +88,9 @@ struct Handle {
   bool op64_valid = false, op32_valid = false, diag_valid = false;
   double2 *A64 = nullptr;  // [32][E] stored element matrices (row-major pairs)
   float4 *A32 = nullptr;   // [16][E]
+  float4 *Ahi = nullptr;   // [16][E] double-float store: hi parts
+  float4 *Alo = nullptr;   // [16][E] double-float store: lo parts
+  int *flag = nullptr;     // device flag: an entry left the FP32 range
   double *diag = nullptr;  // [N] assembled diagonal, 1 on Dirichlet nodes
   double *dinv = nullptr;  // [N] 1/diag (the Jacobi preconditioner)
 
@@ -121,6 +125,8 @@ struct BuildArgs {
   double aH = 1.0, aM = 0.0;     // A_e = aH*H + aM*M
   double2 *A64 = nullptr;        // FP64 element-matrix store
   float4 *A32 = nullptr;         // FP32 element-matrix store
+  float4 *Ahi = nullptr, *Alo = nullptr;  // double-float store
+  int *bad = nullptr;            // set when an entry is outside FP32 range
   double *diag = nullptr;        // += diag(A_e)
   double cf = 1.0, rM = 0.0;     // b += cf*f - (H - rM*M) T_old
   const double *told = nullptr;

@@ -51,6 +51,7 @@ _SCATTER = {"auto": L.SCATTER_AUTO, "atomic": L.SCATTER_ATOMIC,
 _APPLY = {"auto": L.APPLY_AUTO, "stored": L.APPLY_STORED,
           "matrix_free": L.APPLY_MATRIX_FREE}
 _SOLVER = {"bicgstab": L.SOLVER_BICGSTAB, "bicg": L.SOLVER_BICG}
+_STORE = {"auto": L.STORE_AUTO, "fp64": L.STORE_FP64, "df": L.STORE_DF}
 
 
 @dataclass
@@ -61,6 +62,7 @@ class Options:
     solver: str = "bicgstab"
     iters_per_graph: int = 8
     device: int = 0
+    matrix_storage: str = "auto"
 
     def to_c(self, default_variant: int) -> L.VdrOptions:
         o = L.VdrOptions()
@@ -74,6 +76,7 @@ class Options:
         o.solver = _SOLVER[self.solver]
         o.iters_per_graph = int(self.iters_per_graph)
         o.device = int(self.device)
+        o.matrix_storage = _STORE[self.matrix_storage]
         return o
 
 
