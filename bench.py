@@ -71,7 +71,8 @@ def workload_config(a, prob):
                     % (a.nex, a.ney, a.nez, COURANT),
         "elements": prob.mesh.nelem, "nodes": prob.mesh.nnode,
         "dirichlet_nodes": int(prob.bc.sum()),
-        "apply": "stored element matrices (built on GPU each step)",
+        "apply": "stored element matrices, double-float pairs (built on GPU "
+                 "each step)",
         "scatter": a.scatter, "solver": "bicgstab", "precision": "fp64",
         "l2": "inputs larger than L2 (element matrices 4.3 GB per apply)",
     }
@@ -183,7 +184,7 @@ BUILD_FLOP_PER_ELEMENT = 10400.0
 def profile_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu
     summary (a line 'traffic_bytes_per_launch: <number>')."""
-    path = os.path.join(ROOT, "profiles", "stored_apply_f64_rotation_shear.md")
+    path = os.path.join(ROOT, "profiles", "stored_apply_df_rotation_shear.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -462,7 +463,8 @@ def run_native(a):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic,
-                         "kernel": "stored_apply_f64 (EBE apply, atomic scatter)",
+                         "kernel": "stored_apply_df (EBE apply, double-float "
+                                   "element matrices, atomic scatter)",
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "launch_ms": t_apply_ms, "peak_kind": peak_kind},
             "roofline_build": {"bound": "fp64", "achieved": build_tflops,
