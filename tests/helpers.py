@@ -62,5 +62,8 @@ def run_kat_oracle(oracle, prob, steps=20, itmax=1000):
 def rel_l2(a, b):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
-    nb = np.linalg.norm(b)
-    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+    scale = float(np.max(np.abs(b))) if b.size else 0.0
+    if not scale > 0.0 or not np.isfinite(scale):
+        scale = 1.0
+    nb = np.linalg.norm(b / scale)  # scaled: no overflow for |b| ~ 1e200
+    return float(np.linalg.norm((a - b) / scale) / (nb if nb > 0 else 1.0))

@@ -112,4 +112,42 @@ __device__ __forceinline__ void df_fma_acc(DfAcc &acc, float ah, float al,
   acc.c = __fadd_rn(acc.c, __fadd_rn(err, e));
 }
 
+// A normalized double-float value (h + l, |l| <= ulp(h)/2).
+struct Df2 {
+  float h, l;
+};
+
+// d -> Df2 (truncated split, no scaling; |d| must lie in the FP32 range).
+__device__ __forceinline__ Df2 df_from_double(double d) {
+  Df2 r;
+  bool bad = false;
+  df_split(d, r.h, r.l, bad);
+  return r;
+}
+
+// Exact product hi part plus first-order cross terms, renormalized.
+__device__ __forceinline__ Df2 df_mul(Df2 a, Df2 b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  const float s = __fadd_rn(p, e);
+  return Df2{s, __fsub_rn(e, __fsub_rn(s, p))};
+}
+
+// acc += a * b (the accumulator stays unnormalized until read).
+__device__ __forceinline__ void df_acc(DfAcc &acc, Df2 a, Df2 b) {
+  df_fma_acc(acc, a.h, a.l, b.h, b.l);
+}
+
+// acc += a.
+__device__ __forceinline__ void df_acc_add(DfAcc &acc, Df2 a) {
+  const float t = __fadd_rn(acc.s, a.h);
+  const float bp = __fsub_rn(t, acc.s);
+  const float err = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(t, bp)),
+                              __fsub_rn(a.h, bp));
+  acc.s = t;
+  acc.c = __fadd_rn(acc.c, __fadd_rn(err, a.l));
+}
+
 }  // namespace vdr

@@ -326,6 +326,153 @@ __global__ void __launch_bounds__(64) elem_build_kernel(OpArgs a, BuildArgs ba) 
   }
 }
 
+// The FP64 element build with its H/M row accumulation moved to the FP32
+// pipe.  Each lane evaluates its Gauss point in FP64 (Jacobian, inverse,
+// gradients and the DR weight with its sqrt/div/tanh) exactly as
+// elem_build_kernel<double>, splits the results into FP32 pairs with integer
+// operations, and the 8x8 rows of H and M are accumulated in double-float
+// (exact FP32 two-products + TwoSum, ~2^-46 relative), then merged to FP64.
+// On GB300 the FP64 pipe runs at 1/58 of the FP32 rate, so this removes more
+// than half of the kernel's FP64 work.
+struct BuildSmemDF {
+  Df2 g[ROWS_EPB][8][6][8];    // dN/dx, dN/dy, dN/dz, v.gradN + P N, N, W
+  Df2 d[ROWS_EPB][8][2];       // detJ, lambda*detJ
+  Df2 fnw[ROWS_EPB][4][2][8];  // face-3 points: N, W
+  Df2 fd[ROWS_EPB][4];         // alpha*detJs
+  double tab[12][4][8];
+};
+
+__global__ void __launch_bounds__(64) elem_build_df_kernel(OpArgs a, BuildArgs ba) {
+  __shared__ BuildSmemDF sm;
+  fill_shape_tables<double>(sm.tab);
+  const int lane8 = threadIdx.x & 7;
+  const int le = threadIdx.x >> 3;
+  const long E = a.E;
+  for (long base = (long)blockIdx.x * ROWS_EPB; base < E;
+       base += (long)gridDim.x * ROWS_EPB) {
+    const long pe = base + le;
+    const bool valid = pe < E;
+    const long p = valid ? pe : E - 1;
+    Elem<double> el;
+    load_elem<double>(a, p, el);
+    GPData<double> o;
+    gp_core<double>(a.variant, sm.tab[lane8][0], sm.tab[lane8][1],
+                    sm.tab[lane8][2], sm.tab[lane8][3], el.xe, el.ye, el.ze,
+                    el.lam, el.vx, el.vy, el.vz, o);
+    const double vol = group8_sum<double>(o.detj);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      sm.g[le][lane8][0][j] = df_from_double(o.gx[j]);
+      sm.g[le][lane8][1][j] = df_from_double(o.gy[j]);
+      sm.g[le][lane8][2][j] = df_from_double(o.gz[j]);
+      sm.g[le][lane8][3][j] = df_from_double(
+          (el.vx * o.gx[j] + el.vy * o.gy[j] + el.vz * o.gz[j]) + el.pdec * o.n[j]);
+      sm.g[le][lane8][4][j] = df_from_double(o.n[j]);
+      sm.g[le][lane8][5][j] = df_from_double(o.w[j]);
+    }
+    sm.d[le][lane8][0] = df_from_double(o.detj);
+    sm.d[le][lane8][1] = df_from_double(el.lam * o.detj);
+    if (el.robin && lane8 < 4) {
+      const double gc = VDR_GAUSS_C;
+      const double r = (lane8 & 2) ? gc : -gc;
+      const double sgc = (lane8 & 1) ? gc : -gc;
+      const double djs = face3_detjs<double>(el.xe, el.ye, el.ze, r, sgc);
+      gp_core<double>(a.variant, sm.tab[8 + lane8][0], sm.tab[8 + lane8][1],
+                      sm.tab[8 + lane8][2], sm.tab[8 + lane8][3], el.xe, el.ye,
+                      el.ze, el.lam, el.vx, el.vy, el.vz, o);
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        sm.fnw[le][lane8][0][j] = df_from_double(o.n[j]);
+        sm.fnw[le][lane8][1][j] = df_from_double(o.w[j]);
+      }
+      sm.fd[le][lane8] = df_from_double(a.f.robin_alpha * djs);
+    }
+    __syncwarp();
+    const int i = lane8;
+    DfAcc accH[8], accM[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) accH[j] = accM[j] = DfAcc{0.0f, 0.0f};
+    DfAcc fw{0.0f, 0.0f};
+#pragma unroll 1
+    for (int q = 0; q < 8; q++) {
+      const Df2 dj = sm.d[le][q][0];
+      const Df2 dl = sm.d[le][q][1];
+      const Df2 wd = df_mul(sm.g[le][q][5][i], dj);
+      df_acc_add(fw, wd);
+      const Df2 dgx = df_mul(dl, sm.g[le][q][0][i]);
+      const Df2 dgy = df_mul(dl, sm.g[le][q][1][i]);
+      const Df2 dgz = df_mul(dl, sm.g[le][q][2][i]);
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        df_acc(accH[j], dgx, sm.g[le][q][0][j]);
+        df_acc(accH[j], dgy, sm.g[le][q][1][j]);
+        df_acc(accH[j], dgz, sm.g[le][q][2][j]);
+        df_acc(accH[j], wd, sm.g[le][q][3][j]);
+        df_acc(accM[j], wd, sm.g[le][q][4][j]);
+      }
+    }
+    if (el.robin) {
+#pragma unroll
+      for (int f = 0; f < 4; f++) {
+        const Df2 aw = df_mul(sm.fd[le][f], sm.fnw[le][f][1][i]);
+#pragma unroll
+        for (int j = 0; j < 8; j++) df_acc(accH[j], aw, sm.fnw[le][f][0][j]);
+      }
+    }
+    __syncwarp();
+    if (!valid) continue;
+    double Hr[8], Mr[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      Hr[j] = df_to_double(accH[j].s, accH[j].c);
+      Mr[j] = df_to_double(accM[j].s, accM[j].c);
+    }
+    const int ci = el.c[i];
+    if (ba.A64 || ba.Ahi || ba.diag) {
+      double row[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) row[j] = ba.aH * Hr[j] + ba.aM * Mr[j];
+      if (ba.A64) {
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++)
+          ba.A64[(size_t)(4 * i + jj) * E + p] = make_double2(row[2 * jj], row[2 * jj + 1]);
+      }
+      if (ba.Ahi) {
+        bool bad = false;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int ej = df_exp(row[j]);
+          if (ej != 0 && (ej < 1023 - 100 || ej > 1023 + 120)) bad = true;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          float4 vh, vl;
+          df_split(row[4 * h], vh.x, vl.x, bad);
+          df_split(row[4 * h + 1], vh.y, vl.y, bad);
+          df_split(row[4 * h + 2], vh.z, vl.z, bad);
+          df_split(row[4 * h + 3], vh.w, vl.w, bad);
+          ba.Ahi[(size_t)(2 * i + h) * E + p] = vh;
+          ba.Alo[(size_t)(2 * i + h) * E + p] = vl;
+        }
+        if (bad) atomicOr(ba.bad, 1);
+      }
+      if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, row[i]);
+    }
+    if (ba.b && ci >= 0) {
+      const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
+      double val = ba.cf * ((qe / vol) * df_to_double(fw.s, fw.c));
+      if (ba.told) {
+        double ft = 0.0;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+          ft += (Hr[j] - ba.rM * Mr[j]) * __ldg(ba.told + (el.c[j] & NODE_BITS));
+        val -= ft;
+      }
+      atomicAdd(ba.b + ci, val);
+    }
+  }
+}
+
 template <typename T, bool TRANS>
 __global__ void __launch_bounds__(256) mf_apply_kernel(
     OpArgs a, T c1, T c2, const double *__restrict__ x, double *__restrict__ y,
@@ -487,8 +634,10 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
   const int grid = (int)std::min<long>(blocks_needed, (long)sm_count() * 32);
   if (fp32)
     elem_build_kernel<float><<<grid, 64, 0, s>>>(a, ba);
-  else
+  else if (ba.exact_fp64)
     elem_build_kernel<double><<<grid, 64, 0, s>>>(a, ba);
+  else
+    elem_build_df_kernel<<<grid, 64, 0, s>>>(a, ba);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -131,6 +131,7 @@ struct BuildArgs {
   double cf = 1.0, rM = 0.0;     // b += cf*f - (H - rM*M) T_old
   const double *told = nullptr;
   double *b = nullptr;
+  bool exact_fp64 = false;  // H/M rows accumulated in FP64, not double-float
 };
 
 // ---- launchers (element.cu) ----
