@@ -129,57 +129,53 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
   cudaError_t e;
   const bool need_op = !(h.op64_valid && h.diag_valid);
   if (!need_op && !rhs) return VDR_OK;
-  BuildArgs ba;
-  if (rhs) {
-    ba.cf = rhs->cf;
-    ba.rM = rhs->rM;
-    ba.told = rhs->told;
-    ba.b = rhs->b;
-    if ((e = cudaMemsetAsync(ba.b, 0, sizeof(double) * h.N, h.stream)))
-      return cuda_fail(e, "memset rhs");
-  }
   const bool stored = h.apply_mode == VDR_APPLY_STORED;
-  const bool df = stored && h.storage == VDR_STORE_DF;
-  if (need_op) {
-    if ((e = dalloc(&h.diag, h.N)) || (e = dalloc(&h.dinv, h.N)))
-      return cuda_fail(e, "alloc diag");
-    if (stored && !df && (e = dalloc(&h.A64, (size_t)h.E * 32)))
-      return cuda_fail(e, "alloc element matrices");
-    if (df && ((e = dalloc(&h.Ahi, (size_t)h.E * 16)) ||
-               (e = dalloc(&h.Alo, (size_t)h.E * 16)) || (e = dalloc(&h.flag, 1))))
-      return cuda_fail(e, "alloc element matrices");
-    if ((e = cudaMemsetAsync(h.diag, 0, sizeof(double) * h.N, h.stream)))
-      return cuda_fail(e, "memset diag");
-    if (df && (e = cudaMemsetAsync(h.flag, 0, sizeof(int), h.stream)))
+  if ((e = dalloc(&h.flag, 1))) return cuda_fail(e, "alloc flag");
+  if (need_op && ((e = dalloc(&h.diag, h.N)) || (e = dalloc(&h.dinv, h.N))))
+    return cuda_fail(e, "alloc diag");
+  // The H/M rows are accumulated in double-float unless a value left the
+  // pairs' safe window (flag bit 2: redo with FP64 rows), and the store is
+  // double-float unless an entry left the store window (bit 1: FP64 store).
+  for (int attempt = 0; attempt < 3; attempt++) {
+    const bool df = stored && h.storage == VDR_STORE_DF;
+    BuildArgs ba;
+    ba.exact_fp64 = h.exact_build;
+    ba.bad = h.flag;
+    if (rhs) {
+      ba.cf = rhs->cf;
+      ba.rM = rhs->rM;
+      ba.told = rhs->told;
+      ba.b = rhs->b;
+      if ((e = cudaMemsetAsync(ba.b, 0, sizeof(double) * h.N, h.stream)))
+        return cuda_fail(e, "memset rhs");
+    }
+    if (need_op) {
+      if (stored && !df && (e = dalloc(&h.A64, (size_t)h.E * 32)))
+        return cuda_fail(e, "alloc element matrices");
+      if (df && ((e = dalloc(&h.Ahi, (size_t)h.E * 16)) ||
+                 (e = dalloc(&h.Alo, (size_t)h.E * 16))))
+        return cuda_fail(e, "alloc element matrices");
+      if ((e = cudaMemsetAsync(h.diag, 0, sizeof(double) * h.N, h.stream)))
+        return cuda_fail(e, "memset diag");
+      ba.aH = h.aH;
+      ba.aM = h.aM;
+      ba.A64 = (stored && !df) ? h.A64 : nullptr;
+      ba.Ahi = df ? h.Ahi : nullptr;
+      ba.Alo = df ? h.Alo : nullptr;
+      ba.diag = h.diag;
+    }
+    if ((e = cudaMemsetAsync(h.flag, 0, sizeof(int), h.stream)))
       return cuda_fail(e, "memset flag");
-    ba.aH = h.aH;
-    ba.aM = h.aM;
-    ba.A64 = (stored && !df) ? h.A64 : nullptr;
-    ba.Ahi = df ? h.Ahi : nullptr;
-    ba.Alo = df ? h.Alo : nullptr;
-    ba.bad = df ? h.flag : nullptr;
-    ba.diag = h.diag;
-  }
-  if ((e = launch_build(op_args(h), ba, false, h.stream)))
-    return cuda_fail(e, "element matrices");
-  if (need_op && df) {
-    // An entry outside the FP32 exponent range cannot be held as a pair:
-    // rebuild this operator as FP64 and keep the FP64 store for the handle.
+    if ((e = launch_build(op_args(h), ba, false, h.stream)))
+      return cuda_fail(e, "element matrices");
     int bad = 0;
     if ((e = cudaMemcpyAsync(&bad, h.flag, sizeof(int), cudaMemcpyDeviceToHost,
                              h.stream)) ||
         (e = cudaStreamSynchronize(h.stream)))
       return cuda_fail(e, "flag");
-    if (bad) {
-      h.storage = VDR_STORE_FP64;
-      if ((e = dalloc(&h.A64, (size_t)h.E * 32))) return cuda_fail(e, "alloc");
-      BuildArgs b64;
-      b64.aH = h.aH;
-      b64.aM = h.aM;
-      b64.A64 = h.A64;
-      if ((e = launch_build(op_args(h), b64, false, h.stream)))
-        return cuda_fail(e, "element matrices");
-    }
+    if (!bad) break;
+    if (bad & 2) h.exact_build = true;
+    if ((bad & 1) && df) h.storage = VDR_STORE_FP64;
   }
   if (need_op) {
     if ((e = launch_diag_fix(h.diag, h.dinv, h.mask, h.N, h.stream)))

@@ -125,6 +125,15 @@ __device__ __forceinline__ Df2 df_from_double(double d) {
   return r;
 }
 
+// d -> Df2 with a range guard: sets *bad unless d is zero or its magnitude
+// lies in [2^-60, 2^60] (so that products and sums of such values stay far
+// inside the FP32 exponent range), and for inf/NaN.
+__device__ __forceinline__ Df2 df_from_double_chk(double d, bool &bad) {
+  const int e = df_exp(d);
+  if (e != 0 && (e < 1023 - 60 || e > 1023 + 60)) bad = true;
+  return df_from_double(d);
+}
+
 // Exact product hi part plus first-order cross terms, renormalized.
 __device__ __forceinline__ Df2 df_mul(Df2 a, Df2 b) {
   const float p = __fmul_rn(a.h, b.h);

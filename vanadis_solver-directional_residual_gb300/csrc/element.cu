@@ -360,18 +360,20 @@ __global__ void __launch_bounds__(64) elem_build_df_kernel(OpArgs a, BuildArgs b
                     sm.tab[lane8][2], sm.tab[lane8][3], el.xe, el.ye, el.ze,
                     el.lam, el.vx, el.vy, el.vz, o);
     const double vol = group8_sum<double>(o.detj);
+    bool range_bad = false;  // a quantity the pairs cannot hold safely
 #pragma unroll
     for (int j = 0; j < 8; j++) {
-      sm.g[le][lane8][0][j] = df_from_double(o.gx[j]);
-      sm.g[le][lane8][1][j] = df_from_double(o.gy[j]);
-      sm.g[le][lane8][2][j] = df_from_double(o.gz[j]);
-      sm.g[le][lane8][3][j] = df_from_double(
-          (el.vx * o.gx[j] + el.vy * o.gy[j] + el.vz * o.gz[j]) + el.pdec * o.n[j]);
-      sm.g[le][lane8][4][j] = df_from_double(o.n[j]);
-      sm.g[le][lane8][5][j] = df_from_double(o.w[j]);
+      sm.g[le][lane8][0][j] = df_from_double_chk(o.gx[j], range_bad);
+      sm.g[le][lane8][1][j] = df_from_double_chk(o.gy[j], range_bad);
+      sm.g[le][lane8][2][j] = df_from_double_chk(o.gz[j], range_bad);
+      sm.g[le][lane8][3][j] = df_from_double_chk(
+          (el.vx * o.gx[j] + el.vy * o.gy[j] + el.vz * o.gz[j]) + el.pdec * o.n[j],
+          range_bad);
+      sm.g[le][lane8][4][j] = df_from_double_chk(o.n[j], range_bad);
+      sm.g[le][lane8][5][j] = df_from_double_chk(o.w[j], range_bad);
     }
-    sm.d[le][lane8][0] = df_from_double(o.detj);
-    sm.d[le][lane8][1] = df_from_double(el.lam * o.detj);
+    sm.d[le][lane8][0] = df_from_double_chk(o.detj, range_bad);
+    sm.d[le][lane8][1] = df_from_double_chk(el.lam * o.detj, range_bad);
     if (el.robin && lane8 < 4) {
       const double gc = VDR_GAUSS_C;
       const double r = (lane8 & 2) ? gc : -gc;
@@ -382,11 +384,14 @@ __global__ void __launch_bounds__(64) elem_build_df_kernel(OpArgs a, BuildArgs b
                       el.ze, el.lam, el.vx, el.vy, el.vz, o);
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        sm.fnw[le][lane8][0][j] = df_from_double(o.n[j]);
-        sm.fnw[le][lane8][1][j] = df_from_double(o.w[j]);
+        sm.fnw[le][lane8][0][j] = df_from_double_chk(o.n[j], range_bad);
+        sm.fnw[le][lane8][1][j] = df_from_double_chk(o.w[j], range_bad);
       }
-      sm.fd[le][lane8] = df_from_double(a.f.robin_alpha * djs);
+      sm.fd[le][lane8] = df_from_double_chk(a.f.robin_alpha * djs, range_bad);
     }
+    // Any out-of-window value in the element: the host redoes this build
+    // with the FP64 row accumulation (bit 2 of the flag).
+    if (valid && range_bad) atomicOr(ba.bad, 2);
     __syncwarp();
     const int i = lane8;
     DfAcc accH[8], accM[8];
@@ -454,7 +459,7 @@ __global__ void __launch_bounds__(64) elem_build_df_kernel(OpArgs a, BuildArgs b
           ba.Ahi[(size_t)(2 * i + h) * E + p] = vh;
           ba.Alo[(size_t)(2 * i + h) * E + p] = vl;
         }
-        if (bad) atomicOr(ba.bad, 1);
+        if (bad) atomicOr(ba.bad, 1);  // store window (bit 1)
       }
       if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, row[i]);
     }

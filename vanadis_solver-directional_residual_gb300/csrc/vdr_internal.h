@@ -65,6 +65,7 @@ struct Handle {
   int apply_mode = VDR_APPLY_STORED;
   bool apply_fp32 = false;  // operator applies use the FP32 operator
   int storage = VDR_STORE_DF;  // element-matrix store (resolved, never AUTO)
+  bool exact_build = false;    // H/M rows in FP64 (values outside the pair window)
 
   // geometry / topology (device, storage order)
   double *xx = nullptr, *yy = nullptr, *zz = nullptr;
