@@ -180,6 +180,41 @@ int vdr_time_steps(vdr_handle *h, int nsteps, double cf, double rM,
                    double *d_t, double tol, int itmax, double *masses,
                    int *iters, double *errs, int *steps_done);
 
+/* ---- many right-hand sides with one operator ----
+ * Block arrays are N x K, node-major: X[n*K + k] (the K values of a node
+ * contiguous).  K <= VDR_MAX_BLOCK_RHS; the TF32 tensor-core paths need
+ * K = 16, 32 or 64. */
+#define VDR_MAX_BLOCK_RHS 64
+#define VDR_BLOCK_FP64 0 /* FP64 vectors, FP64-accurate (double-float) apply */
+#define VDR_BLOCK_TF32 1 /* FP32 vectors, TF32 tensor-core apply
+                            (mma.sync m16n8k8, FP32 accumulate) */
+#define VDR_BLOCK_TF32X3 2 /* FP32 vectors, split TF32 (three MMAs per
+                              product: FP32-level accuracy) */
+
+/* B[n*K + k] = cf * f(Q_k): the right-hand sides of K source fields at once.
+ * d_Q is K x E (row k = per-element source of column k, kg/s, the caller's
+ * element order).  Dirichlet rows are zero. */
+int vdr_assemble_rhs_block_device(vdr_handle *h, int K, const double *d_Q,
+                                  double cf, double *d_B);
+/* Y = P A P X for K columns at once; precision VDR_BLOCK_FP64 (double
+ * arrays, any K <= 64) or VDR_BLOCK_TF32 / VDR_BLOCK_TF32X3 (float arrays,
+ * K = 16, 32 or 64). */
+int vdr_apply_block_device(vdr_handle *h, int K, const void *d_X, void *d_Y,
+                           int precision);
+/* Solves A X = B for K columns (K = 16, 32 or 64): FP64 refinement per
+ * column (residual with the FP64-accurate operator, FP64 update) around K
+ * simultaneous FP32 Jacobi-BiCGStab inner solves with the tensor-core apply
+ * (precision VDR_BLOCK_TF32 or VDR_BLOCK_TF32X3), each to inner_tol
+ * relative to its column's residual; columns already at tol sit out.
+ * d_X holds the initial guess.  Returns VDR_OK when every column's FP64
+ * relative residual is <= tol.  errs: K host doubles (final per-column FP64
+ * residuals) or NULL.  No counterpart in the reference, which solves one
+ * right-hand side per call. */
+int vdr_solve_block_device(vdr_handle *h, int K, int precision,
+                           const double *d_B, double *d_X, double tol,
+                           double inner_tol, int max_outer, int inner_itmax,
+                           int *outer_iters, int *inner_iters, double *errs);
+
 /* Statistics of the handle's most recent solve. */
 typedef struct vdr_solve_stats {
   int iterations;      /* Krylov iterations done */

@@ -60,6 +60,10 @@ SIGNATURES = {
     "vdr_solve": (_i, [_P, _D, _D, _d, _i, _I, _D]),
     "vdr_solve_device": (_i, [_P, _P, _P, _d, _i, _I, _D]),
     "vdr_solve_mixed_device": (_i, [_P, _P, _P, _d, _d, _i, _i, _I, _I, _D]),
+    "vdr_assemble_rhs_block_device": (_i, [_P, _i, _P, _d, _P]),
+    "vdr_apply_block_device": (_i, [_P, _i, _P, _P, _i]),
+    "vdr_solve_block_device": (_i, [_P, _i, _i, _P, _P, _d, _d, _i, _i, _I,
+                                    _I, _D]),
     "vdr_true_residual_device": (_i, [_P, _P, _P, _D]),
     "vdr_time_steps": (_i, [_P, _i, _d, _d, _P, _d, _i, _D, _I, _D, _I]),
     "vdr_mass": (_i, [_P, _D, _D]),

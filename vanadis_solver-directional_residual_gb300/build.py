@@ -15,7 +15,8 @@ OBJ_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(LIB_DIR, "libvdr.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["element.cu", "apply.cu", "krylov.cu", "abi.cu", "noalloc.cu"]
+SOURCES = ["element.cu", "apply.cu", "krylov.cu", "abi.cu", "noalloc.cu",
+           "block.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-Wall", "--expt-relaxed-constexpr"]

@@ -163,6 +163,10 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
       ba.Ahi = df ? h.Ahi : nullptr;
       ba.Alo = df ? h.Alo : nullptr;
       ba.diag = h.diag;
+      if (h.want_phi) {
+        if ((e = dalloc(&h.phi, (size_t)h.E * 8))) return cuda_fail(e, "alloc phi");
+        ba.phi = h.phi;
+      }
     }
     if ((e = cudaMemsetAsync(h.flag, 0, sizeof(int), h.stream)))
       return cuda_fail(e, "memset flag");
@@ -182,6 +186,7 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
       return cuda_fail(e, "diag");
     h.op64_valid = true;
     h.diag_valid = true;
+    h.phi_valid = h.want_phi;
   }
   return VDR_OK;
 }
@@ -210,6 +215,7 @@ int ensure_operator32(Handle &h) {
 
 void invalidate(Handle &h) {
   h.op64_valid = h.op32_valid = h.diag_valid = false;
+  h.aos_valid = h.phi_valid = false;
 }
 
 int upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
@@ -226,6 +232,9 @@ void free_handle(Handle &h) {
   dfree(h.vel32); dfree(h.lam32); dfree(h.pdec32); dfree(h.robin);
   dfree(h.A64); dfree(h.A32); dfree(h.diag); dfree(h.dinv);
   dfree(h.Ahi); dfree(h.Alo); dfree(h.flag);
+  dfree(h.Aaos); dfree(h.phi); dfree(h.perm_d); dfree(h.dinv32);
+  dfree(h.bk_f); dfree(h.bk_d);
+  if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
   dfree(h.work); dfree(h.st); dfree(h.partials);
   if (h.h_st) cudaFreeHost(h.h_st);
   for (int k = 0; k < 4; k++)
@@ -399,6 +408,13 @@ int vdr_create(vdr_handle **out, int nnode, int nelem, const double *xx,
     if ((e = cudaMemsetAsync(h.mask, 0, nnode, h.stream))) {
       st = cuda_fail(e, "memset");
       break;
+    }
+    if (h.scatter == VDR_SCATTER_COLOR) {
+      if ((e = dalloc(&h.perm_d, E))) {
+        st = cuda_fail(e, "alloc");
+        break;
+      }
+      if ((st = upload(h.perm_d, h.perm.data(), sizeof(int) * E, h.stream))) break;
     }
     if (any_robin) {
       if ((e = dalloc(&h.robin, E))) {
@@ -655,6 +671,77 @@ int vdr_solve_mixed_device(vdr_handle *H, const double *b, double *x,
   if (inner_iters) *inner_iters = ms.inner;
   if (err) *err = ms.err;
   return st;
+}
+
+int vdr_assemble_rhs_block_device(vdr_handle *H, int K, const double *Q,
+                                  double cf, double *B) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (K < 1 || K > VDR_MAX_BLOCK_RHS || !Q || !B) {
+    set_error("vdr_assemble_rhs_block_device: bad arguments");
+    return VDR_BAD_ARGUMENT;
+  }
+  if (!h.phi_valid) {
+    h.want_phi = true;
+    h.op64_valid = false;
+  }
+  if ((st = ensure_operator(h))) return st;
+  cudaError_t e = cudaMemsetAsync(B, 0, sizeof(double) * h.N * (size_t)K, h.stream);
+  if (!e) e = launch_block_rhs(h, h.phi, K, Q, cf, B, h.stream);
+  return e ? cuda_fail(e, "block rhs") : VDR_OK;
+}
+
+int vdr_apply_block_device(vdr_handle *H, int K, const void *X, void *Y,
+                           int precision) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (K < 1 || K > VDR_MAX_BLOCK_RHS || !X || !Y ||
+      (precision != VDR_BLOCK_FP64 && precision != VDR_BLOCK_TF32 &&
+       precision != VDR_BLOCK_TF32X3) ||
+      (precision != VDR_BLOCK_FP64 && K != 16 && K != 32 && K != 64) ||
+      h.apply_mode != VDR_APPLY_STORED) {
+    set_error("vdr_apply_block_device: bad arguments (TF32 needs K = 16, 32 "
+              "or 64; block applies need the stored operator)");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator(h))) return st;
+  cudaError_t e;
+  if (precision != VDR_BLOCK_FP64) {
+    float4 *Aaos = nullptr;
+    if ((e = ensure_aos(h, &Aaos))) return cuda_fail(e, "block operator copy");
+    if ((e = cudaMemsetAsync(Y, 0, sizeof(float) * h.N * (size_t)K, h.stream)))
+      return cuda_fail(e, "memset");
+    if (block_apply_launches_tf32(h, K, precision == VDR_BLOCK_TF32X3,
+                                  static_cast<const float *>(X),
+                                  static_cast<float *>(Y), Aaos, nullptr,
+                                  h.stream))
+      return cuda_fail(cudaGetLastError(), "block apply");
+    return VDR_OK;
+  }
+  if ((e = cudaMemsetAsync(Y, 0, sizeof(double) * h.N * (size_t)K, h.stream)) ||
+      (e = launch_block_apply64(h, K, static_cast<const double *>(X),
+                                static_cast<double *>(Y), h.stream)))
+    return cuda_fail(e, "block apply");
+  return VDR_OK;
+}
+
+int vdr_solve_block_device(vdr_handle *H, int K, int precision,
+                           const double *B, double *X, double tol,
+                           double inner_tol, int max_outer, int inner_itmax,
+                           int *outer_iters, int *inner_iters, double *errs) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!B || !X || !(tol >= 0.0) || !(inner_tol > 0.0) || max_outer < 0 ||
+      h.apply_mode != VDR_APPLY_STORED) {
+    set_error("vdr_solve_block_device: bad arguments");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator(h))) return st;
+  return solve_block_device(h, K, precision, B, X, tol, inner_tol, max_outer,
+                            inner_itmax, outer_iters, inner_iters, errs);
 }
 
 int vdr_solve(vdr_handle *H, const double *b, double *x, double tol,

@@ -310,6 +310,7 @@ __global__ void __launch_bounds__(64) elem_build_kernel(OpArgs a, BuildArgs ba) 
       }
       if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, (double)row[i]);
     }
+    if (ba.phi) ba.phi[(size_t)i * E + p] = (double)fw / (double)vol;
     if (ba.b && ci >= 0) {
       const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
       double val = ba.cf * ((qe / (double)vol) * (double)fw);
@@ -463,6 +464,7 @@ __global__ void __launch_bounds__(64) elem_build_df_kernel(OpArgs a, BuildArgs b
       }
       if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, row[i]);
     }
+    if (ba.phi) ba.phi[(size_t)i * E + p] = df_to_double(fw.s, fw.c) / vol;
     if (ba.b && ci >= 0) {
       const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
       double val = ba.cf * ((qe / vol) * df_to_double(fw.s, fw.c));

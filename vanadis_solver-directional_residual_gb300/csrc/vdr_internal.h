@@ -111,6 +111,19 @@ struct Handle {
   size_t h_stage_bytes = 0;
 
   vdr_solve_stats last{};
+
+  // many right-hand sides (block.cu)
+  float4 *Aaos = nullptr;    // element-major FP32 copy [E][64] for the TF32 apply
+  bool aos_valid = false;
+  double *phi = nullptr;     // [8][E] source weights (1/vol) int W_i
+  bool want_phi = false, phi_valid = false;
+  int *perm_d = nullptr;     // storage position -> caller element (colour mode)
+  float *dinv32 = nullptr;
+  int bk_K = 0;
+  float *bk_f = nullptr;
+  double *bk_d = nullptr;
+  cudaGraphExec_t bk_graph = nullptr;
+  bool bk_graph_split = false;
 };
 
 // Process-wide count of kernels launched by this library (graph nodes
@@ -133,6 +146,7 @@ struct BuildArgs {
   const double *told = nullptr;
   double *b = nullptr;
   bool exact_fp64 = false;  // H/M rows accumulated in FP64, not double-float
+  double *phi = nullptr;     // [8][E] (1/vol) int W_i dOmega, per element
 };
 
 // ---- launchers (element.cu) ----
@@ -177,6 +191,21 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
                        double tol, double inner_tol, int max_outer,
                        int inner_itmax, MixedStats *ms);
 cudaError_t ensure_solver_workspace(Handle &h, int nvec);
+
+// ---- many right-hand sides (block.cu) ----
+int solve_block_device(Handle &h, int K, int precision, const double *B,
+                       double *X, double tol, double inner_tol, int max_outer,
+                       int inner_itmax, int *outer_iters, int *inner_iters,
+                       double *errs_host);
+cudaError_t launch_block_apply64(const Handle &h, int K, const double *X,
+                                 double *Y, cudaStream_t s);
+int block_apply_launches_tf32(const Handle &h, int K, bool split,
+                              const float *X, float *Y, const float4 *Aaos,
+                              const int *skip, cudaStream_t s);
+cudaError_t launch_block_rhs(const Handle &h, const double *phi, int K,
+                             const double *Q, double cf, double *B,
+                             cudaStream_t s);
+cudaError_t ensure_aos(Handle &h, float4 **out);
 
 // ---- errors ----
 void set_error(const std::string &msg);

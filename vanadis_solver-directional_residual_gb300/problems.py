@@ -246,6 +246,22 @@ def _gauss_sources(cx, cy, cz, centres, sigma, cell_volume):
     return g * cell_volume
 
 
+def random_gaussian_sources(mesh: Mesh, K: int, seed: int = 2001,
+                            cell_volume: float | None = None) -> np.ndarray:
+    """K per-element source fields (K x E), each one Gaussian blob with a
+    seeded uniform centre in the unit cube and sigma uniform in
+    [0.03, 0.1]: the right-hand sides of the batched workload."""
+    cx, cy, cz = centroids(mesh)
+    if cell_volume is None:
+        cell_volume = 1.0 / mesh.nelem
+    u = uniform(seed, 21, 4 * K).reshape(K, 4)
+    Q = np.empty((K, mesh.nelem))
+    for k in range(K):
+        Q[k] = _gauss_sources(cx, cy, cz, [tuple(u[k, :3])],
+                              [0.03 + 0.07 * u[k, 3]], cell_volume)
+    return Q
+
+
 def constant_advection(nex=32, ney=32, nez=16, seed=1001) -> Problem:
     """Small FP64 case: constant velocity (1,0.5,0.25)/|.|, diffusivity
     1e-3, Gaussian source (sigma 0.08) at (0.3,0.5,0.5), zero Dirichlet on

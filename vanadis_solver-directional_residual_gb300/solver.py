@@ -201,6 +201,42 @@ class Solver:
                 allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
         return no.value, ni.value, err.value, st
 
+    # ---- many right-hand sides: node-major N x K device arrays ----
+    BLOCK_PRECISION = {"fp64": 0, "tf32": 1, "tf32x3": 2}
+
+    def assemble_rhs_block_device(self, Q, B, cf=1.0):
+        """B (N x K float64) = cf * f(Q_k) for the K x E per-element
+        sources Q (caller's element order)."""
+        K = int(Q.shape[0])
+        L.check(self.lib.vdr_assemble_rhs_block_device(
+            self.h, K, _ptr(Q), float(cf), _ptr(B)),
+            "vdr_assemble_rhs_block_device")
+
+    def apply_block_device(self, X, Y, precision="fp64"):
+        """Y = P A P X for the K columns of X (N x K; float64 for "fp64",
+        float32 for "tf32" / "tf32x3")."""
+        K = int(X.shape[1])
+        L.check(self.lib.vdr_apply_block_device(
+            self.h, K, _ptr(X), _ptr(Y), self.BLOCK_PRECISION[precision]),
+            "vdr_apply_block_device")
+
+    def solve_block_device(self, B, X, tol=None, inner_tol=1e-3,
+                           precision="tf32x3", max_outer=30, inner_itmax=1000):
+        """FP64 refinement around K simultaneous FP32 tensor-core inner
+        solves.  Returns (outer corrections, inner iterations, per-column
+        FP64 relative residuals, status)."""
+        K = int(B.shape[1])
+        no, ni = ctypes.c_int(0), ctypes.c_int(0)
+        errs = np.zeros(K)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve_block_device(
+            self.h, K, self.BLOCK_PRECISION[precision], _ptr(B), _ptr(X),
+            float(tol), float(inner_tol), int(max_outer), int(inner_itmax),
+            ctypes.byref(no), ctypes.byref(ni), _dp(errs))
+        L.check(st, "vdr_solve_block_device",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return no.value, ni.value, errs, st
+
     def time_steps_device(self, t, nsteps, cf, rM, tol=None, itmax=1000):
         """The reference's time loop on the device (vdr_time_steps): t (device
         array) holds T_0 and returns T_nsteps.  Returns (masses, iterations,
