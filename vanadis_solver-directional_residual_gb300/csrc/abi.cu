@@ -714,7 +714,7 @@ int vdr_apply_block_device(vdr_handle *H, int K, const void *X, void *Y,
     if ((e = cudaMemsetAsync(Y, 0, sizeof(float) * h.N * (size_t)K, h.stream)))
       return cuda_fail(e, "memset");
     if (block_apply_launches_tf32(h, K, precision == VDR_BLOCK_TF32X3,
-                                  static_cast<const float *>(X),
+                                  static_cast<const float *>(X), nullptr,
                                   static_cast<float *>(Y), Aaos, nullptr,
                                   h.stream))
       return cuda_fail(cudaGetLastError(), "block apply");

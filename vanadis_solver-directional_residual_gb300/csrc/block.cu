@@ -29,7 +29,7 @@
 namespace vdr {
 namespace {
 
-constexpr int BT = 256;  // threads per block of the block-vector kernels
+constexpr int BT = 512;  // threads per block of the block-vector kernels
 constexpr unsigned FULL = 0xffffffffu;
 
 int sm_count_b() {
@@ -76,49 +76,87 @@ __global__ void aos_from_f64(const double2 *__restrict__ A64, int E,
   }
 }
 
-// K = 16 * tiles columns.  Warp per element; lane = (g = lane/4, t = lane%4)
-// in the m16n8k8 fragment layout: the MMA's M dimension is the column k
-// (16 per tile), N the element's output node i, K its input node j, so
-// D[k][i] += sum_j X[node j][k] * A[i][j].  SPLIT: each operand is split
-// into a TF32 head and a TF32 tail and three MMAs (hi.hi + hi.lo + lo.hi)
-// give FP32-level products; the apply is bound by memory traffic, so the
-// extra MMAs cost little.
-template <bool SPLIT>
+// K = 16 * tiles columns.  Warp per element.  The MMA's M dimension is the
+// column k (16 per tile), N the element's output node i, K its input node
+// j: D[k][i] = sum_j X[node j][k] * A[i][j].  Per tile, lane (c = lane/4,
+// q = lane%4) loads the 16 bytes X[node c][16m + 4q .. +3] (times the
+// optional per-node scale: the Jacobi preconditioner folded into the
+// gather), the warp re-reads them from shared memory in the m16n8k8 TF32
+// A-fragment layout (g = lane/4, t = lane%4), and the D fragment goes back
+// through shared memory so that lane (c, q) adds 4 contiguous columns of
+// node c with one float4 atomic.  Dirichlet nodes (negative conn) read as
+// zero and receive nothing.  SPLIT: each operand is split into a TF32 head
+// and tail and three MMAs (hi.hi + hi.lo + lo.hi) give FP32-level
+// products; the apply is bound by memory traffic, so the extra MMAs cost
+// little.
+constexpr int XS = 24;  // row stride (floats) of the X stage: no conflicts
+constexpr int DS = 20;  // row stride of the D stage
+// The next element's connectivity and operator fragment are loaded while
+// the current one is processed, and all TILES column tiles of X are
+// gathered at once, so each warp keeps several loads in flight.
+template <bool SPLIT, int TILES>
 __global__ void __launch_bounds__(256) block_apply_tf32(
-    const float *__restrict__ Aaos, const int *__restrict__ conn, int E, int K,
-    const float *__restrict__ X, float *__restrict__ Y, const int *skip) {
+    const float *__restrict__ Aaos, const int *__restrict__ conn, int E,
+    const float *__restrict__ X, const float *__restrict__ dscale,
+    float *__restrict__ Y, const int *skip) {
+  constexpr int K = 16 * TILES;
   if (skip && *(volatile const int *)skip) return;
+  __shared__ __align__(16) float xs_all[8][8 * XS];
+  __shared__ __align__(16) float ds_all[8][8 * DS];
+  float *xs = xs_all[threadIdx.x >> 5];
+  float *ds = ds_all[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  const int g = lane >> 2, t = lane & 3;
+  const int g = lane >> 2, t = lane & 3;  // fragment coordinates
+  const int c = lane >> 2, q = lane & 3;  // staging coordinates
   const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
-  const int tiles = K >> 4;
-  for (long p = warp; p < E; p += nwarps) {
-    const int cl = lane < 8 ? __ldg(conn + (size_t)lane * E + p) : 0;
-    const int na = __shfl_sync(FULL, cl, t);          // A-fragment columns
-    const int nb = __shfl_sync(FULL, cl, t + 4);
-    const int o0 = __shfl_sync(FULL, cl, 2 * t);      // output rows
-    const int o1 = __shfl_sync(FULL, cl, 2 * t + 1);
-    const float *ae = Aaos + (size_t)p * 64;
-    const float f0 = __ldg(ae + 8 * g + t), f1 = __ldg(ae + 8 * g + t + 4);
+  long p = warp;
+  int cl = 0;
+  float f0 = 0.f, f1 = 0.f;
+  if (p < E) {
+    if (lane < 8) cl = __ldg(conn + (size_t)lane * E + p);
+    f0 = __ldg(Aaos + (size_t)p * 64 + 8 * g + t);
+    f1 = __ldg(Aaos + (size_t)p * 64 + 8 * g + t + 4);
+  }
+  for (; p < E; p += nwarps) {
+    const long pn = p + nwarps;
+    int cln = 0;
+    float f0n = 0.f, f1n = 0.f;
+    if (pn < E) {
+      if (lane < 8) cln = __ldg(conn + (size_t)lane * E + pn);
+      f0n = __ldg(Aaos + (size_t)pn * 64 + 8 * g + t);
+      f1n = __ldg(Aaos + (size_t)pn * 64 + 8 * g + t + 4);
+    }
+    const int nc = __shfl_sync(FULL, cl, c);
+    float4 xv[TILES];
+#pragma unroll
+    for (int m = 0; m < TILES; m++)
+      xv[m] = nc >= 0
+          ? __ldg(reinterpret_cast<const float4 *>(X + (size_t)nc * K + 16 * m) + q)
+          : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float sc = (nc >= 0 && dscale) ? __ldg(dscale + nc) : 1.f;
     const unsigned b0 = to_tf32(f0), b1 = to_tf32(f1);
     unsigned c0 = 0u, c1 = 0u;
     if (SPLIT) {
       c0 = to_tf32(f0 - __uint_as_float(b0));
       c1 = to_tf32(f1 - __uint_as_float(b1));
     }
-    for (int m = 0; m < tiles; m++) {
-      const int k0 = 16 * m + g, k1 = k0 + 8;
+#pragma unroll
+    for (int m = 0; m < TILES; m++) {
+      float4 x4 = xv[m];
+      x4.x *= sc; x4.y *= sc; x4.z *= sc; x4.w *= sc;
+      *reinterpret_cast<float4 *>(xs + c * XS + 4 * q) = x4;
+      __syncwarp();
       float xa[4];
-      xa[0] = na < 0 ? 0.f : __ldg(X + (size_t)na * K + k0);
-      xa[1] = na < 0 ? 0.f : __ldg(X + (size_t)na * K + k1);
-      xa[2] = nb < 0 ? 0.f : __ldg(X + (size_t)nb * K + k0);
-      xa[3] = nb < 0 ? 0.f : __ldg(X + (size_t)nb * K + k1);
+      xa[0] = xs[t * XS + g];
+      xa[1] = xs[t * XS + g + 8];
+      xa[2] = xs[(t + 4) * XS + g];
+      xa[3] = xs[(t + 4) * XS + g + 8];
       unsigned ah[4], al[4];
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        ah[q] = to_tf32(xa[q]);
-        al[q] = SPLIT ? to_tf32(xa[q] - __uint_as_float(ah[q])) : 0u;
+      for (int u = 0; u < 4; u++) {
+        ah[u] = to_tf32(xa[u]);
+        al[u] = SPLIT ? to_tf32(xa[u] - __uint_as_float(ah[u])) : 0u;
       }
       float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
       if (SPLIT) {
@@ -138,15 +176,20 @@ __global__ void __launch_bounds__(256) block_apply_tf32(
           "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
           : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
           : "r"(ah[0]), "r"(ah[1]), "r"(ah[2]), "r"(ah[3]), "r"(b0), "r"(b1));
-      if (o0 >= 0) {
-        atomicAdd(Y + (size_t)o0 * K + k0, d0);
-        atomicAdd(Y + (size_t)o0 * K + k1, d2);
-      }
-      if (o1 >= 0) {
-        atomicAdd(Y + (size_t)o1 * K + k0, d1);
-        atomicAdd(Y + (size_t)o1 * K + k1, d3);
-      }
+      // D[k][i]: d0 (g, 2t), d1 (g, 2t+1), d2 (g+8, 2t), d3 (g+8, 2t+1)
+      ds[(2 * t) * DS + g] = d0;
+      ds[(2 * t + 1) * DS + g] = d1;
+      ds[(2 * t) * DS + g + 8] = d2;
+      ds[(2 * t + 1) * DS + g + 8] = d3;
+      __syncwarp();
+      if (nc >= 0)
+        atomicAdd(reinterpret_cast<float4 *>(Y + (size_t)nc * K + 16 * m) + q,
+                  *reinterpret_cast<const float4 *>(ds + c * DS + 4 * q));
+      __syncwarp();
     }
+    cl = cln;
+    f0 = f0n;
+    f1 = f1n;
   }
 }
 
@@ -296,49 +339,79 @@ struct BVec {
   double *partials;  // [q][k][block]
   const float *b, *dinv;  // dinv per node
   const unsigned char *m; // per node
-  float *x, *r, *rh, *p, *v, *ph, *s, *sh, *t;
+  float *x, *r, *rh, *p, *v, *s, *t;
+  int kshift;               // K = 1 << kshift
   const double *outer_err;  // per column FP64 residual of the refinement
   double outer_tol;         // columns already at outer_tol stay inactive
 };
 
-// Per-column block reduction: thread tid owns column tid % K (blockDim is a
-// multiple of K, grid stride keeps the column).  Returns in threads
-// tid < K the block's per-column sums of NQ quantities; then the last block
-// sums the per-block partials of each column in fixed order.
+// Per-column grid reduction: thread tid owns column tid % K (blockDim is a
+// multiple of K and the grid stride keeps the column).  Each block writes
+// its per-column sums of NQ quantities to partials[q][k][block]; the last
+// block to finish (ticket) combines them: BT/K threads per column each
+// take a strided slice of the blocks (four loads in flight), then one
+// thread per column adds the slices in fixed order -- deterministic for a
+// given grid.  Returns true in threads tid < K of the last block, with
+// out[q*K + k] the column totals.  MAX: maxima of non-negative values.
 template <int NQ, bool MAX = false>
 __device__ __forceinline__ bool col_grid_sum(double (&v)[NQ], const BVec &a,
                                              double *out /* [NQ][K] */) {
   __shared__ double sm[NQ][BT];
   __shared__ bool last;
   const int K = a.K;
-  for (int q = 0; q < NQ; q++) sm[q][threadIdx.x] = v[q];
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int q = 0; q < NQ; q++) sm[q][tid] = v[q];
   __syncthreads();
-  if (threadIdx.x < K) {
+  if (tid < K) {
+#pragma unroll
     for (int q = 0; q < NQ; q++) {
       double s = 0.0;
-      for (int r = threadIdx.x; r < BT; r += K)
-        s = MAX ? fmax(s, sm[q][r]) : s + sm[q][r];
-      a.partials[((size_t)q * K + threadIdx.x) * gridDim.x + blockIdx.x] = s;
+      for (int r = tid; r < BT; r += K) s = MAX ? fmax(s, sm[q][r]) : s + sm[q][r];
+      a.partials[((size_t)q * K + tid) * gridDim.x + blockIdx.x] = s;
     }
   }
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(&a.st->ticket, 1u) == gridDim.x - 1;
+  if (tid == 0) last = atomicAdd(&a.st->ticket, 1u) == gridDim.x - 1;
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  if (threadIdx.x < K) {
+  const int T = BT >> a.kshift;  // threads per column
+  const int k = tid & (K - 1), sub = tid >> a.kshift;
+  const int G = (int)gridDim.x;
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    const double *pp = a.partials + ((size_t)q * K + k) * G;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int b = sub;
+    for (; b + 3 * T < G; b += 4 * T) {
+      const double v0 = __ldcg(pp + b), v1 = __ldcg(pp + b + T);
+      const double v2 = __ldcg(pp + b + 2 * T), v3 = __ldcg(pp + b + 3 * T);
+      s0 = MAX ? fmax(s0, v0) : s0 + v0;
+      s1 = MAX ? fmax(s1, v1) : s1 + v1;
+      s2 = MAX ? fmax(s2, v2) : s2 + v2;
+      s3 = MAX ? fmax(s3, v3) : s3 + v3;
+    }
+    for (; b < G; b += T) {
+      const double v0 = __ldcg(pp + b);
+      s0 = MAX ? fmax(s0, v0) : s0 + v0;
+    }
+    sm[q][tid] = MAX ? fmax(fmax(s0, s1), fmax(s2, s3)) : (s0 + s1) + (s2 + s3);
+  }
+  __syncthreads();
+  if (tid < K) {
+#pragma unroll
     for (int q = 0; q < NQ; q++) {
       double s = 0.0;
-      const double *pp = a.partials + ((size_t)q * K + threadIdx.x) * gridDim.x;
-      for (unsigned b = 0; b < gridDim.x; b++)
-        s = MAX ? fmax(s, __ldcg(pp + b)) : s + __ldcg(pp + b);
-      out[q * K + threadIdx.x] = s;
+      for (int u = 0; u < T; u++)
+        s = MAX ? fmax(s, sm[q][u * K + tid]) : s + sm[q][u * K + tid];
+      out[q * K + tid] = s;
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) a.st->ticket = 0u;
-  return threadIdx.x < K;
+  if (tid == 0) a.st->ticket = 0u;
+  return tid < K;
 }
 
 // Per-thread inner-product accumulation in double-float: exact FP32
@@ -351,22 +424,42 @@ __device__ __forceinline__ double dot_val(const DfAcc &acc) {
   return df_to_double(acc.s, acc.c);
 }
 
+// Grid-stride loops over the N*K block entries, four entries per thread
+// per trip (all loads issued before use).  The stride is a multiple of K,
+// so a thread's column k = threadIdx.x % K never changes.
+#define BSTRIDE ((long)gridDim.x * blockDim.x)
 #define BLOOP(i)                                                      \
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; \
-       i += (long)gridDim.x * blockDim.x)
+       i += BSTRIDE)
+#define BLOOP4(i0) \
+  for (long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x; i0 < a.n; \
+       i0 += 4 * BSTRIDE)
 
 // r = b - r (r holds A x); rh = r; per-column norms; columns with b = 0 are
 // inactive from the start.
-__global__ void __launch_bounds__(BT) bb_start(BVec a) {
-  const int k = threadIdx.x % a.K;
+__global__ void __launch_bounds__(BT, 2) bb_start(BVec a) {
+  const int k = threadIdx.x & (a.K - 1);
   DfAcc d0{0.f, 0.f}, d1{0.f, 0.f};
-  BLOOP(i) {
-    const float bi = a.b[i];
-    const float ri = bi - a.r[i];
-    a.r[i] = ri;
-    a.rh[i] = ri;
-    dot_acc(d0, bi, bi);
-    dot_acc(d1, ri, ri);
+  BLOOP4(i0) {
+    float bv[4], rv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      const bool ok = i < a.n;
+      bv[u] = ok ? a.b[i] : 0.f;
+      rv[u] = ok ? a.r[i] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      const float ri = bv[u] - rv[u];
+      if (i < a.n) {
+        a.r[i] = ri;
+        a.rh[i] = ri;
+      }
+      dot_acc(d0, bv[u], bv[u]);
+      dot_acc(d1, ri, ri);
+    }
   }
   double v[2] = {dot_val(d0), dot_val(d1)};
   __shared__ double out[2 * 64];
@@ -398,29 +491,52 @@ __global__ void bb_finish_start(BVec a) {  // one block: any column active?
   }
 }
 
-__global__ void __launch_bounds__(BT) bb_p(BVec a) {
+// p = r + beta (p - omega v) (p = r on the first iteration); v = 0.
+__global__ void __launch_bounds__(BT, 2) bb_p(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x % a.K;
+  const int k = threadIdx.x & (a.K - 1);
   const bool act = a.c.active[k];
   const bool first = a.st->iter == 0;
   const float beta = first ? 0.f
       : (float)((a.c.rho[k] / a.c.rho_old[k]) * (a.c.alpha[k] / a.c.omega[k]));
   const float om = (float)a.c.omega[k];
-  BLOOP(i) {
-    const long node = i / a.K;
-    float pi = 0.f;
-    if (act) pi = first ? a.r[i] : a.r[i] + beta * (a.p[i] - om * a.v[i]);
-    a.p[i] = pi;
-    a.ph[i] = a.m[node] ? 0.f : pi * a.dinv[node];
-    a.v[i] = 0.f;
+  BLOOP4(i0) {
+    float rv[4], pv[4], vv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      const bool ok = i < a.n && act;
+      rv[u] = ok ? a.r[i] : 0.f;
+      pv[u] = (ok && !first) ? a.p[i] : 0.f;
+      vv[u] = (ok && !first) ? a.v[i] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      if (i < a.n) {
+        a.p[i] = first ? rv[u] : rv[u] + beta * (pv[u] - om * vv[u]);
+        a.v[i] = 0.f;
+      }
+    }
   }
 }
 
-__global__ void __launch_bounds__(BT) bb_alpha(BVec a) {
+__global__ void __launch_bounds__(BT, 2) bb_alpha(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x % a.K;
+  const int k = threadIdx.x & (a.K - 1);
   DfAcc d0{0.f, 0.f};
-  BLOOP(i) dot_acc(d0, a.rh[i], a.v[i]);
+  BLOOP4(i0) {
+    float hv[4], vv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      const bool ok = i < a.n;
+      hv[u] = ok ? a.rh[i] : 0.f;
+      vv[u] = ok ? a.v[i] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) dot_acc(d0, hv[u], vv[u]);
+  }
   double v[1] = {dot_val(d0)};
   __shared__ double out[64];
   if (col_grid_sum<1>(v, a, out)) {
@@ -437,18 +553,31 @@ __global__ void __launch_bounds__(BT) bb_alpha(BVec a) {
   }
 }
 
-__global__ void __launch_bounds__(BT) bb_s(BVec a) {
+// s = r - alpha v; t = 0; ||s|| per column.
+__global__ void __launch_bounds__(BT, 2) bb_s(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x % a.K;
+  const int k = threadIdx.x & (a.K - 1);
   const float al = a.c.active[k] ? (float)a.c.alpha[k] : 0.f;
   DfAcc d0{0.f, 0.f};
-  BLOOP(i) {
-    const long node = i / a.K;
-    const float si = a.r[i] - al * a.v[i];
-    a.s[i] = si;
-    a.sh[i] = a.m[node] ? 0.f : si * a.dinv[node];
-    a.t[i] = 0.f;
-    dot_acc(d0, si, si);
+  BLOOP4(i0) {
+    float rv[4], vv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      const bool ok = i < a.n;
+      rv[u] = ok ? a.r[i] : 0.f;
+      vv[u] = ok ? a.v[i] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      const float si = rv[u] - al * vv[u];
+      if (i < a.n) {
+        a.s[i] = si;
+        a.t[i] = 0.f;
+      }
+      dot_acc(d0, si, si);
+    }
   }
   double v[1] = {dot_val(d0)};
   __shared__ double out[64];
@@ -459,14 +588,24 @@ __global__ void __launch_bounds__(BT) bb_s(BVec a) {
   }
 }
 
-__global__ void __launch_bounds__(BT) bb_omega(BVec a) {
+__global__ void __launch_bounds__(BT, 2) bb_omega(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x % a.K;
+  const int k = threadIdx.x & (a.K - 1);
   DfAcc d0{0.f, 0.f}, d1{0.f, 0.f};
-  BLOOP(i) {
-    const float ti = a.t[i];
-    dot_acc(d0, ti, a.s[i]);
-    dot_acc(d1, ti, ti);
+  BLOOP4(i0) {
+    float tv[4], sv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      const bool ok = i < a.n;
+      tv[u] = ok ? a.t[i] : 0.f;
+      sv[u] = ok ? a.s[i] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      dot_acc(d0, tv[u], sv[u]);
+      dot_acc(d1, tv[u], tv[u]);
+    }
   }
   double v[2] = {dot_val(d0), dot_val(d1)};
   __shared__ double out[2 * 64];
@@ -482,23 +621,46 @@ __global__ void __launch_bounds__(BT) bb_omega(BVec a) {
   }
 }
 
-__global__ void __launch_bounds__(BT) bb_xr(BVec a) {
+// x += D^-1 (alpha p + omega s) (Dirichlet entries stay); r = s - omega t
+// (r = s when s already met the tolerance); norms for the next iteration.
+__global__ void __launch_bounds__(BT, 2) bb_xr(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x % a.K;
+  const int k = threadIdx.x & (a.K - 1);
   const bool act = a.c.active[k];
   const bool sc = a.c.sconv[k];
   const float al = act ? (float)a.c.alpha[k] : 0.f;
   const float om = (act && !sc) ? (float)a.c.omega[k] : 0.f;
   DfAcc d0{0.f, 0.f}, d1{0.f, 0.f};
-  BLOOP(i) {
-    if (act) {
-      a.x[i] = a.x[i] + al * a.ph[i] + om * a.sh[i];
-      const float rn = sc ? a.s[i] : a.s[i] - om * a.t[i];
-      a.r[i] = rn;
+  BLOOP4(i0) {
+    float xv[4], pv[4], sv[4], tv[4], hv[4], rv[4], dn[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      const bool ok = i < a.n;
+      const bool oa = ok && act;
+      const long node = i >> a.kshift;
+      xv[u] = oa ? a.x[i] : 0.f;
+      pv[u] = oa ? a.p[i] : 0.f;
+      sv[u] = oa ? a.s[i] : 0.f;
+      tv[u] = (oa && !sc) ? a.t[i] : 0.f;
+      rv[u] = (ok && !act) ? a.r[i] : 0.f;
+      hv[u] = ok ? a.rh[i] : 0.f;
+      dn[u] = (oa && !a.m[node]) ? a.dinv[node] : 0.f;
     }
-    const float ri = a.r[i];
-    dot_acc(d0, ri, ri);
-    dot_acc(d1, a.rh[i], ri);
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long i = i0 + u * BSTRIDE;
+      float ri = rv[u];
+      if (act) {
+        ri = sv[u] - om * tv[u];
+        if (i < a.n) {
+          a.x[i] = xv[u] + dn[u] * (al * pv[u] + om * sv[u]);
+          a.r[i] = ri;
+        }
+      }
+      dot_acc(d0, ri, ri);
+      dot_acc(d1, hv[u], ri);
+    }
   }
   double v[2] = {dot_val(d0), dot_val(d1)};
   __shared__ double out[2 * 64];
@@ -539,9 +701,9 @@ __global__ void bb_tail(BVec a) {
 
 // ------------------------------------------------ FP64 <-> FP32 block glue
 // R = B - R (R holds A X) in FP64; per-column max |R| and max |B|.
-__global__ void __launch_bounds__(BT) bo_residual(BVec a, const double *B,
+__global__ void __launch_bounds__(BT, 2) bo_residual(BVec a, const double *B,
                                                   double *R, double *mx) {
-  const int k = threadIdx.x % a.K;
+  const int k = threadIdx.x & (a.K - 1);
   double v[2] = {0.0, 0.0};
   BLOOP(i) {
     const double bi = B[i];
@@ -560,11 +722,11 @@ __global__ void __launch_bounds__(BT) bo_residual(BVec a, const double *B,
 // Per-column scale 2^e >= max |R_k| (a power of two, so scaling is exact);
 // Rf = R / scale in FP32 (values in [-1, 1]); err_k = ||R_k|| / ||B_k||
 // from the norms of the max-scaled columns (no overflow or underflow).
-__global__ void __launch_bounds__(BT) bo_scale(BVec a, const double *B,
+__global__ void __launch_bounds__(BT, 2) bo_scale(BVec a, const double *B,
                                                const double *R, float *Rf,
                                                const double *mx, double *scale,
                                                double *err_out) {
-  const int k = threadIdx.x % a.K;
+  const int k = threadIdx.x & (a.K - 1);
   const double rm = mx[k], bm = mx[a.K + k];
   int er = 0;
   if (rm > 0.0 && isfinite(rm)) frexp(rm, &er);
@@ -594,13 +756,13 @@ __global__ void bo_update(long n, int K, double *X, const float *D,
                           const double *scale) {
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long)gridDim.x * blockDim.x)
-    X[i] += (double)D[i] * scale[i % K];
+    X[i] += (double)D[i] * scale[i & (K - 1)];
 }
 
-__global__ void bo_mask(long n, int K, double *X, const unsigned char *m) {
+__global__ void bo_mask(long n, int kshift, double *X, const unsigned char *m) {
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long)gridDim.x * blockDim.x)
-    if (m[i / K]) X[i] = 0.0;
+    if (m[i >> kshift]) X[i] = 0.0;
 }
 
 __global__ void dinv_to_f32(const double *__restrict__ d, float *__restrict__ f,
@@ -619,14 +781,32 @@ int grid_n(long n, int threads, int per_sm) {
 
 // ------------------------------------------------------------ host side
 int block_apply_launches_tf32(const Handle &h, int K, bool split,
-                              const float *X, float *Y, const float4 *Aaos,
-                              const int *skip, cudaStream_t s) {
-  const int grid = grid_n((long)h.E * 32, 256, 8);
+                              const float *X, const float *dscale, float *Y,
+                              const float4 *Aaos, const int *skip,
+                              cudaStream_t s) {
   const float *A = reinterpret_cast<const float *>(Aaos);
-  if (split)
-    block_apply_tf32<true><<<grid, 256, 0, s>>>(A, h.conn, h.E, K, X, Y, skip);
-  else
-    block_apply_tf32<false><<<grid, 256, 0, s>>>(A, h.conn, h.E, K, X, Y, skip);
+#define VDR_BLOCK_APPLY(SPLIT, TILES)                                        \
+  do {                                                                       \
+    static int per_sm = 0;                                                   \
+    if (!per_sm) {                                                           \
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(                         \
+          &per_sm, block_apply_tf32<SPLIT, TILES>, 256, 0);                  \
+      if (per_sm < 1) per_sm = 1;                                            \
+    }                                                                        \
+    block_apply_tf32<SPLIT, TILES><<<grid_n((long)h.E * 32, 256, per_sm),    \
+                                     256, 0, s>>>(A, h.conn, h.E, X, dscale, \
+                                                  Y, skip);                  \
+  } while (0)
+  if (split) {
+    if (K == 16) VDR_BLOCK_APPLY(true, 1);
+    else if (K == 32) VDR_BLOCK_APPLY(true, 2);
+    else VDR_BLOCK_APPLY(true, 4);
+  } else {
+    if (K == 16) VDR_BLOCK_APPLY(false, 1);
+    else if (K == 32) VDR_BLOCK_APPLY(false, 2);
+    else VDR_BLOCK_APPLY(false, 4);
+  }
+#undef VDR_BLOCK_APPLY
   count_launches(1);
   return cudaGetLastError() == cudaSuccess ? VDR_OK : VDR_CUDA_ERROR;
 }
@@ -707,7 +887,7 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
     h.bk_K = 0;
     if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
     h.bk_graph = nullptr;
-    if ((e = cudaMalloc(&h.bk_f, sizeof(float) * 10 * (size_t)n)) ||
+    if ((e = cudaMalloc(&h.bk_f, sizeof(float) * 8 * (size_t)n)) ||
         (e = cudaMalloc(&h.bk_d, sizeof(double) * ((size_t)n + BK_COLS +
                                                    BK_PARTIALS + 8))))
       return cuda_fail(e, "block workspace");
@@ -723,6 +903,7 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
   BVec a{};
   a.n = n;
   a.K = K;
+  a.kshift = K == 16 ? 4 : (K == 32 ? 5 : 6);
   a.st = st;
   a.partials = partials;
   a.c.bnrm2 = colsd + 0 * 64;
@@ -750,16 +931,14 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
   a.rh = fv + 3 * n;
   a.p = fv + 4 * n;
   a.v = fv + 5 * n;
-  a.ph = fv + 6 * n;
-  a.s = fv + 7 * n;
-  a.sh = fv + 8 * n;
-  a.t = fv + 9 * n;
+  a.s = fv + 6 * n;
+  a.t = fv + 7 * n;
 
   dinv_to_f32<<<grid_n(h.N, 256, 8), 256, 0, s>>>(h.dinv, h.dinv32, h.N);
   count_launches(1);
-  const int gv = std::min(BK_MAX_GRID, grid_n(n, BT, 8));
+  const int gv = std::min(BK_MAX_GRID, grid_n(n, BT, 2));  // one wave
   const int gm = grid_n(n, 256, 8);
-  bo_mask<<<gm, 256, 0, s>>>(n, K, X, h.mask);
+  bo_mask<<<gm, 256, 0, s>>>(n, a.kshift, X, h.mask);
   count_launches(1);
   if ((e = cudaGetLastError())) return cuda_fail(e, "block setup");
 
@@ -773,10 +952,12 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
       return cuda_fail(e, "capture");
     for (int it = 0; it < KI; it++) {
       bb_p<<<gv, BT, 0, s>>>(a);
-      block_apply_launches_tf32(h, K, split, a.ph, a.v, Aaos, &st->done, s);
+      block_apply_launches_tf32(h, K, split, a.p, h.dinv32, a.v, Aaos,
+                                &st->done, s);
       bb_alpha<<<gv, BT, 0, s>>>(a);
       bb_s<<<gv, BT, 0, s>>>(a);
-      block_apply_launches_tf32(h, K, split, a.sh, a.t, Aaos, &st->done, s);
+      block_apply_launches_tf32(h, K, split, a.s, h.dinv32, a.t, Aaos,
+                                &st->done, s);
       bb_omega<<<gv, BT, 0, s>>>(a);
       bb_xr<<<gv, BT, 0, s>>>(a);
       bb_tail<<<1, 64, 0, s>>>(a);

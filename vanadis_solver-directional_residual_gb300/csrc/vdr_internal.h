@@ -200,8 +200,9 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
 cudaError_t launch_block_apply64(const Handle &h, int K, const double *X,
                                  double *Y, cudaStream_t s);
 int block_apply_launches_tf32(const Handle &h, int K, bool split,
-                              const float *X, float *Y, const float4 *Aaos,
-                              const int *skip, cudaStream_t s);
+                              const float *X, const float *dscale, float *Y,
+                              const float4 *Aaos, const int *skip,
+                              cudaStream_t s);
 cudaError_t launch_block_rhs(const Handle &h, const double *phi, int K,
                              const double *Q, double cf, double *B,
                              cudaStream_t s);

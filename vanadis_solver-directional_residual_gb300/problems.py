@@ -246,19 +246,21 @@ def _gauss_sources(cx, cy, cz, centres, sigma, cell_volume):
     return g * cell_volume
 
 
-def random_gaussian_sources(mesh: Mesh, K: int, seed: int = 2001,
+def random_gaussian_sources(mesh: Mesh, K: int, seed: int = 3001,
                             cell_volume: float | None = None) -> np.ndarray:
-    """K per-element source fields (K x E), each one Gaussian blob with a
-    seeded uniform centre in the unit cube and sigma uniform in
-    [0.03, 0.1]: the right-hand sides of the batched workload."""
+    """K per-element source fields (K x E): source k is one Gaussian blob,
+    seeded by seed + k, with centre uniform in [0.1, 0.9]^3 and sigma
+    uniform in [0.03, 0.1] -- the right-hand sides of the batched
+    many-right-hand-side workload."""
     cx, cy, cz = centroids(mesh)
     if cell_volume is None:
         cell_volume = 1.0 / mesh.nelem
-    u = uniform(seed, 21, 4 * K).reshape(K, 4)
     Q = np.empty((K, mesh.nelem))
     for k in range(K):
-        Q[k] = _gauss_sources(cx, cy, cz, [tuple(u[k, :3])],
-                              [0.03 + 0.07 * u[k, 3]], cell_volume)
+        u = uniform(seed + k, 21, 4)
+        centre = tuple(0.1 + 0.8 * u[:3])
+        Q[k] = _gauss_sources(cx, cy, cz, [centre], [0.03 + 0.07 * u[3]],
+                              cell_volume)
     return Q
 
 
