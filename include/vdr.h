@@ -215,6 +215,94 @@ int vdr_solve_block_device(vdr_handle *h, int K, int precision,
                            double inner_tol, int max_outer, int inner_itmax,
                            int *outer_iters, int *inner_iters, double *errs);
 
+/* ---- learned preconditioner ----
+ * A 3-level 3D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights
+ * and activations, FP32 accumulation) on the structured node grid of the
+ * handle's mesh.  Inputs: r / rms(r) and the nodal velocity and
+ * ln(lambda) - ln(1e-4) (element values averaged at the nodes); output: a
+ * nodal correction c.  As a right preconditioner
+ *     M(r) = D^-1 r + (rms(r) / dbar) c(r / rms(r)),
+ * dbar = mean assembled diagonal over free nodes, zero on Dirichlet nodes.
+ * Training pairs come from the solver's own iterates: r = b - A x_k,
+ * e = x* - x_k, target (e - D^-1 r) dbar / rms(r).  No counterpart in the
+ * reference. */
+typedef struct vdr_net vdr_net;
+/* Needs the structured numbering (the handle detected nax, nay, naz).  The
+ * network is bound to the handle (its stream, mask and operator). */
+int vdr_net_create(vdr_handle *h, unsigned long long seed, vdr_net **net);
+int vdr_net_destroy(vdr_net *net);
+int vdr_net_param_count(vdr_net *net, long long *count);
+/* FP32 master parameters / last gradients (host arrays of param_count). */
+int vdr_net_get_params(vdr_net *net, float *host);
+int vdr_net_set_params(vdr_net *net, const float *host);
+int vdr_net_get_grads(vdr_net *net, float *host);
+/* Nodal features and dbar from the handle's current fields and operator;
+ * d_feat_out (N x 4 floats, nullable) and dbar_out receive copies. */
+int vdr_net_update_features(vdr_net *net, float *d_feat_out, double *dbar_out);
+int vdr_net_set_features_device(vdr_net *net, const float *d_feat, double dbar);
+/* Training pair from an iterate x_k of the solve A x = b with converged
+ * solution x*: r = b - A x_k, e = x* - x_k (FP64, length N) ->
+ * rhat = r / rms(r), target = (e - D^-1 r) dbar / rms(r) (FP32). */
+int vdr_net_make_pair_device(vdr_net *net, const double *d_b,
+                             const double *d_xk, const double *d_xstar,
+                             float *d_rhat, float *d_target);
+/* Network output c for the normalised residual rhat (FP32, length N). */
+int vdr_net_forward_device(vdr_net *net, const float *d_rhat, float *d_out);
+/* Relative loss sum_free (c - t)^2 / sum_free t^2 and the gradients of
+ * every parameter (read them with vdr_net_get_grads). */
+int vdr_net_loss_grad_device(vdr_net *net, const float *d_rhat,
+                             const float *d_target, double *loss);
+/* Residual loss of a normalised residual rhat with the handle's current
+ * operator: z = D^-1 rhat + c / dbar, L = ||rhat - A z||^2 / ||rhat||^2 over
+ * free nodes (the quantity a minimal-residual Krylov step reduces), and the
+ * gradients of every parameter (back through A with the transpose apply). */
+int vdr_net_residual_loss_grad_device(vdr_net *net, const float *d_rhat,
+                                      double *loss);
+int vdr_net_adam_step(vdr_net *net, float lr, float beta1, float beta2,
+                      float eps);
+/* residual_loss_grad + Adam (0.9, 0.999, 1e-8). */
+int vdr_net_train_step_residual_device(vdr_net *net, const float *d_rhat,
+                                       float lr, double *loss);
+/* loss_grad + Adam (0.9, 0.999, 1e-8); loss (nullable) is the step's loss. */
+int vdr_net_train_step_device(vdr_net *net, const float *d_rhat,
+                              const float *d_target, float lr, double *loss);
+/* Jacobi post-smoothing of the preconditioner: after the network,
+ * `steps` times out += omega D^-1 (in - A out) (default 1 step, omega 1). */
+int vdr_net_set_smoothing(vdr_net *net, int steps, double omega);
+/* d_out = M(d_in). */
+int vdr_net_precondition_device(vdr_net *net, const double *d_in,
+                                double *d_out);
+/* Flexible BiCGStab (FP64) right-preconditioned by M.  A solve whose
+ * residual has not dropped 1% in stall_window iterations (0: never) or that
+ * breaks down continues with plain Jacobi-BiCGStab from its iterate
+ * (*fell_back = 1).  iter counts both phases. */
+int vdr_solve_learned_device(vdr_handle *h, vdr_net *net, const double *d_b,
+                             double *d_x, double tol, int itmax,
+                             int stall_window, int *iter, double *err,
+                             int *fell_back);
+/* Restarted GCR(restart) (1 <= restart <= 32), FP64, right-preconditioned
+ * by Jacobi or, with net, by M: the flexible minimal-residual method (M is
+ * applied to the current residual and ||r|| never increases).  With a
+ * network, a stall (no 1% residual drop in stall_window iterations) or a
+ * breakdown continues with Jacobi-BiCGStab from the iterate
+ * (*fell_back = 1). */
+int vdr_solve_gcr_device(vdr_handle *h, vdr_net *net, const double *d_b,
+                         double *d_x, double tol, int itmax, int restart,
+                         int stall_window, int *iter, double *err,
+                         int *fell_back);
+/* vdr_solve_gcr_device (no fallback) recording x after every iteration into
+ * d_hist (max_hist x N doubles); *n_hist = number recorded. */
+int vdr_solve_gcr_record_device(vdr_handle *h, vdr_net *net, const double *d_b,
+                                double *d_x, double tol, int itmax,
+                                int restart, double *d_hist, int max_hist,
+                                int *n_hist, int *iter, double *err);
+/* Jacobi-BiCGStab recording the iterate x after every iteration into d_hist
+ * (max_hist x N doubles); *n_hist = number recorded (the last entries may
+ * repeat the converged x). */
+int vdr_solve_record_device(vdr_handle *h, const double *d_b, double *d_x,
+                            double tol, int itmax, double *d_hist,
+                            int max_hist, int *n_hist, int *iter, double *err);
+
 /* Statistics of the handle's most recent solve. */
 typedef struct vdr_solve_stats {
   int iterations;      /* Krylov iterations done */
@@ -222,7 +310,8 @@ typedef struct vdr_solve_stats {
   int graph_launches;  /* CUDA-graph launches (iters_per_graph iterations each) */
   int kernel_launches; /* kernels launched by the solve, graph nodes included */
   int breakdown;       /* 0, or which quantity vanished: 1 (r0,r) 2 (r0,v)
-                          3 (t,t) 4 omega 5 non-finite residual */
+                          3 (t,t) 4 omega 5 non-finite residual; 6 the
+                          solve stalled (stall_window) */
   int reserved[3];
 } vdr_solve_stats;
 int vdr_last_solve_stats(vdr_handle *h, vdr_solve_stats *stats);

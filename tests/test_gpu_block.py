@@ -38,8 +38,12 @@ def oracle_bb(oracle, prob, aH, aM):
 
 
 def to_dev(a, dtype):
+    """Device copy, complete before returning (the library's stream does
+    not wait for torch's)."""
     import torch
-    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype, device="cuda")
+    t = torch.as_tensor(np.ascontiguousarray(a), dtype=dtype, device="cuda")
+    torch.cuda.synchronize()
+    return t
 
 
 @pytest.fixture(scope="module")

@@ -7,11 +7,12 @@ terms there.  The compute lives in ``lib/libvdr.so`` (hand-written CUDA for
 sm_103a + C++ host runtime, C ABI in ``include/vdr.h``); this package is its
 Python host binding.
 """
-from . import problems
+from . import learned, problems
 from ._lib import (VdrError, build_library, last_error, library_path,
                    load_library)
-from .solver import Options, Solver, kernel_dbcg_simple, kernel_launch_count
+from .solver import (LearnedNet, Options, Solver, kernel_dbcg_simple,
+                     kernel_launch_count)
 
-__all__ = ["problems", "Options", "Solver", "kernel_dbcg_simple",
+__all__ = ["problems", "learned", "Options", "Solver", "LearnedNet", "kernel_dbcg_simple",
            "kernel_launch_count", "VdrError",
            "build_library", "load_library", "library_path", "last_error"]

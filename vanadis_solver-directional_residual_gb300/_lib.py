@@ -43,6 +43,8 @@ _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.POINTER(ctypes.c_int)
 _i = ctypes.c_int
 _d = ctypes.c_double
+_f = ctypes.c_float
+_F = ctypes.POINTER(ctypes.c_float)
 SIGNATURES = {
     "vdr_default_options": (_i, [ctypes.POINTER(VdrOptions)]),
     "vdr_create": (_i, [ctypes.POINTER(_P), _i, _i, _D, _D, _D, _I, _I,
@@ -65,6 +67,29 @@ SIGNATURES = {
     "vdr_solve_block_device": (_i, [_P, _i, _i, _P, _P, _d, _d, _i, _i, _I,
                                     _I, _D]),
     "vdr_true_residual_device": (_i, [_P, _P, _P, _D]),
+    "vdr_net_create": (_i, [_P, ctypes.c_ulonglong, ctypes.POINTER(_P)]),
+    "vdr_net_destroy": (_i, [_P]),
+    "vdr_net_param_count": (_i, [_P, ctypes.POINTER(ctypes.c_longlong)]),
+    "vdr_net_get_params": (_i, [_P, _F]),
+    "vdr_net_set_params": (_i, [_P, _F]),
+    "vdr_net_get_grads": (_i, [_P, _F]),
+    "vdr_net_update_features": (_i, [_P, _P, _D]),
+    "vdr_net_set_features_device": (_i, [_P, _P, _d]),
+    "vdr_net_make_pair_device": (_i, [_P, _P, _P, _P, _P, _P]),
+    "vdr_net_forward_device": (_i, [_P, _P, _P]),
+    "vdr_net_loss_grad_device": (_i, [_P, _P, _P, _D]),
+    "vdr_net_adam_step": (_i, [_P, _f, _f, _f, _f]),
+    "vdr_net_residual_loss_grad_device": (_i, [_P, _P, _D]),
+    "vdr_net_train_step_residual_device": (_i, [_P, _P, _f, _D]),
+    "vdr_net_train_step_device": (_i, [_P, _P, _P, _f, _D]),
+    "vdr_net_precondition_device": (_i, [_P, _P, _P]),
+    "vdr_net_set_smoothing": (_i, [_P, _i, _d]),
+    "vdr_solve_learned_device": (_i, [_P, _P, _P, _P, _d, _i, _i, _I, _D, _I]),
+    "vdr_solve_gcr_device": (_i, [_P, _P, _P, _P, _d, _i, _i, _i, _I, _D,
+                                  _I]),
+    "vdr_solve_gcr_record_device": (_i, [_P, _P, _P, _P, _d, _i, _i, _P, _i,
+                                         _I, _I, _D]),
+    "vdr_solve_record_device": (_i, [_P, _P, _P, _d, _i, _P, _i, _I, _I, _D]),
     "vdr_time_steps": (_i, [_P, _i, _d, _d, _P, _d, _i, _D, _I, _D, _I]),
     "vdr_mass": (_i, [_P, _D, _D]),
     "vdr_mass_device": (_i, [_P, _P, _D]),

@@ -235,9 +235,11 @@ void free_handle(Handle &h) {
   dfree(h.Aaos); dfree(h.phi); dfree(h.perm_d); dfree(h.dinv32);
   dfree(h.bk_f); dfree(h.bk_d);
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
+  dfree(h.gcr_work);
+  if (h.gcr_graph) cudaGraphExecDestroy(h.gcr_graph);
   dfree(h.work); dfree(h.st); dfree(h.partials);
   if (h.h_st) cudaFreeHost(h.h_st);
-  for (int k = 0; k < 4; k++)
+  for (int k = 0; k < Handle::NGRAPH; k++)
     if (h.graph_exec[k]) cudaGraphExecDestroy(h.graph_exec[k]);
   for (int k = 0; k < 2; k++)
     if (h.ev[k]) cudaEventDestroy(h.ev[k]);
@@ -246,6 +248,9 @@ void free_handle(Handle &h) {
 }
 
 }  // namespace
+
+int prepare_operator(Handle &h) { return ensure_operator(h); }
+Handle &handle_of(vdr_handle *H) { return H->h; }
 
 void set_error(const std::string &msg) { g_err = msg; }
 
@@ -950,7 +955,7 @@ int legacy_prepare(Legacy &L, int N, int E) {
     dfree(h.st); h.st = nullptr;
     if (h.h_st) cudaFreeHost(h.h_st);
     h.h_st = nullptr;
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < Handle::NGRAPH; k++) {
       if (h.graph_exec[k]) cudaGraphExecDestroy(h.graph_exec[k]);
       h.graph_exec[k] = nullptr;
       h.graph_key[k] = nullptr;

@@ -324,6 +324,15 @@ __global__ void __launch_bounds__(RED_THREADS) bs_xr(Vec a) {
     } else if (st->iter >= st->itmax) {
       st->status = VDR_NOT_CONVERGED;
       st->done = 1;
+    } else if (st->stall_window > 0) {
+      if (st->err < 0.99 * st->best_err) {
+        st->best_err = st->err;
+        st->since_best = 0;
+      } else if (++st->since_best >= st->stall_window) {
+        st->status = VDR_NOT_CONVERGED;
+        st->reason = 6;  // stalled
+        st->done = 1;
+      }
     }
   }
 }
@@ -451,15 +460,21 @@ Vec make_vec(Handle &h, const double *b, double *x) {
   return a;
 }
 
-cudaError_t launch_iteration(Handle &h, int method, const Vec &a) {
+cudaError_t launch_iteration(Handle &h, int method, const Vec &a,
+                             const Precond *prec) {
   const int g = red_grid(h.N);
   cudaStream_t s = h.stream;
   cudaError_t e;
   if (method == VDR_SOLVER_BICGSTAB) {
     bs_p<<<g, RED_THREADS, 0, s>>>(a);
+    if (prec && (e = prec->enqueue(prec->ctx, a.p, a.ph, &h.st->done, nullptr, s)))
+      return e;
     if ((e = launch_apply(h, false, a.ph, a.v, &h.st->done, nullptr, s))) return e;
     bs_alpha<<<g, RED_THREADS, 0, s>>>(a);
     bs_s<<<g, RED_THREADS, 0, s>>>(a);
+    if (prec && (e = prec->enqueue(prec->ctx, a.s, a.sh, &h.st->done,
+                                   &h.st->sconv, s)))
+      return e;
     if ((e = launch_apply(h, false, a.sh, a.t, &h.st->done, &h.st->sconv, s))) return e;
     bs_omega<<<g, RED_THREADS, 0, s>>>(a);
     bs_xr<<<g, RED_THREADS, 0, s>>>(a);
@@ -483,7 +498,7 @@ cudaError_t ensure_solver_workspace(Handle &h, int nvec) {
     h.nwork = 0;
     if ((e = cudaMalloc(&h.work, sizeof(double) * (size_t)h.N * nvec))) return e;
     h.nwork = nvec;
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < Handle::NGRAPH; k++) {
       if (h.graph_exec[k]) cudaGraphExecDestroy(h.graph_exec[k]);
       h.graph_exec[k] = nullptr;
       h.graph_key[k] = nullptr;
@@ -503,9 +518,23 @@ cudaError_t ensure_solver_workspace(Handle &h, int nvec) {
   return cudaSuccess;
 }
 
-// Solves A x = b on device arrays b (length N) and x (in/out).
+// Kernels of one captured iteration.
+long launches_graph_nodes(Handle &h, int method, const Precond *prec) {
+  long n = (method == VDR_SOLVER_BICGSTAB ? 5 : 3) + 2 * apply_launches(h);
+  if (prec) n += 2 * prec->launches;
+  return n;
+}
+
+// Solves A x = b on device arrays b (length N) and x (in/out).  With
+// `prec`, BiCGStab is right-preconditioned by M (flexible: x is updated with
+// the preconditioned vectors actually used, so M may change between
+// applications); `stall_window` > 0 stops a solve whose residual has not
+// dropped 1% in that many iterations (status NOT_CONVERGED, reason 6);
+// `hist` (max_hist x N) receives x after every graph launch.
 int solve_device(Handle &h, int method, const double *b, double *x,
-                 double tol, int itmax, int *iter, double *err) {
+                 double tol, int itmax, int *iter, double *err,
+                 const Precond *prec, int stall_window, double *hist,
+                 int max_hist, int *n_hist) {
   cudaError_t e = ensure_solver_workspace(h, 8);
   if (e) return cuda_fail(e, "solver workspace");
   cudaStream_t s = h.stream;
@@ -518,6 +547,8 @@ int solve_device(Handle &h, int method, const double *b, double *x,
   KState init{};
   init.tol = tol;
   init.itmax = itmax;
+  init.best_err = INFINITY;
+  init.stall_window = stall_window;
   std::memcpy(&h.h_st[0], &init, sizeof(KState));
   if ((e = cudaMemcpyAsync(h.st, &h.h_st[0], sizeof(KState),
                            cudaMemcpyHostToDevice, s)))
@@ -539,11 +570,16 @@ int solve_device(Handle &h, int method, const double *b, double *x,
   // One graph per method; its kernels only see handle-owned buffers plus
   // b and x, which are part of the key.
   const int K = h.opt.iters_per_graph > 0 ? h.opt.iters_per_graph : 8;
-  const int slot = (method & 1) | (h.apply_fp32 ? 2 : 0);
+  if (prec && method != VDR_SOLVER_BICGSTAB) {
+    set_error("a preconditioner needs the BiCGStab solver");
+    return VDR_BAD_ARGUMENT;
+  }
+  const int slot = (method & 1) | (h.apply_fp32 ? 2 : 0) | (prec ? 4 : 0);
   const void *key = (const void *)((uintptr_t)b ^ ((uintptr_t)x << 1) ^
                                    ((uintptr_t)h.work << 2) ^ (uintptr_t)K ^
                                    ((uintptr_t)h.apply_mode << 8) ^
-                                   ((uintptr_t)h.scatter << 12));
+                                   ((uintptr_t)h.scatter << 12) ^
+                                   ((uintptr_t)(prec ? prec->ctx : nullptr) << 3));
   if (!h.graph_exec[slot] || h.graph_key[slot] != key) {
     if (h.graph_exec[slot]) cudaGraphExecDestroy(h.graph_exec[slot]);
     h.graph_exec[slot] = nullptr;
@@ -552,7 +588,7 @@ int solve_device(Handle &h, int method, const double *b, double *x,
       return cuda_fail(e, "begin capture");
     const long long before = launches_so_far();
     for (int k = 0; k < K; k++) {
-      e = launch_iteration(h, method, a);
+      e = launch_iteration(h, method, a, prec);
       if (e) break;
     }
     count_launches(before - launches_so_far());  // captured, not launched
@@ -564,14 +600,20 @@ int solve_device(Handle &h, int method, const double *b, double *x,
     if (e) return cuda_fail(e, "graph instantiate");
     h.graph_key[slot] = key;
   }
-  const int per_iter = (method == VDR_SOLVER_BICGSTAB ? 5 : 3) + 2 * apply_launches(h);
+  const long graph_nodes = launches_graph_nodes(h, method, prec);
 
   const int max_launches = (itmax + K - 1) / K + 1;
   int launched = 0;
   bool finished = false;
   for (int c = 0; c < max_launches && !finished; c++) {
     if ((e = cudaGraphLaunch(h.graph_exec[slot], s))) return cuda_fail(e, "graph launch");
-    count_launches((long)K * per_iter);
+    count_launches((long)K * graph_nodes);
+    if (hist && n_hist && *n_hist < max_hist) {
+      if ((e = cudaMemcpyAsync(hist + (size_t)(*n_hist) * h.N, x,
+                               sizeof(double) * h.N, cudaMemcpyDeviceToDevice, s)))
+        return cuda_fail(e, "record iterate");
+      (*n_hist)++;
+    }
     if ((e = cudaMemcpyAsync(&h.h_st[c & 1], h.st, sizeof(KState),
                              cudaMemcpyDeviceToHost, s)))
       return cuda_fail(e, "state readback");
@@ -595,7 +637,7 @@ int solve_device(Handle &h, int method, const double *b, double *x,
   h.last.status = status;
   h.last.graph_launches = launched;
   h.last.kernel_launches = (int)(launches_so_far() - launches0);
-  h.last.breakdown = status == VDR_BREAKDOWN ? fin.reason : 0;
+  h.last.breakdown = (status == VDR_BREAKDOWN || fin.reason == 6) ? fin.reason : 0;
   if (iter) *iter = fin.iter;
   if (err) *err = fin.err;
   return status;

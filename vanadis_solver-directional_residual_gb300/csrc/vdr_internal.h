@@ -19,6 +19,7 @@ constexpr int NODE_BITS = 0x7fffffff;
 // Reduction scratch: per-block partial sums of up to MAXQ quantities.
 constexpr int MAXQ = 4;
 constexpr int RED_THREADS = 256;
+constexpr int GCR_MAX_RESTART = 32;
 
 // Device-resident Krylov state.  Scalars live here so that a captured
 // iteration never needs the host; `done` gates every kernel of the graph.
@@ -27,9 +28,22 @@ struct KState {
   double rho, rho_old, alpha, omega;       // BiCGStab
   double bknum, bkden, ak;                 // BiCG
   double tol;
+  double best_err;   // lowest residual so far (stall detection)
   int iter, itmax, done, sconv, status, reason;  // reason: see vdr_solve_stats
+  int since_best, stall_window;  // iterations without a 1% gain; 0 = off
   unsigned int ticket;
   unsigned int pad2;
+};
+
+// A right preconditioner for BiCGStab beyond Jacobi: `enqueue` adds
+// (M(in) - D^-1 in) to `out`, which already holds D^-1 in (zero on
+// Dirichlet nodes).  Every kernel it enqueues returns at entry while
+// *skip or *skip2 is nonzero, so the iteration can be captured in a graph.
+struct Precond {
+  cudaError_t (*enqueue)(void *ctx, const double *in, double *out,
+                         const int *skip, const int *skip2, cudaStream_t s);
+  void *ctx;
+  int launches;  // kernels per enqueue
 };
 
 struct DeviceOp;  // forward
@@ -102,8 +116,9 @@ struct Handle {
   KState *h_st = nullptr;  // pinned mirror
   double *partials = nullptr;
   int red_blocks = 0;
-  cudaGraphExec_t graph_exec[4] = {nullptr, nullptr, nullptr, nullptr};
-  const void *graph_key[4] = {nullptr, nullptr, nullptr, nullptr};
+  static constexpr int NGRAPH = 8;
+  cudaGraphExec_t graph_exec[NGRAPH] = {};
+  const void *graph_key[NGRAPH] = {};
   cudaEvent_t ev[2] = {nullptr, nullptr};
 
   // host staging
@@ -124,6 +139,13 @@ struct Handle {
   double *bk_d = nullptr;
   cudaGraphExec_t bk_graph = nullptr;
   bool bk_graph_split = false;
+
+  // restarted GCR (gcr.cu)
+  double *gcr_work = nullptr;
+  size_t gcr_words = 0;
+  cudaGraphExec_t gcr_graph = nullptr;
+  const void *gcr_key = nullptr;
+  long gcr_cycle_launches = 0;
 };
 
 // Process-wide count of kernels launched by this library (graph nodes
@@ -181,7 +203,10 @@ cudaError_t launch_bc_to_mask(const int *bc, unsigned char *mask, int N,
 
 // ---- solvers (krylov.cu) ----
 int solve_device(Handle &h, int method, const double *b, double *x,
-                 double tol, int itmax, int *iter, double *err);
+                 double tol, int itmax, int *iter, double *err,
+                 const Precond *prec = nullptr, int stall_window = 0,
+                 double *hist = nullptr, int max_hist = 0,
+                 int *n_hist = nullptr);
 // FP64 iterative refinement around an inner solve with the FP32 operator.
 struct MixedStats {
   int outer = 0, inner = 0;
@@ -191,6 +216,17 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
                        double tol, double inner_tol, int max_outer,
                        int inner_itmax, MixedStats *ms);
 cudaError_t ensure_solver_workspace(Handle &h, int nvec);
+
+// Restarted GCR(m) with Jacobi and, if given, the preconditioner `prec`
+// (gcr.cu).
+int solve_gcr_device(Handle &h, const double *b, double *x, double tol,
+                     int itmax, int m, const Precond *prec, int stall_window,
+                     int *iter, double *err, double *hist = nullptr,
+                     int max_hist = 0, int *n_hist = nullptr);
+
+// Builds the element matrices and the Jacobi diagonal if stale (abi.cu).
+int prepare_operator(Handle &h);
+Handle &handle_of(vdr_handle *H);
 
 // ---- many right-hand sides (block.cu) ----
 int solve_block_device(Handle &h, int K, int precision, const double *B,

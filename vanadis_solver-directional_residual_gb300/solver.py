@@ -15,6 +15,8 @@ without copies.
 from __future__ import annotations
 
 import ctypes
+import functools
+import sys
 from dataclasses import dataclass
 
 import numpy as np
@@ -43,6 +45,39 @@ def _i32(a):
 
 def _ptr(t):
     return None if t is None else ctypes.c_void_p(int(t.data_ptr()))
+
+
+def _stream_order(owner):
+    """(torch current stream, the library stream as a torch stream) when
+    torch has initialised CUDA, else None.  The handle's stream is
+    non-blocking, so device arrays written by torch must be ordered before
+    a library call and torch's later work after it."""
+    torch = sys.modules.get("torch")
+    if torch is None or not torch.cuda.is_initialized():
+        return None
+    if owner._ext_stream is None:
+        owner._ext_stream = torch.cuda.ExternalStream(owner.stream())
+    cur = torch.cuda.current_stream()
+    if cur.cuda_stream == owner._ext_stream.cuda_stream:
+        return None
+    return cur, owner._ext_stream
+
+
+def _device_call(fn):
+    """Orders a device-array call between torch's current stream and the
+    library's stream (events, no host synchronisation)."""
+    @functools.wraps(fn)
+    def wrapper(self, *args, **kwargs):
+        owner = getattr(self, "solver", self)
+        so = _stream_order(owner)
+        if so:
+            so[1].wait_stream(so[0])
+        try:
+            return fn(self, *args, **kwargs)
+        finally:
+            if so:
+                so[0].wait_stream(so[1])
+    return wrapper
 
 
 _VARIANTS = {"ot": L.DR_OT, "gp": L.DR_GP, "vf": L.DR_VF}
@@ -85,6 +120,7 @@ class Solver:
 
     def __init__(self, problem, options: Options | None = None,
                  aH: float = 1.0, aM: float = 0.0):
+        self._ext_stream = None
         self.lib = L.load_library()
         self.problem = problem
         self.options = options or Options()
@@ -156,25 +192,30 @@ class Solver:
         return m.value
 
     # -- device-array calls (torch CUDA tensors or anything with data_ptr)
+    @_device_call
     def apply_device(self, x, y, transpose=False):
         L.check(self.lib.vdr_apply_device(self.h, _ptr(x), _ptr(y),
                                           int(transpose)), "vdr_apply_device")
 
+    @_device_call
     def apply_accumulate_device(self, x, y, transpose=False):
         L.check(self.lib.vdr_apply_accumulate_device(self.h, _ptr(x), _ptr(y),
                                                      int(transpose)),
                 "vdr_apply_accumulate_device")
 
+    @_device_call
     def apply32_device(self, x, y, transpose=False):
         """y = P A32 P x with the FP32 operator."""
         L.check(self.lib.vdr_apply32_device(self.h, _ptr(x), _ptr(y),
                                             int(transpose)), "vdr_apply32_device")
 
+    @_device_call
     def assemble_rhs_device(self, b, cf=1.0, rM=0.0, t_old=None):
         L.check(self.lib.vdr_assemble_rhs_device(self.h, float(cf), float(rM),
                                                  _ptr(t_old), _ptr(b)),
                 "vdr_assemble_rhs_device")
 
+    @_device_call
     def solve_device(self, b, x, tol=None, itmax=1000):
         it, err = ctypes.c_int(0), ctypes.c_double(0.0)
         tol = self.problem.tol if tol is None else tol
@@ -185,6 +226,70 @@ class Solver:
                 allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
         return it.value, err.value, st
 
+    @_device_call
+    def solve_learned_device(self, net, b, x, tol=None, itmax=1000,
+                             stall_window=20):
+        """Flexible BiCGStab right-preconditioned by the learned network
+        (Jacobi-BiCGStab takes over on a stall).  Returns (iterations,
+        relative residual, status, fell_back)."""
+        it, err, fb = ctypes.c_int(0), ctypes.c_double(0.0), ctypes.c_int(0)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve_learned_device(
+            self.h, net.h, _ptr(b), _ptr(x), float(tol), int(itmax),
+            int(stall_window), ctypes.byref(it), ctypes.byref(err),
+            ctypes.byref(fb))
+        L.check(st, "vdr_solve_learned_device",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return it.value, err.value, st, bool(fb.value)
+
+    @_device_call
+    def solve_gcr_device(self, b, x, net=None, tol=None, itmax=1000,
+                         restart=20, stall_window=0):
+        """Restarted GCR (flexible minimal residual) with Jacobi, or with
+        the learned network as right preconditioner (Jacobi-BiCGStab takes
+        over on a stall).  Returns (iterations, relative residual, status,
+        fell_back)."""
+        it, err, fb = ctypes.c_int(0), ctypes.c_double(0.0), ctypes.c_int(0)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve_gcr_device(
+            self.h, net.h if net is not None else None, _ptr(b), _ptr(x),
+            float(tol), int(itmax), int(restart), int(stall_window),
+            ctypes.byref(it), ctypes.byref(err), ctypes.byref(fb))
+        L.check(st, "vdr_solve_gcr_device",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return it.value, err.value, st, bool(fb.value)
+
+    @_device_call
+    def solve_gcr_record_device(self, b, x, hist, net=None, tol=None,
+                                itmax=1000, restart=20):
+        """GCR recording every iterate into hist.  Returns (recorded,
+        iterations, relative residual, status)."""
+        it, err, nh = ctypes.c_int(0), ctypes.c_double(0.0), ctypes.c_int(0)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve_gcr_record_device(
+            self.h, net.h if net is not None else None, _ptr(b), _ptr(x),
+            float(tol), int(itmax), int(restart), _ptr(hist),
+            int(hist.shape[0]), ctypes.byref(nh), ctypes.byref(it),
+            ctypes.byref(err))
+        L.check(st, "vdr_solve_gcr_record_device",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return nh.value, it.value, err.value, st
+
+    @_device_call
+    def solve_record_device(self, b, x, hist, tol=None, itmax=1000):
+        """Jacobi-BiCGStab recording every iterate into hist (rows of N).
+        Returns (recorded, iterations, relative residual, status)."""
+        it, err, nh = ctypes.c_int(0), ctypes.c_double(0.0), ctypes.c_int(0)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve_record_device(
+            self.h, _ptr(b), _ptr(x), float(tol), int(itmax), _ptr(hist),
+            int(hist.shape[0]), ctypes.byref(nh), ctypes.byref(it),
+            ctypes.byref(err))
+        L.check(st, "vdr_solve_record_device",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return nh.value, it.value, err.value, st
+
+    @_device_call
     def solve_mixed_device(self, b, x, tol=None, inner_tol=1e-5, max_outer=20,
                            inner_itmax=1000):
         """FP64 refinement around FP32-operator inner solves.  Returns
@@ -204,6 +309,7 @@ class Solver:
     # ---- many right-hand sides: node-major N x K device arrays ----
     BLOCK_PRECISION = {"fp64": 0, "tf32": 1, "tf32x3": 2}
 
+    @_device_call
     def assemble_rhs_block_device(self, Q, B, cf=1.0):
         """B (N x K float64) = cf * f(Q_k) for the K x E per-element
         sources Q (caller's element order)."""
@@ -212,6 +318,7 @@ class Solver:
             self.h, K, _ptr(Q), float(cf), _ptr(B)),
             "vdr_assemble_rhs_block_device")
 
+    @_device_call
     def apply_block_device(self, X, Y, precision="fp64"):
         """Y = P A P X for the K columns of X (N x K; float64 for "fp64",
         float32 for "tf32" / "tf32x3")."""
@@ -220,6 +327,7 @@ class Solver:
             self.h, K, _ptr(X), _ptr(Y), self.BLOCK_PRECISION[precision]),
             "vdr_apply_block_device")
 
+    @_device_call
     def solve_block_device(self, B, X, tol=None, inner_tol=1e-3,
                            precision="tf32x3", max_outer=30, inner_itmax=1000):
         """FP64 refinement around K simultaneous FP32 tensor-core inner
@@ -237,6 +345,7 @@ class Solver:
                 allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
         return no.value, ni.value, errs, st
 
+    @_device_call
     def time_steps_device(self, t, nsteps, cf, rM, tol=None, itmax=1000):
         """The reference's time loop on the device (vdr_time_steps): t (device
         array) holds T_0 and returns T_nsteps.  Returns (masses, iterations,
@@ -254,6 +363,7 @@ class Solver:
                 allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
         return masses, iters, errs, st, done.value
 
+    @_device_call
     def true_residual_device(self, b, x):
         r = ctypes.c_double()
         L.check(self.lib.vdr_true_residual_device(self.h, _ptr(b), _ptr(x),
@@ -261,6 +371,7 @@ class Solver:
                 "vdr_true_residual_device")
         return r.value
 
+    @_device_call
     def mass_device(self, c):
         m = ctypes.c_double()
         L.check(self.lib.vdr_mass_device(self.h, _ptr(c), ctypes.byref(m)),
@@ -283,6 +394,143 @@ class Solver:
     def close(self):
         if getattr(self, "h", None):
             self.lib.vdr_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_FP = ctypes.POINTER(ctypes.c_float)
+
+
+class LearnedNet:
+    """The learned preconditioner bound to a Solver's mesh (libvdr's
+    vdr_net_*): a 3-level 3D U-Net with BF16 weights, trained on the GPU by
+    the library's own forward/backward kernels."""
+
+    def __init__(self, solver: Solver, seed: int = 0):
+        self.lib = solver.lib
+        self.solver = solver
+        h = ctypes.c_void_p()
+        L.check(self.lib.vdr_net_create(solver.h, int(seed), ctypes.byref(h)),
+                "vdr_net_create")
+        self.h = h
+        n = ctypes.c_longlong(0)
+        L.check(self.lib.vdr_net_param_count(self.h, ctypes.byref(n)),
+                "vdr_net_param_count")
+        self.nparam = n.value
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.nparam, dtype=np.float32)
+        L.check(self.lib.vdr_net_get_params(self.h, out.ctypes.data_as(_FP)),
+                "vdr_net_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparam
+        L.check(self.lib.vdr_net_set_params(self.h, p.ctypes.data_as(_FP)),
+                "vdr_net_set_params")
+
+    def get_grads(self) -> np.ndarray:
+        out = np.empty(self.nparam, dtype=np.float32)
+        L.check(self.lib.vdr_net_get_grads(self.h, out.ctypes.data_as(_FP)),
+                "vdr_net_get_grads")
+        return out
+
+    @_device_call
+    def update_features(self, feat_out=None) -> float:
+        dbar = ctypes.c_double(0.0)
+        L.check(self.lib.vdr_net_update_features(self.h, _ptr(feat_out),
+                                                 ctypes.byref(dbar)),
+                "vdr_net_update_features")
+        return dbar.value
+
+    @_device_call
+    def set_features(self, feat, dbar: float):
+        L.check(self.lib.vdr_net_set_features_device(self.h, _ptr(feat),
+                                                     float(dbar)),
+                "vdr_net_set_features_device")
+
+    @_device_call
+    def make_pair(self, b, xk, xstar, rhat, target):
+        """Training pair from iterate xk of the solve A x = b (solution
+        xstar): rhat = r/rms(r), target = (e - D^-1 r) dbar/rms(r)."""
+        L.check(self.lib.vdr_net_make_pair_device(self.h, _ptr(b), _ptr(xk),
+                                                  _ptr(xstar), _ptr(rhat),
+                                                  _ptr(target)),
+                "vdr_net_make_pair_device")
+
+    @_device_call
+    def forward(self, rhat, out):
+        L.check(self.lib.vdr_net_forward_device(self.h, _ptr(rhat), _ptr(out)),
+                "vdr_net_forward_device")
+
+    @_device_call
+    def loss_grad(self, rhat, target) -> float:
+        loss = ctypes.c_double(0.0)
+        L.check(self.lib.vdr_net_loss_grad_device(self.h, _ptr(rhat),
+                                                  _ptr(target),
+                                                  ctypes.byref(loss)),
+                "vdr_net_loss_grad_device")
+        return loss.value
+
+    @_device_call
+    def residual_loss_grad(self, rhat) -> float:
+        """||rhat - A M(rhat)||^2 / ||rhat||^2 with the current operator, and
+        the parameter gradients."""
+        loss = ctypes.c_double(0.0)
+        L.check(self.lib.vdr_net_residual_loss_grad_device(self.h, _ptr(rhat),
+                                                           ctypes.byref(loss)),
+                "vdr_net_residual_loss_grad_device")
+        return loss.value
+
+    @_device_call
+    def train_step_residual(self, rhat, lr, want_loss=False):
+        loss = ctypes.c_double(0.0)
+        L.check(self.lib.vdr_net_train_step_residual_device(
+            self.h, _ptr(rhat), float(lr),
+            ctypes.byref(loss) if want_loss else None),
+            "vdr_net_train_step_residual_device")
+        return loss.value if want_loss else None
+
+    @_device_call
+    def adam_step(self, lr, beta1=0.9, beta2=0.999, eps=1e-8):
+        L.check(self.lib.vdr_net_adam_step(self.h, float(lr), float(beta1),
+                                           float(beta2), float(eps)),
+                "vdr_net_adam_step")
+
+    @_device_call
+    def train_step(self, rhat, target, lr, want_loss=False):
+        loss = ctypes.c_double(0.0)
+        L.check(self.lib.vdr_net_train_step_device(
+            self.h, _ptr(rhat), _ptr(target), float(lr),
+            ctypes.byref(loss) if want_loss else None),
+            "vdr_net_train_step_device")
+        return loss.value if want_loss else None
+
+    def set_smoothing(self, steps=1, omega=1.0):
+        """Jacobi post-smoothing steps after the network (0 = none)."""
+        L.check(self.lib.vdr_net_set_smoothing(self.h, int(steps), float(omega)),
+                "vdr_net_set_smoothing")
+
+    @_device_call
+    def precondition(self, x, y):
+        L.check(self.lib.vdr_net_precondition_device(self.h, _ptr(x), _ptr(y)),
+                "vdr_net_precondition_device")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vdr_net_destroy(self.h)
             self.h = None
 
     def __enter__(self):
