@@ -54,6 +54,10 @@ def args_parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the many-right-hand-side section")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-preconditioner section")
+    ap.add_argument("--learn-steps", type=int, default=LEARN_STEPS)
+    ap.add_argument("--learn-epochs", type=int, default=1)
     ap.add_argument("--cpu-iters", type=int, default=4,
                     help="BiCGStab iterations timed in the CPU sample")
     return ap.parse_args()
@@ -357,6 +361,111 @@ def batched_rhs_section(vdr, device):
     return out
 
 
+LEARN_MESH = (128, 128, 64)
+LEARN_STEPS = 200
+LEARN_TRAIN_STEPS = 40
+LEARN_PAIRS = 50           # per training step: 2000 pairs
+LEARN_DAGGER_PAIRS = 25    # per training step, from the learned solver
+LEARN_TILT = 0.5
+
+
+def learned_section(vdr, device, a):
+    """The learned preconditioner on the tilting-axis transient problem
+    (128x128x64, theta-step at Courant 10, rotation axis tilting 0.5 degrees
+    per step, every step to FP64 relative residual 1e-8).  Steps 0-39 give
+    2000 (residual, error) pairs from the Jacobi-BiCGStab solves' iterates;
+    the network is trained on the GPU (residual loss), then once more on
+    pairs from its own GCR solves of the same steps; steps 40-199 are solved
+    by Jacobi-BiCGStab and by two learned GCR steps followed by
+    Jacobi-BiCGStab, from the same T_old each step; pure learned GCR is
+    measured on the first 8 of them."""
+    import numpy as np
+    import torch
+    L = vdr.learned
+    nx, ny, nz = LEARN_MESH
+    t_all = time.perf_counter()
+    run = L.TiltingRun(nx, ny, nz, seed=1005, courant=COURANT, tol=TOL,
+                       tilt_deg=LEARN_TILT, device=device)
+    net = vdr.LearnedNet(run.s, seed=5)
+    net.set_smoothing(0)
+    steps_train = list(range(LEARN_TRAIN_STEPS))
+    total = a.learn_steps
+    t0 = time.perf_counter()
+    T0 = run.T.clone()
+    data = L.collect_pairs(run, net, steps_train, pairs_per_step=LEARN_PAIRS)
+    T_after = run.T.clone()
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    curve0 = L.train(net, data, epochs=a.learn_epochs, lr=1e-3, loss="residual",
+                     run=run)
+    t_train0 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    with torch.cuda.stream(run.stream):
+        run.T.copy_(T0)
+    more = L.collect_pairs_learned(run, net, steps_train,
+                                   pairs_per_step=LEARN_DAGGER_PAIRS,
+                                   max_iters=40)
+    curve1 = L.train(net, more, epochs=1, lr=5e-4, loss="residual", run=run,
+                     seed=1)
+    t_train1 = time.perf_counter() - t0
+    with torch.cuda.stream(run.stream):
+        run.T.copy_(T_after)
+    torch.cuda.synchronize()
+    # every remaining step: Jacobi-BiCGStab vs 2 learned GCR steps then
+    # Jacobi-BiCGStab
+    res = L.evaluate(run, net, range(LEARN_TRAIN_STEPS, total), method="hybrid",
+                     restart=2)
+    # pure learned GCR(20) on the first 8 of them (capped at 300 iterations,
+    # Jacobi-BiCGStab after a 20-iteration stall)
+    with torch.cuda.stream(run.stream):
+        run.T.copy_(T_after)
+    torch.cuda.synchronize()
+    pure = L.evaluate(run, net, range(LEARN_TRAIN_STEPS, LEARN_TRAIN_STEPS + 8),
+                      method="gcr", restart=20, stall_window=20, itmax=300)
+
+    def summary(rows, key):
+        its = [r[key + "_iters"] for r in rows]
+        return {"solve_s_total": sum(r[key + "_s"] for r in rows),
+                "mean_iterations": float(np.mean(its)),
+                "max_iterations": int(max(its))}
+
+    jt = sum(r["jacobi_s"] for r in res)
+    lt = sum(r["learned_s"] for r in res)
+    out = {
+        "workload": "tilting-axis rotation_shear %dx%dx%d, %d theta-steps at "
+                    "Courant %g (axis tilts %g deg/step), each to FP64 "
+                    "relative residual %g" % (nx, ny, nz, total, COURANT,
+                                              LEARN_TILT, TOL),
+        "network": "3-level 3D U-Net 16/32/64 channels, 3^3 kernels, BF16 "
+                   "weights/activations, FP32 accumulate (mma.sync m16n8k16)",
+        "training": {"pairs": int(data["rhat"].shape[0]),
+                     "pairs_from_learned_solves": int(more["rhat"].shape[0]),
+                     "epochs": a.learn_epochs, "loss": "residual",
+                     "loss_curve": curve0 + curve1,
+                     "collect_s": t_collect, "train_s": t_train0,
+                     "second_round_s": t_train1},
+        "eval_steps": len(res),
+        "jacobi_bicgstab": summary(res, "jacobi"),
+        "learned_then_jacobi": dict(
+            summary(res, "learned"),
+            what="2 GCR steps with the network, then Jacobi-BiCGStab",
+            worst_true_residual=float(max(r["learned_true_residual"]
+                                          for r in res)),
+            all_converged=all(r["learned_status"] == 0 for r in res),
+            worst_rel_diff_vs_fp64=float(max(r["rel_diff"] for r in res))),
+        "learned_vs_plain_time": lt / jt if jt > 0 else None,
+        "pure_learned_gcr_first_8_steps": dict(
+            summary(pure, "learned"),
+            jacobi_bicgstab=summary(pure, "jacobi"),
+            fell_back=int(sum(r["fell_back"] for r in pure)),
+            all_converged=all(r["learned_status"] == 0 for r in pure)),
+        "section_s": time.perf_counter() - t_all,
+    }
+    net.close()
+    run.close()
+    return out
+
+
 def run_native(a):
     import numpy as np
     import torch
@@ -518,6 +627,7 @@ def run_native(a):
     sc.close()
 
     batched = None if a.no_batched else batched_rhs_section(vdr, local)
+    learned = None if a.no_learned else learned_section(vdr, local, a)
 
     # ---- e2e through the C ABI with host buffers ----
     vel, lam, pdec, q = prob.vel, prob.lam, prob.pdec, prob.q
@@ -581,6 +691,7 @@ def run_native(a):
             "scatter_variants": scatter_variants,
             "mixed_precision": mixed,
             "batched_rhs": batched,
+            "learned_preconditioner": learned,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,

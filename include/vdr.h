@@ -290,6 +290,13 @@ int vdr_solve_gcr_device(vdr_handle *h, vdr_net *net, const double *d_b,
                          double *d_x, double tol, int itmax, int restart,
                          int stall_window, int *iter, double *err,
                          int *fell_back);
+/* learned_steps (1..32) GCR steps with the network's preconditioner, then
+ * Jacobi-BiCGStab from that iterate: the network only improves the start
+ * of the solve.  iter counts both phases. */
+int vdr_solve_learned_hybrid_device(vdr_handle *h, vdr_net *net,
+                                    const double *d_b, double *d_x,
+                                    double tol, int itmax, int learned_steps,
+                                    int *iter, double *err);
 /* vdr_solve_gcr_device (no fallback) recording x after every iteration into
  * d_hist (max_hist x N doubles); *n_hist = number recorded. */
 int vdr_solve_gcr_record_device(vdr_handle *h, vdr_net *net, const double *d_b,

@@ -87,6 +87,8 @@ SIGNATURES = {
     "vdr_solve_learned_device": (_i, [_P, _P, _P, _P, _d, _i, _i, _I, _D, _I]),
     "vdr_solve_gcr_device": (_i, [_P, _P, _P, _P, _d, _i, _i, _i, _I, _D,
                                   _I]),
+    "vdr_solve_learned_hybrid_device": (_i, [_P, _P, _P, _P, _d, _i, _i, _I,
+                                             _D]),
     "vdr_solve_gcr_record_device": (_i, [_P, _P, _P, _P, _d, _i, _i, _P, _i,
                                          _I, _I, _D]),
     "vdr_solve_record_device": (_i, [_P, _P, _P, _d, _i, _P, _i, _I, _I, _D]),

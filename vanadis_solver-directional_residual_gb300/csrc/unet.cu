@@ -250,88 +250,152 @@ __global__ void __launch_bounds__(128) conv3_kernel(ConvArgs a) {
     }
 }
 
-// Weight and bias gradients of one 3x3x3 layer: blockIdx.y = tap, blockIdx.x
-// = a chunk of voxels.  dW[tap][co][ci] += sum_v dY'[v][co] X[v + off][ci]
-// with dY' = dY where the layer output Y > 0 (ReLU), X = [in1 | up(in2)].
+// Weight and bias gradients of one 3x3x3 layer on the tensor cores:
+// dW[tap][co][ci] += sum_v dY'[v][co] X[v + off(tap)][ci], an implicit GEMM
+// with M = output channels, N = input channels, K = voxels (16 per MMA),
+// X = [in1 | up(in2)].  dY' (the ReLU-masked output gradient) is first
+// written transposed in BF16, dyt[co][v], so that A fragments load as
+// pairs of consecutive voxels; B fragments are single loads of the shifted
+// inputs.  Grid: (voxel chunks, 27 taps, groups of NG input-channel
+// tiles); a block's chunk is a range of 16-voxel x-row segments, each warp
+// takes every fourth one, and adds its tile to dW with atomics.  db
+// accumulates in the centre-tap blocks.
 struct WgArgs {
   const bf16 *in1, *in2;
-  const float *dy;
-  const bf16 *y;
+  const bf16 *dyt;  // [COUT][V]
   float *dw, *db;
   int W, H, D, Wc, Hc;
   long V, chunk;
 };
-template <int CIN1, int CIN2, int COUT>
-__global__ void __launch_bounds__(256) conv3_wgrad(WgArgs a) {
-  constexpr int CIN = CIN1 + CIN2, TV = 32, ENT = COUT * CIN;
-  constexpr int PER = (ENT + 255) / 256;
-  __shared__ float sdy[TV][COUT + 1];
-  __shared__ float sx[TV][CIN + 1];
+
+template <int C>
+__global__ void mask_transpose(const float *dy, const bf16 *y, bf16 *dyt, long V) {
+  const long total = V * C;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    const long v = idx / C;
+    const int c = (int)(idx % C);
+    const float d = __bfloat162float(y[idx]) > 0.f ? dy[idx] : 0.f;
+    dyt[(long)c * V + v] = __float2bfloat16_rn(d);
+  }
+}
+
+template <int CIN1, int CIN2, int COUT, int NG>
+__global__ void __launch_bounds__(128) conv3_wgrad_tc(WgArgs a) {
+  constexpr int CIN = CIN1 + CIN2, MT = COUT / 16, NT = CIN / 8;
+  static_assert(COUT % 16 == 0 && CIN % 8 == 0, "shape");
   const int tap = blockIdx.y;
   const int dz = tap / 9 - 1, dyy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-  const int tid = threadIdx.x;
+  const int ntile0 = blockIdx.z * NG;
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int warp = threadIdx.x >> 5;
   const long WH = (long)a.W * a.H;
-  float acc[PER];
+  // k-steps are 16-voxel segments of x rows: row = y + H z, segment s
+  // covers x in [16 s, 16 s + 16).
+  const int segs = (a.W + 15) >> 4;
+  const long nks = (long)a.H * a.D * segs;
+  const long ks0 = (long)blockIdx.x * a.chunk;
+  const long ks1 = nks < ks0 + a.chunk ? nks : ks0 + a.chunk;
+  float acc[MT][NG][4];
 #pragma unroll
-  for (int j = 0; j < PER; j++) acc[j] = 0.f;
-  float dbacc = 0.f;
-  const long v0 = (long)blockIdx.x * a.chunk;
-  const long v1 = a.V < v0 + a.chunk ? a.V : v0 + a.chunk;
-  for (long vt = v0; vt < v1; vt += TV) {
-    for (int i = tid; i < TV * COUT; i += 256) {
-      const int lv = i / COUT, co = i % COUT;
-      const long v = vt + lv;
-      float d = 0.f;
-      if (v < v1) {
-        const long k = v * COUT + co;
-        d = a.dy[k];
-        if (!(__bfloat162float(a.y[k]) > 0.f)) d = 0.f;
-      }
-      sdy[lv][co] = d;
+  for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+    for (int j = 0; j < NG; j++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[mt][j][q] = 0.f;
+  float dbs[MT][2] = {};
+  const int jv[4] = {2 * t, 2 * t + 1, 2 * t + 8, 2 * t + 9};
+  for (long ks = ks0 + warp; ks < ks1; ks += 4) {
+    const int row = (int)(ks / segs), seg = (int)(ks - (long)row * segs);
+    const int y = row % a.H, z = row / a.H, xs = seg << 4;
+    const long vb = (long)row * a.W + xs;
+    const int yn = y + dyy, zn = z + dz;
+    const bool rowok = yn >= 0 && yn < a.H && zn >= 0 && zn < a.D;
+    const long crow = (long)a.Wc * ((yn >> 1) + (long)a.Hc * (zn >> 1));
+    long nf[4], nc[4];
+    bool vin[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int x = xs + jv[u];
+      vin[u] = x < a.W;
+      const int xn = x + dx;
+      const bool ok = rowok && vin[u] && xn >= 0 && xn < a.W;
+      nf[u] = ok ? vb + jv[u] + dx + (long)dyy * a.W + (long)dz * WH : -1;
+      nc[u] = ok ? (long)(xn >> 1) + crow : -1;
     }
-    for (int i = tid; i < TV * CIN; i += 256) {
-      const int lv = i / CIN, ci = i % CIN;
-      const long v = vt + lv;
-      float xv = 0.f;
-      if (v < v1) {
-        const int x = (int)(v % a.W) + dx, y = (int)((v / a.W) % a.H) + dyy,
-                  z = (int)(v / WH) + dz;
-        if (x >= 0 && x < a.W && y >= 0 && y < a.H && z >= 0 && z < a.D) {
-          if (ci < CIN1) {
-            xv = __bfloat162float(a.in1[(v + dx + (long)dyy * a.W + (long)dz * WH) * CIN1 + ci]);
-          } else {
-            const long nc = (long)(x >> 1) + (long)a.Wc * ((y >> 1) + (long)a.Hc * (z >> 1));
-            xv = __bfloat162float(a.in2[nc * (CIN2 > 0 ? CIN2 : 1) + (ci - CIN1)]);
-          }
+    // A fragments: dyt[co][v] for v = vb + (2t, 2t+1) and vb + (2t+8, 2t+9)
+    uint32_t af[MT][4];
+#pragma unroll
+    for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {  // rows g, g+8
+        const long base = (long)(mt * 16 + g + 8 * h) * a.V;
+        const bf16 *rp = a.dyt + base + vb;
+        uint32_t lo, hi;
+        const bool even = !((base + vb) & 1);  // 4-byte aligned pairs
+        if (vin[1] && even) {
+          lo = ld2(rp + 2 * t);
+        } else {
+          lo = pack2(vin[0] ? __bfloat162float(rp[2 * t]) : 0.f,
+                     vin[1] ? __bfloat162float(rp[2 * t + 1]) : 0.f);
+        }
+        if (vin[3] && even) {
+          hi = ld2(rp + 2 * t + 8);
+        } else {
+          hi = pack2(vin[2] ? __bfloat162float(rp[2 * t + 8]) : 0.f,
+                     vin[3] ? __bfloat162float(rp[2 * t + 9]) : 0.f);
+        }
+        af[mt][h] = lo;      // a0 (row g) / a1 (row g+8): k = 2t, 2t+1
+        af[mt][2 + h] = hi;  // a2 / a3: k = 2t+8, 2t+9
+        if (tap == 13 && blockIdx.z == 0)
+          dbs[mt][h] += bf_lo(lo) + bf_hi(lo) + bf_lo(hi) + bf_hi(hi);
+      }
+#pragma unroll
+    for (int j = 0; j < NG; j++) {
+      const int nt = ntile0 + j;
+      if (nt >= NT) break;
+      const int ci = nt * 8 + g;
+      float xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        xv[u] = 0.f;
+        if (ci < CIN1) {
+          if (nf[u] >= 0) xv[u] = __bfloat162float(a.in1[nf[u] * CIN1 + ci]);
+        } else if (CIN2 > 0) {
+          if (nc[u] >= 0)
+            xv[u] = __bfloat162float(a.in2[nc[u] * (CIN2 > 0 ? CIN2 : 1) + (ci - CIN1)]);
         }
       }
-      sx[lv][ci] = xv;
-    }
-    __syncthreads();
+      const uint32_t b0 = pack2(xv[0], xv[1]), b1 = pack2(xv[2], xv[3]);
 #pragma unroll
-    for (int j = 0; j < PER; j++) {
-      const int e = tid + 256 * j;
-      if (e < ENT) {
-        const int co = e / CIN, ci = e % CIN;
-        float s = 0.f;
-#pragma unroll 8
-        for (int lv = 0; lv < TV; lv++) s += sdy[lv][co] * sx[lv][ci];
-        acc[j] += s;
+      for (int mt = 0; mt < MT; mt++)
+        mma_bf16(acc[mt][j], af[mt][0], af[mt][1], af[mt][2], af[mt][3], b0, b1);
+    }
+  }
+  // D fragment: rows co = g (c0, c1), g+8 (c2, c3); cols ci = 2t, 2t+1
+#pragma unroll
+  for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+    for (int j = 0; j < NG; j++) {
+      const int nt = ntile0 + j;
+      if (nt >= NT) break;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int co = mt * 16 + g + 8 * (q >> 1), ci = nt * 8 + 2 * t + (q & 1);
+        atomicAdd(a.dw + ((size_t)tap * COUT + co) * CIN + ci, acc[mt][j][q]);
       }
     }
-    if (tap == 13 && tid < COUT)
-      for (int lv = 0; lv < TV; lv++) dbacc += sdy[lv][tid];
-    __syncthreads();
-  }
+  if (tap == 13 && blockIdx.z == 0) {
 #pragma unroll
-  for (int j = 0; j < PER; j++) {
-    const int e = tid + 256 * j;
-    if (e < ENT) {
-      const int co = e / CIN, ci = e % CIN;
-      atomicAdd(a.dw + ((size_t)tap * COUT + co) * CIN + ci, acc[j]);
-    }
+    for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        float x = dbs[mt][h];
+        x += __shfl_xor_sync(FULLM, x, 1);
+        x += __shfl_xor_sync(FULLM, x, 2);
+        if (t == 0) atomicAdd(a.db + mt * 16 + g + 8 * h, x);
+      }
   }
-  if (tap == 13 && tid < COUT) atomicAdd(a.db + tid, dbacc);
 }
 
 // --------------------------------------------------------- pooling
@@ -807,6 +871,7 @@ struct Net {
   double *rbuf = nullptr;     // [N] residual scratch (training pairs)
   double *zbuf = nullptr, *qbuf = nullptr, *pbuf = nullptr, *gbuf = nullptr;  // residual loss
   float *dc = nullptr;
+  bf16 *dyt = nullptr;  // [C][V] masked transposed output gradient (wgrad)
   double *scal = nullptr;  // [0] rms [1] loss [2] dbar [3] sum t^2 [4] residual loss [5] ||rhat||^2
   double *partials = nullptr;
   unsigned *ticket = nullptr;
@@ -854,15 +919,22 @@ cudaError_t conv_launch(const ConvArgs &a, cudaStream_t s) {
 }
 
 template <int CIN1, int CIN2, int COUT>
-cudaError_t wgrad_launch(const WgArgs &a0, cudaStream_t s) {
-  WgArgs a = a0;
-  const long nchunk_target = std::max<long>(1, (long)sm_count_u() * 16 / 27);
-  long chunk = (a.V + nchunk_target - 1) / nchunk_target;
-  chunk = std::max<long>(256, ((chunk + 31) / 32) * 32);
+cudaError_t wgrad_launch(const Net &n, WgArgs a, const float *dy, const bf16 *y,
+                         cudaStream_t s) {
+  constexpr int CIN = CIN1 + CIN2, NT = CIN / 8;
+  constexpr int NG = NT < 4 ? NT : 4;
+  constexpr int NGROUPS = (NT + NG - 1) / NG;
+  // masked, transposed BF16 output gradient (scratch sized for the largest)
+  mask_transpose<COUT><<<grid_for(a.V * COUT, 256), 256, 0, s>>>(dy, y, n.dyt, a.V);
+  a.dyt = n.dyt;
+  const long nks = (long)a.H * a.D * ((a.W + 15) / 16);  // 16-voxel row segments
+  const long target = std::max<long>(1, (long)sm_count_u() * 8 / (27 * NGROUPS));
+  long chunk = (nks + target - 1) / target;
+  chunk = std::max<long>(16, ((chunk + 3) / 4) * 4);
   a.chunk = chunk;
-  const long nchunk = (a.V + chunk - 1) / chunk;
-  conv3_wgrad<CIN1, CIN2, COUT><<<dim3((unsigned)nchunk, 27), 256, 0, s>>>(a);
-  count_launches(1);
+  const long nchunk = (nks + chunk - 1) / chunk;
+  conv3_wgrad_tc<CIN1, CIN2, COUT, NG><<<dim3((unsigned)nchunk, 27, NGROUPS), 128, 0, s>>>(a);
+  count_launches(2);
   return cudaGetLastError();
 }
 
@@ -891,14 +963,11 @@ ConvArgs conv_args(const Net &n, int level, const void *in1, const bf16 *mask1,
   return a;
 }
 
-WgArgs wg_args(const Net &n, int l, const bf16 *in1, const bf16 *in2,
-               const float *dy, const bf16 *y) {
+WgArgs wg_args(const Net &n, int l, const bf16 *in1, const bf16 *in2) {
   WgArgs a{};
   const Dims &f = n.d[DEFS[l].level];
   a.in1 = in1;
   a.in2 = in2;
-  a.dy = dy;
-  a.y = y;
   a.dw = n.grad + n.woff[l];
   a.db = n.grad + n.boff[l];
   a.W = f.W;
@@ -953,12 +1022,12 @@ cudaError_t net_backward(Net &n, cudaStream_t s) {
   cudaError_t e;
   const Dims &f0 = n.d[0], &f1 = n.d[1], &f2 = n.d[2];
   // d0b: u0 = relu(conv(a4))
-  if ((e = wgrad_launch<16, 0, 16>(wg_args(n, L_D0B, n.a4, nullptr, n.g_u0, n.u0), s))) return e;
+  if ((e = wgrad_launch<16, 0, 16>(n, wg_args(n, L_D0B, n.a4, nullptr), n.g_u0, n.u0, s))) return e;
   if ((e = conv_launch<16, 0, 16, true, true>(
            conv_args(n, 0, n.g_u0, n.u0, nullptr, wt(n, L_D0B), nullptr, n.g_a4, false,
                      nullptr, nullptr), s))) return e;
   // d0a: a4 = relu(conv([s0 | up(u1)]))
-  if ((e = wgrad_launch<16, 32, 16>(wg_args(n, L_D0A, n.s0, n.u1, n.g_a4, n.a4), s))) return e;
+  if ((e = wgrad_launch<16, 32, 16>(n, wg_args(n, L_D0A, n.s0, n.u1), n.g_a4, n.a4, s))) return e;
   if ((e = conv_launch<16, 0, 48, true, true>(
            conv_args(n, 0, n.g_a4, n.a4, nullptr, wt(n, L_D0A), nullptr, n.g_cat0, false,
                      nullptr, nullptr), s))) return e;
@@ -966,12 +1035,12 @@ cudaError_t net_backward(Net &n, cudaStream_t s) {
   upcat_bwd_coarse<<<grid_for(f1.V * 32, 256), 256, 0, s>>>(n.g_cat0, n.g_u1, f0, f1, 16, 32);
   count_launches(2);
   // d1b: u1 = relu(conv(a3))
-  if ((e = wgrad_launch<32, 0, 32>(wg_args(n, L_D1B, n.a3, nullptr, n.g_u1, n.u1), s))) return e;
+  if ((e = wgrad_launch<32, 0, 32>(n, wg_args(n, L_D1B, n.a3, nullptr), n.g_u1, n.u1, s))) return e;
   if ((e = conv_launch<32, 0, 32, true, true>(
            conv_args(n, 1, n.g_u1, n.u1, nullptr, wt(n, L_D1B), nullptr, n.g_a3, false,
                      nullptr, nullptr), s))) return e;
   // d1a: a3 = relu(conv([s1 | up(b2)]))
-  if ((e = wgrad_launch<32, 64, 32>(wg_args(n, L_D1A, n.s1, n.b2, n.g_a3, n.a3), s))) return e;
+  if ((e = wgrad_launch<32, 64, 32>(n, wg_args(n, L_D1A, n.s1, n.b2), n.g_a3, n.a3, s))) return e;
   if ((e = conv_launch<32, 0, 96, true, true>(
            conv_args(n, 1, n.g_a3, n.a3, nullptr, wt(n, L_D1A), nullptr, n.g_cat1, false,
                      nullptr, nullptr), s))) return e;
@@ -979,36 +1048,36 @@ cudaError_t net_backward(Net &n, cudaStream_t s) {
   upcat_bwd_coarse<<<grid_for(f2.V * 64, 256), 256, 0, s>>>(n.g_cat1, n.g_b2, f1, f2, 32, 64);
   count_launches(2);
   // btb: b2 = relu(conv(a2))
-  if ((e = wgrad_launch<64, 0, 64>(wg_args(n, L_BTB, n.a2, nullptr, n.g_b2, n.b2), s))) return e;
+  if ((e = wgrad_launch<64, 0, 64>(n, wg_args(n, L_BTB, n.a2, nullptr), n.g_b2, n.b2, s))) return e;
   if ((e = conv_launch<64, 0, 64, true, true>(
            conv_args(n, 2, n.g_b2, n.b2, nullptr, wt(n, L_BTB), nullptr, n.g_a2, false,
                      nullptr, nullptr), s))) return e;
   // bta: a2 = relu(conv(p1))
-  if ((e = wgrad_launch<32, 0, 64>(wg_args(n, L_BTA, n.p1, nullptr, n.g_a2, n.a2), s))) return e;
+  if ((e = wgrad_launch<32, 0, 64>(n, wg_args(n, L_BTA, n.p1, nullptr), n.g_a2, n.a2, s))) return e;
   if ((e = conv_launch<64, 0, 32, true, true>(
            conv_args(n, 2, n.g_a2, n.a2, nullptr, wt(n, L_BTA), nullptr, n.g_p1, false,
                      nullptr, nullptr), s))) return e;
   pool_bwd_add<<<grid_for(f1.V * 32, 256), 256, 0, s>>>(n.g_p1, n.g_s1, f1, f2, 32);
   count_launches(1);
   // e1b: s1 = relu(conv(a1))
-  if ((e = wgrad_launch<32, 0, 32>(wg_args(n, L_E1B, n.a1, nullptr, n.g_s1, n.s1), s))) return e;
+  if ((e = wgrad_launch<32, 0, 32>(n, wg_args(n, L_E1B, n.a1, nullptr), n.g_s1, n.s1, s))) return e;
   if ((e = conv_launch<32, 0, 32, true, true>(
            conv_args(n, 1, n.g_s1, n.s1, nullptr, wt(n, L_E1B), nullptr, n.g_a1, false,
                      nullptr, nullptr), s))) return e;
   // e1a: a1 = relu(conv(p0))
-  if ((e = wgrad_launch<16, 0, 32>(wg_args(n, L_E1A, n.p0, nullptr, n.g_a1, n.a1), s))) return e;
+  if ((e = wgrad_launch<16, 0, 32>(n, wg_args(n, L_E1A, n.p0, nullptr), n.g_a1, n.a1, s))) return e;
   if ((e = conv_launch<32, 0, 16, true, true>(
            conv_args(n, 1, n.g_a1, n.a1, nullptr, wt(n, L_E1A), nullptr, n.g_p0, false,
                      nullptr, nullptr), s))) return e;
   pool_bwd_add<<<grid_for(f0.V * 16, 256), 256, 0, s>>>(n.g_p0, n.g_s0, f0, f1, 16);
   count_launches(1);
   // e0b: s0 = relu(conv(a0))
-  if ((e = wgrad_launch<16, 0, 16>(wg_args(n, L_E0B, n.a0, nullptr, n.g_s0, n.s0), s))) return e;
+  if ((e = wgrad_launch<16, 0, 16>(n, wg_args(n, L_E0B, n.a0, nullptr), n.g_s0, n.s0, s))) return e;
   if ((e = conv_launch<16, 0, 16, true, true>(
            conv_args(n, 0, n.g_s0, n.s0, nullptr, wt(n, L_E0B), nullptr, n.g_a0, false,
                      nullptr, nullptr), s))) return e;
   // e0a: a0 = relu(conv(x0)); the input needs no gradient
-  if ((e = wgrad_launch<16, 0, 16>(wg_args(n, L_E0A, n.x0, nullptr, n.g_a0, n.a0), s))) return e;
+  if ((e = wgrad_launch<16, 0, 16>(n, wg_args(n, L_E0A, n.x0, nullptr), n.g_a0, n.a0, s))) return e;
   return cudaGetLastError();
 }
 
@@ -1179,6 +1248,7 @@ extern "C" int vdr_net_create(vdr_handle *H, unsigned long long seed, vdr_net **
         (e = nalloc(n, &n.rbuf, V0)) || (e = nalloc(n, &n.zbuf, V0)) ||
         (e = nalloc(n, &n.qbuf, V0)) || (e = nalloc(n, &n.pbuf, V0)) ||
         (e = nalloc(n, &n.gbuf, V0)) || (e = nalloc(n, &n.dc, V0)) ||
+        (e = nalloc(n, &n.dyt, std::max(V0 * 16, V1 * 32))) ||
         (e = nalloc(n, &n.scal, 8)) || (e = nalloc(n, &n.partials, 2L * n.red_grid)) ||
         (e = nalloc(n, &n.ticket, 1))) {
       st = cuda_fail(e, "network allocation");
@@ -1543,6 +1613,38 @@ extern "C" int vdr_solve_gcr_device(vdr_handle *H, vdr_net *N, const double *d_b
     if (fell_back) *fell_back = 1;
   }
   if (iter) *iter = it1;
+  if (err) *err = e1;
+  return st;
+}
+
+extern "C" int vdr_solve_learned_hybrid_device(vdr_handle *H, vdr_net *N,
+                                               const double *d_b, double *d_x,
+                                               double tol, int itmax, int learned_steps,
+                                               int *iter, double *err) {
+  if (!H || !N || !d_b || !d_x || learned_steps < 1 ||
+      learned_steps > GCR_MAX_RESTART) {
+    set_error("vdr_solve_learned_hybrid_device: bad arguments");
+    return VDR_BAD_ARGUMENT;
+  }
+  Handle &h = handle_of(H);
+  cudaError_t e = cudaSetDevice(h.device);
+  if (e) return cuda_fail(e, "cudaSetDevice");
+  if (N->n.h != &h || !N->n.features_set) {
+    set_error("vdr_solve_learned_hybrid_device: network of another handle, or features not set");
+    return VDR_BAD_ARGUMENT;
+  }
+  int st = prepare_operator(h);
+  if (st) return st;
+  Precond pc{net_enqueue, &N->n, net_enqueue_launches(N->n)};
+  int it1 = 0, it2 = 0;
+  double e1 = 0.0;
+  st = solve_gcr_device(h, d_b, d_x, tol, std::min(learned_steps, itmax), learned_steps,
+                        &pc, 0, &it1, &e1);
+  if (st == VDR_NOT_CONVERGED || st == VDR_BREAKDOWN) {
+    st = solve_device(h, VDR_SOLVER_BICGSTAB, d_b, d_x, tol, std::max(0, itmax - it1),
+                      &it2, &e1);
+  }
+  if (iter) *iter = it1 + it2;
   if (err) *err = e1;
   return st;
 }

@@ -35,11 +35,12 @@ from .solver import LearnedNet, Options, Solver
 
 
 def tilted_velocity(mesh, step: int, tilt_deg: float = 0.5,
-                    shear: float = 0.3) -> np.ndarray:
+                    shear: float = 0.3, cents=None) -> np.ndarray:
     """Rotation about the axis (sin t, 0, cos t), t = tilt_deg * step,
     through the cube centre, plus the shear u_x += shear * z; scaled to
-    max |u_e| = 1.  Step 0 is the rotation_shear field."""
-    cx, cy, cz = P.centroids(mesh)
+    max |u_e| = 1.  Step 0 is the rotation_shear field.  `cents`: the
+    element centroids, if already computed."""
+    cx, cy, cz = P.centroids(mesh) if cents is None else cents
     th = math.radians(tilt_deg * step)
     a = (math.sin(th), 0.0, math.cos(th))
     rx, ry, rz = cx - 0.5, cy - 0.5, cz - 0.5
@@ -66,6 +67,7 @@ class TiltingRun:
         self.cf, self.rM = 3.0, 3.0 / self.dt
         self.tol = tol
         self.tilt = tilt_deg
+        self.cents = P.centroids(self.mesh)
         self.s = Solver(self.prob, Options(apply_mode="stored", device=device),
                         aH=self.aH, aM=self.aM)
         self.stream = torch.cuda.ExternalStream(self.s.stream())
@@ -77,7 +79,7 @@ class TiltingRun:
     def set_step(self, step: int):
         """Fields, mask and operator of time step `step`; b from T."""
         p = self.prob
-        vel = tilted_velocity(self.mesh, step, self.tilt)
+        vel = tilted_velocity(self.mesh, step, self.tilt, cents=self.cents)
         self.s.set_fields(vel, p.lam, p.pdec, p.q, p.robin_alpha)
         self.s.set_dirichlet(P.inflow_mask(self.mesh, vel))
         self.s.set_operator(self.aH, self.aM)
@@ -237,14 +239,19 @@ def train(net: LearnedNet, data, epochs: int, lr: float = 1e-3,
 def evaluate(run: TiltingRun, net: LearnedNet, steps, itmax=5000,
              stall_window=20, method="gcr", restart=20):
     """Solves each step twice from the same T_old (Jacobi-BiCGStab, then
-    the learned solve: restarted GCR, method "gcr", or flexible BiCGStab,
-    "bicgstab") and advances with the Jacobi solution."""
+    the learned solve: restarted GCR, method "gcr"; flexible BiCGStab,
+    "bicgstab"; or `restart` learned GCR steps then Jacobi-BiCGStab,
+    "hybrid") and advances with the Jacobi solution."""
     torch = run.torch
     with torch.cuda.stream(run.stream):
         return _evaluate(run, net, steps, itmax, stall_window, method, restart)
 
 
 def learned_solve(run, net, x, itmax, stall_window, method, restart):
+    if method == "hybrid":
+        return run.s.solve_learned_hybrid_device(net, run.b, x, tol=run.tol,
+                                                 itmax=itmax,
+                                                 learned_steps=restart)
     if method == "gcr":
         return run.s.solve_gcr_device(run.b, x, net=net, tol=run.tol,
                                       itmax=itmax, restart=restart,

@@ -260,6 +260,20 @@ class Solver:
         return it.value, err.value, st, bool(fb.value)
 
     @_device_call
+    def solve_learned_hybrid_device(self, net, b, x, tol=None, itmax=1000,
+                                    learned_steps=2):
+        """learned_steps GCR steps with the network, then Jacobi-BiCGStab.
+        Returns (iterations, relative residual, status, False)."""
+        it, err = ctypes.c_int(0), ctypes.c_double(0.0)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve_learned_hybrid_device(
+            self.h, net.h, _ptr(b), _ptr(x), float(tol), int(itmax),
+            int(learned_steps), ctypes.byref(it), ctypes.byref(err))
+        L.check(st, "vdr_solve_learned_hybrid_device",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return it.value, err.value, st, False
+
+    @_device_call
     def solve_gcr_record_device(self, b, x, hist, net=None, tol=None,
                                 itmax=1000, restart=20):
         """GCR recording every iterate into hist.  Returns (recorded,
