@@ -310,6 +310,25 @@ int vdr_solve_record_device(vdr_handle *h, const double *d_b, double *d_x,
                             double tol, int itmax, double *d_hist,
                             int max_hist, int *n_hist, int *iter, double *err);
 
+/* ---- many independent meshes in one handle ----
+ * Build the handle on the concatenation of the meshes (node ids of mesh m
+ * offset by node_off[m], elements concatenated); vdr_set_segments declares
+ * the node ranges [node_off[m], node_off[m+1]) (nseg + 1 offsets; no element
+ * may couple two ranges).  The element build and the operator applies then
+ * cover every mesh in single launches, and the segmented solve runs
+ * Jacobi-BiCGStab with per-mesh scalars and per-mesh convergence (a mesh
+ * that converges freezes), all meshes advancing together in one CUDA graph.
+ * The tile shape of the per-mesh reductions is chosen by measurement at the
+ * first segmented solve (vdr_segment_tuning reports it).  No counterpart in
+ * the reference, which solves one mesh per call. */
+int vdr_set_segments(vdr_handle *h, int nseg, const int *node_off);
+/* iters, errs, statuses: host arrays of nseg (nullable).  Returns VDR_OK
+ * when every mesh met tol. */
+int vdr_solve_segmented_device(vdr_handle *h, const double *d_b, double *d_x,
+                               double tol, int itmax, int *iters,
+                               double *errs, int *statuses);
+int vdr_segment_tuning(vdr_handle *h, int *tile_nodes, int *threads);
+
 /* Statistics of the handle's most recent solve. */
 typedef struct vdr_solve_stats {
   int iterations;      /* Krylov iterations done */

@@ -132,3 +132,27 @@ def test_openmp_apply_matches_serial(vdr, oracle):
         y2 = oracle.matvec0_omp(m.iss, bb, prob.bc, ce, co, x, transpose=tr,
                                 nthreads=4)
         assert rel_l2(y2, y) < 1e-14
+
+
+def test_mesh_union_layout(vdr):
+    """Concatenated meshes: node ids offset per mesh, every element inside
+    its own node range, the cube sizes inside the drawn range."""
+    P = vdr.problems
+    sizes = P.cube_sizes(64, seed=2001, nmin=8, nmax=48)
+    assert sizes.min() >= 8 and sizes.max() <= 48
+    probs = P.cube_batch(5, seed=2001, nmin=2, nmax=5)
+    u = P.concat(probs)
+    m = u.mesh
+    E = m.nelem
+    assert E == sum(p.mesh.nelem for p in probs)
+    assert m.nnode == sum(p.mesh.nnode for p in probs) == m.xx.size
+    iss = m.iss.reshape(8, E).astype(np.int64) - 1
+    seg = np.searchsorted(m.node_off, iss[0], side="right") - 1
+    for k in range(8):
+        assert np.all(iss[k] >= m.node_off[seg])
+        assert np.all(iss[k] < m.node_off[seg + 1])
+    for i, p in enumerate(probs):
+        a, b = m.elem_off[i], m.elem_off[i + 1]
+        assert np.array_equal(iss[:, a:b] - m.node_off[i],
+                              p.mesh.iss.reshape(8, -1) - 1)
+    assert u.bc.size == m.nnode and u.vel.size == 3 * E

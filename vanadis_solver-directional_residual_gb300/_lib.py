@@ -67,6 +67,9 @@ SIGNATURES = {
     "vdr_solve_block_device": (_i, [_P, _i, _i, _P, _P, _d, _d, _i, _i, _I,
                                     _I, _D]),
     "vdr_true_residual_device": (_i, [_P, _P, _P, _D]),
+    "vdr_set_segments": (_i, [_P, _i, _I]),
+    "vdr_solve_segmented_device": (_i, [_P, _P, _P, _d, _i, _I, _D, _I]),
+    "vdr_segment_tuning": (_i, [_P, _I, _I]),
     "vdr_net_create": (_i, [_P, ctypes.c_ulonglong, ctypes.POINTER(_P)]),
     "vdr_net_destroy": (_i, [_P]),
     "vdr_net_param_count": (_i, [_P, ctypes.POINTER(ctypes.c_longlong)]),

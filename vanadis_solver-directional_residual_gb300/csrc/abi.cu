@@ -237,6 +237,8 @@ void free_handle(Handle &h) {
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
   dfree(h.gcr_work);
   if (h.gcr_graph) cudaGraphExecDestroy(h.gcr_graph);
+  dfree(h.seg_d); dfree(h.seg_i); dfree(h.seg_ticket); dfree(h.seg_of_elem);
+  if (h.seg_graph) cudaGraphExecDestroy(h.seg_graph);
   dfree(h.work); dfree(h.st); dfree(h.partials);
   if (h.h_st) cudaFreeHost(h.h_st);
   for (int k = 0; k < Handle::NGRAPH; k++)
@@ -747,6 +749,34 @@ int vdr_solve_block_device(vdr_handle *H, int K, int precision,
   if ((st = ensure_operator(h))) return st;
   return solve_block_device(h, K, precision, B, X, tol, inner_tol, max_outer,
                             inner_itmax, outer_iters, inner_iters, errs);
+}
+
+int vdr_set_segments(vdr_handle *H, int nseg, const int *node_off) {
+  int st = check_handle(H);
+  if (st) return st;
+  return set_segments(H->h, nseg, node_off);
+}
+
+int vdr_segment_tuning(vdr_handle *H, int *tile_nodes, int *threads) {
+  int st = check_handle(H);
+  if (st) return st;
+  if (tile_nodes) *tile_nodes = H->h.seg_tile;
+  if (threads) *threads = H->h.seg_threads;
+  return VDR_OK;
+}
+
+int vdr_solve_segmented_device(vdr_handle *H, const double *b, double *x,
+                               double tol, int itmax, int *iters, double *errs,
+                               int *statuses) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!b || !x || !(tol >= 0.0) || itmax < 0) {
+    set_error("vdr_solve_segmented_device: bad arguments");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator(h))) return st;
+  return solve_segmented_device(h, b, x, tol, itmax, iters, errs, statuses);
 }
 
 int vdr_solve(vdr_handle *H, const double *b, double *x, double tol,

@@ -192,11 +192,12 @@ __global__ void __launch_bounds__(256) stored_apply_df(
     const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
     const int *__restrict__ conn, int E, int p0, int p1,
     const double *__restrict__ x, double *__restrict__ y, const int *skip,
-    const int *skip2) {
+    const int *skip2, ElemGate gate) {
   if (skip && *(volatile const int *)skip) return;
   if (skip2 && *(volatile const int *)skip2) return;
   for (long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x; p < p1;
        p += (long)gridDim.x * blockDim.x) {
+    if (gate.active && !gate.active[__ldg(gate.eseg + p)]) continue;
     int c[8];
     double xv[8];
     float xh[8], xl[8];
@@ -365,7 +366,8 @@ cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
   K<<<grid, 256, 0, s>>>(AP, h.conn, h.E, p0, p1, x, y, skip, skip2)
     if (!fp32 && h.storage == VDR_STORE_DF) {
 #define VDR_LAUNCH_DF(K)                                                      \
-  K<<<grid, 256, 0, s>>>(h.Ahi, h.Alo, h.conn, h.E, p0, p1, x, y, skip, skip2)
+  K<<<grid, 256, 0, s>>>(h.Ahi, h.Alo, h.conn, h.E, p0, p1, x, y, skip, skip2, \
+                         ElemGate{h.gate_eseg, h.gate_active})
       if (transpose) {
         if (color) VDR_LAUNCH_DF((stored_apply_df<true, false>));
         else VDR_LAUNCH_DF((stored_apply_df<true, true>));

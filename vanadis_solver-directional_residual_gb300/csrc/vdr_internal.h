@@ -48,6 +48,13 @@ struct Precond {
 
 struct DeviceOp;  // forward
 
+// Optional gate of the stored-matrix applies: element p is skipped when
+// active[eseg[p]] == 0 (segments that have converged).
+struct ElemGate {
+  const int *eseg = nullptr;
+  const int *active = nullptr;
+};
+
 // Element-wise fields, device pointers in storage order.
 struct Fields {
   const double *vel = nullptr;   // [3][E]
@@ -140,6 +147,22 @@ struct Handle {
   cudaGraphExec_t bk_graph = nullptr;
   bool bk_graph_split = false;
 
+  // many meshes as segments (batch.cu)
+  std::vector<int> seg_off;  // node offsets, nseg + 1
+  int seg_tile = 0, seg_threads = 256;  // autotuned tile shape (0: not yet)
+  double *seg_d = nullptr;
+  size_t seg_dwords = 0;
+  int *seg_i = nullptr;
+  size_t seg_iwords = 0;
+  unsigned *seg_ticket = nullptr;
+  int seg_ticket_n = 0;
+  cudaGraphExec_t seg_graph = nullptr;
+  const void *seg_key = nullptr;
+  long seg_graph_launches = 0;
+  int *seg_of_elem = nullptr;         // [E] storage order
+  const int *gate_eseg = nullptr;     // apply gate while a segmented solve runs
+  const int *gate_active = nullptr;
+
   // restarted GCR (gcr.cu)
   double *gcr_work = nullptr;
   size_t gcr_words = 0;
@@ -223,6 +246,12 @@ int solve_gcr_device(Handle &h, const double *b, double *x, double tol,
                      int itmax, int m, const Precond *prec, int stall_window,
                      int *iter, double *err, double *hist = nullptr,
                      int max_hist = 0, int *n_hist = nullptr);
+
+// Segments (independent meshes in one handle) and their batched solve
+// (batch.cu).
+int set_segments(Handle &h, int nseg, const int *node_off);
+int solve_segmented_device(Handle &h, const double *b, double *x, double tol,
+                           int itmax, int *iters, double *errs, int *statuses);
 
 // Builds the element matrices and the Jacobi diagonal if stale (abi.cu).
 int prepare_operator(Handle &h);

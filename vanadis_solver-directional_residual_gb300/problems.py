@@ -74,6 +74,24 @@ class Mesh:
 
 
 @dataclass
+class MeshUnion(Mesh):
+    """Several meshes side by side (no element couples two of them): node
+    ids of mesh m are offset by node_off[m], elements concatenated."""
+    n_node: int = 0
+    n_elem: int = 0
+    node_off: np.ndarray = None
+    elem_off: np.ndarray = None
+
+    @property
+    def nnode(self) -> int:
+        return self.n_node
+
+    @property
+    def nelem(self) -> int:
+        return self.n_elem
+
+
+@dataclass
 class Problem:
     name: str
     mesh: Mesh
@@ -262,6 +280,75 @@ def random_gaussian_sources(mesh: Mesh, K: int, seed: int = 3001,
         Q[k] = _gauss_sources(cx, cy, cz, [centre], [0.03 + 0.07 * u[3]],
                               cell_volume)
     return Q
+
+
+def rotation_cube(n: int, seed: int, variant=DR_VF) -> Problem:
+    """One mesh of the many-mesh workload: n^3 elements on the jittered
+    unit cube, solid-body rotation about a seeded random axis through the
+    centre scaled to max |u_e| = 1, lognormal diffusivity exp(ln 1e-4 + xi),
+    one Gaussian source (seeded centre in [0.2, 0.8]^3, sigma in
+    [0.05, 0.1]), zero Dirichlet on inflow faces, tolerance 1e-8."""
+    mesh = structured_mesh(n, n, n, 0.1, seed)
+    E = mesh.nelem
+    cx, cy, cz = centroids(mesh)
+    g = normal(seed, 31, 3)
+    ax = g / np.linalg.norm(g)
+    rx, ry, rz = cx - 0.5, cy - 0.5, cz - 0.5
+    ux = ax[1] * rz - ax[2] * ry
+    uy = ax[2] * rx - ax[0] * rz
+    uz = ax[0] * ry - ax[1] * rx
+    sc = 1.0 / np.sqrt(ux * ux + uy * uy + uz * uz).max()
+    vel = np.concatenate([ux * sc, uy * sc, uz * sc])
+    lam = np.exp(math.log(1e-4) + normal(seed, 11, E))
+    u = uniform(seed, 33, 4)
+    q = _gauss_sources(cx, cy, cz, [tuple(0.2 + 0.6 * u[:3])],
+                       [0.05 + 0.05 * u[3]], 1.0 / E)
+    return Problem("rotation_cube_%d" % n, mesh, vel, lam, np.zeros(E), q,
+                   inflow_mask(mesh, vel), 0.0, variant, 1e-8, {"seed": seed})
+
+
+def cube_sizes(nmesh: int = 256, seed: int = 2001, nmin: int = 8,
+               nmax: int = 48) -> np.ndarray:
+    """Cube edges (elements) drawn uniformly from nmin..nmax."""
+    u = uniform(seed, 41, nmesh)
+    return (nmin + np.floor(u * (nmax - nmin + 1))).astype(int)
+
+
+def cube_batch(nmesh: int = 256, seed: int = 2001, nmin: int = 8,
+               nmax: int = 48) -> list:
+    """The many-mesh workload: mesh m is rotation_cube(n_m, seed + m)."""
+    return [rotation_cube(int(n), seed + m)
+            for m, n in enumerate(cube_sizes(nmesh, seed, nmin, nmax))]
+
+
+def concat(problems: list) -> Problem:
+    """One problem holding several meshes side by side (the block-diagonal
+    system of all of them); its mesh records node_off / elem_off."""
+    Ns = [p.mesh.nnode for p in problems]
+    Es = [p.mesh.nelem for p in problems]
+    node_off = np.concatenate([[0], np.cumsum(Ns)]).astype(np.int64)
+    elem_off = np.concatenate([[0], np.cumsum(Es)]).astype(np.int64)
+    iss = np.concatenate(
+        [p.mesh.iss.reshape(8, E).astype(np.int64) + o
+         for p, E, o in zip(problems, Es, node_off[:-1])], axis=1)
+    kod = np.concatenate([p.mesh.kod.reshape(6, E)
+                          for p, E in zip(problems, Es)], axis=1)
+    vel = np.concatenate([p.vel.reshape(3, E) for p, E in zip(problems, Es)],
+                         axis=1)
+    mesh = MeshUnion(0, 0, 0,
+                     np.concatenate([p.mesh.xx for p in problems]),
+                     np.concatenate([p.mesh.yy for p in problems]),
+                     np.concatenate([p.mesh.zz for p in problems]),
+                     iss.astype(np.int32).ravel(), kod.astype(np.int32).ravel(),
+                     n_node=int(node_off[-1]), n_elem=int(elem_off[-1]),
+                     node_off=node_off, elem_off=elem_off)
+    return Problem("union_of_%d" % len(problems), mesh, vel.ravel(),
+                   np.concatenate([p.lam for p in problems]),
+                   np.concatenate([p.pdec for p in problems]),
+                   np.concatenate([p.q for p in problems]),
+                   np.concatenate([p.bc for p in problems]),
+                   problems[0].robin_alpha, problems[0].variant,
+                   problems[0].tol, {"meshes": len(problems)})
 
 
 def constant_advection(nex=32, ney=32, nez=16, seed=1001) -> Problem:

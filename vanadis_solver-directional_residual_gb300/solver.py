@@ -226,6 +226,36 @@ class Solver:
                 allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
         return it.value, err.value, st
 
+    def set_segments(self, node_off):
+        """Declare independent meshes: node ranges [off[m], off[m+1])."""
+        off = _i32(node_off)
+        L.check(self.lib.vdr_set_segments(self.h, int(off.size - 1), _ip(off)),
+                "vdr_set_segments")
+        self.nseg = int(off.size - 1)
+
+    @_device_call
+    def solve_segmented_device(self, b, x, tol=None, itmax=1000):
+        """All meshes at once, per-mesh convergence.  Returns (iterations,
+        relative residuals, statuses) per mesh and the overall status."""
+        n = self.nseg
+        its = np.zeros(n, dtype=np.int32)
+        errs = np.zeros(n)
+        sts = np.zeros(n, dtype=np.int32)
+        tol = self.problem.tol if tol is None else tol
+        st = self.lib.vdr_solve_segmented_device(self.h, _ptr(b), _ptr(x),
+                                                 float(tol), int(itmax), _ip(its),
+                                                 _dp(errs), _ip(sts))
+        L.check(st, "vdr_solve_segmented_device",
+                allow=(L.OK, L.NOT_CONVERGED, L.BREAKDOWN))
+        return its, errs, sts, st
+
+    def segment_tuning(self):
+        t, th = ctypes.c_int(0), ctypes.c_int(0)
+        L.check(self.lib.vdr_segment_tuning(self.h, ctypes.byref(t),
+                                            ctypes.byref(th)),
+                "vdr_segment_tuning")
+        return t.value, th.value
+
     @_device_call
     def solve_learned_device(self, net, b, x, tol=None, itmax=1000,
                              stall_window=20):
