@@ -188,7 +188,7 @@ __device__ __noinline__ void df_element_fallback(
 }
 
 template <bool TRANS, bool ATOMIC>
-__global__ void __launch_bounds__(256) stored_apply_df(
+__global__ void __launch_bounds__(256, 4) stored_apply_df(
     const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
     const int *__restrict__ conn, int E, int p0, int p1,
     const double *__restrict__ x, double *__restrict__ y, const int *skip,
@@ -218,8 +218,9 @@ __global__ void __launch_bounds__(256) stored_apply_df(
       df_element_fallback(Ahi, Alo, conn, E, p, TRANS, ATOMIC, x, y);
       continue;
     }
-    double out[8];
     if (!TRANS) {
+      // each row is scattered as soon as it is complete (fewer live
+      // registers: 4 blocks of 256 threads per SM)
 #pragma unroll
       for (int i = 0; i < 8; i++) {
         const float4 h0 = __ldcs(Ahi + (size_t)(2 * i) * E + p);
@@ -235,9 +236,19 @@ __global__ void __launch_bounds__(256) stored_apply_df(
         df_fma_acc(acc, h1.y, l1.y, xh[5], xl[5]);
         df_fma_acc(acc, h1.z, l1.z, xh[6], xl[6]);
         df_fma_acc(acc, h1.w, l1.w, xh[7], xl[7]);
-        out[i] = df_to_double(acc.s, acc.c);
+        double o = df_to_double(acc.s, acc.c);
+        if (!df_scale(o, shift)) o = ldexp(o, shift);
+        if (c[i] >= 0) {
+          if (ATOMIC)
+            atomicAdd(y + c[i], o);
+          else
+            y[c[i]] += o;
+        }
       }
-    } else {
+      continue;
+    }
+    double out[8];
+    {
       DfAcc acc[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) acc[j] = DfAcc{0.0f, 0.0f};
