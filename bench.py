@@ -60,6 +60,10 @@ def args_parse():
                     help="skip the learned-preconditioner section")
     ap.add_argument("--learn-steps", type=int, default=LEARN_STEPS)
     ap.add_argument("--learn-epochs", type=int, default=1)
+    ap.add_argument("--case", default=None,
+                    choices=["apply", "block_apply", "unet_train"],
+                    help="run one small fixed workload for a profiler "
+                         "capture instead of the benchmark")
     ap.add_argument("--cpu-iters", type=int, default=4,
                     help="BiCGStab iterations timed in the CPU sample")
     return ap.parse_args()
@@ -801,8 +805,52 @@ def run_native(a):
     return 0
 
 
+def run_case(a):
+    """Small fixed workloads for profiler captures (not benchmarks): the
+    stored double-float apply (--case apply), the K=64 block solve
+    (--case block_apply) and learned-network training steps
+    (--case unet_train), each on the --nex x --ney x --nez mesh."""
+    import torch
+    import __graft_entry__
+    vdr = __graft_entry__.package()
+    vdr.load_library()
+    P = vdr.problems
+    prob = P.rotation_shear(a.nex, a.ney, a.nez, seed=1002)
+    dt = COURANT / max(a.nex, a.ney, a.nez)
+    if a.case == "apply":
+        s = vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=2.0, aM=3.0 / dt)
+        x = torch.randn(prob.mesh.nnode, dtype=torch.float64, device="cuda")
+        y = torch.zeros_like(x)
+        torch.cuda.synchronize()
+        for _ in range(3):
+            s.apply_accumulate_device(x, y)
+    elif a.case == "block_apply":
+        s = vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=2.0, aM=3.0 / dt)
+        K = BATCH_K
+        Q = torch.as_tensor(P.random_gaussian_sources(prob.mesh, K), device="cuda")
+        B = torch.empty((prob.mesh.nnode, K), dtype=torch.float64, device="cuda")
+        s.assemble_rhs_block_device(Q, B, 3.0)
+        X = torch.zeros_like(B)
+        s.solve_block_device(B, X, tol=TOL, inner_tol=1e-3, precision="tf32x3")
+    elif a.case == "unet_train":
+        L = vdr.learned
+        run = L.TiltingRun(a.nex, a.ney, a.nez, seed=1005, courant=COURANT,
+                           tol=TOL, tilt_deg=LEARN_TILT)
+        net = vdr.LearnedNet(run.s, seed=11)
+        data = L.collect_pairs(run, net, range(0, 1), pairs_per_step=4)
+        run.set_step(0)
+        net.set_features(data["feats"][0], float(data["dbars"][0]))
+        for i in range(3):
+            net.train_step_residual(data["rhat"][i], 1e-4)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": a.case, "elements": prob.mesh.nelem}))
+    return 0
+
+
 def main():
     a = args_parse()
+    if a.case:
+        return run_case(a)
     if a.impl == "reference":
         return run_reference(a)
     return run_native(a)
