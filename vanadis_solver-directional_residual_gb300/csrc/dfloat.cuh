@@ -149,6 +149,27 @@ __device__ __forceinline__ void df_acc(DfAcc &acc, Df2 a, Df2 b) {
   df_fma_acc(acc, a.h, a.l, b.h, b.l);
 }
 
+// The accumulator as a normalized pair (TwoSum of its two parts).
+__device__ __forceinline__ Df2 df_norm(const DfAcc &a) {
+  const float s = __fadd_rn(a.s, a.c);
+  const float bp = __fsub_rn(s, a.s);
+  const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bp)), __fsub_rn(a.c, bp));
+  return Df2{s, e};
+}
+
+// a + b and a - b, normalized.
+__device__ __forceinline__ Df2 df_add(Df2 a, Df2 b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float bp = __fsub_rn(s, a.h);
+  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bp)), __fsub_rn(b.h, bp));
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, e);
+  const float bq = __fsub_rn(h, s);
+  return Df2{h, __fadd_rn(__fsub_rn(s, __fsub_rn(h, bq)), __fsub_rn(e, bq))};
+}
+__device__ __forceinline__ Df2 df_neg(Df2 a) { return Df2{-a.h, -a.l}; }
+__device__ __forceinline__ Df2 df_sub(Df2 a, Df2 b) { return df_add(a, df_neg(b)); }
+
 // acc += a.
 __device__ __forceinline__ void df_acc_add(DfAcc &acc, Df2 a) {
   const float t = __fadd_rn(acc.s, a.h);

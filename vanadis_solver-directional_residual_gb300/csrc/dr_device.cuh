@@ -128,6 +128,55 @@ __device__ __forceinline__ void shape_at(const T xi, const T eta, const T zeta,
 // Geometry and DR weight of one point given its shape data: detJ, grad N
 // (x,y,z) and W.  xe/ye/ze hold the 8 node coordinates in local order;
 // (vx,vy,vz), lam are the element's velocity and isotropic diffusivity.
+// The DR stabilization parameter tau at one point from the inverse
+// Jacobian (i_ab = d xi_a / d x_b) and the element's velocity and
+// diffusivity: streamline length h (OT: axis edge lengths; GP/VF: 2/|J^-1 e|,
+// e = v/|v|), streamline diffusivity (VF: e^T Lambda e), Peclet number and
+// beta(Pe) as the three reference variants define them.
+template <typename T>
+__device__ __forceinline__ T dr_tau(const int variant, const T i11, const T i12,
+                                    const T i13, const T i21, const T i22,
+                                    const T i23, const T i31, const T i32,
+                                    const T i33, const T (&xe)[8],
+                                    const T (&ye)[8], const T (&ze)[8],
+                                    const T lam, const T vx, const T vy,
+                                    const T vz) {
+  const T eps = T(1.0e-14);
+  const T vmag = dr_sqrt(vx * vx + vy * vy + vz * vz);
+  T h, lams;
+  if (variant == DR_OT) {
+    const T dlx = dr_abs(xe[1] - xe[0]);
+    const T dly = dr_abs(ye[3] - ye[0]);
+    const T dlz = dr_abs(ze[4] - ze[0]);
+    h = (vmag > eps)
+            ? T(2) / (dr_abs(vx) / dlx + dr_abs(vy) / dly + dr_abs(vz) / dlz + eps)
+            : T(0);
+    lams = lam;
+  } else {
+    T ex = 0, ey = 0, ez = 0;
+    if (vmag > eps) {
+      const T iv = T(1) / vmag;
+      ex = vx * iv;
+      ey = vy * iv;
+      ez = vz * iv;
+    }
+    const T gx = i11 * ex + i12 * ey + i13 * ez;
+    const T gy = i21 * ex + i22 * ey + i23 * ez;
+    const T gz = i31 * ex + i32 * ey + i33 * ez;
+    const T gn = dr_sqrt(gx * gx + gy * gy + gz * gz);
+    h = (gn > eps) ? T(2) / gn : T(0);
+    lams = (variant == DR_VF) ? (lam * ex * ex + lam * ey * ey + lam * ez * ez) : lam;
+  }
+  T pe = 0;
+  if (vmag > eps && lams > eps) pe = vmag * h / (T(2) * lams);
+  T tau = 0;
+  if (pe > T(1.0e-12) && vmag > eps) {
+    const T beta = (variant == DR_VF) ? beta_safe<T>(pe) : beta_exp(pe);
+    tau = T(0.5) * h / vmag * beta;
+  }
+  return tau;
+}
+
 template <typename T>
 __device__ __forceinline__ void gp_core(const int variant, const T *nsh,
                                         const T *d0, const T *d1, const T *d2,
@@ -171,39 +220,8 @@ __device__ __forceinline__ void gp_core(const int variant, const T *nsh,
     o.gz[i] = i13 * d0[i] + i23 * d1[i] + i33 * d2[i];
   }
 
-  const T eps = T(1.0e-14);
-  const T vmag = dr_sqrt(vx * vx + vy * vy + vz * vz);
-  T h, lams;
-  if (variant == DR_OT) {
-    const T dlx = dr_abs(xe[1] - xe[0]);
-    const T dly = dr_abs(ye[3] - ye[0]);
-    const T dlz = dr_abs(ze[4] - ze[0]);
-    h = (vmag > eps)
-            ? T(2) / (dr_abs(vx) / dlx + dr_abs(vy) / dly + dr_abs(vz) / dlz + eps)
-            : T(0);
-    lams = lam;
-  } else {
-    T ex = 0, ey = 0, ez = 0;
-    if (vmag > eps) {
-      const T iv = T(1) / vmag;
-      ex = vx * iv;
-      ey = vy * iv;
-      ez = vz * iv;
-    }
-    const T gx = i11 * ex + i12 * ey + i13 * ez;
-    const T gy = i21 * ex + i22 * ey + i23 * ez;
-    const T gz = i31 * ex + i32 * ey + i33 * ez;
-    const T gn = dr_sqrt(gx * gx + gy * gy + gz * gz);
-    h = (gn > eps) ? T(2) / gn : T(0);
-    lams = (variant == DR_VF) ? (lam * ex * ex + lam * ey * ey + lam * ez * ez) : lam;
-  }
-  T pe = 0;
-  if (vmag > eps && lams > eps) pe = vmag * h / (T(2) * lams);
-  T tau = 0;
-  if (pe > T(1.0e-12) && vmag > eps) {
-    const T beta = (variant == DR_VF) ? beta_safe<T>(pe) : beta_exp(pe);
-    tau = T(0.5) * h / vmag * beta;
-  }
+  const T tau = dr_tau<T>(variant, i11, i12, i13, i21, i22, i23, i31, i32, i33,
+                          xe, ye, ze, lam, vx, vy, vz);
 #pragma unroll
   for (int i = 0; i < 8; i++)
     o.w[i] = o.n[i] + tau * (vx * o.gx[i] + vy * o.gy[i] + vz * o.gz[i]);

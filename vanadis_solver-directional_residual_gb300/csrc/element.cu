@@ -341,11 +341,17 @@ struct BuildSmemDF {
   Df2 fnw[ROWS_EPB][4][2][8];  // face-3 points: N, W
   Df2 fd[ROWS_EPB][4];         // alpha*detJs
   double tab[12][4][8];
+  Df2 tabdf[8][4][8];          // the volume points' tables as pairs
 };
 
-__global__ void __launch_bounds__(64) elem_build_df_kernel(OpArgs a, BuildArgs ba) {
+__global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArgs ba) {
   __shared__ BuildSmemDF sm;
   fill_shape_tables<double>(sm.tab);
+  for (int t = threadIdx.x; t < 8 * 4 * 8; t += blockDim.x) {
+    const int q = t >> 5, k = (t >> 3) & 3, i = t & 7;
+    sm.tabdf[q][k][i] = df_from_double(sm.tab[q][k][i]);
+  }
+  __syncthreads();
   const int lane8 = threadIdx.x & 7;
   const int le = threadIdx.x >> 3;
   const long E = a.E;
@@ -356,25 +362,95 @@ __global__ void __launch_bounds__(64) elem_build_df_kernel(OpArgs a, BuildArgs b
     const long p = valid ? pe : E - 1;
     Elem<double> el;
     load_elem<double>(a, p, el);
-    GPData<double> o;
-    gp_core<double>(a.variant, sm.tab[lane8][0], sm.tab[lane8][1],
-                    sm.tab[lane8][2], sm.tab[lane8][3], el.xe, el.ye, el.ze,
-                    el.lam, el.vx, el.vy, el.vz, o);
-    const double vol = group8_sum<double>(o.detj);
+    // Gauss point lane8 in double-float on the FP32 pipe: Jacobian from the
+    // node coordinates relative to local node 1 (differences formed in
+    // FP64, so they keep full precision), cofactors, inverse, gradients and
+    // W; only 1/detJ and the DR parameter tau are FP64.
     bool range_bad = false;  // a quantity the pairs cannot hold safely
+    const Df2 *tn = sm.tabdf[lane8][0], *t0 = sm.tabdf[lane8][1],
+              *t1 = sm.tabdf[lane8][2], *t2 = sm.tabdf[lane8][3];
+    DfAcc J[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) J[k] = DfAcc{0.0f, 0.0f};
+#pragma unroll
+    for (int k = 1; k < 8; k++) {  // local node 1 is the origin
+      const Df2 rx = df_from_double_chk(el.xe[k] - el.xe[0], range_bad);
+      const Df2 ry = df_from_double_chk(el.ye[k] - el.ye[0], range_bad);
+      const Df2 rz = df_from_double_chk(el.ze[k] - el.ze[0], range_bad);
+      df_acc(J[0], rx, t0[k]);
+      df_acc(J[1], rx, t1[k]);
+      df_acc(J[2], rx, t2[k]);
+      df_acc(J[3], ry, t0[k]);
+      df_acc(J[4], ry, t1[k]);
+      df_acc(J[5], ry, t2[k]);
+      df_acc(J[6], rz, t0[k]);
+      df_acc(J[7], rz, t1[k]);
+      df_acc(J[8], rz, t2[k]);
+    }
+    const Df2 j11 = df_norm(J[0]), j12 = df_norm(J[1]), j13 = df_norm(J[2]);
+    const Df2 j21 = df_norm(J[3]), j22 = df_norm(J[4]), j23 = df_norm(J[5]);
+    const Df2 j31 = df_norm(J[6]), j32 = df_norm(J[7]), j33 = df_norm(J[8]);
+    const Df2 c11 = df_sub(df_mul(j22, j33), df_mul(j23, j32));
+    const Df2 c12 = df_sub(df_mul(j21, j33), df_mul(j23, j31));
+    const Df2 c13 = df_sub(df_mul(j21, j32), df_mul(j22, j31));
+    const Df2 detp =
+        df_add(df_sub(df_mul(j11, c11), df_mul(j12, c12)), df_mul(j13, c13));
+    const double detj = df_to_double(detp.h, detp.l);
+    const Df2 r = df_from_double_chk(1.0 / detj, range_bad);
+    const Df2 di11 = df_mul(r, c11);
+    const Df2 di12 = df_mul(r, df_sub(df_mul(j13, j32), df_mul(j12, j33)));
+    const Df2 di13 = df_mul(r, df_sub(df_mul(j12, j23), df_mul(j13, j22)));
+    const Df2 di21 = df_neg(df_mul(r, c12));
+    const Df2 di22 = df_mul(r, df_sub(df_mul(j11, j33), df_mul(j13, j31)));
+    const Df2 di23 = df_mul(r, df_sub(df_mul(j13, j21), df_mul(j11, j23)));
+    const Df2 di31 = df_mul(r, c13);
+    const Df2 di32 = df_mul(r, df_sub(df_mul(j12, j31), df_mul(j11, j32)));
+    const Df2 di33 = df_mul(r, df_sub(df_mul(j11, j22), df_mul(j12, j21)));
+    const double tau = dr_tau<double>(
+        a.variant, df_to_double(di11.h, di11.l), df_to_double(di12.h, di12.l),
+        df_to_double(di13.h, di13.l), df_to_double(di21.h, di21.l),
+        df_to_double(di22.h, di22.l), df_to_double(di23.h, di23.l),
+        df_to_double(di31.h, di31.l), df_to_double(di32.h, di32.l),
+        df_to_double(di33.h, di33.l), el.xe, el.ye, el.ze, el.lam, el.vx,
+        el.vy, el.vz);
+    const Df2 vxd = df_from_double_chk(el.vx, range_bad);
+    const Df2 vyd = df_from_double_chk(el.vy, range_bad);
+    const Df2 vzd = df_from_double_chk(el.vz, range_bad);
+    const Df2 pd = df_from_double_chk(el.pdec, range_bad);
+    const Df2 taud = df_from_double_chk(tau, range_bad);
 #pragma unroll
     for (int j = 0; j < 8; j++) {
-      sm.g[le][lane8][0][j] = df_from_double_chk(o.gx[j], range_bad);
-      sm.g[le][lane8][1][j] = df_from_double_chk(o.gy[j], range_bad);
-      sm.g[le][lane8][2][j] = df_from_double_chk(o.gz[j], range_bad);
-      sm.g[le][lane8][3][j] = df_from_double_chk(
-          (el.vx * o.gx[j] + el.vy * o.gy[j] + el.vz * o.gz[j]) + el.pdec * o.n[j],
-          range_bad);
-      sm.g[le][lane8][4][j] = df_from_double_chk(o.n[j], range_bad);
-      sm.g[le][lane8][5][j] = df_from_double_chk(o.w[j], range_bad);
+      DfAcc ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
+      df_acc(ax, di11, t0[j]);
+      df_acc(ax, di21, t1[j]);
+      df_acc(ax, di31, t2[j]);
+      df_acc(ay, di12, t0[j]);
+      df_acc(ay, di22, t1[j]);
+      df_acc(ay, di32, t2[j]);
+      df_acc(az, di13, t0[j]);
+      df_acc(az, di23, t1[j]);
+      df_acc(az, di33, t2[j]);
+      const Df2 gx = df_norm(ax), gy = df_norm(ay), gz = df_norm(az);
+      DfAcc av{0.0f, 0.0f};
+      df_acc(av, vxd, gx);
+      df_acc(av, vyd, gy);
+      df_acc(av, vzd, gz);
+      const Df2 vg = df_norm(av);
+      DfAcc aw{0.0f, 0.0f}, aa = av;
+      df_acc_add(aw, tn[j]);
+      df_acc(aw, taud, vg);
+      df_acc(aa, pd, tn[j]);
+      sm.g[le][lane8][0][j] = gx;
+      sm.g[le][lane8][1][j] = gy;
+      sm.g[le][lane8][2][j] = gz;
+      sm.g[le][lane8][3][j] = df_norm(aa);
+      sm.g[le][lane8][4][j] = tn[j];
+      sm.g[le][lane8][5][j] = df_norm(aw);
     }
-    sm.d[le][lane8][0] = df_from_double_chk(o.detj, range_bad);
-    sm.d[le][lane8][1] = df_from_double_chk(el.lam * o.detj, range_bad);
+    const double vol = group8_sum<double>(detj);
+    sm.d[le][lane8][0] = df_from_double_chk(detj, range_bad);
+    sm.d[le][lane8][1] = df_from_double_chk(el.lam * detj, range_bad);
+    GPData<double> o;  // face-3 points (Robin term)
     if (el.robin && lane8 < 4) {
       const double gc = VDR_GAUSS_C;
       const double r = (lane8 & 2) ? gc : -gc;
