@@ -503,14 +503,43 @@ __global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArg
     }
     __syncwarp();
     if (!valid) continue;
-    double Hr[8], Mr[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      Hr[j] = df_to_double(accH[j].s, accH[j].c);
-      Mr[j] = df_to_double(accM[j].s, accM[j].c);
-    }
     const int ci = el.c[i];
-    if (ba.A64 || ba.Ahi || ba.diag) {
+    if (ba.Ahi && !ba.A64) {
+      // double-float store: A_e row = aH H + aM M formed in double-float,
+      // stored as its (hi, lo) pair; the store window is checked on hi
+      // (FP32 biased exponent 27..247 = FP64 exponent -100..120)
+      const Df2 aHd = df_from_double(ba.aH), aMd = df_from_double(ba.aM);
+      Df2 rowd[8];
+      bool bad = false;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        DfAcc acc{0.0f, 0.0f};
+        df_acc(acc, aHd, df_norm(accH[j]));
+        df_acc(acc, aMd, df_norm(accM[j]));
+        rowd[j] = df_norm(acc);
+        const unsigned eb = (__float_as_uint(rowd[j].h) >> 23) & 0xffu;
+        if (rowd[j].h != 0.0f && (eb < 27u || eb > 247u)) bad = true;
+      }
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        ba.Ahi[(size_t)(2 * i + h) * E + p] =
+            make_float4(rowd[4 * h].h, rowd[4 * h + 1].h, rowd[4 * h + 2].h, rowd[4 * h + 3].h);
+        ba.Alo[(size_t)(2 * i + h) * E + p] =
+            make_float4(rowd[4 * h].l, rowd[4 * h + 1].l, rowd[4 * h + 2].l, rowd[4 * h + 3].l);
+      }
+      if (bad) atomicOr(ba.bad, 1);  // store window (bit 1)
+      if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, df_to_double(rowd[i].h, rowd[i].l));
+    }
+    double Hr[8], Mr[8];
+    const bool need64 = ba.A64 || (ba.diag && !ba.Ahi) || (ba.b && ba.told);
+    if (need64) {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        Hr[j] = df_to_double(accH[j].s, accH[j].c);
+        Mr[j] = df_to_double(accM[j].s, accM[j].c);
+      }
+    }
+    if (!ba.Ahi && (ba.A64 || ba.diag)) {
       double row[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) row[j] = ba.aH * Hr[j] + ba.aM * Mr[j];
@@ -518,25 +547,6 @@ __global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArg
 #pragma unroll
         for (int jj = 0; jj < 4; jj++)
           ba.A64[(size_t)(4 * i + jj) * E + p] = make_double2(row[2 * jj], row[2 * jj + 1]);
-      }
-      if (ba.Ahi) {
-        bool bad = false;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const int ej = df_exp(row[j]);
-          if (ej != 0 && (ej < 1023 - 100 || ej > 1023 + 120)) bad = true;
-        }
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          float4 vh, vl;
-          df_split(row[4 * h], vh.x, vl.x, bad);
-          df_split(row[4 * h + 1], vh.y, vl.y, bad);
-          df_split(row[4 * h + 2], vh.z, vl.z, bad);
-          df_split(row[4 * h + 3], vh.w, vl.w, bad);
-          ba.Ahi[(size_t)(2 * i + h) * E + p] = vh;
-          ba.Alo[(size_t)(2 * i + h) * E + p] = vl;
-        }
-        if (bad) atomicOr(ba.bad, 1);  // store window (bit 1)
       }
       if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, row[i]);
     }
