@@ -728,19 +728,33 @@ def run_native(a):
     learned = None if a.no_learned else learned_section(vdr, local, a)
 
     # ---- e2e through the C ABI with host buffers ----
-    vel, lam, pdec, q = prob.vel, prob.lam, prob.pdec, prob.q
+    # The step's inputs (per-element fields) and outputs (right-hand side,
+    # solution) live in pinned host memory; every step uploads the fields,
+    # assembles and downloads b, uploads b and x and downloads x.
+    keep = []
+
+    def pinned(arr):
+        t = torch.empty(arr.shape, dtype=torch.float64, pin_memory=True)
+        keep.append(t)
+        view = t.numpy()
+        view[:] = arr
+        return view
+
+    vel, lam, pdec, q = (pinned(v) for v in (prob.vel, prob.lam, prob.pdec,
+                                             prob.q))
+    bh = pinned(np.zeros(N))
+    xh = pinned(np.zeros(N))
     h2d = 8 * (vel.size + lam.size + pdec.size + q.size) + 8 * N + 8 * N
     d2h = 8 * N + 8 * N
     e2e_times = []
-    xh = np.zeros(N)
     for k in range(2 + a.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         s.set_fields(vel, lam, pdec, q, prob.robin_alpha)   # H2D fields
         s.set_operator(aH, aM)
-        bh = s.assemble_rhs(cf, rM, None)                    # D2H b
+        s.assemble_rhs(cf, rM, None, out=bh)                 # D2H b
         xh[:] = 0.0
-        xh2, it2, err2, st2 = s.solve(bh, xh, tol=TOL, itmax=20000)  # H2D b,x; D2H x
+        s.solve(bh, tol=TOL, itmax=20000, out=xh)            # H2D b,x; D2H x
         e2e_times.append(time.perf_counter() - t0)
     e2e = statistics.mean(e2e_times[2:])
 

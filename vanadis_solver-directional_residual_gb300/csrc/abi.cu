@@ -218,6 +218,32 @@ void invalidate(Handle &h) {
   h.aos_valid = h.phi_valid = false;
 }
 
+// d64[c][p] = src[c][perm[p]] (perm null: identity), d32 the FP32 copy.
+__global__ void fields_convert_kernel(const double *__restrict__ src, int ncols, long E,
+                                      const int *__restrict__ perm, double *d64,
+                                      float *d32) {
+  const long total = (long)ncols * E;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long)gridDim.x * blockDim.x) {
+    const long c = t / E, p = t - c * E;
+    const double v = src[c * E + (perm ? perm[p] : p)];
+    d64[t] = v;
+    if (d32) d32[t] = (float)v;
+  }
+}
+
+cudaError_t launch_fields_convert(const double *src, int ncols, long E, const int *perm,
+                                  double *d64, float *d32, cudaStream_t s) {
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long need = ((long)ncols * E + 255) / 256;
+  const int grid = (int)std::max<long>(1, std::min<long>(need, (long)sms * 8));
+  fields_convert_kernel<<<grid, 256, 0, s>>>(src, ncols, E, perm, d64, d32);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 int upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
   cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
   if (e) return cuda_fail(e, "upload");
@@ -235,7 +261,7 @@ void free_handle(Handle &h) {
   dfree(h.Aaos); dfree(h.phi); dfree(h.perm_d); dfree(h.dinv32);
   dfree(h.bk_f); dfree(h.bk_d);
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
-  dfree(h.gcr_work);
+  dfree(h.gcr_work); dfree(h.stage_d);
   if (h.gcr_graph) cudaGraphExecDestroy(h.gcr_graph);
   dfree(h.seg_d); dfree(h.seg_i); dfree(h.seg_ticket); dfree(h.seg_of_elem);
   if (h.seg_graph) cudaGraphExecDestroy(h.seg_graph);
@@ -457,27 +483,25 @@ int vdr_set_fields(vdr_handle *H, const double *vel, const double *lam,
       (e = dalloc(&h.vel32, 3 * E)) || (e = dalloc(&h.lam32, E)) ||
       (e = dalloc(&h.pdec32, E)))
     return cuda_fail(e, "vdr_set_fields: alloc");
-  std::vector<double> buf(3 * E);
-  std::vector<float> buf32(3 * E);
+  // Each field goes straight from the caller's array into a device staging
+  // buffer (a DMA when the caller's memory is pinned); a kernel puts it into
+  // storage order and writes the FP32 copy.  One synchronisation at the end
+  // (the caller may reuse its arrays after the call).
+  if ((e = dalloc(&h.stage_d, 3 * E))) return cuda_fail(e, "vdr_set_fields: alloc");
   auto put = [&](const double *src, int ncols, double *d64, float *d32) -> int {
-    if (src) {
-      permute_cols(src, buf.data(), E, ncols, h.perm);
-    } else {
-      std::fill(buf.begin(), buf.begin() + ncols * E, 0.0);
-    }
-    int s2 = upload(d64, buf.data(), sizeof(double) * ncols * E, h.stream);
-    if (s2) return s2;
-    if (d32) {
-      for (long i = 0; i < ncols * E; i++) buf32[i] = (float)buf[i];
-      s2 = upload(d32, buf32.data(), sizeof(float) * ncols * E, h.stream);
-      if (s2) return s2;
-    }
-    cudaError_t e3 = cudaStreamSynchronize(h.stream);  // buf is reused
-    return e3 ? cuda_fail(e3, "vdr_set_fields") : VDR_OK;
+    cudaError_t e2;
+    if (src)
+      e2 = cudaMemcpyAsync(h.stage_d, src, sizeof(double) * ncols * E,
+                           cudaMemcpyHostToDevice, h.stream);
+    else
+      e2 = cudaMemsetAsync(h.stage_d, 0, sizeof(double) * ncols * E, h.stream);
+    if (!e2) e2 = launch_fields_convert(h.stage_d, ncols, E, h.perm_d, d64, d32, h.stream);
+    return e2 ? cuda_fail(e2, "vdr_set_fields") : VDR_OK;
   };
   if ((st = put(vel, 3, h.vel, h.vel32)) || (st = put(lam, 1, h.lam, h.lam32)) ||
       (st = put(pdec, 1, h.pdec, h.pdec32)) || (st = put(q, 1, h.q, nullptr)))
     return st;
+  if ((e = cudaStreamSynchronize(h.stream))) return cuda_fail(e, "vdr_set_fields");
   h.robin_alpha = robin_alpha;
   h.fields_set = true;
   invalidate(h);

@@ -131,6 +131,7 @@ struct Handle {
   // host staging
   double *h_stage = nullptr;
   size_t h_stage_bytes = 0;
+  double *stage_d = nullptr;  // [3E] device staging of uploaded fields
 
   vdr_solve_stats last{};
 

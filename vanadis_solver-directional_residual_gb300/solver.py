@@ -162,8 +162,10 @@ class Solver:
                 "vdr_apply")
         return y
 
-    def assemble_rhs(self, cf=1.0, rM=0.0, t_old=None):
-        b = np.empty(self.N)
+    def assemble_rhs(self, cf=1.0, rM=0.0, t_old=None, out=None):
+        """Right-hand side into a new array, or into `out` (float64, N;
+        pinned host memory makes the copy a DMA)."""
+        b = np.empty(self.N) if out is None else out
         L.check(self.lib.vdr_assemble_rhs(self.h, float(cf), float(rM),
                                           _dp(_f64(t_old)), _dp(b)),
                 "vdr_assemble_rhs")
@@ -174,10 +176,17 @@ class Solver:
         L.check(self.lib.vdr_get_diag(self.h, _dp(d)), "vdr_get_diag")
         return d
 
-    def solve(self, b, x0=None, tol=None, itmax=1000):
-        """Returns (x, iterations, relative residual, status)."""
+    def solve(self, b, x0=None, tol=None, itmax=1000, out=None):
+        """Returns (x, iterations, relative residual, status).  With `out`
+        (float64, N) the solution is written there, starting from x0 (or
+        from out's own contents when x0 is None)."""
         b = _f64(b)
-        x = np.zeros(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        if out is not None:
+            x = out
+            if x0 is not None and x0 is not out:
+                x[:] = x0
+        else:
+            x = np.zeros(self.N) if x0 is None else np.array(x0, dtype=np.float64)
         it, err = ctypes.c_int(0), ctypes.c_double(0.0)
         tol = self.problem.tol if tol is None else tol
         st = self.lib.vdr_solve(self.h, _dp(b), _dp(x), float(tol), int(itmax),
