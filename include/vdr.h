@@ -191,6 +191,17 @@ int vdr_time_steps(vdr_handle *h, int nsteps, double cf, double rM,
 #define VDR_BLOCK_TF32X3 2 /* FP32 vectors, split TF32 (three MMAs per
                               product: FP32-level accuracy) */
 
+/* Data movement of the tensor-core block apply: VDR_BLOCK_APPLY_LSU
+ * (default, the faster by measurement) gathers X rows with 16-byte loads and
+ * scatters with float4 atomics; VDR_BLOCK_APPLY_BULK moves each element's
+ * K-wide node rows into shared memory with cp.async.bulk (mbarrier
+ * completion, three elements ahead per warp) and scatters with
+ * cp.reduce.async.bulk -- limited by the copy engine's per-operation cost
+ * on 64-256-byte rows. */
+#define VDR_BLOCK_APPLY_BULK 0
+#define VDR_BLOCK_APPLY_LSU 1
+int vdr_set_block_apply(vdr_handle *h, int variant);
+
 /* B[n*K + k] = cf * f(Q_k): the right-hand sides of K source fields at once.
  * d_Q is K x E (row k = per-element source of column k, kg/s, the caller's
  * element order).  Dirichlet rows are zero. */

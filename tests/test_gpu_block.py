@@ -82,12 +82,15 @@ TF32_TOL = {"tf32": 5e-3, "tf32x3": 2e-5}
 
 @pytest.mark.parametrize("K", [16, 32, 64])
 @pytest.mark.parametrize("precision", ["tf32", "tf32x3"])
-def test_block_apply_tensor_core(vdr, oracle, gpu_lib, case, K, precision):
+@pytest.mark.parametrize("variant", ["bulk", "lsu"])
+def test_block_apply_tensor_core(vdr, oracle, gpu_lib, case, K, precision,
+                                 variant):
     import torch
     prob, aH, aM, bb = case
     N = prob.mesh.nnode
     X = np.random.default_rng(100 + K).standard_normal((N, K)).astype(np.float32)
     with vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=aH, aM=aM) as s:
+        s.set_block_apply(variant)
         Xd = to_dev(X, torch.float32)
         Yd = torch.empty_like(Xd)
         s.apply_block_device(Xd, Yd, precision)
@@ -167,14 +170,17 @@ def column_residuals(oracle, prob, bb, B, X):
     return np.array(out)
 
 
-@pytest.mark.parametrize("precision", ["tf32x3", "tf32"])
-def test_block_solve_parity(vdr, oracle, gpu_lib, case, precision):
+@pytest.mark.parametrize("precision,variant", [("tf32x3", "bulk"),
+                                               ("tf32", "bulk"),
+                                               ("tf32x3", "lsu")])
+def test_block_solve_parity(vdr, oracle, gpu_lib, case, precision, variant):
     import torch
     prob, aH, aM, bb = case
     m = prob.mesh
     K, tol = 16, 1e-10
     Q = vdr.problems.random_gaussian_sources(m, K, seed=43)
     with vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=aH, aM=aM) as s:
+        s.set_block_apply(variant)
         Bd = torch.empty((m.nnode, K), dtype=torch.float64, device="cuda")
         s.assemble_rhs_block_device(to_dev(Q, torch.float64), Bd, 3.0)
         Xd = torch.zeros_like(Bd)

@@ -258,7 +258,7 @@ void free_handle(Handle &h) {
   dfree(h.vel32); dfree(h.lam32); dfree(h.pdec32); dfree(h.robin);
   dfree(h.A64); dfree(h.A32); dfree(h.diag); dfree(h.dinv);
   dfree(h.Ahi); dfree(h.Alo); dfree(h.flag);
-  dfree(h.Aaos); dfree(h.phi); dfree(h.perm_d); dfree(h.dinv32);
+  dfree(h.Aaos); dfree(h.phi); dfree(h.perm_d); dfree(h.dinv32); dfree(h.block_err);
   dfree(h.bk_f); dfree(h.bk_d);
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
   dfree(h.gcr_work); dfree(h.stage_d);
@@ -749,12 +749,36 @@ int vdr_apply_block_device(vdr_handle *H, int K, const void *X, void *Y,
                                   static_cast<float *>(Y), Aaos, nullptr,
                                   h.stream))
       return cuda_fail(cudaGetLastError(), "block apply");
+    int tma_err = 0;
+    if ((e = cudaMemcpyAsync(&tma_err, h.block_err, sizeof(int), cudaMemcpyDeviceToHost,
+                             h.stream)) ||
+        (e = cudaStreamSynchronize(h.stream)))
+      return cuda_fail(e, "block apply");
+    if (tma_err) {
+      cudaMemset(h.block_err, 0, sizeof(int));
+      set_error("block apply: a bulk-copy wait ran out of time");
+      return VDR_TIMEOUT;
+    }
     return VDR_OK;
   }
   if ((e = cudaMemsetAsync(Y, 0, sizeof(double) * h.N * (size_t)K, h.stream)) ||
       (e = launch_block_apply64(h, K, static_cast<const double *>(X),
                                 static_cast<double *>(Y), h.stream)))
     return cuda_fail(e, "block apply");
+  return VDR_OK;
+}
+
+int vdr_set_block_apply(vdr_handle *H, int variant) {
+  int st = check_handle(H);
+  if (st) return st;
+  if (variant != VDR_BLOCK_APPLY_BULK && variant != VDR_BLOCK_APPLY_LSU) {
+    set_error("vdr_set_block_apply: unknown variant");
+    return VDR_BAD_ARGUMENT;
+  }
+  Handle &h = H->h;
+  h.block_tma = variant == VDR_BLOCK_APPLY_BULK;
+  if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
+  h.bk_graph = nullptr;
   return VDR_OK;
 }
 

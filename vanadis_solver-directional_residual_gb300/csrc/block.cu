@@ -193,6 +193,226 @@ __global__ void __launch_bounds__(256) block_apply_tf32(
   }
 }
 
+// ---------------------------------------------- bulk-copy (TMA) variant
+// The same contraction with the data movement taken off the LSU pipe: the
+// eight X rows of an element (K floats each, contiguous in the node-major
+// block vector) arrive in shared memory by cp.async.bulk (one per node,
+// completion on an mbarrier), three elements ahead per warp, and the 8 x K
+// result rows leave by cp.reduce.async.bulk .add.f32 straight from shared
+// memory.  Every mbarrier wait is bounded by a clock budget; a wait that
+// runs out sets *err, drains this warp's copies (again bounded) and
+// returns, so the host can report VDR_TIMEOUT.
+constexpr int TMA_WARPS = 4, TMA_S = 3;
+constexpr long long TMA_WAIT_CYCLES = 4000000000LL;  // about 2 s
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned a) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ void mbar_expect(unsigned a, unsigned bytes) {
+  unsigned long long st;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+               : "=l"(st)
+               : "r"(a), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned a, unsigned parity) {
+  unsigned d;
+  asm volatile(
+      "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+      "selp.u32 %0, 1, 0, p; }"
+      : "=r"(d)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return d != 0u;
+}
+// Warp-uniform bounded wait; false when the budget ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned a, unsigned parity) {
+  const long long t0 = clock64();
+  while (!__all_sync(FULL, mbar_try(a, parity))) {
+    if (__any_sync(FULL, clock64() - t0 > TMA_WAIT_CYCLES)) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void bulk_load(unsigned dst, const void *src, unsigned bytes,
+                                          unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_reduce_add(float *dst, unsigned src, unsigned bytes) {
+  asm volatile(
+      "cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f32 [%0], [%1], %2;" ::"l"(dst),
+      "r"(src), "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read1() {
+  asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+template <int K>
+__device__ __forceinline__ void tma_issue(unsigned xs_a, unsigned bar, int b, int lane,
+                                          int cl, const float *X) {
+  constexpr int XR = K + 8, XBUF = 8 * XR;
+  if (lane == 0) mbar_expect(bar, 8u * K * 4u);
+  __syncwarp();
+  if (lane < 8)
+    bulk_load(xs_a + (unsigned)(b * XBUF + lane * XR) * 4u,
+              X + (size_t)(cl & NODE_BITS) * K, K * 4u, bar);
+}
+
+template <bool SPLIT, int TILES>
+__global__ void __launch_bounds__(TMA_WARPS * 32) block_apply_tma(
+    const float *__restrict__ Aaos, const int *__restrict__ conn, int E,
+    const float *__restrict__ X, const float *__restrict__ dscale,
+    float *__restrict__ Y, const int *skip, int *err) {
+  constexpr int K = 16 * TILES, XR = K + 8, DR = K + 4;
+  constexpr int XBUF = 8 * XR, DBUF = 8 * DR;
+  if (skip && *(volatile const int *)skip) return;
+  extern __shared__ __align__(128) float tma_smem[];
+  __shared__ __align__(8) unsigned long long bars[TMA_WARPS][TMA_S];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, t = lane & 3;
+  float *xs = tma_smem + w * (TMA_S * XBUF + 2 * DBUF);
+  float *ds = xs + TMA_S * XBUF;
+  const unsigned xs_a = smem_u32(xs), ds_a = smem_u32(ds);
+  unsigned bar_a[TMA_S];
+#pragma unroll
+  for (int s = 0; s < TMA_S; s++) bar_a[s] = smem_u32(&bars[w][s]);
+  if (lane == 0) {
+#pragma unroll
+    for (int s = 0; s < TMA_S; s++) mbar_init(bar_a[s]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  const long gw = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long nw = ((long)gridDim.x * blockDim.x) >> 5;
+  int cn[TMA_S];
+  long issued = 0;  // elements whose rows were requested
+#pragma unroll
+  for (int s = 0; s < TMA_S; s++) {
+    const long pe = gw + s * nw;
+    cn[s] = (pe < E && lane < 8) ? __ldg(conn + (size_t)lane * E + pe) : 0;
+    if (pe < E) {
+      tma_issue<K>(xs_a, bar_a[s], s, lane, cn[s], X);
+      issued++;
+    }
+  }
+  float f0 = 0.f, f1 = 0.f;
+  if (gw < E) {
+    f0 = __ldg(Aaos + (size_t)gw * 64 + 8 * g + t);
+    f1 = __ldg(Aaos + (size_t)gw * 64 + 8 * g + t + 4);
+  }
+  long it = 0;
+  bool failed = false;
+  for (long p = gw; p < E; p += nw, it++) {
+    const int b = (int)(it % TMA_S);
+    if (!mbar_wait(bar_a[b], (unsigned)((it / TMA_S) & 1))) {
+      failed = true;
+      break;
+    }
+    const long pn = p + nw;
+    float f0n = 0.f, f1n = 0.f;
+    if (pn < E) {
+      f0n = __ldg(Aaos + (size_t)pn * 64 + 8 * g + t);
+      f1n = __ldg(Aaos + (size_t)pn * 64 + 8 * g + t + 4);
+    }
+    const int cl = cn[0];
+    const int na = __shfl_sync(FULL, cl, t), nb = __shfl_sync(FULL, cl, t + 4);
+    const float sa = (na >= 0 && dscale) ? __ldg(dscale + na) : 1.f;
+    const float sb = (nb >= 0 && dscale) ? __ldg(dscale + nb) : 1.f;
+    const unsigned b0 = to_tf32(f0), b1 = to_tf32(f1);
+    unsigned c0 = 0u, c1 = 0u;
+    if (SPLIT) {
+      c0 = to_tf32(f0 - __uint_as_float(b0));
+      c1 = to_tf32(f1 - __uint_as_float(b1));
+    }
+    const int db = (int)(it & 1);
+    if (lane < 8) bulk_wait_read1();  // the reduce that last read this D buffer
+    __syncwarp();
+    const float *xb = xs + b * XBUF;
+    float *dbp = ds + db * DBUF;
+#pragma unroll
+    for (int m = 0; m < TILES; m++) {
+      float xa[4];
+      xa[0] = na < 0 ? 0.f : xb[t * XR + 16 * m + g] * sa;
+      xa[1] = na < 0 ? 0.f : xb[t * XR + 16 * m + g + 8] * sa;
+      xa[2] = nb < 0 ? 0.f : xb[(t + 4) * XR + 16 * m + g] * sb;
+      xa[3] = nb < 0 ? 0.f : xb[(t + 4) * XR + 16 * m + g + 8] * sb;
+      unsigned ah[4], al[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        ah[u] = to_tf32(xa[u]);
+        al[u] = SPLIT ? to_tf32(xa[u] - __uint_as_float(ah[u])) : 0u;
+      }
+      float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
+      if (SPLIT) {
+        asm volatile(
+            "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+            "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+            : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
+            : "r"(al[0]), "r"(al[1]), "r"(al[2]), "r"(al[3]), "r"(b0), "r"(b1));
+        asm volatile(
+            "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+            "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+            : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
+            : "r"(ah[0]), "r"(ah[1]), "r"(ah[2]), "r"(ah[3]), "r"(c0), "r"(c1));
+      }
+      asm volatile(
+          "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+          "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+          : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
+          : "r"(ah[0]), "r"(ah[1]), "r"(ah[2]), "r"(ah[3]), "r"(b0), "r"(b1));
+      // D[k][i] -> row i of the output stage: d0 (k=g, i=2t), d1 (g, 2t+1),
+      // d2 (g+8, 2t), d3 (g+8, 2t+1)
+      dbp[(2 * t) * DR + 16 * m + g] = d0;
+      dbp[(2 * t + 1) * DR + 16 * m + g] = d1;
+      dbp[(2 * t) * DR + 16 * m + g + 8] = d2;
+      dbp[(2 * t + 1) * DR + 16 * m + g + 8] = d3;
+    }
+    fence_proxy_async();
+    __syncwarp();
+    if (lane < 8) {
+      if (cl >= 0)
+        bulk_reduce_add(Y + (size_t)cl * K, ds_a + (unsigned)(db * DBUF + lane * DR) * 4u,
+                        K * 4u);
+      bulk_commit();
+    }
+    // refill this stage with the element TMA_S ahead (every lane has read it)
+    const long p2 = p + TMA_S * nw;
+#pragma unroll
+    for (int s = 0; s + 1 < TMA_S; s++) cn[s] = cn[s + 1];
+    cn[TMA_S - 1] = (p2 < E && lane < 8) ? __ldg(conn + (size_t)lane * E + p2) : 0;
+    if (p2 < E) {
+      fence_proxy_async();
+      tma_issue<K>(xs_a, bar_a[b], b, lane, cn[TMA_S - 1], X);
+      issued++;
+    }
+    f0 = f0n;
+    f1 = f1n;
+  }
+  if (lane < 8) bulk_wait_all();
+  if (failed) {
+    if (lane == 0) atomicOr(err, 1);
+    // drain the loads this warp still has in flight (bounded)
+    for (long j = it; j < issued; j++)
+      if (!mbar_wait(bar_a[(int)(j % TMA_S)], (unsigned)((j / TMA_S) & 1))) break;
+  }
+}
+
 // FP64-accurate block apply over the pair store: warp per element, lane =
 // columns lane, lane+32.  The element's 64 pairs are staged in shared memory.
 __global__ void __launch_bounds__(256) block_apply_df(
@@ -785,6 +1005,39 @@ int block_apply_launches_tf32(const Handle &h, int K, bool split,
                               const float4 *Aaos, const int *skip,
                               cudaStream_t s) {
   const float *A = reinterpret_cast<const float *>(Aaos);
+  // Bulk copies need 16-byte aligned rows (K * 4 bytes is a multiple of 16).
+  const bool tma = h.block_tma && h.block_err &&
+                   !(reinterpret_cast<uintptr_t>(X) & 15) &&
+                   !(reinterpret_cast<uintptr_t>(Y) & 15);
+  if (tma) {
+#define VDR_BLOCK_TMA(SPLIT, TILES)                                               \
+  do {                                                                            \
+    constexpr int KK = 16 * TILES;                                                \
+    const int smem = TMA_WARPS * (TMA_S * 8 * (KK + 8) + 2 * 8 * (KK + 4)) * 4;   \
+    static int per_sm = 0;                                                        \
+    if (!per_sm) {                                                                \
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(                              \
+          &per_sm, block_apply_tma<SPLIT, TILES>, TMA_WARPS * 32, smem);          \
+      if (per_sm < 1) per_sm = 1;                                                 \
+    }                                                                             \
+    block_apply_tma<SPLIT, TILES><<<grid_n((long)h.E * 32, TMA_WARPS * 32,        \
+                                           per_sm),                               \
+                                    TMA_WARPS * 32, smem, s>>>(                   \
+        A, h.conn, h.E, X, dscale, Y, skip, h.block_err);                         \
+  } while (0)
+    if (split) {
+      if (K == 16) VDR_BLOCK_TMA(true, 1);
+      else if (K == 32) VDR_BLOCK_TMA(true, 2);
+      else VDR_BLOCK_TMA(true, 4);
+    } else {
+      if (K == 16) VDR_BLOCK_TMA(false, 1);
+      else if (K == 32) VDR_BLOCK_TMA(false, 2);
+      else VDR_BLOCK_TMA(false, 4);
+    }
+#undef VDR_BLOCK_TMA
+    count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? VDR_OK : VDR_CUDA_ERROR;
+  }
 #define VDR_BLOCK_APPLY(SPLIT, TILES)                                        \
   do {                                                                       \
     static int per_sm = 0;                                                   \
@@ -831,9 +1084,14 @@ cudaError_t launch_block_rhs(const Handle &h, const double *phi, int K,
   return cudaGetLastError();
 }
 
-// Element-major FP32 copy of the operator for the tensor-core apply.
+// Element-major FP32 copy of the operator for the tensor-core apply (and
+// the error flag of the bulk-copy block apply).
 cudaError_t ensure_aos(Handle &h, float4 **out) {
   cudaError_t e;
+  if (!h.block_err) {
+    if ((e = cudaMalloc(&h.block_err, sizeof(int)))) return e;
+    if ((e = cudaMemset(h.block_err, 0, sizeof(int)))) return e;
+  }
   if (!h.Aaos) {
     if ((e = cudaMalloc(&h.Aaos, sizeof(float4) * 16 * (size_t)h.E))) return e;
     h.aos_valid = false;
@@ -1028,6 +1286,14 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
     if ((e = cudaGetLastError())) return cuda_fail(e, "update");
   }
   if ((e = cudaStreamSynchronize(s))) return cuda_fail(e, "block solve");
+  int tma_err = 0;
+  if ((e = cudaMemcpy(&tma_err, h.block_err, sizeof(int), cudaMemcpyDeviceToHost)))
+    return cuda_fail(e, "block solve");
+  if (tma_err) {
+    cudaMemset(h.block_err, 0, sizeof(int));
+    set_error("block solve: a bulk-copy wait ran out of time");
+    return VDR_TIMEOUT;
+  }
   if (outer_iters) *outer_iters = outer;
   if (inner_iters) *inner_iters = total_inner;
   if (errs_host)

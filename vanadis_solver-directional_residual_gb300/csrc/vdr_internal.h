@@ -147,6 +147,8 @@ struct Handle {
   double *bk_d = nullptr;
   cudaGraphExec_t bk_graph = nullptr;
   bool bk_graph_split = false;
+  bool block_tma = false;     // bulk-copy block apply (default: the LSU variant)
+  int *block_err = nullptr;   // set when a bulk-copy wait ran out
 
   // many meshes as segments (batch.cu)
   std::vector<int> seg_off;  // node offsets, nseg + 1

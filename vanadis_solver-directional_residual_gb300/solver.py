@@ -362,6 +362,12 @@ class Solver:
     # ---- many right-hand sides: node-major N x K device arrays ----
     BLOCK_PRECISION = {"fp64": 0, "tf32": 1, "tf32x3": 2}
 
+    def set_block_apply(self, variant="lsu"):
+        """Data movement of the tensor-core block apply: "lsu" (default) or
+        "bulk" (bulk copies and bulk reductions through shared memory)."""
+        L.check(self.lib.vdr_set_block_apply(self.h, {"bulk": 0, "lsu": 1}[variant]),
+                "vdr_set_block_apply")
+
     @_device_call
     def assemble_rhs_block_device(self, Q, B, cf=1.0):
         """B (N x K float64) = cf * f(Q_k) for the K x E per-element
