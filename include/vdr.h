@@ -161,6 +161,13 @@ int vdr_solve_device(vdr_handle *h, const double *d_b, double *d_x,
  * element matrices), each to inner_tol relative to ||r||.  Stops when the
  * FP64 true relative residual ||b - A x||/||b|| <= tol or after max_outer
  * corrections; *err is that FP64 residual.  Device arrays. */
+/* The FP32 operator of vdr_apply32_device and of the mixed solve:
+ * VDR_MIXED_ROUNDED (default) -- the FP64 element matrices rounded to FP32
+ * (the hi parts of the double-float store; no second build);
+ * VDR_MIXED_RECOMPUTE -- element Jacobians and DR terms recomputed in FP32. */
+#define VDR_MIXED_ROUNDED 0
+#define VDR_MIXED_RECOMPUTE 1
+int vdr_set_mixed_operator(vdr_handle *h, int mode);
 int vdr_solve_mixed_device(vdr_handle *h, const double *d_b, double *d_x,
                            double tol, double inner_tol, int max_outer,
                            int inner_itmax, int *outer_iters, int *inner_iters,

@@ -1,7 +1,8 @@
-"""Mixed precision: the FP32 operator (DR terms and element matrices
-recomputed in FP32) against the FP64 oracle, and FP64 iterative refinement
-around FP32 inner solves reaching the FP64 tolerance, with its error against
-the FP64 oracle solution reported and bounded."""
+"""Mixed precision: the FP32 operator (the FP64 element matrices rounded to
+FP32, or DR terms and element matrices recomputed in FP32) against the FP64
+oracle, and FP64 iterative refinement around FP32 inner solves reaching the
+FP64 tolerance, with its error against the FP64 oracle solution reported and
+bounded."""
 import numpy as np
 import pytest
 
@@ -26,9 +27,11 @@ def fp32_cases(vdr):
 
 @pytest.mark.parametrize("name", ["rotation_VF_64", "const_adv_OT",
                                   "kat_VF_robin"])
-@pytest.mark.parametrize("mode", ["stored", "matrix_free"])
+@pytest.mark.parametrize("mode,op", [("stored", "rounded"),
+                                     ("stored", "recompute"),
+                                     ("matrix_free", "recompute")])
 def test_fp32_operator_against_fp64_oracle(vdr, oracle, gpu_lib, torch, name,
-                                           mode):
+                                           mode, op):
     prob = fp32_cases(vdr)[name]
     m = prob.mesh
     aH, aM = 2.0, 0.7
@@ -38,6 +41,7 @@ def test_fp32_operator_against_fp64_oracle(vdr, oracle, gpu_lib, torch, name,
                                want_b=False, want_diag=False, nthreads=8)
     x = np.random.default_rng(8).standard_normal(m.nnode)
     with vdr.Solver(prob, vdr.Options(apply_mode=mode), aH=aH, aM=aM) as s:
+        s.set_mixed_operator(op)
         dx = torch.tensor(x, device="cuda")
         dy = torch.empty_like(dx)
         torch.cuda.synchronize()
@@ -50,13 +54,17 @@ def test_fp32_operator_against_fp64_oracle(vdr, oracle, gpu_lib, torch, name,
             assert err > 1e-12  # really computed in FP32
 
 
-@pytest.mark.parametrize("solver", ["bicgstab", "bicg"])
-def test_mixed_refinement_reaches_fp64_tolerance(vdr, gpu_lib, torch, solver):
+@pytest.mark.parametrize("solver,op", [("bicgstab", "rounded"),
+                                       ("bicg", "rounded"),
+                                       ("bicgstab", "recompute")])
+def test_mixed_refinement_reaches_fp64_tolerance(vdr, gpu_lib, torch, solver,
+                                                 op):
     prob = vdr.problems.rotation_shear(32, 32, 16, seed=33)
     dt = 10.0 / 32
     aH, aM = 2.0, 3.0 / dt
     opts = vdr.Options(solver=solver)
     with vdr.Solver(prob, opts, aH=aH, aM=aM) as s:
+        s.set_mixed_operator(op)
         b = torch.empty(prob.mesh.nnode, dtype=torch.float64, device="cuda")
         s.assemble_rhs_device(b, 3.0, 3.0 / dt, None)
         x64 = torch.zeros_like(b)

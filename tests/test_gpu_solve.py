@@ -188,3 +188,28 @@ def test_kat_run_device_time_loop(vdr, gpu_lib):
     ref_m = np.array(k["log"]["masses"])
     assert np.max(np.abs(masses - ref_m) / ref_m) < 1e-6
     assert np.all(errs <= k["tol"])
+
+
+@pytest.mark.parametrize("restart", [1, 5, 20])
+def test_gcr_jacobi_matches_bicgstab(vdr, oracle, gpu_lib, restart):
+    """Restarted GCR with Jacobi (the flexible solver of the learned path)
+    reaches the tolerance and the same solution as BiCGStab; its residual
+    never increases (the reported residual is the true FP64 residual)."""
+    import torch
+    prob = vdr.problems.rotation_shear(9, 8, 6, seed=61)
+    aH, aM = 2.0, 3.0 / (10.0 / 9)
+    with vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=aH, aM=aM) as s:
+        b = torch.as_tensor(s.assemble_rhs(3.0, 0.0, None), device="cuda")
+        x1 = torch.zeros_like(b)
+        x2 = torch.zeros_like(b)
+        torch.cuda.synchronize()
+        it1, e1, st1 = s.solve_device(b, x1, tol=1e-11, itmax=5000)
+        it2, e2, st2, fb = s.solve_gcr_device(b, x2, tol=1e-11, itmax=5000,
+                                              restart=restart)
+        true2 = s.true_residual_device(b, x2)
+        torch.cuda.synchronize()
+        X1, X2 = x1.cpu().numpy(), x2.cpu().numpy()
+    assert st1 == 0 and st2 == 0 and not fb
+    assert e2 <= 1e-11 and true2 <= 1.01e-11
+    assert rel_l2(X2, X1) < 1e-8
+    assert np.all(X2[prob.bc == 1] == 0.0)

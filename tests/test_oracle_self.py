@@ -156,3 +156,26 @@ def test_mesh_union_layout(vdr):
         assert np.array_equal(iss[:, a:b] - m.node_off[i],
                               p.mesh.iss.reshape(8, -1) - 1)
     assert u.bc.size == m.nnode and u.vel.size == 3 * E
+
+
+def test_tilting_velocity_and_sources(vdr):
+    """The learned workload's velocity: step 0 is the rotation_shear field,
+    every step is scaled to max |u_e| = 1 and the axis tilts about y; the
+    many-right-hand-side sources are seeded per column."""
+    P = vdr.problems
+    L = vdr.learned
+    prob = P.rotation_shear(6, 5, 4, seed=7)
+    v0 = L.tilted_velocity(prob.mesh, 0)
+    assert np.allclose(v0, prob.vel, rtol=0, atol=1e-15)
+    E = prob.mesh.nelem
+    for step in (1, 40, 180):
+        v = L.tilted_velocity(prob.mesh, step, tilt_deg=0.5).reshape(3, E)
+        assert abs(np.sqrt((v * v).sum(axis=0)).max() - 1.0) < 1e-14
+    # tilting 90 degrees puts the axis along x: no x component of rotation
+    v90 = L.tilted_velocity(prob.mesh, 1, tilt_deg=90.0, shear=0.0).reshape(3, E)
+    assert np.abs(v90[0]).max() < 1e-12
+    Q1 = P.random_gaussian_sources(prob.mesh, 3, seed=3001)
+    Q2 = P.random_gaussian_sources(prob.mesh, 3, seed=3001)
+    assert np.array_equal(Q1, Q2) and not np.array_equal(Q1[0], Q1[1])
+    assert np.array_equal(P.random_gaussian_sources(prob.mesh, 1, seed=3002)[0],
+                          Q1[1])

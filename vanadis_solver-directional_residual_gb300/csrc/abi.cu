@@ -201,6 +201,17 @@ int ensure_operator32(Handle &h) {
     h.op32_valid = true;  // matrix-free: recomputed in FP32 at each apply
     return VDR_OK;
   }
+  if (h.mixed_op == VDR_MIXED_ROUNDED) {
+    // the hi parts of the double-float store are the FP64 element matrices
+    // rounded to FP32, in the FP32 store's layout: no second build
+    int st = ensure_operator(h);
+    if (st) return st;
+    if (h.storage == VDR_STORE_DF && h.Ahi) {
+      h.A32v = h.Ahi;
+      h.op32_valid = true;
+      return VDR_OK;
+    }
+  }
   cudaError_t e;
   if ((e = dalloc(&h.A32, (size_t)h.E * 16))) return cuda_fail(e, "alloc FP32 matrices");
   BuildArgs ba;
@@ -209,6 +220,7 @@ int ensure_operator32(Handle &h) {
   ba.A32 = h.A32;
   if ((e = launch_build(op_args(h), ba, true, h.stream)))
     return cuda_fail(e, "FP32 element matrices");
+  h.A32v = h.A32;
   h.op32_valid = true;
   return VDR_OK;
 }
@@ -765,6 +777,21 @@ int vdr_apply_block_device(vdr_handle *H, int K, const void *X, void *Y,
       (e = launch_block_apply64(h, K, static_cast<const double *>(X),
                                 static_cast<double *>(Y), h.stream)))
     return cuda_fail(e, "block apply");
+  return VDR_OK;
+}
+
+int vdr_set_mixed_operator(vdr_handle *H, int mode) {
+  int st = check_handle(H);
+  if (st) return st;
+  if (mode != VDR_MIXED_ROUNDED && mode != VDR_MIXED_RECOMPUTE) {
+    set_error("vdr_set_mixed_operator: unknown mode");
+    return VDR_BAD_ARGUMENT;
+  }
+  Handle &h = H->h;
+  if (h.mixed_op != mode) {
+    h.mixed_op = mode;
+    h.op32_valid = false;
+  }
   return VDR_OK;
 }
 

@@ -397,11 +397,11 @@ cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
       }
     } else {
       if (transpose) {
-        if (color) VDR_LAUNCH((stored_apply_f32<true, false>), h.A32);
-        else VDR_LAUNCH((stored_apply_f32<true, true>), h.A32);
+        if (color) VDR_LAUNCH((stored_apply_f32<true, false>), h.A32v);
+        else VDR_LAUNCH((stored_apply_f32<true, true>), h.A32v);
       } else {
-        if (color) VDR_LAUNCH((stored_apply_f32<false, false>), h.A32);
-        else VDR_LAUNCH((stored_apply_f32<false, true>), h.A32);
+        if (color) VDR_LAUNCH((stored_apply_f32<false, false>), h.A32v);
+        else VDR_LAUNCH((stored_apply_f32<false, true>), h.A32v);
       }
     }
 #undef VDR_LAUNCH

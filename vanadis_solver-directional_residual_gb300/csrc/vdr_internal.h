@@ -110,6 +110,8 @@ struct Handle {
   bool op64_valid = false, op32_valid = false, diag_valid = false;
   double2 *A64 = nullptr;  // [32][E] stored element matrices (row-major pairs)
   float4 *A32 = nullptr;   // [16][E]
+  const float4 *A32v = nullptr;  // the FP32 operator the FP32 apply reads (A32 or Ahi)
+  int mixed_op = VDR_MIXED_ROUNDED;
   float4 *Ahi = nullptr;   // [16][E] double-float store: hi parts
   float4 *Alo = nullptr;   // [16][E] double-float store: lo parts
   int *flag = nullptr;     // device flag: an entry left the FP32 range

@@ -362,6 +362,12 @@ class Solver:
     # ---- many right-hand sides: node-major N x K device arrays ----
     BLOCK_PRECISION = {"fp64": 0, "tf32": 1, "tf32x3": 2}
 
+    def set_mixed_operator(self, mode="rounded"):
+        """FP32 operator of the mixed solve: "rounded" (the FP64 element
+        matrices rounded to FP32) or "recompute" (DR terms in FP32)."""
+        L.check(self.lib.vdr_set_mixed_operator(self.h, {"rounded": 0, "recompute": 1}[mode]),
+                "vdr_set_mixed_operator")
+
     def set_block_apply(self, variant="lsu"):
         """Data movement of the tensor-core block apply: "lsu" (default) or
         "bulk" (bulk copies and bulk reductions through shared memory)."""
