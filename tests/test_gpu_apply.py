@@ -97,6 +97,36 @@ def test_diag_and_rhs_parity(vdr, oracle, gpu_lib, problems, name):
             assert rel_l2(s.assemble_rhs(1.0, 0.0, None), bs) < TOL
 
 
+@pytest.mark.parametrize("scale", [1e-30, 1.0, 1e30])
+def test_rhs_told_magnitudes(vdr, oracle, gpu_lib, problems, scale):
+    """b = -(H - rM M) T_old (no source) for T_old of any magnitude, with
+    zero nodes mixed in: the double-float build scales each element's T_old
+    by a power of two, so it stays on its two launches (per-element DR
+    scalars + build) without the FP64 redo."""
+    import copy
+    prob = copy.deepcopy(problems["rotation_decay_robin"])
+    prob.q[:] = 0.0
+    m = prob.mesh
+    dt = 100.0
+    aH, aM, cf, rM = 2.0, 3.0 / dt, 3.0, 3.0 / dt
+    t_old = np.random.default_rng(8).standard_normal(m.nnode) * scale
+    t_old[::3] = 0.0
+    t_old[prob.bc == 1] = 0.0
+    _, b, _ = oracle.assemble(prob.variant, m.xx, m.yy, m.zz, m.iss, prob.vel,
+                              prob.lam, prob.pdec, prob.q, kod=m.kod,
+                              robin_alpha=prob.robin_alpha, aH=aH, aM=aM,
+                              cf=cf, rM=rM, t_old=t_old, want_bb=False,
+                              want_diag=False)
+    b[prob.bc == 1] = 0.0
+    with vdr.Solver(prob, aH=aH, aM=aM) as s:
+        s.diag()  # operator built
+        n0 = vdr.kernel_launch_count()
+        bg = s.assemble_rhs(cf, rM, t_old)
+        launches = vdr.kernel_launch_count() - n0
+    assert rel_l2(bg, b) < TOL
+    assert launches == 2
+
+
 def test_mass_parity(vdr, oracle, gpu_lib, problems):
     prob = problems["kat_VF_robin"]
     m = prob.mesh

@@ -141,6 +141,10 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
     BuildArgs ba;
     ba.exact_fp64 = h.exact_build;
     ba.bad = h.flag;
+    if (!h.exact_build) {
+      if ((e = dalloc(&h.drs, (size_t)h.E * 5))) return cuda_fail(e, "alloc DR scalars");
+      ba.drs = h.drs;
+    }
     if (rhs) {
       ba.cf = rhs->cf;
       ba.rM = rhs->rM;
@@ -273,7 +277,7 @@ void free_handle(Handle &h) {
   dfree(h.Aaos); dfree(h.phi); dfree(h.perm_d); dfree(h.dinv32); dfree(h.block_err);
   dfree(h.bk_f); dfree(h.bk_d);
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
-  dfree(h.gcr_work); dfree(h.stage_d);
+  dfree(h.gcr_work); dfree(h.stage_d); dfree(h.drs);
   if (h.gcr_graph) cudaGraphExecDestroy(h.gcr_graph);
   dfree(h.seg_d); dfree(h.seg_i); dfree(h.seg_ticket); dfree(h.seg_of_elem);
   if (h.seg_graph) cudaGraphExecDestroy(h.seg_graph);

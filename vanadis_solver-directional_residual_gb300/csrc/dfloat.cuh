@@ -170,6 +170,22 @@ __device__ __forceinline__ Df2 df_add(Df2 a, Df2 b) {
 __device__ __forceinline__ Df2 df_neg(Df2 a) { return Df2{-a.h, -a.l}; }
 __device__ __forceinline__ Df2 df_sub(Df2 a, Df2 b) { return df_add(a, df_neg(b)); }
 
+// 1/a for a normal nonzero pair: the FP32 reciprocal r0 of a.h refined by
+// one Newton step r0 (1 + e + e^2) with e = 1 - a r0 formed from the exact
+// product a.h r0 (1 - p is exact, p lying within an ulp of 1) and a.l r0;
+// relative error ~2^-46.
+__device__ __forceinline__ Df2 df_rcp(Df2 a) {
+  const float r0 = __frcp_rn(a.h);
+  const float p = __fmul_rn(a.h, r0);
+  const float pl = __fmaf_rn(a.h, r0, -p);
+  float e = __fsub_rn(1.0f, p);
+  e = __fsub_rn(e, pl);
+  e = __fmaf_rn(-a.l, r0, e);
+  const float c = __fmul_rn(r0, __fmaf_rn(e, e, e));
+  const float h = __fadd_rn(r0, c);
+  return Df2{h, __fsub_rn(c, __fsub_rn(h, r0))};
+}
+
 // acc += a.
 __device__ __forceinline__ void df_acc_add(DfAcc &acc, Df2 a) {
   const float t = __fadd_rn(acc.s, a.h);

@@ -125,9 +125,35 @@ __device__ __forceinline__ void shape_at(const T xi, const T eta, const T zeta,
   d2[7] = T(0.125) * xm * yp;
 }
 
-// Geometry and DR weight of one point given its shape data: detJ, grad N
-// (x,y,z) and W.  xe/ye/ze hold the 8 node coordinates in local order;
-// (vx,vy,vz), lam are the element's velocity and isotropic diffusivity.
+// The OT streamline length from the element's axis edge lengths
+// dl = |x2-x1|, |y4-y1|, |z5-z1| (local nodes 1, 2, 4, 5).
+template <typename T>
+__device__ __forceinline__ T dr_h_axes(const T vx, const T vy, const T vz,
+                                       const T vmag, const T dlx, const T dly,
+                                       const T dlz) {
+  const T eps = T(1.0e-14);
+  return (vmag > eps)
+             ? T(2) / (dr_abs(vx) / dlx + dr_abs(vy) / dly + dr_abs(vz) / dlz + eps)
+             : T(0);
+}
+
+// tau from the streamline length h, |v| and the streamline diffusivity:
+// Pe = |v| h / (2 lambda_s), tau = h/(2|v|) beta(Pe), zero unless |v| and
+// lambda_s exceed 1e-14 and Pe exceeds 1e-12.
+template <typename T>
+__device__ __forceinline__ T dr_tau_from(const int variant, const T h,
+                                         const T vmag, const T lams) {
+  const T eps = T(1.0e-14);
+  T pe = 0;
+  if (vmag > eps && lams > eps) pe = vmag * h / (T(2) * lams);
+  T tau = 0;
+  if (pe > T(1.0e-12) && vmag > eps) {
+    const T beta = (variant == DR_VF) ? beta_safe<T>(pe) : beta_exp(pe);
+    tau = T(0.5) * h / vmag * beta;
+  }
+  return tau;
+}
+
 // The DR stabilization parameter tau at one point from the inverse
 // Jacobian (i_ab = d xi_a / d x_b) and the element's velocity and
 // diffusivity: streamline length h (OT: axis edge lengths; GP/VF: 2/|J^-1 e|,
@@ -145,12 +171,8 @@ __device__ __forceinline__ T dr_tau(const int variant, const T i11, const T i12,
   const T vmag = dr_sqrt(vx * vx + vy * vy + vz * vz);
   T h, lams;
   if (variant == DR_OT) {
-    const T dlx = dr_abs(xe[1] - xe[0]);
-    const T dly = dr_abs(ye[3] - ye[0]);
-    const T dlz = dr_abs(ze[4] - ze[0]);
-    h = (vmag > eps)
-            ? T(2) / (dr_abs(vx) / dlx + dr_abs(vy) / dly + dr_abs(vz) / dlz + eps)
-            : T(0);
+    h = dr_h_axes<T>(vx, vy, vz, vmag, dr_abs(xe[1] - xe[0]),
+                     dr_abs(ye[3] - ye[0]), dr_abs(ze[4] - ze[0]));
     lams = lam;
   } else {
     T ex = 0, ey = 0, ez = 0;
@@ -167,16 +189,12 @@ __device__ __forceinline__ T dr_tau(const int variant, const T i11, const T i12,
     h = (gn > eps) ? T(2) / gn : T(0);
     lams = (variant == DR_VF) ? (lam * ex * ex + lam * ey * ey + lam * ez * ez) : lam;
   }
-  T pe = 0;
-  if (vmag > eps && lams > eps) pe = vmag * h / (T(2) * lams);
-  T tau = 0;
-  if (pe > T(1.0e-12) && vmag > eps) {
-    const T beta = (variant == DR_VF) ? beta_safe<T>(pe) : beta_exp(pe);
-    tau = T(0.5) * h / vmag * beta;
-  }
-  return tau;
+  return dr_tau_from<T>(variant, h, vmag, lams);
 }
 
+// Geometry and DR weight of one point given its shape data: detJ, grad N
+// (x,y,z) and W.  xe/ye/ze hold the 8 node coordinates in local order;
+// (vx,vy,vz), lam are the element's velocity and isotropic diffusivity.
 template <typename T>
 __device__ __forceinline__ void gp_core(const int variant, const T *nsh,
                                         const T *d0, const T *d1, const T *d2,

@@ -327,56 +327,168 @@ __global__ void __launch_bounds__(64) elem_build_kernel(OpArgs a, BuildArgs ba) 
   }
 }
 
-// The FP64 element build with its H/M row accumulation moved to the FP32
-// pipe.  Each lane evaluates its Gauss point in FP64 (Jacobian, inverse,
-// gradients and the DR weight with its sqrt/div/tanh) exactly as
-// elem_build_kernel<double>, splits the results into FP32 pairs with integer
-// operations, and the 8x8 rows of H and M are accumulated in double-float
-// (exact FP32 two-products + TwoSum, ~2^-46 relative), then merged to FP64.
-// On GB300 the FP64 pipe runs at 1/58 of the FP32 rate, so this removes more
-// than half of the kernel's FP64 work.
+// Per-element DR scalars of the double-float build, one thread per element,
+// in FP64 with the operations of dr_tau.  GP and VF variants:
+// drs[0..2][p] = e = v/|v|, drs[3][p] = kpe = |v|/(2 lambda_s) and
+// drs[4][p] = khalf = 0.5/|v|, the last two zero where Pe is zero at every
+// point (|v| or lambda_s <= 1e-14), so that a point with streamline length h
+// has Pe = h kpe and tau = h khalf beta(Pe).  OT, whose tau does not depend
+// on the point: drs[0][p] = tau.
+__global__ void __launch_bounds__(256) elem_dr_scalars_kernel(OpArgs a,
+                                                              double *__restrict__ drs) {
+  const long E = a.E;
+  const double eps = 1.0e-14;
+  for (long p = (long)blockIdx.x * blockDim.x + threadIdx.x; p < E;
+       p += (long)gridDim.x * blockDim.x) {
+    const double vx = __ldg(a.f.vel + p), vy = __ldg(a.f.vel + E + p),
+                 vz = __ldg(a.f.vel + 2 * E + p);
+    const double lam = __ldg(a.f.lam + p);
+    const double vmag = sqrt(vx * vx + vy * vy + vz * vz);
+    if (a.variant == DR_OT) {
+      const int n0 = __ldg(a.conn + p) & NODE_BITS;
+      const int n1 = __ldg(a.conn + (size_t)1 * E + p) & NODE_BITS;
+      const int n3 = __ldg(a.conn + (size_t)3 * E + p) & NODE_BITS;
+      const int n4 = __ldg(a.conn + (size_t)4 * E + p) & NODE_BITS;
+      const double h = dr_h_axes<double>(
+          vx, vy, vz, vmag, fabs(__ldg(a.xx + n1) - __ldg(a.xx + n0)),
+          fabs(__ldg(a.yy + n3) - __ldg(a.yy + n0)),
+          fabs(__ldg(a.zz + n4) - __ldg(a.zz + n0)));
+      drs[p] = dr_tau_from<double>(DR_OT, h, vmag, lam);
+    } else {
+      double ex = 0.0, ey = 0.0, ez = 0.0;
+      if (vmag > eps) {
+        const double iv = 1.0 / vmag;
+        ex = vx * iv;
+        ey = vy * iv;
+        ez = vz * iv;
+      }
+      const double lams =
+          (a.variant == DR_VF) ? (lam * ex * ex + lam * ey * ey + lam * ez * ez) : lam;
+      const bool on = vmag > eps && lams > eps;
+      drs[p] = ex;
+      drs[E + p] = ey;
+      drs[2 * E + p] = ez;
+      drs[3 * E + p] = on ? vmag / (2.0 * lams) : 0.0;
+      drs[4 * E + p] = on ? 0.5 / vmag : 0.0;
+    }
+  }
+}
+
+// The FP64-accurate element build with its arithmetic moved to the FP32
+// pipe (on GB300 the FP64 pipe runs at 1/58 of the FP32 rate and is the
+// scarce unit).  Per element, on 8 lanes:
+//   lane k = node k: connectivity, coordinates relative to local node 1
+//     (differences formed in FP64, then split into pairs) and, for the
+//     right-hand side, T_old scaled by a power of two so that the element's
+//     largest |T_old| lies in [1, 2);
+//   lane q = Gauss point q: Jacobian, cofactors, 1/detJ, inverse, gradients
+//     and W in double-float; |J^-1 e| in double-float; only sqrt, the
+//     Peclet number and beta(Pe) (tanh) are FP64, with the element's
+//     velocity scalars from elem_dr_scalars_kernel;
+//   lane i = row i: the rows accumulated in double-float (exact FP32
+//     two-products + TwoSum), then A_e, diag(A_e) and b += cf f or, with
+//     T_old, b += cf f - (H - rM M) T_old.  SPLIT (T_old given) keeps H and
+//     M apart; otherwise aH and aM are folded into the point weights and
+//     A_e = aH H + aM M is accumulated directly (4 pair products per point
+//     and node instead of 5, one accumulator row instead of two).
+// Any value outside the pairs' safe window sets bit 2 of the flag and the
+// host redoes the build with FP64 rows (elem_build_kernel<double>).
 struct BuildSmemDF {
-  Df2 g[ROWS_EPB][8][6][8];    // dN/dx, dN/dy, dN/dz, v.gradN + P N, N, W
-  Df2 d[ROWS_EPB][8][2];       // detJ, lambda*detJ
-  Df2 fnw[ROWS_EPB][4][2][8];  // face-3 points: N, W
-  Df2 fd[ROWS_EPB][4];         // alpha*detJs
-  double tab[12][4][8];
-  Df2 tabdf[8][4][8];          // the volume points' tables as pairs
+  Df2 g[ROWS_EPB][8][5][8];  // per element, point q, node j: dNj/dx, dNj/dy,
+                             // dNj/dz, v.gradNj + P Nj, Wj
+  Df2 d[ROWS_EPB][8][2];     // detJ, lambda*detJ
+  Df2 fw[ROWS_EPB][4][8];    // face-3 points: W
+  Df2 fd[ROWS_EPB][4];       // alpha*detJs
+  Df2 rel[ROWS_EPB][24];     // node k's (x, y, z) - node 1's at [3k..3k+2]
+  Df2 told[ROWS_EPB][8];     // T_old at the nodes times 2^-shift
+  Df2 tab[8][4][8];          // N, dN/dxi, dN/deta, dN/dzeta at the 8 points
+  Df2 ftab[4][8];            // N at the 4 face-3 points
 };
 
-__global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArgs ba) {
+template <bool SPLIT>
+__global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArgs ba) {
   __shared__ BuildSmemDF sm;
-  fill_shape_tables<double>(sm.tab);
-  for (int t = threadIdx.x; t < 8 * 4 * 8; t += blockDim.x) {
-    const int q = t >> 5, k = (t >> 3) & 3, i = t & 7;
-    sm.tabdf[q][k][i] = df_from_double(sm.tab[q][k][i]);
+  for (int t = threadIdx.x; t < 12; t += blockDim.x) {
+    double xi, eta, zeta;
+    if (t < 8) {
+      xi = gauss_coord<double>(t, 0);
+      eta = gauss_coord<double>(t, 1);
+      zeta = gauss_coord<double>(t, 2);
+    } else {
+      const double gc = VDR_GAUSS_C;
+      xi = -1.0;
+      eta = ((t - 8) & 2) ? gc : -gc;
+      zeta = ((t - 8) & 1) ? gc : -gc;
+    }
+    double n[8], d0[8], d1[8], d2[8];
+    shape_at<double>(xi, eta, zeta, n, d0, d1, d2);
+    if (t >= 8) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) sm.ftab[t - 8][i] = df_from_double(n[i]);
+      continue;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      sm.tab[t][0][i] = df_from_double(n[i]);
+      sm.tab[t][1][i] = df_from_double(d0[i]);
+      sm.tab[t][2][i] = df_from_double(d1[i]);
+      sm.tab[t][3][i] = df_from_double(d2[i]);
+    }
   }
   __syncthreads();
   const int lane8 = threadIdx.x & 7;
   const int le = threadIdx.x >> 3;
   const long E = a.E;
+  bool range_bad = false;  // a quantity the pairs cannot hold safely
+  const Df2 aHd = df_from_double_chk(ba.aH, range_bad);
+  const Df2 aMd = df_from_double_chk(ba.aM, range_bad);
+  const Df2 nrMd = df_neg(df_from_double_chk(SPLIT ? ba.rM : 0.0, range_bad));
+  const bool need_rows = SPLIT || ba.Ahi || ba.A64 || ba.diag;
+  const double *V = a.f.vel;
   for (long base = (long)blockIdx.x * ROWS_EPB; base < E;
        base += (long)gridDim.x * ROWS_EPB) {
     const long pe = base + le;
     const bool valid = pe < E;
     const long p = valid ? pe : E - 1;
-    Elem<double> el;
-    load_elem<double>(a, p, el);
-    // Gauss point lane8 in double-float on the FP32 pipe: Jacobian from the
-    // node coordinates relative to local node 1 (differences formed in
-    // FP64, so they keep full precision), cofactors, inverse, gradients and
-    // W; only 1/detJ and the DR parameter tau are FP64.
-    bool range_bad = false;  // a quantity the pairs cannot hold safely
-    const Df2 *tn = sm.tabdf[lane8][0], *t0 = sm.tabdf[lane8][1],
-              *t1 = sm.tabdf[lane8][2], *t2 = sm.tabdf[lane8][3];
+    __syncwarp();  // the previous element's shared data has been read
+    // ---- lane k = node k
+    const int ck = __ldg(a.conn + (size_t)lane8 * E + p);
+    const int nk = ck & NODE_BITS;
+    const double xk = __ldg(a.xx + nk), yk = __ldg(a.yy + nk), zk = __ldg(a.zz + nk);
+    const double x0 = __shfl_sync(FULL, xk, 0, 8);
+    const double y0 = __shfl_sync(FULL, yk, 0, 8);
+    const double z0 = __shfl_sync(FULL, zk, 0, 8);
+    sm.rel[le][3 * lane8] = df_from_double_chk(xk - x0, range_bad);
+    sm.rel[le][3 * lane8 + 1] = df_from_double_chk(yk - y0, range_bad);
+    sm.rel[le][3 * lane8 + 2] = df_from_double_chk(zk - z0, range_bad);
+    int tshift = 0;
+    if constexpr (SPLIT) {
+      const double tk = __ldg(ba.told + nk);
+      int em = df_exp(tk);
+      em = max(em, __shfl_xor_sync(FULL, em, 1));
+      em = max(em, __shfl_xor_sync(FULL, em, 2));
+      em = max(em, __shfl_xor_sync(FULL, em, 4));
+      if (em == 0 && tk != 0.0) range_bad = true;  // all subnormal
+      tshift = em - 1023;
+      Df2 t;
+      df_split(tk, t.h, t.l, range_bad, tshift);  // inf/NaN: bad
+      sm.told[le][lane8] = t;
+    }
+    const double vx = __ldg(V + p), vy = __ldg(V + E + p), vz = __ldg(V + 2 * E + p);
+    const double lam = __ldg(a.f.lam + p);
+    const double pdec = a.f.pdec ? __ldg(a.f.pdec + p) : 0.0;
+    const bool robin = a.f.robin ? (__ldg(a.f.robin + p) != 0) : false;
+    __syncwarp();
+    // ---- lane q = Gauss point q
+    const Df2 *tn = sm.tab[lane8][0], *t0 = sm.tab[lane8][1],
+              *t1 = sm.tab[lane8][2], *t2 = sm.tab[lane8][3];
     DfAcc J[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) J[k] = DfAcc{0.0f, 0.0f};
-#pragma unroll
+#pragma unroll 1
     for (int k = 1; k < 8; k++) {  // local node 1 is the origin
-      const Df2 rx = df_from_double_chk(el.xe[k] - el.xe[0], range_bad);
-      const Df2 ry = df_from_double_chk(el.ye[k] - el.ye[0], range_bad);
-      const Df2 rz = df_from_double_chk(el.ze[k] - el.ze[0], range_bad);
+      const Df2 rx = sm.rel[le][3 * k], ry = sm.rel[le][3 * k + 1],
+                rz = sm.rel[le][3 * k + 2];
       df_acc(J[0], rx, t0[k]);
       df_acc(J[1], rx, t1[k]);
       df_acc(J[2], rx, t2[k]);
@@ -396,7 +508,11 @@ __global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArg
     const Df2 detp =
         df_add(df_sub(df_mul(j11, c11), df_mul(j12, c12)), df_mul(j13, c13));
     const double detj = df_to_double(detp.h, detp.l);
-    const Df2 r = df_from_double_chk(1.0 / detj, range_bad);
+    {
+      const int ed = df_exp(detj);  // zero, subnormal, inf, NaN included
+      if (ed < 1023 - 60 || ed > 1023 + 60) range_bad = true;
+    }
+    const Df2 r = df_rcp(detp);
     const Df2 di11 = df_mul(r, c11);
     const Df2 di12 = df_mul(r, df_sub(df_mul(j13, j32), df_mul(j12, j33)));
     const Df2 di13 = df_mul(r, df_sub(df_mul(j12, j23), df_mul(j13, j22)));
@@ -406,19 +522,45 @@ __global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArg
     const Df2 di31 = df_mul(r, c13);
     const Df2 di32 = df_mul(r, df_sub(df_mul(j12, j31), df_mul(j11, j32)));
     const Df2 di33 = df_mul(r, df_sub(df_mul(j11, j22), df_mul(j12, j21)));
-    const double tau = dr_tau<double>(
-        a.variant, df_to_double(di11.h, di11.l), df_to_double(di12.h, di12.l),
-        df_to_double(di13.h, di13.l), df_to_double(di21.h, di21.l),
-        df_to_double(di22.h, di22.l), df_to_double(di23.h, di23.l),
-        df_to_double(di31.h, di31.l), df_to_double(di32.h, di32.l),
-        df_to_double(di33.h, di33.l), el.xe, el.ye, el.ze, el.lam, el.vx,
-        el.vy, el.vz);
-    const Df2 vxd = df_from_double_chk(el.vx, range_bad);
-    const Df2 vyd = df_from_double_chk(el.vy, range_bad);
-    const Df2 vzd = df_from_double_chk(el.vz, range_bad);
-    const Df2 pd = df_from_double_chk(el.pdec, range_bad);
+    double tau;
+    if (a.variant == DR_OT) {
+      tau = __ldg(ba.drs + p);
+    } else {
+      // h = 2/|J^-1 e| (zero for |J^-1 e| <= 1e-14), Pe = h kpe,
+      // tau = h khalf beta(Pe)
+      const Df2 exd = df_from_double(__ldg(ba.drs + p));
+      const Df2 eyd = df_from_double(__ldg(ba.drs + E + p));
+      const Df2 ezd = df_from_double(__ldg(ba.drs + 2 * E + p));
+      DfAcc gxa{0.0f, 0.0f}, gya{0.0f, 0.0f}, gza{0.0f, 0.0f};
+      df_acc(gxa, di11, exd);
+      df_acc(gxa, di12, eyd);
+      df_acc(gxa, di13, ezd);
+      df_acc(gya, di21, exd);
+      df_acc(gya, di22, eyd);
+      df_acc(gya, di23, ezd);
+      df_acc(gza, di31, exd);
+      df_acc(gza, di32, eyd);
+      df_acc(gza, di33, ezd);
+      const Df2 gx = df_norm(gxa), gy = df_norm(gya), gz = df_norm(gza);
+      DfAcc n2{0.0f, 0.0f};
+      df_acc(n2, gx, gx);
+      df_acc(n2, gy, gy);
+      df_acc(n2, gz, gz);
+      const double gn2 = df_to_double(n2.s, n2.c);
+      const double h = (gn2 > 1.0e-28) ? 2.0 * rsqrt(gn2) : 0.0;
+      const double pe = h * __ldg(ba.drs + 3 * E + p);
+      tau = 0.0;
+      if (pe > 1.0e-12) {
+        const double beta = (a.variant == DR_VF) ? beta_safe<double>(pe) : beta_exp(pe);
+        tau = h * __ldg(ba.drs + 4 * E + p) * beta;
+      }
+    }
+    const Df2 vxd = df_from_double_chk(vx, range_bad);
+    const Df2 vyd = df_from_double_chk(vy, range_bad);
+    const Df2 vzd = df_from_double_chk(vz, range_bad);
+    const Df2 pd = df_from_double_chk(pdec, range_bad);
     const Df2 taud = df_from_double_chk(tau, range_bad);
-#pragma unroll
+#pragma unroll 1
     for (int j = 0; j < 8; j++) {
       DfAcc ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
       df_acc(ax, di11, t0[j]);
@@ -443,44 +585,62 @@ __global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArg
       sm.g[le][lane8][0][j] = gx;
       sm.g[le][lane8][1][j] = gy;
       sm.g[le][lane8][2][j] = gz;
-      sm.g[le][lane8][3][j] = df_norm(aa);
-      sm.g[le][lane8][4][j] = tn[j];
-      sm.g[le][lane8][5][j] = df_norm(aw);
+      if constexpr (SPLIT) {
+        sm.g[le][lane8][3][j] = df_norm(aa);
+      } else {  // aH (v.gradN_j + P N_j) + aM N_j
+        DfAcc bw{0.0f, 0.0f};
+        df_acc(bw, aHd, df_norm(aa));
+        df_acc(bw, aMd, tn[j]);
+        sm.g[le][lane8][3][j] = df_norm(bw);
+      }
+      sm.g[le][lane8][4][j] = df_norm(aw);
     }
     const double vol = group8_sum<double>(detj);
-    sm.d[le][lane8][0] = df_from_double_chk(detj, range_bad);
-    sm.d[le][lane8][1] = df_from_double_chk(el.lam * detj, range_bad);
-    GPData<double> o;  // face-3 points (Robin term)
-    if (el.robin && lane8 < 4) {
-      const double gc = VDR_GAUSS_C;
-      const double r = (lane8 & 2) ? gc : -gc;
-      const double sgc = (lane8 & 1) ? gc : -gc;
-      const double djs = face3_detjs<double>(el.xe, el.ye, el.ze, r, sgc);
-      gp_core<double>(a.variant, sm.tab[8 + lane8][0], sm.tab[8 + lane8][1],
-                      sm.tab[8 + lane8][2], sm.tab[8 + lane8][3], el.xe, el.ye,
-                      el.ze, el.lam, el.vx, el.vy, el.vz, o);
+    sm.d[le][lane8][0] = detp;
+    {
+      const Df2 lamd = df_from_double_chk(lam, range_bad);
+      sm.d[le][lane8][1] = df_mul(SPLIT ? lamd : df_mul(aHd, lamd), detp);
+    }
+    if (robin && lane8 < 4) {
+      // face-3 point lane8 (Robin term) in FP64 from the element's
+      // coordinates relative to local node 1
+      double xe[8], ye[8], ze[8];
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        sm.fnw[le][lane8][0][j] = df_from_double_chk(o.n[j], range_bad);
-        sm.fnw[le][lane8][1][j] = df_from_double_chk(o.w[j], range_bad);
+      for (int k = 0; k < 8; k++) {
+        const int n = __ldg(a.conn + (size_t)k * E + p) & NODE_BITS;
+        xe[k] = __ldg(a.xx + n) - x0;
+        ye[k] = __ldg(a.yy + n) - y0;
+        ze[k] = __ldg(a.zz + n) - z0;
       }
+      const double gc = VDR_GAUSS_C;
+      const double rr = (lane8 & 2) ? gc : -gc;
+      const double ss = (lane8 & 1) ? gc : -gc;
+      const double djs = face3_detjs<double>(xe, ye, ze, rr, ss);
+      double n[8], d0[8], d1[8], d2[8];
+      shape_at<double>(-1.0, rr, ss, n, d0, d1, d2);
+      GPData<double> o;
+      gp_core<double>(a.variant, n, d0, d1, d2, xe, ye, ze, lam, vx, vy, vz, o);
+#pragma unroll
+      for (int j = 0; j < 8; j++) sm.fw[le][lane8][j] = df_from_double_chk(o.w[j], range_bad);
       sm.fd[le][lane8] = df_from_double_chk(a.f.robin_alpha * djs, range_bad);
     }
-    // Any out-of-window value in the element: the host redoes this build
-    // with the FP64 row accumulation (bit 2 of the flag).
-    if (valid && range_bad) atomicOr(ba.bad, 2);
     __syncwarp();
+    // ---- lane i = row i
     const int i = lane8;
-    DfAcc accH[8], accM[8];
+    // accH: H (SPLIT) or A_e; accM: M (SPLIT only)
+    DfAcc accH[8], accM[SPLIT ? 8 : 1];
 #pragma unroll
-    for (int j = 0; j < 8; j++) accH[j] = accM[j] = DfAcc{0.0f, 0.0f};
+    for (int j = 0; j < 8; j++) accH[j] = DfAcc{0.0f, 0.0f};
+#pragma unroll
+    for (int j = 0; j < (SPLIT ? 8 : 1); j++) accM[j] = DfAcc{0.0f, 0.0f};
     DfAcc fw{0.0f, 0.0f};
 #pragma unroll 1
     for (int q = 0; q < 8; q++) {
       const Df2 dj = sm.d[le][q][0];
-      const Df2 dl = sm.d[le][q][1];
-      const Df2 wd = df_mul(sm.g[le][q][5][i], dj);
+      const Df2 wd = df_mul(sm.g[le][q][4][i], dj);
       df_acc_add(fw, wd);
+      if (!need_rows) continue;
+      const Df2 dl = sm.d[le][q][1];
       const Df2 dgx = df_mul(dl, sm.g[le][q][0][i]);
       const Df2 dgy = df_mul(dl, sm.g[le][q][1][i]);
       const Df2 dgz = df_mul(dl, sm.g[le][q][2][i]);
@@ -490,33 +650,36 @@ __global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArg
         df_acc(accH[j], dgy, sm.g[le][q][1][j]);
         df_acc(accH[j], dgz, sm.g[le][q][2][j]);
         df_acc(accH[j], wd, sm.g[le][q][3][j]);
-        df_acc(accM[j], wd, sm.g[le][q][4][j]);
+        if constexpr (SPLIT) df_acc(accM[j], wd, sm.tab[q][0][j]);
       }
     }
-    if (el.robin) {
+    if (robin && need_rows) {
 #pragma unroll
       for (int f = 0; f < 4; f++) {
-        const Df2 aw = df_mul(sm.fd[le][f], sm.fnw[le][f][1][i]);
+        Df2 aw = df_mul(sm.fd[le][f], sm.fw[le][f][i]);
+        if constexpr (!SPLIT) aw = df_mul(aHd, aw);
 #pragma unroll
-        for (int j = 0; j < 8; j++) df_acc(accH[j], aw, sm.fnw[le][f][0][j]);
+        for (int j = 0; j < 8; j++) df_acc(accH[j], aw, sm.ftab[f][j]);
       }
     }
-    __syncwarp();
     if (!valid) continue;
-    const int ci = el.c[i];
+    const int ci = ck;  // row i's node
     if (ba.Ahi && !ba.A64) {
       // double-float store: A_e row = aH H + aM M formed in double-float,
       // stored as its (hi, lo) pair; the store window is checked on hi
       // (FP32 biased exponent 27..247 = FP64 exponent -100..120)
-      const Df2 aHd = df_from_double(ba.aH), aMd = df_from_double(ba.aM);
       Df2 rowd[8];
       bool bad = false;
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        DfAcc acc{0.0f, 0.0f};
-        df_acc(acc, aHd, df_norm(accH[j]));
-        df_acc(acc, aMd, df_norm(accM[j]));
-        rowd[j] = df_norm(acc);
+        if constexpr (SPLIT) {
+          DfAcc acc{0.0f, 0.0f};
+          df_acc(acc, aHd, df_norm(accH[j]));
+          df_acc(acc, aMd, df_norm(accM[j % (SPLIT ? 8 : 1)]));
+          rowd[j] = df_norm(acc);
+        } else {
+          rowd[j] = df_norm(accH[j]);
+        }
         const unsigned eb = (__float_as_uint(rowd[j].h) >> 23) & 0xffu;
         if (rowd[j].h != 0.0f && (eb < 27u || eb > 247u)) bad = true;
       }
@@ -530,19 +693,14 @@ __global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArg
       if (bad) atomicOr(ba.bad, 1);  // store window (bit 1)
       if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, df_to_double(rowd[i].h, rowd[i].l));
     }
-    double Hr[8], Mr[8];
-    const bool need64 = ba.A64 || (ba.diag && !ba.Ahi) || (ba.b && ba.told);
-    if (need64) {
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        Hr[j] = df_to_double(accH[j].s, accH[j].c);
-        Mr[j] = df_to_double(accM[j].s, accM[j].c);
-      }
-    }
     if (!ba.Ahi && (ba.A64 || ba.diag)) {
       double row[8];
 #pragma unroll
-      for (int j = 0; j < 8; j++) row[j] = ba.aH * Hr[j] + ba.aM * Mr[j];
+      for (int j = 0; j < 8; j++)
+        row[j] = SPLIT ? ba.aH * df_to_double(accH[j].s, accH[j].c) +
+                             ba.aM * df_to_double(accM[j % (SPLIT ? 8 : 1)].s,
+                                                  accM[j % (SPLIT ? 8 : 1)].c)
+                       : df_to_double(accH[j].s, accH[j].c);
       if (ba.A64) {
 #pragma unroll
         for (int jj = 0; jj < 4; jj++)
@@ -554,16 +712,25 @@ __global__ void __launch_bounds__(64, 6) elem_build_df_kernel(OpArgs a, BuildArg
     if (ba.b && ci >= 0) {
       const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
       double val = ba.cf * ((qe / vol) * df_to_double(fw.s, fw.c));
-      if (ba.told) {
-        double ft = 0.0;
+      if constexpr (SPLIT) {
+        // (H - rM M) T_old in double-float on the scaled T_old, scaled back
+        DfAcc ft{0.0f, 0.0f};
 #pragma unroll
-        for (int j = 0; j < 8; j++)
-          ft += (Hr[j] - ba.rM * Mr[j]) * __ldg(ba.told + (el.c[j] & NODE_BITS));
-        val -= ft;
+        for (int j = 0; j < 8; j++) {
+          DfAcc rowj = accH[j];
+          df_acc(rowj, nrMd, df_norm(accM[j % (SPLIT ? 8 : 1)]));
+          df_acc(ft, df_norm(rowj), sm.told[le][j]);
+        }
+        double f = df_to_double(ft.s, ft.c);
+        if (!df_scale(f, tshift)) f = ldexp(f, tshift);
+        val -= f;
       }
       atomicAdd(ba.b + ci, val);
     }
   }
+  // Any out-of-window value: the host redoes this build with the FP64 rows
+  // (bit 2 of the flag).
+  if (range_bad) atomicOr(ba.bad, 2);
 }
 
 template <typename T, bool TRANS>
@@ -729,8 +896,24 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
     elem_build_kernel<float><<<grid, 64, 0, s>>>(a, ba);
   else if (ba.exact_fp64)
     elem_build_kernel<double><<<grid, 64, 0, s>>>(a, ba);
-  else
-    elem_build_df_kernel<<<grid, 64, 0, s>>>(a, ba);
+  else {
+    if (!ba.drs) return cudaErrorInvalidValue;
+    static bool carveout = false;  // 8 blocks of 27.5 KB need the full carveout
+    if (!carveout) {
+      cudaFuncSetAttribute(elem_build_df_kernel<true>,
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      cudaFuncSetAttribute(elem_build_df_kernel<false>,
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      carveout = true;
+    }
+    const int g2 = (int)std::min<long>(((long)a.E + 255) / 256, (long)sm_count() * 8);
+    elem_dr_scalars_kernel<<<g2, 256, 0, s>>>(a, ba.drs);
+    if (ba.told)
+      elem_build_df_kernel<true><<<grid, 64, 0, s>>>(a, ba);
+    else
+      elem_build_df_kernel<false><<<grid, 64, 0, s>>>(a, ba);
+    count_launches(1);
+  }
   count_launches(1);
   return cudaGetLastError();
 }

@@ -134,6 +134,7 @@ struct Handle {
   double *h_stage = nullptr;
   size_t h_stage_bytes = 0;
   double *stage_d = nullptr;  // [3E] device staging of uploaded fields
+  double *drs = nullptr;      // [5E] per-element DR scalars of the build
 
   vdr_solve_stats last{};
 
@@ -197,6 +198,7 @@ struct BuildArgs {
   double *b = nullptr;
   bool exact_fp64 = false;  // H/M rows accumulated in FP64, not double-float
   double *phi = nullptr;     // [8][E] (1/vol) int W_i dOmega, per element
+  double *drs = nullptr;     // [5][E] per-element DR scalars (double-float build)
 };
 
 // ---- launchers (element.cu) ----
