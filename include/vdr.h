@@ -157,10 +157,11 @@ int vdr_solve_device(vdr_handle *h, const double *d_b, double *d_x,
 
 /* Mixed precision: FP64 iterative refinement (residual b - A x and update
  * x += d in FP64 with the FP64 operator) around inner solves A32 d = r with
- * the FP32 operator (element Jacobians and DR terms recomputed in FP32, FP32
- * element matrices), each to inner_tol relative to ||r||.  Stops when the
- * FP64 true relative residual ||b - A x||/||b|| <= tol or after max_outer
- * corrections; *err is that FP64 residual.  Device arrays. */
+ * the FP32 operator (see vdr_set_mixed_operator).  Each inner solve stops at
+ * max(inner_tol, 0.5 tol ||b|| / ||r||) relative to ||r||: no tighter than
+ * the outer residual needs to reach tol.  Stops when the FP64 true relative
+ * residual ||b - A x||/||b|| <= tol or after max_outer corrections; *err is
+ * that FP64 residual.  Device arrays. */
 /* The FP32 operator of vdr_apply32_device and of the mixed solve:
  * VDR_MIXED_ROUNDED (default) -- the FP64 element matrices rounded to FP32
  * (the hi parts of the double-float store; no second build);

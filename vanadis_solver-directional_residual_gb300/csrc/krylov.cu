@@ -669,7 +669,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_axpy1(Vec a, const double *d) {
 
 // Iterative refinement: the residual r = b - A x and the update x += d are
 // FP64 (FP64 operator); each correction d solves A32 d = r with the FP32
-// operator to inner_tol relative to ||r||.
+// operator to max(inner_tol, 0.5 tol / rel) relative to ||r|| (rel =
+// ||r||/||b||): a correction is solved no further than the outer residual
+// needs to reach tol, so a tight first correction is followed by a short
+// second one instead of two full-depth inner solves.
 int solve_mixed_device(Handle &h, int method, const double *b, double *x,
                        double tol, double inner_tol, int max_outer,
                        int inner_itmax, MixedStats *ms) {
@@ -711,7 +714,8 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
     h.apply_fp32 = true;
     int it = 0;
     double ierr = 0.0;
-    const int ist = solve_device(h, method, r, d, inner_tol, inner_itmax, &it, &ierr);
+    const double itol = std::max(inner_tol, 0.5 * tol / rel);
+    const int ist = solve_device(h, method, r, d, itol, inner_itmax, &it, &ierr);
     h.apply_fp32 = false;
     if (ist == VDR_CUDA_ERROR || ist == VDR_BAD_ARGUMENT) return ist;
     st.inner += it;
