@@ -54,15 +54,18 @@ def test_fp32_operator_against_fp64_oracle(vdr, oracle, gpu_lib, torch, name,
             assert err > 1e-12  # really computed in FP32
 
 
-@pytest.mark.parametrize("solver,op", [("bicgstab", "rounded"),
-                                       ("bicg", "rounded"),
-                                       ("bicgstab", "recompute")])
+@pytest.mark.parametrize("solver,op,mode,scatter", [
+    ("bicgstab", "rounded", "stored", "atomic"),    # FP32-vector inner solves
+    ("bicgstab", "rounded", "stored", "color"),
+    ("bicgstab", "recompute", "stored", "atomic"),
+    ("bicg", "rounded", "stored", "atomic"),        # FP64-vector inner solves
+    ("bicgstab", "recompute", "matrix_free", "atomic")])
 def test_mixed_refinement_reaches_fp64_tolerance(vdr, gpu_lib, torch, solver,
-                                                 op):
+                                                 op, mode, scatter):
     prob = vdr.problems.rotation_shear(32, 32, 16, seed=33)
     dt = 10.0 / 32
     aH, aM = 2.0, 3.0 / dt
-    opts = vdr.Options(solver=solver)
+    opts = vdr.Options(solver=solver, apply_mode=mode, scatter=scatter)
     with vdr.Solver(prob, opts, aH=aH, aM=aM) as s:
         s.set_mixed_operator(op)
         b = torch.empty(prob.mesh.nnode, dtype=torch.float64, device="cuda")

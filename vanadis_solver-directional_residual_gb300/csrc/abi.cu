@@ -277,7 +277,8 @@ void free_handle(Handle &h) {
   dfree(h.Aaos); dfree(h.phi); dfree(h.perm_d); dfree(h.dinv32); dfree(h.block_err);
   dfree(h.bk_f); dfree(h.bk_d);
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
-  dfree(h.gcr_work); dfree(h.stage_d); dfree(h.drs);
+  dfree(h.gcr_work); dfree(h.stage_d); dfree(h.drs); dfree(h.work32);
+  if (h.graph32) cudaGraphExecDestroy(h.graph32);
   if (h.gcr_graph) cudaGraphExecDestroy(h.gcr_graph);
   dfree(h.seg_d); dfree(h.seg_i); dfree(h.seg_ticket); dfree(h.seg_of_elem);
   if (h.seg_graph) cudaGraphExecDestroy(h.seg_graph);

@@ -146,6 +146,42 @@ __global__ void __launch_bounds__(256) stored_apply_f32(
   }
 }
 
+// The FP32 operator on FP32 vectors (the mixed solve's inner BiCGStab):
+// y += A x with x gathered as float and the outputs scattered with FP32
+// atomics (or plain adds within a colour) -- no float<->double conversions,
+// which GB300 runs on its FP64 pipe.
+template <bool ATOMIC>
+__global__ void __launch_bounds__(256) stored_apply_f32v(
+    const float4 *__restrict__ A, const int *__restrict__ conn, int E, int p0,
+    int p1, const float *__restrict__ x, float *__restrict__ y, const int *skip,
+    const int *skip2) {
+  if (skip && *(volatile const int *)skip) return;
+  if (skip2 && *(volatile const int *)skip2) return;
+  for (long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x; p < p1;
+       p += (long)gridDim.x * blockDim.x) {
+    int c[8];
+    float xv[8];
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      c[s] = __ldg(conn + (size_t)s * E + p);
+      xv[s] = c[s] < 0 ? 0.f : __ldg(x + c[s]);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const float4 a0 = __ldcs(A + (size_t)(2 * i) * E + p);
+      const float4 a1 = __ldcs(A + (size_t)(2 * i + 1) * E + p);
+      const float o = a0.x * xv[0] + a0.y * xv[1] + a0.z * xv[2] + a0.w * xv[3] +
+                      a1.x * xv[4] + a1.y * xv[5] + a1.z * xv[6] + a1.w * xv[7];
+      if (c[i] >= 0) {
+        if (ATOMIC)
+          atomicAdd(y + c[i], o);
+        else
+          y[c[i]] += o;
+      }
+    }
+  }
+}
+
 // Double-float store: entry (i,j) = hi + lo with hi in Ahi, lo in Alo, both
 // float4 [(2i + j/4)*E + p].  x is split into FP32 pairs with integer bit
 // operations; the 64-term contraction is FP32 two-products + TwoSum; each
@@ -354,6 +390,27 @@ int grid_for(long n, int threads, int per_sm) {
 }
 
 }  // namespace
+
+cudaError_t launch_stored_apply32v(const Handle &h, const float *x, float *y,
+                                   const int *skip, const int *skip2,
+                                   cudaStream_t s) {
+  const bool color = h.scatter == VDR_SCATTER_COLOR;
+  const int nranges = color ? h.ncolors : 1;
+  for (int r = 0; r < nranges; r++) {
+    const int p0 = color ? h.color_off[r] : 0;
+    const int p1 = color ? h.color_off[r + 1] : h.E;
+    if (p1 <= p0) continue;
+    const int grid = grid_for(p1 - p0, 256, 8);
+    if (color)
+      stored_apply_f32v<false><<<grid, 256, 0, s>>>(h.A32v, h.conn, h.E, p0, p1, x, y,
+                                                    skip, skip2);
+    else
+      stored_apply_f32v<true><<<grid, 256, 0, s>>>(h.A32v, h.conn, h.E, p0, p1, x, y,
+                                                   skip, skip2);
+    count_launches(1);
+  }
+  return cudaGetLastError();
+}
 
 int apply_launches(const Handle &h) {
   if (h.apply_mode == VDR_APPLY_MATRIX_FREE || h.scatter != VDR_SCATTER_COLOR)

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "dfloat.cuh"
 #include "vdr_internal.h"
 
 namespace vdr {
@@ -655,8 +656,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_residual(Vec a, double *r,
         v[0] += ri * ri;
         v[1] += bv[u] * bv[u];)
   double o[2];
-  if (grid_sum<2>(v, a.partials, &a.st->ticket, o))
-    *out = o[1] > 0.0 ? sqrt(o[0]) / sqrt(o[1]) : 0.0;
+  if (grid_sum<2>(v, a.partials, &a.st->ticket, o)) {
+    out[0] = o[1] > 0.0 ? sqrt(o[0]) / sqrt(o[1]) : 0.0;
+    out[1] = sqrt(o[0]);
+  }
 }
 
 // x += d
@@ -665,6 +668,339 @@ __global__ void __launch_bounds__(RED_THREADS) k_axpy1(Vec a, const double *d) {
   VLOOP(xv[u] = ok ? a.x[i] : 0.0; dv[u] = ok ? d[i] : 0.0;,
         a.x[i] = xv[u] + dv[u];)
 }
+
+// ------- FP32-vector BiCGStab (the inner solves of the mixed path) -------
+// Vectors are FP32; every inner product and norm accumulates exact FP32
+// two-products per thread in double-float (TwoSum) and is reduced across
+// the grid in FP64; all Krylov scalars stay FP64 in KState.  The operator is
+// the FP32 store applied to FP32 vectors (launch_stored_apply32v), so no
+// float<->double conversion (an FP64-pipe operation on GB300) runs per node.
+struct Vec32 {
+  int n;
+  KState *st;
+  double *partials;
+  const float *dinv;
+  const unsigned char *m;
+  float *b, *x, *r, *rh, *p, *v, *ph, *s, *sh, *t;
+};
+
+__device__ __forceinline__ void dot_acc(DfAcc &a, float x, float y) {
+  const float p = __fmul_rn(x, y);
+  const float e = __fmaf_rn(x, y, -p);
+  const float t = __fadd_rn(a.s, p);
+  const float bp = __fsub_rn(t, a.s);
+  const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  a.s = t;
+  a.c = __fadd_rn(a.c, __fadd_rn(err, e));
+}
+__device__ __forceinline__ double dot_val(const DfAcc &a) {
+  return df_to_double(a.s, a.c);
+}
+
+// x = 0, r = rh = b, rho = ||b||^2.
+__global__ void __launch_bounds__(RED_THREADS) k32_start(Vec32 a) {
+  DfAcc n2{0.f, 0.f};
+  float bv[U];
+  VLOOP(bv[u] = ok ? a.b[i] : 0.f;,
+        a.x[i] = 0.f;
+        a.r[i] = bv[u];
+        a.rh[i] = bv[u];
+        dot_acc(n2, bv[u], bv[u]);)
+  double v[1] = {dot_val(n2)};
+  double o[1];
+  if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    st->bnrm2 = o[0];
+    st->iter = 0;
+    st->sconv = 0;
+    st->status = VDR_NOT_CONVERGED;
+    st->done = 0;
+    st->rho = o[0];
+    st->rho_old = 1.0;
+    st->alpha = 1.0;
+    st->omega = 1.0;
+    st->reason = 0;
+    if (o[0] == 0.0) {
+      st->err = 0.0;
+      st->status = VDR_OK;
+      st->done = 1;
+      return;
+    }
+    st->err = 1.0;
+    if (!finite(o[0])) {
+      st->status = VDR_BREAKDOWN;
+      st->reason = 5;
+      st->done = 1;
+    } else if (st->err <= st->tol) {
+      st->status = VDR_OK;
+      st->done = 1;
+    } else if (st->itmax <= 0) {
+      st->done = 1;
+    }
+  }
+}
+
+// p = r + beta (p - omega v); ph = M^-1 p (0 on Dirichlet); v = 0.
+__global__ void __launch_bounds__(RED_THREADS) b32_p(Vec32 a) {
+  const KState *st = a.st;
+  if (st->done) return;
+  const bool first = st->iter == 0;
+  const float beta =
+      first ? 0.f : (float)((st->rho / st->rho_old) * (st->alpha / st->omega));
+  const float om = (float)st->omega;
+  float rv[U], pv[U], vv[U], dv[U];
+  unsigned char mv[U];
+  VLOOP(rv[u] = ok ? a.r[i] : 0.f; pv[u] = (ok && !first) ? a.p[i] : 0.f;
+        vv[u] = (ok && !first) ? a.v[i] : 0.f; dv[u] = ok ? a.dinv[i] : 0.f;
+        mv[u] = ok ? a.m[i] : 1;,
+        const float pi = first ? rv[u] : rv[u] + beta * (pv[u] - om * vv[u]);
+        a.p[i] = pi;
+        a.ph[i] = mv[u] ? 0.f : pi * dv[u];
+        a.v[i] = 0.f;)
+}
+
+// alpha = rho / (rh, v)
+__global__ void __launch_bounds__(RED_THREADS) b32_alpha(Vec32 a) {
+  if (a.st->done) return;
+  DfAcc d{0.f, 0.f};
+  float hv[U], vv[U];
+  VLOOP(hv[u] = ok ? a.rh[i] : 0.f; vv[u] = ok ? a.v[i] : 0.f;,
+        dot_acc(d, hv[u], vv[u]);)
+  double v[1] = {dot_val(d)};
+  double o[1];
+  if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    if (o[0] == 0.0 || !finite(o[0])) {
+      st->status = VDR_BREAKDOWN;
+      st->reason = 2;
+      st->done = 1;
+    } else {
+      st->alpha = st->rho / o[0];
+    }
+  }
+}
+
+// s = r - alpha v; sh = M^-1 s; t = 0; ||s||.
+__global__ void __launch_bounds__(RED_THREADS) b32_s(Vec32 a) {
+  if (a.st->done) return;
+  const float al = (float)a.st->alpha;
+  DfAcc n2{0.f, 0.f};
+  float rv[U], vv[U], dv[U];
+  unsigned char mv[U];
+  VLOOP(rv[u] = ok ? a.r[i] : 0.f; vv[u] = ok ? a.v[i] : 0.f;
+        dv[u] = ok ? a.dinv[i] : 0.f; mv[u] = ok ? a.m[i] : 1;,
+        const float si = rv[u] - al * vv[u];
+        a.s[i] = si;
+        a.sh[i] = mv[u] ? 0.f : si * dv[u];
+        a.t[i] = 0.f;
+        dot_acc(n2, si, si);)
+  double v[1] = {dot_val(n2)};
+  double o[1];
+  if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    st->snrm = sqrt(o[0]) / sqrt(st->bnrm2);
+    if (st->snrm <= st->tol) st->sconv = 1;
+  }
+}
+
+// omega = (t, s) / (t, t)
+__global__ void __launch_bounds__(RED_THREADS) b32_omega(Vec32 a) {
+  if (a.st->done || a.st->sconv) return;
+  DfAcc ts{0.f, 0.f}, tt{0.f, 0.f};
+  float tv[U], sv[U];
+  VLOOP(tv[u] = ok ? a.t[i] : 0.f; sv[u] = ok ? a.s[i] : 0.f;,
+        dot_acc(ts, tv[u], sv[u]);
+        dot_acc(tt, tv[u], tv[u]);)
+  double v[2] = {dot_val(ts), dot_val(tt)};
+  double o[2];
+  if (grid_sum<2>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    if (o[1] == 0.0 || !finite(o[1]) || !finite(o[0])) {
+      st->status = VDR_BREAKDOWN;
+      st->reason = 3;
+      st->done = 1;
+    } else {
+      st->omega = o[0] / o[1];
+    }
+  }
+}
+
+// x += alpha ph + omega sh; r = s - omega t; rho_new = (rh, r); ||r||.
+__global__ void __launch_bounds__(RED_THREADS) b32_xr(Vec32 a) {
+  KState *stc = a.st;
+  if (stc->done) return;
+  const float al = (float)stc->alpha;
+  if (stc->sconv) {
+    float xv[U], pv[U], sv[U];
+    VLOOP(xv[u] = ok ? a.x[i] : 0.f; pv[u] = ok ? a.ph[i] : 0.f;
+          sv[u] = ok ? a.s[i] : 0.f;,
+          a.x[i] = xv[u] + al * pv[u];
+          a.r[i] = sv[u];)
+    double v[1] = {0.0};
+    double o[1];
+    if (grid_sum<1>(v, a.partials, &a.st->ticket, o)) {
+      KState *st = a.st;
+      st->iter += 1;
+      st->err = st->snrm;
+      st->status = VDR_OK;
+      st->done = 1;
+    }
+    return;
+  }
+  const float om = (float)stc->omega;
+  DfAcc rr{0.f, 0.f}, hr{0.f, 0.f};
+  float xv[U], pv[U], shv[U], sv[U], tv[U], hv[U];
+  VLOOP(xv[u] = ok ? a.x[i] : 0.f; pv[u] = ok ? a.ph[i] : 0.f;
+        shv[u] = ok ? a.sh[i] : 0.f; sv[u] = ok ? a.s[i] : 0.f;
+        tv[u] = ok ? a.t[i] : 0.f; hv[u] = ok ? a.rh[i] : 0.f;,
+        a.x[i] = xv[u] + al * pv[u] + om * shv[u];
+        const float ri = sv[u] - om * tv[u];
+        a.r[i] = ri;
+        dot_acc(rr, ri, ri);
+        dot_acc(hr, hv[u], ri);)
+  double v[2] = {dot_val(rr), dot_val(hr)};
+  double o[2];
+  if (grid_sum<2>(v, a.partials, &a.st->ticket, o)) {
+    KState *st = a.st;
+    const double om64 = st->omega;
+    st->iter += 1;
+    st->rho_old = st->rho;
+    st->rho = o[1];
+    st->err = sqrt(o[0]) / sqrt(st->bnrm2);
+    if (!(st->err == st->err) || !finite(o[1])) {
+      st->status = VDR_BREAKDOWN;
+      st->reason = 5;
+      st->done = 1;
+    } else if (st->err <= st->tol) {
+      st->status = VDR_OK;
+      st->done = 1;
+    } else if (o[1] == 0.0 || om64 == 0.0) {
+      st->status = VDR_BREAKDOWN;
+      st->reason = o[1] == 0.0 ? 1 : 4;
+      st->done = 1;
+    } else if (st->iter >= st->itmax) {
+      st->status = VDR_NOT_CONVERGED;
+      st->done = 1;
+    }
+  }
+}
+
+// b32 = (float)(r * scale); dinv32 = (float)dinv.
+__global__ void __launch_bounds__(RED_THREADS) k32_in(Vec32 a, const double *r,
+                                                      double scale, const double *dinv,
+                                                      float *dinv32) {
+  double rv[U], dv[U];
+  VLOOP(rv[u] = ok ? r[i] : 0.0; dv[u] = ok ? dinv[i] : 0.0;,
+        a.b[i] = (float)(rv[u] * scale);
+        dinv32[i] = (float)dv[u];)
+}
+
+// x += scale * x32 (FP64 update).
+__global__ void __launch_bounds__(RED_THREADS) k32_out(Vec32 a, double *x, double scale) {
+  double xv[U];
+  float dv[U];
+  VLOOP(xv[u] = ok ? x[i] : 0.0; dv[u] = ok ? a.x[i] : 0.f;,
+        x[i] = xv[u] + scale * (double)dv[u];)
+}
+
+Vec32 make_vec32(Handle &h) {
+  Vec32 a{};
+  a.n = h.N;
+  a.st = h.st;
+  a.partials = h.partials;
+  a.dinv = h.dinv32;
+  a.m = h.mask;
+  float *w = h.work32;
+  const size_t N = h.N;
+  a.b = w;
+  a.x = w + N;
+  a.r = w + 2 * N;
+  a.rh = w + 3 * N;
+  a.p = w + 4 * N;
+  a.v = w + 5 * N;
+  a.ph = w + 6 * N;
+  a.s = w + 7 * N;
+  a.sh = w + 8 * N;
+  a.t = w + 9 * N;
+  return a;
+}
+
+cudaError_t launch_iteration32(Handle &h, const Vec32 &a) {
+  const int g = red_grid(h.N);
+  cudaStream_t s = h.stream;
+  cudaError_t e;
+  b32_p<<<g, RED_THREADS, 0, s>>>(a);
+  if ((e = launch_stored_apply32v(h, a.ph, a.v, &h.st->done, nullptr, s))) return e;
+  b32_alpha<<<g, RED_THREADS, 0, s>>>(a);
+  b32_s<<<g, RED_THREADS, 0, s>>>(a);
+  if ((e = launch_stored_apply32v(h, a.sh, a.t, &h.st->done, &h.st->sconv, s))) return e;
+  b32_omega<<<g, RED_THREADS, 0, s>>>(a);
+  b32_xr<<<g, RED_THREADS, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// Inner solve A32 x32 = b32 (FP32 vectors in work32, x32 from zero) to `tol`
+// relative residual; graph-captured like solve_device.
+int solve32_inner(Handle &h, double tol, int itmax, int *iter, double *err) {
+  cudaError_t e;
+  if (!h.work32 && (e = cudaMalloc(&h.work32, sizeof(float) * 10 * (size_t)h.N)))
+    return cuda_fail(e, "FP32 workspace");
+  cudaStream_t s = h.stream;
+  Vec32 a = make_vec32(h);
+  const int g = red_grid(h.N);
+  KState init{};
+  init.tol = tol;
+  init.itmax = itmax;
+  init.best_err = INFINITY;
+  std::memcpy(&h.h_st[0], &init, sizeof(KState));
+  if ((e = cudaMemcpyAsync(h.st, &h.h_st[0], sizeof(KState), cudaMemcpyHostToDevice, s)))
+    return cuda_fail(e, "state upload");
+  k32_start<<<g, RED_THREADS, 0, s>>>(a);
+  count_launches(1);
+  if ((e = cudaGetLastError())) return cuda_fail(e, "start kernel");
+  const int K = h.opt.iters_per_graph > 0 ? h.opt.iters_per_graph : 8;
+  const void *key = (const void *)((uintptr_t)h.work32 ^ ((uintptr_t)h.A32v << 1) ^
+                                   (uintptr_t)K ^ ((uintptr_t)h.scatter << 12));
+  if (!h.graph32 || h.graph32_key != key) {
+    if (h.graph32) cudaGraphExecDestroy(h.graph32);
+    h.graph32 = nullptr;
+    cudaGraph_t graph;
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)))
+      return cuda_fail(e, "begin capture");
+    const long long before = launches_so_far();
+    for (int k = 0; k < K && !e; k++) e = launch_iteration32(h, a);
+    count_launches(before - launches_so_far());  // captured, not launched
+    cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (e) return cuda_fail(e, "capture");
+    if (e2) return cuda_fail(e2, "end capture");
+    e = cudaGraphInstantiate(&h.graph32, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e) return cuda_fail(e, "graph instantiate");
+    h.graph32_key = key;
+  }
+  const long nodes = 5 + 2 * apply_launches(h);
+  const int max_launches = (itmax + K - 1) / K + 1;
+  bool finished = false;
+  for (int c = 0; c < max_launches && !finished; c++) {
+    if ((e = cudaGraphLaunch(h.graph32, s))) return cuda_fail(e, "graph launch");
+    count_launches((long)K * nodes);
+    if ((e = cudaMemcpyAsync(&h.h_st[c & 1], h.st, sizeof(KState),
+                             cudaMemcpyDeviceToHost, s)))
+      return cuda_fail(e, "state readback");
+    if ((e = cudaEventRecord(h.ev[c & 1], s))) return cuda_fail(e, "event");
+    if (c > 0) {
+      if ((e = cudaEventSynchronize(h.ev[(c - 1) & 1]))) return cuda_fail(e, "sync");
+      if (h.h_st[(c - 1) & 1].done) finished = true;
+    }
+  }
+  if ((e = cudaStreamSynchronize(s))) return cuda_fail(e, "solve");
+  KState fin;
+  if ((e = cudaMemcpy(&fin, h.st, sizeof(KState), cudaMemcpyDeviceToHost)))
+    return cuda_fail(e, "final state");
+  if (iter) *iter = fin.iter;
+  if (err) *err = fin.err;
+  return fin.done ? fin.status : VDR_NOT_CONVERGED;
+}
 }  // namespace
 
 // Iterative refinement: the residual r = b - A x and the update x += d are
@@ -672,7 +1008,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_axpy1(Vec a, const double *d) {
 // operator to max(inner_tol, 0.5 tol / rel) relative to ||r|| (rel =
 // ||r||/||b||): a correction is solved no further than the outer residual
 // needs to reach tol, so a tight first correction is followed by a short
-// second one instead of two full-depth inner solves.
+// second one instead of two full-depth inner solves.  With the stored
+// operator and BiCGStab the inner solve runs on FP32 vectors (r scaled by
+// 1/||r||, inner products in double-float/FP64); otherwise on FP64 vectors.
 int solve_mixed_device(Handle &h, int method, const double *b, double *x,
                        double tol, double inner_tol, int max_outer,
                        int inner_itmax, MixedStats *ms) {
@@ -687,6 +1025,13 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
   MixedStats st;
   int status = VDR_NOT_CONVERGED;
   if ((e = launch_mask_vec(x, h.mask, h.N, s))) return cuda_fail(e, "mask x");
+  // The stored FP32 operator runs its inner BiCGStab on FP32 vectors.
+  const bool f32v = h.apply_mode == VDR_APPLY_STORED && method == VDR_SOLVER_BICGSTAB;
+  if (f32v && !h.dinv32 && (e = cudaMalloc(&h.dinv32, sizeof(float) * (size_t)h.N)))
+    return cuda_fail(e, "FP32 diagonal");
+  if (f32v && !h.work32 &&
+      (e = cudaMalloc(&h.work32, sizeof(float) * 10 * (size_t)h.N)))
+    return cuda_fail(e, "FP32 workspace");
   for (int outer = 0; outer <= max_outer; outer++) {
     h.apply_fp32 = false;
     if ((e = cudaMemsetAsync(r, 0, sizeof(double) * h.N, s)) ||
@@ -694,10 +1039,11 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
       return cuda_fail(e, "outer residual");
     k_residual<<<g, RED_THREADS, 0, s>>>(a, r, scal);
     count_launches(1);
-    double rel = 0.0;
-    if ((e = cudaMemcpyAsync(&rel, scal, sizeof(double), cudaMemcpyDeviceToHost, s)) ||
+    double rr[2] = {0.0, 0.0};  // ||r||/||b||, ||r||
+    if ((e = cudaMemcpyAsync(rr, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
       return cuda_fail(e, "outer residual");
+    const double rel = rr[0];
     st.err = rel;
     if (rel <= tol) {
       status = VDR_OK;
@@ -709,18 +1055,31 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
     }
     if (outer == max_outer) break;
     st.outer = outer + 1;
-    if ((e = cudaMemsetAsync(d, 0, sizeof(double) * h.N, s)))
-      return cuda_fail(e, "memset");
-    h.apply_fp32 = true;
     int it = 0;
     double ierr = 0.0;
     const double itol = std::max(inner_tol, 0.5 * tol / rel);
-    const int ist = solve_device(h, method, r, d, itol, inner_itmax, &it, &ierr);
-    h.apply_fp32 = false;
-    if (ist == VDR_CUDA_ERROR || ist == VDR_BAD_ARGUMENT) return ist;
+    if (f32v) {
+      // d solves A32 d = r / ||r|| on FP32 vectors; x += ||r|| d in FP64
+      Vec32 a32 = make_vec32(h);
+      k32_in<<<g, RED_THREADS, 0, s>>>(a32, r, 1.0 / rr[1], h.dinv, h.dinv32);
+      count_launches(1);
+      h.apply_fp32 = true;
+      const int ist = solve32_inner(h, itol, inner_itmax, &it, &ierr);
+      h.apply_fp32 = false;
+      if (ist == VDR_CUDA_ERROR || ist == VDR_BAD_ARGUMENT) return ist;
+      k32_out<<<g, RED_THREADS, 0, s>>>(a32, x, rr[1]);
+      count_launches(1);
+    } else {
+      if ((e = cudaMemsetAsync(d, 0, sizeof(double) * h.N, s)))
+        return cuda_fail(e, "memset");
+      h.apply_fp32 = true;
+      const int ist = solve_device(h, method, r, d, itol, inner_itmax, &it, &ierr);
+      h.apply_fp32 = false;
+      if (ist == VDR_CUDA_ERROR || ist == VDR_BAD_ARGUMENT) return ist;
+      k_axpy1<<<g, RED_THREADS, 0, s>>>(a, d);
+      count_launches(1);
+    }
     st.inner += it;
-    k_axpy1<<<g, RED_THREADS, 0, s>>>(a, d);
-    count_launches(1);
     if ((e = cudaGetLastError())) return cuda_fail(e, "update");
   }
   if (ms) *ms = st;

@@ -121,6 +121,11 @@ struct Handle {
   // solver workspace
   double *work = nullptr;
   int nwork = 0;
+  // FP32-vector inner BiCGStab of the mixed solve: [10][N] floats (b, x, r,
+  // rh, p, v, ph, s, sh, t) and its captured iterations
+  float *work32 = nullptr;
+  cudaGraphExec_t graph32 = nullptr;
+  const void *graph32_key = nullptr;
   KState *st = nullptr;
   KState *h_st = nullptr;  // pinned mirror
   double *partials = nullptr;
@@ -214,6 +219,10 @@ cudaError_t launch_mass(const Handle &h, const double *c, double *partials,
 cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
                                 const double *x, double *y, const int *skip,
                                 const int *skip2, cudaStream_t s);
+// The FP32 operator (A32v) on FP32 vectors, y += A x (stored mode only).
+cudaError_t launch_stored_apply32v(const Handle &h, const float *x, float *y,
+                                   const int *skip, const int *skip2,
+                                   cudaStream_t s);
 cudaError_t launch_apply(const Handle &h, bool transpose, const double *x,
                          double *y, const int *skip, const int *skip2,
                          cudaStream_t s);
