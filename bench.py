@@ -56,6 +56,8 @@ def args_parse():
                     help="skip the many-right-hand-side section")
     ap.add_argument("--no-meshes", action="store_true",
                     help="skip the many-mesh section")
+    ap.add_argument("--no-dropin", action="store_true",
+                    help="skip the kernel_dbcg_simple_ section")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-preconditioner section")
     ap.add_argument("--learn-steps", type=int, default=LEARN_STEPS)
@@ -466,6 +468,63 @@ LEARN_DAGGER_PAIRS = 25    # per training step, from the learned solver
 LEARN_TILT = 0.5
 
 
+def dropin_section(vdr, s, prob, cf, rM):
+    """The reference's own solve entry at C2: kernel_dbcg_simple_ called with
+    host arrays as VANADIS.FOR:809 calls it -- B, X, BB (64E doubles, 4.3 GB),
+    ISS, DIAG and bc uploaded and X downloaded on every call -- on the
+    GPU-built theta-step operator, exported once in the reference's BB layout
+    (vdr_get_element_matrices); Jacobi-preconditioned BiCG, the reference's
+    method, to 1e-8 from X = 0."""
+    import ctypes
+    import numpy as np
+    import torch
+    m = prob.mesh
+    N, E = m.nnode, m.nelem
+    keep = []
+
+    def pinned(n, dtype):
+        t = torch.empty(n, dtype=dtype, pin_memory=True)
+        keep.append(t)
+        return t.numpy()
+
+    bb = pinned(64 * E, torch.float64)
+    s.element_matrices(out=bb)
+    diag = pinned(N, torch.float64)
+    diag[:] = s.diag()
+    b = pinned(N, torch.float64)
+    s.assemble_rhs(cf, rM, None, out=b)
+    iss = pinned(8 * E, torch.int32)
+    iss[:] = np.ascontiguousarray(m.iss, dtype=np.int32).ravel()
+    bc = pinned(N, torch.int32)
+    bc[:] = np.asarray(prob.bc, dtype=np.int32)
+    x = pinned(N, torch.float64)
+    lib = vdr.load_library()
+    n_, tol_, itmax_ = ctypes.c_int(N), ctypes.c_double(TOL), ctypes.c_int(20000)
+    it_, err_ = ctypes.c_int(0), ctypes.c_double(0.0)
+    nax, nay, naz = (ctypes.c_int(int(v)) for v in (m.nax, m.nay, m.naz))
+    pd = lambda arr: arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    pi = lambda arr: arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    times = []
+    for k in range(4):
+        x[:] = 0.0
+        t0 = time.perf_counter()
+        lib.kernel_dbcg_simple_(ctypes.byref(n_), pd(b), pd(x), ctypes.byref(tol_),
+                                ctypes.byref(itmax_), ctypes.byref(it_),
+                                ctypes.byref(err_), pd(bb), pi(iss), pd(diag),
+                                ctypes.byref(nax), ctypes.byref(nay),
+                                ctypes.byref(naz), pi(bc))
+        times.append(time.perf_counter() - t0)
+    h2d = 8 * (64 * E + 3 * N) + 4 * (8 * E + N)
+    return {"workload": "rotation_shear 256x256x128 theta-step system, BB from "
+                        "the GPU build; Jacobi BiCG to 1e-8 from X = 0",
+            "call_s": statistics.mean(times[1:]), "iterations": it_.value,
+            "err": err_.value, "h2d_bytes_per_call": h2d,
+            "d2h_bytes_per_call": 8 * N,
+            "what": "kernel_dbcg_simple_ with host arrays: uploads, BB to the "
+                    "double-float store, graph-captured BiCG with the fused "
+                    "A p / A^T p~ apply, X download"}
+
+
 def learned_section(vdr, device, a):
     """The learned preconditioner on the tilting-axis transient problem
     (128x128x64, theta-step at Courant 10, rotation axis tilting 0.5 degrees
@@ -739,6 +798,7 @@ def run_native(a):
     batched = None if a.no_batched else batched_rhs_section(vdr, local)
     meshes = None if a.no_meshes else batched_meshes_section(vdr, local)
     learned = None if a.no_learned else learned_section(vdr, local, a)
+    dropin = None if a.no_dropin else dropin_section(vdr, s, prob, cf, rM)
 
     # ---- e2e through the C ABI with host buffers ----
     # The step's inputs (per-element fields) and outputs (right-hand side,
@@ -818,6 +878,7 @@ def run_native(a):
             "batched_rhs": batched,
             "batched_meshes": meshes,
             "learned_preconditioner": learned,
+            "dropin_bicg": dropin,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,

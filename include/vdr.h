@@ -144,6 +144,15 @@ int vdr_assemble_rhs_device(vdr_handle *h, double cf, double rM,
 /* Jacobi diagonal of the current operator (1 on Dirichlet nodes). */
 int vdr_get_diag(vdr_handle *h, double *diag);
 
+/* The current operator's element matrices in the reference's BB layout
+ * (sklad_wd, vanadis_full_DR_OpenMP_timing.for:880-904): bb[64 e + 8 i + j]
+ * = A_e(i,j) in FP64, e in the caller's element order, unmasked (Dirichlet
+ * rows and columns are applied by the solver, as the reference does).  What
+ * kernel_dbcg_simple_ takes as BB.  bb holds 64 E doubles (host array, or
+ * device array for the _device form).  Stored operator only. */
+int vdr_get_element_matrices(vdr_handle *h, double *bb);
+int vdr_get_element_matrices_device(vdr_handle *h, double *d_bb);
+
 /* Solves A x = b.  x holds the initial guess on entry (Dirichlet entries
  * are zeroed, as the reference does) and the solution on exit.  Stops when
  * ||r||_2/||b||_2 <= tol (recursively updated residual, as dbcg_simple) or

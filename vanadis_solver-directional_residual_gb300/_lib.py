@@ -59,6 +59,8 @@ SIGNATURES = {
     "vdr_assemble_rhs": (_i, [_P, _d, _d, _D, _D]),
     "vdr_assemble_rhs_device": (_i, [_P, _d, _d, _P, _P]),
     "vdr_get_diag": (_i, [_P, _D]),
+    "vdr_get_element_matrices": (_i, [_P, _D]),
+    "vdr_get_element_matrices_device": (_i, [_P, _P]),
     "vdr_solve": (_i, [_P, _D, _D, _d, _i, _I, _D]),
     "vdr_solve_device": (_i, [_P, _P, _P, _d, _i, _I, _D]),
     "vdr_solve_mixed_device": (_i, [_P, _P, _P, _d, _d, _i, _i, _I, _I, _D]),

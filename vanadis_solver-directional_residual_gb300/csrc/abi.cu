@@ -669,6 +669,44 @@ int vdr_get_diag(vdr_handle *H, double *diag) {
   return e ? cuda_fail(e, "vdr_get_diag") : VDR_OK;
 }
 
+int vdr_get_element_matrices_device(vdr_handle *H, double *bb) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!bb) {
+    set_error("vdr_get_element_matrices_device: null bb");
+    return VDR_BAD_ARGUMENT;
+  }
+  if (h.apply_mode != VDR_APPLY_STORED) {
+    set_error("vdr_get_element_matrices: the matrix-free operator stores no matrices");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator(h))) return st;
+  cudaError_t e = launch_export_bb(h, bb, h.stream);
+  if (!e) e = cudaStreamSynchronize(h.stream);
+  return e ? cuda_fail(e, "vdr_get_element_matrices_device") : VDR_OK;
+}
+
+int vdr_get_element_matrices(vdr_handle *H, double *bb) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!bb) {
+    set_error("vdr_get_element_matrices: null bb");
+    return VDR_BAD_ARGUMENT;
+  }
+  double *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(double) * 64 * (size_t)std::max(h.E, 1));
+  if (e) return cuda_fail(e, "vdr_get_element_matrices: alloc");
+  st = vdr_get_element_matrices_device(H, d);
+  if (!st) {
+    e = cudaMemcpy(bb, d, sizeof(double) * 64 * (size_t)h.E, cudaMemcpyDeviceToHost);
+    if (e) st = cuda_fail(e, "vdr_get_element_matrices: download");
+  }
+  cudaFree(d);
+  return st;
+}
+
 int vdr_solve_device(vdr_handle *H, const double *b, double *x, double tol,
                      int itmax, int *iter, double *err) {
   int st = check_handle(H);
@@ -1047,10 +1085,12 @@ int legacy_prepare(Legacy &L, int N, int E) {
       return cuda_fail(e, "stream");
     h.scatter = VDR_SCATTER_ATOMIC;
     h.apply_mode = VDR_APPLY_STORED;
-    h.storage = VDR_STORE_FP64;
+    h.storage = VDR_STORE_DF;
   }
   if (N > L.capN || E > L.capE) {
     dfree(h.A64); h.A64 = nullptr;
+    dfree(h.Ahi); h.Ahi = nullptr;
+    dfree(h.Alo); h.Alo = nullptr;
     dfree(h.conn); h.conn = nullptr;
     dfree(h.diag); h.diag = nullptr;
     dfree(h.dinv); h.dinv = nullptr;
@@ -1075,7 +1115,8 @@ int legacy_prepare(Legacy &L, int N, int E) {
       h.ev[k] = nullptr;
     }
     const size_t cN = std::max(N, L.capN), cE = std::max(E, L.capE);
-    if ((e = dalloc(&h.A64, cE * 32)) || (e = dalloc(&h.conn, cE * 8)) ||
+    if ((e = dalloc(&h.A64, cE * 32)) || (e = dalloc(&h.Ahi, cE * 16)) ||
+        (e = dalloc(&h.Alo, cE * 16)) || (e = dalloc(&h.conn, cE * 8)) ||
         (e = dalloc(&h.diag, cN)) || (e = dalloc(&h.dinv, cN)) ||
         (e = dalloc(&h.mask, cN)) ||
         (e = dalloc(&L.bb, cE * 64)) || (e = dalloc(&L.b, cN)) ||
@@ -1141,18 +1182,21 @@ void kernel_dbcg_simple_(int *Np, double *B, double *X, double *TOLp,
     if ((e = cudaMemsetAsync(L.bad, 0, sizeof(int), s)) ||
         (e = launch_legacy_conn(L.iss, (int)E, N, bc_dirichlet ? L.bc : nullptr,
                                 h.conn, L.bad, s)) ||
-        (e = launch_legacy_bb(L.bb, (int)E, h.A64, s)) ||
+        (e = launch_legacy_bb_df(L.bb, (int)E, h.Ahi, h.Alo, L.bad, s)) ||
         (e = launch_diag_fix(h.diag, h.dinv, nullptr, N, s)) ||
         (e = cudaMemcpyAsync(&bad, L.bad, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
       break;
+    // BB entries outside the double-float window: the FP64 store
+    h.storage = (bad & 2) ? VDR_STORE_FP64 : VDR_STORE_DF;
+    if ((bad & 2) && (e = launch_legacy_bb(L.bb, (int)E, h.A64, s))) break;
   } while (0);
   if (e) {
     cuda_fail(e, "kernel_dbcg_simple_: upload");
     *ERRp = inf;
     return;
   }
-  if (bad) {
+  if (bad & 1) {
     set_error("kernel_dbcg_simple_: ISS entry outside 1..N");
     *ERRp = inf;
     return;

@@ -319,6 +319,98 @@ __global__ void __launch_bounds__(256, 4) stored_apply_df(
   }
 }
 
+// BiCG's two products in one pass over the double-float store: y1 += A x1
+// and y2 += A^T x2 (A p and A^T p~ of one iteration), each element matrix
+// read once.  Both inputs are split per element as in stored_apply_df; rows
+// of A x1 are scattered as they complete, the columns of A^T x2 accumulate
+// in registers.  Elements with an input outside the FP32 range take the
+// FP64 fallback for both products.
+template <bool ATOMIC>
+__global__ void __launch_bounds__(256, 2) stored_apply_df_both(
+    const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
+    const int *__restrict__ conn, int E, int p0, int p1,
+    const double *__restrict__ x1, double *__restrict__ y1,
+    const double *__restrict__ x2, double *__restrict__ y2, const int *skip) {
+  if (skip && *(volatile const int *)skip) return;
+  for (long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x; p < p1;
+       p += (long)gridDim.x * blockDim.x) {
+    int c[8];
+    float ah[8], al[8], bh[8], bl[8];
+    bool bad = false;
+    int sa, sb;
+    {
+      double va[8], vb[8];
+      int ea = 0, eb = 0;
+#pragma unroll
+      for (int s = 0; s < 8; s++) {
+        c[s] = __ldg(conn + (size_t)s * E + p);
+        va[s] = c[s] < 0 ? 0.0 : __ldg(x1 + c[s]);
+        vb[s] = c[s] < 0 ? 0.0 : __ldg(x2 + c[s]);
+        ea = max(ea, df_exp(va[s]));
+        eb = max(eb, df_exp(vb[s]));
+      }
+      sa = ea - 1023;
+      sb = eb - 1023;
+#pragma unroll
+      for (int s = 0; s < 8; s++) {
+        df_split(va[s], ah[s], al[s], bad, sa);
+        df_split(vb[s], bh[s], bl[s], bad, sb);
+      }
+    }
+    if (bad) {
+      df_element_fallback(Ahi, Alo, conn, E, p, false, ATOMIC, x1, y1);
+      df_element_fallback(Ahi, Alo, conn, E, p, true, ATOMIC, x2, y2);
+      continue;
+    }
+    DfAcc acc2[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc2[j] = DfAcc{0.0f, 0.0f};
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const float4 h0 = __ldcs(Ahi + (size_t)(2 * i) * E + p);
+      const float4 h1 = __ldcs(Ahi + (size_t)(2 * i + 1) * E + p);
+      const float4 l0 = __ldcs(Alo + (size_t)(2 * i) * E + p);
+      const float4 l1 = __ldcs(Alo + (size_t)(2 * i + 1) * E + p);
+      DfAcc acc{0.0f, 0.0f};
+      df_fma_acc(acc, h0.x, l0.x, ah[0], al[0]);
+      df_fma_acc(acc, h0.y, l0.y, ah[1], al[1]);
+      df_fma_acc(acc, h0.z, l0.z, ah[2], al[2]);
+      df_fma_acc(acc, h0.w, l0.w, ah[3], al[3]);
+      df_fma_acc(acc, h1.x, l1.x, ah[4], al[4]);
+      df_fma_acc(acc, h1.y, l1.y, ah[5], al[5]);
+      df_fma_acc(acc, h1.z, l1.z, ah[6], al[6]);
+      df_fma_acc(acc, h1.w, l1.w, ah[7], al[7]);
+      df_fma_acc(acc2[0], h0.x, l0.x, bh[i], bl[i]);
+      df_fma_acc(acc2[1], h0.y, l0.y, bh[i], bl[i]);
+      df_fma_acc(acc2[2], h0.z, l0.z, bh[i], bl[i]);
+      df_fma_acc(acc2[3], h0.w, l0.w, bh[i], bl[i]);
+      df_fma_acc(acc2[4], h1.x, l1.x, bh[i], bl[i]);
+      df_fma_acc(acc2[5], h1.y, l1.y, bh[i], bl[i]);
+      df_fma_acc(acc2[6], h1.z, l1.z, bh[i], bl[i]);
+      df_fma_acc(acc2[7], h1.w, l1.w, bh[i], bl[i]);
+      double o = df_to_double(acc.s, acc.c);
+      if (!df_scale(o, sa)) o = ldexp(o, sa);
+      if (c[i] >= 0) {
+        if (ATOMIC)
+          atomicAdd(y1 + c[i], o);
+        else
+          y1[c[i]] += o;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      double o = df_to_double(acc2[j].s, acc2[j].c);
+      if (!df_scale(o, sb)) o = ldexp(o, sb);
+      if (c[j] >= 0) {
+        if (ATOMIC)
+          atomicAdd(y2 + c[j], o);
+        else
+          y2[c[j]] += o;
+      }
+    }
+  }
+}
+
 // Reference BB (BB[64e + 8i + j], sklad_wd) -> pair store A64[(4i+j/2)*E+e];
 // reference ISS (iss(E,8) column-major, 1-based) -> masked 0-based conn.
 __global__ void legacy_convert_kernel(const double2 *__restrict__ bb, int E,
@@ -332,6 +424,65 @@ __global__ void legacy_convert_kernel(const double2 *__restrict__ bb, int E,
   }
 }
 
+// Reference BB -> double-float store Ahi/Alo[(2i + j/4)*E + e] (chunk c =
+// 2i + j/4 holds BB[64e + 4c .. 4c+3]).  Entries outside the store window
+// (nonzero with magnitude outside [2^-100, 2^120], inf, NaN) set bit 2 of
+// *bad: the caller then uses the FP64 store.
+__global__ void legacy_convert_df_kernel(const double *__restrict__ bb, int E,
+                                         float4 *__restrict__ Ahi,
+                                         float4 *__restrict__ Alo, int *bad) {
+  const long total = (long)E * 16;
+  bool out = false;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long)gridDim.x * blockDim.x) {
+    const long e = t >> 4;
+    const int c = (int)(t & 15);
+    const double2 v0 = __ldg(reinterpret_cast<const double2 *>(bb) + 2 * t);
+    const double2 v1 = __ldg(reinterpret_cast<const double2 *>(bb) + 2 * t + 1);
+    const double v[4] = {v0.x, v0.y, v1.x, v1.y};
+    float hi[4], lo[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int ex = df_exp(v[k]);
+      if (ex != 0 && (ex < 1023 - 100 || ex > 1023 + 120)) out = true;
+      df_split(v[k], hi[k], lo[k], out);
+    }
+    Ahi[(size_t)c * E + e] = make_float4(hi[0], hi[1], hi[2], hi[3]);
+    Alo[(size_t)c * E + e] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+  }
+  if (out) atomicOr(bad, 2);
+}
+
+// Element matrices -> the reference's BB layout, FP64: BB[64 e + 8i + j] =
+// A_e(i,j), e the caller's element at storage position p (perm, or the
+// identity).  Chunk c = 2i + j/4 of a storage element holds entries
+// 8i + 4(j/4) .. +3 = 4c .. 4c+3 (double-float or FP64 pair store).
+__global__ void export_bb_kernel(const float4 *__restrict__ Ahi,
+                                 const float4 *__restrict__ Alo,
+                                 const double2 *__restrict__ A64,
+                                 const int *__restrict__ perm, int E,
+                                 double *__restrict__ bb) {
+  const long total = (long)E * 16;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long)gridDim.x * blockDim.x) {
+    const long p = t >> 4;
+    const int c = (int)(t & 15);
+    const long e = perm ? __ldg(perm + p) : p;
+    double2 v0, v1;
+    if (Ahi) {
+      const float4 h = Ahi[(size_t)c * E + p], l = Alo[(size_t)c * E + p];
+      v0 = make_double2(df_to_double(h.x, l.x), df_to_double(h.y, l.y));
+      v1 = make_double2(df_to_double(h.z, l.z), df_to_double(h.w, l.w));
+    } else {
+      v0 = A64[(size_t)(2 * c) * E + p];
+      v1 = A64[(size_t)(2 * c + 1) * E + p];
+    }
+    double2 *o = reinterpret_cast<double2 *>(bb + 64 * e + 4 * c);
+    o[0] = v0;
+    o[1] = v1;
+  }
+}
+
 __global__ void legacy_conn_kernel(const int *__restrict__ iss, int E, int N,
                                    const int *__restrict__ bc,
                                    int *__restrict__ conn, int *bad) {
@@ -340,7 +491,7 @@ __global__ void legacy_conn_kernel(const int *__restrict__ iss, int E, int N,
        t += (long)gridDim.x * blockDim.x) {
     const int n = iss[t] - 1;
     if (n < 0 || n >= N) {
-      atomicExch(bad, 1);
+      atomicOr(bad, 1);
       conn[t] = MASK_BIT;  // node 0, masked: never read or written
       continue;
     }
@@ -412,6 +563,32 @@ cudaError_t launch_stored_apply32v(const Handle &h, const float *x, float *y,
   return cudaGetLastError();
 }
 
+bool can_apply_both(const Handle &h) {
+  return h.apply_mode == VDR_APPLY_STORED && !h.apply_fp32 &&
+         h.storage == VDR_STORE_DF && h.Ahi && h.Alo;
+}
+
+cudaError_t launch_apply_both(const Handle &h, const double *x1, double *y1,
+                              const double *x2, double *y2, const int *skip,
+                              cudaStream_t s) {
+  const bool color = h.scatter == VDR_SCATTER_COLOR;
+  const int nranges = color ? h.ncolors : 1;
+  for (int r = 0; r < nranges; r++) {
+    const int p0 = color ? h.color_off[r] : 0;
+    const int p1 = color ? h.color_off[r + 1] : h.E;
+    if (p1 <= p0) continue;
+    const int grid = grid_for(p1 - p0, 256, 6);
+    if (color)
+      stored_apply_df_both<false><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, h.conn, h.E, p0, p1,
+                                                       x1, y1, x2, y2, skip);
+    else
+      stored_apply_df_both<true><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, h.conn, h.E, p0, p1,
+                                                      x1, y1, x2, y2, skip);
+    count_launches(1);
+  }
+  return cudaGetLastError();
+}
+
 int apply_launches(const Handle &h) {
   if (h.apply_mode == VDR_APPLY_MATRIX_FREE || h.scatter != VDR_SCATTER_COLOR)
     return 1;
@@ -471,6 +648,23 @@ cudaError_t launch_legacy_bb(const double *bb_ref, int E, double2 *A64,
                              cudaStream_t s) {
   legacy_convert_kernel<<<grid_for((long)E * 32, 256, 16), 256, 0, s>>>(
       reinterpret_cast<const double2 *>(bb_ref), E, A64);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_legacy_bb_df(const double *bb_ref, int E, float4 *Ahi, float4 *Alo,
+                                int *bad, cudaStream_t s) {
+  legacy_convert_df_kernel<<<grid_for((long)E * 16, 256, 16), 256, 0, s>>>(
+      bb_ref, E, Ahi, Alo, bad);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_export_bb(const Handle &h, double *bb, cudaStream_t s) {
+  const bool df = h.storage == VDR_STORE_DF && h.Ahi;
+  const int *perm = h.scatter == VDR_SCATTER_COLOR ? h.perm_d : nullptr;
+  export_bb_kernel<<<grid_for((long)h.E * 16, 256, 16), 256, 0, s>>>(
+      df ? h.Ahi : nullptr, df ? h.Alo : nullptr, df ? nullptr : h.A64, perm, h.E, bb);
   count_launches(1);
   return cudaGetLastError();
 }

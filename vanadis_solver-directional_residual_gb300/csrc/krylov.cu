@@ -481,8 +481,12 @@ cudaError_t launch_iteration(Handle &h, int method, const Vec &a,
     bs_xr<<<g, RED_THREADS, 0, s>>>(a);
   } else {
     bc_p<<<g, RED_THREADS, 0, s>>>(a);
-    if ((e = launch_apply(h, false, a.p, a.z, &h.st->done, nullptr, s))) return e;
-    if ((e = launch_apply(h, true, a.pp, a.zz, &h.st->done, nullptr, s))) return e;
+    if (can_apply_both(h)) {  // A p and A^T pp in one pass over the store
+      if ((e = launch_apply_both(h, a.p, a.z, a.pp, a.zz, &h.st->done, s))) return e;
+    } else {
+      if ((e = launch_apply(h, false, a.p, a.z, &h.st->done, nullptr, s))) return e;
+      if ((e = launch_apply(h, true, a.pp, a.zz, &h.st->done, nullptr, s))) return e;
+    }
     bc_ak<<<g, RED_THREADS, 0, s>>>(a);
     bc_upd<<<g, RED_THREADS, 0, s>>>(a);
   }
@@ -521,7 +525,9 @@ cudaError_t ensure_solver_workspace(Handle &h, int nvec) {
 
 // Kernels of one captured iteration.
 long launches_graph_nodes(Handle &h, int method, const Precond *prec) {
-  long n = (method == VDR_SOLVER_BICGSTAB ? 5 : 3) + 2 * apply_launches(h);
+  long n = (method == VDR_SOLVER_BICGSTAB ? 5 : 3) +
+           (method != VDR_SOLVER_BICGSTAB && can_apply_both(h) ? 1 : 2) *
+               apply_launches(h);
   if (prec) n += 2 * prec->launches;
   return n;
 }
@@ -580,6 +586,7 @@ int solve_device(Handle &h, int method, const double *b, double *x,
                                    ((uintptr_t)h.work << 2) ^ (uintptr_t)K ^
                                    ((uintptr_t)h.apply_mode << 8) ^
                                    ((uintptr_t)h.scatter << 12) ^
+                                   ((uintptr_t)h.storage << 16) ^
                                    ((uintptr_t)(prec ? prec->ctx : nullptr) << 3));
   if (!h.graph_exec[slot] || h.graph_key[slot] != key) {
     if (h.graph_exec[slot]) cudaGraphExecDestroy(h.graph_exec[slot]);

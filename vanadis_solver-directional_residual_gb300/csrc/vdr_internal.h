@@ -219,6 +219,11 @@ cudaError_t launch_mass(const Handle &h, const double *c, double *partials,
 cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
                                 const double *x, double *y, const int *skip,
                                 const int *skip2, cudaStream_t s);
+// y1 += A x1 and y2 += A^T x2 in one pass (BiCG), when can_apply_both.
+bool can_apply_both(const Handle &h);
+cudaError_t launch_apply_both(const Handle &h, const double *x1, double *y1,
+                              const double *x2, double *y2, const int *skip,
+                              cudaStream_t s);
 // The FP32 operator (A32v) on FP32 vectors, y += A x (stored mode only).
 cudaError_t launch_stored_apply32v(const Handle &h, const float *x, float *y,
                                    const int *skip, const int *skip2,
@@ -230,6 +235,13 @@ cudaError_t launch_mask_conn(int *conn, int E, const unsigned char *mask,
                              cudaStream_t s);
 cudaError_t launch_legacy_bb(const double *bb_ref, int E, double2 *A64,
                              cudaStream_t s);
+// The stored element matrices in the reference's BB layout (FP64, caller's
+// element order); the operator must be stored and valid.
+cudaError_t launch_export_bb(const Handle &h, double *bb, cudaStream_t s);
+// Reference BB -> double-float store; bit 2 of *bad when an entry is
+// outside the store window (use launch_legacy_bb instead).
+cudaError_t launch_legacy_bb_df(const double *bb_ref, int E, float4 *Ahi, float4 *Alo,
+                                int *bad, cudaStream_t s);
 cudaError_t launch_legacy_conn(const int *iss_ref, int E, int N, const int *bc,
                                int *conn, int *bad, cudaStream_t s);
 // diag = 1 on Dirichlet nodes (when mask != null); dinv = 1/diag.

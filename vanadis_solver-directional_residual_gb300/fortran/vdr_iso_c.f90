@@ -104,6 +104,13 @@ module vdr_iso_c
        real(c_double), intent(out) :: diag(*)
      end function vdr_get_diag
 
+     integer(c_int) function vdr_get_element_matrices(h, bb) &
+          bind(c, name="vdr_get_element_matrices")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: h
+       real(c_double), intent(out) :: bb(*)
+     end function vdr_get_element_matrices
+
      integer(c_int) function vdr_solve(h, b, x, tol, itmax, iter, err) &
           bind(c, name="vdr_solve")
        import :: c_int, c_double, c_ptr

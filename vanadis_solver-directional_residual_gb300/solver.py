@@ -176,6 +176,15 @@ class Solver:
         L.check(self.lib.vdr_get_diag(self.h, _dp(d)), "vdr_get_diag")
         return d
 
+    def element_matrices(self, out=None):
+        """The operator's element matrices in the reference's BB layout
+        (64 E float64, bb[64e + 8i + j] = A_e(i, j)): what
+        kernel_dbcg_simple takes as BB.  `out` may be pinned host memory."""
+        bb = np.empty(64 * self.problem.mesh.nelem) if out is None else out
+        L.check(self.lib.vdr_get_element_matrices(self.h, _dp(bb)),
+                "vdr_get_element_matrices")
+        return bb
+
     def solve(self, b, x0=None, tol=None, itmax=1000, out=None):
         """Returns (x, iterations, relative residual, status).  With `out`
         (float64, N) the solution is written there, starting from x0 (or
