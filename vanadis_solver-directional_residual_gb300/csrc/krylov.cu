@@ -1067,6 +1067,7 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
     const double itol = std::max(inner_tol, 0.5 * tol / rel);
     if (f32v) {
       // d solves A32 d = r / ||r|| on FP32 vectors; x += ||r|| d in FP64
+      if (!(1.0 / rr[1] < INFINITY)) break;  // ||r|| at the denormal floor
       Vec32 a32 = make_vec32(h);
       k32_in<<<g, RED_THREADS, 0, s>>>(a32, r, 1.0 / rr[1], h.dinv, h.dinv32);
       count_launches(1);
