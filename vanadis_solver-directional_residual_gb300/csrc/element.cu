@@ -560,7 +560,7 @@ __global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArg
     const Df2 vzd = df_from_double_chk(vz, range_bad);
     const Df2 pd = df_from_double_chk(pdec, range_bad);
     const Df2 taud = df_from_double_chk(tau, range_bad);
-#pragma unroll 1
+#pragma unroll 2
     for (int j = 0; j < 8; j++) {
       DfAcc ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
       df_acc(ax, di11, t0[j]);
