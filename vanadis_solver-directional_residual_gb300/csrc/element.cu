@@ -355,9 +355,9 @@ __global__ void __launch_bounds__(256) elem_dr_scalars_kernel(OpArgs a,
           fabs(__ldg(a.zz + n4) - __ldg(a.zz + n0)));
       drs[p] = dr_tau_from<double>(DR_OT, h, vmag, lam);
     } else {
-      double ex = 0.0, ey = 0.0, ez = 0.0;
+      double ex = 0.0, ey = 0.0, ez = 0.0, iv = 0.0;
       if (vmag > eps) {
-        const double iv = 1.0 / vmag;
+        iv = 1.0 / vmag;
         ex = vx * iv;
         ey = vy * iv;
         ez = vz * iv;
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(256) elem_dr_scalars_kernel(OpArgs a,
       drs[E + p] = ey;
       drs[2 * E + p] = ez;
       drs[3 * E + p] = on ? vmag / (2.0 * lams) : 0.0;
-      drs[4 * E + p] = on ? 0.5 / vmag : 0.0;
+      drs[4 * E + p] = on ? 0.5 * iv : 0.0;
     }
   }
 }
