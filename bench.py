@@ -63,7 +63,7 @@ def args_parse():
     ap.add_argument("--learn-steps", type=int, default=LEARN_STEPS)
     ap.add_argument("--learn-epochs", type=int, default=1)
     ap.add_argument("--case", default=None,
-                    choices=["apply", "block_apply", "unet_train"],
+                    choices=["apply", "block_apply", "bicg", "mixed", "unet_train"],
                     help="run one small fixed workload for a profiler "
                          "capture instead of the benchmark")
     ap.add_argument("--cpu-iters", type=int, default=4,
@@ -909,8 +909,10 @@ def run_native(a):
 def run_case(a):
     """Small fixed workloads for profiler captures (not benchmarks): the
     stored double-float apply (--case apply), the K=64 block solve
-    (--case block_apply) and learned-network training steps
-    (--case unet_train), each on the --nex x --ney x --nez mesh."""
+    (--case block_apply), a BiCG solve (--case bicg, fused A/A^T apply), a
+    mixed-precision solve (--case mixed, FP32-vector inner apply) and
+    learned-network training steps (--case unet_train), each on the
+    --nex x --ney x --nez mesh."""
     import torch
     import __graft_entry__
     vdr = __graft_entry__.package()
@@ -933,6 +935,21 @@ def run_case(a):
         s.assemble_rhs_block_device(Q, B, 3.0)
         X = torch.zeros_like(B)
         s.solve_block_device(B, X, tol=TOL, inner_tol=1e-3, precision="tf32x3")
+    elif a.case == "bicg":
+        # BiCG: the fused A p / A^T p~ apply over the double-float store
+        s = vdr.Solver(prob, vdr.Options(apply_mode="stored", solver="bicg"),
+                       aH=2.0, aM=3.0 / dt)
+        b = torch.empty(prob.mesh.nnode, dtype=torch.float64, device="cuda")
+        s.assemble_rhs_device(b, 3.0, 0.0, None)
+        x = torch.zeros_like(b)
+        s.solve_device(b, x, tol=TOL, itmax=20000)
+    elif a.case == "mixed":
+        # FP64 refinement around FP32-vector inner BiCGStab (FP32 apply)
+        s = vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=2.0, aM=3.0 / dt)
+        b = torch.empty(prob.mesh.nnode, dtype=torch.float64, device="cuda")
+        s.assemble_rhs_device(b, 3.0, 0.0, None)
+        x = torch.zeros_like(b)
+        s.solve_mixed_device(b, x, tol=TOL, inner_tol=1e-5)
     elif a.case == "unet_train":
         L = vdr.learned
         run = L.TiltingRun(a.nex, a.ney, a.nez, seed=1005, courant=COURANT,
