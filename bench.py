@@ -58,6 +58,8 @@ def args_parse():
                     help="skip the many-mesh section")
     ap.add_argument("--no-dropin", action="store_true",
                     help="skip the kernel_dbcg_simple_ section")
+    ap.add_argument("--no-time-loop", action="store_true",
+                    help="skip the device time-loop section")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-preconditioner section")
     ap.add_argument("--learn-steps", type=int, default=LEARN_STEPS)
@@ -538,6 +540,35 @@ def dropin_section(vdr, s, prob, cf, rM):
                     "A p / A^T p~ apply, X download"}
 
 
+def time_loop_section(vdr, s, prob, aH, aM, cf, rM):
+    """The device time loop (vdr_time_steps) on the 256x256x128 rotation +
+    shear theta step: per step the right-hand side from T, the solve to 1e-8
+    and the mass integral, T kept on the device.  The first step of a call
+    builds the element matrices (keeping M and F = sum f_e); every later step
+    forms its right-hand side from the stored A and M.  Calls of 1 and 6
+    steps from T = 0; a later step costs (t6 - t1) / 5."""
+    import torch
+    N = prob.mesh.nnode
+    runs = {}
+    for n in (1, 6, 1, 6):
+        t = torch.zeros(N, dtype=torch.float64, device="cuda")
+        s.set_operator(aH, aM)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        masses, its, errs, st, done = s.time_steps_device(t, n, cf, rM, tol=TOL,
+                                                          itmax=20000)
+        torch.cuda.synchronize()
+        runs[n] = (time.perf_counter() - t0, [int(v) for v in its], int(st),
+                   float(max(errs)))
+    t1, t6 = runs[1][0], runs[6][0]
+    return {"steps_1_s": t1, "steps_6_s": t6, "later_step_s": (t6 - t1) / 5,
+            "iterations": runs[6][1], "status": runs[6][2],
+            "worst_rel_residual": runs[6][3],
+            "what": "vdr_time_steps from T = 0: first step = element build "
+                    "(A, M, F) + solve, later steps = RHS from two applies + "
+                    "solve; mass integral every step"}
+
+
 def learned_section(vdr, device, a):
     """The learned preconditioner on the tilting-axis transient problem
     (128x128x64, theta-step at Courant 10, rotation axis tilting 0.5 degrees
@@ -812,6 +843,7 @@ def run_native(a):
     meshes = None if a.no_meshes else batched_meshes_section(vdr, local)
     learned = None if a.no_learned else learned_section(vdr, local, a)
     dropin = None if a.no_dropin else dropin_section(vdr, s, prob, cf, rM)
+    tloop = None if a.no_time_loop else time_loop_section(vdr, s, prob, aH, aM, cf, rM)
 
     # ---- e2e through the C ABI with host buffers ----
     # The step's inputs (per-element fields) and outputs (right-hand side,
@@ -892,6 +924,7 @@ def run_native(a):
             "batched_meshes": meshes,
             "learned_preconditioner": learned,
             "dropin_bicg": dropin,
+            "time_loop": tloop,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,

@@ -192,7 +192,10 @@ int vdr_solve_mixed_device(vdr_handle *h, const double *d_b, double *d_x,
  * with A the operator set by vdr_set_operator.  d_t holds T_0 on entry and
  * T_nsteps on exit.  masses, iters, errs are host arrays of nsteps entries
  * (each may be NULL).  Stops at the first solve that does not return
- * VDR_OK and returns its status; *steps_done counts completed steps. */
+ * VDR_OK and returns its status; *steps_done counts completed steps.  With
+ * the stored operator the first step also keeps M and F = sum_e f_e, and
+ * the later steps (whose T is zero on Dirichlet nodes) form b from them as
+ * cf*F - (A T)/aH + (aM/aH + rM) M T. */
 int vdr_time_steps(vdr_handle *h, int nsteps, double cf, double rM,
                    double *d_t, double tol, int itmax, double *masses,
                    int *iters, double *errs, int *steps_done);

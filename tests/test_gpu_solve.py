@@ -249,6 +249,41 @@ def test_kat_run_device_time_loop(vdr, gpu_lib):
     assert np.all(errs <= k["tol"])
 
 
+@pytest.mark.parametrize("scatter,store", [("atomic", "df"), ("color", "df"),
+                                           ("atomic", "fp64")])
+def test_time_loop_stored_mass_matches_step_by_step(vdr, gpu_lib, scatter, store):
+    """From its second step the device time loop forms the right-hand side
+    from the stored A and M (b = cf F - (A T)/aH + (aM/aH + rM) M T); the
+    trajectory equals a step-by-step loop whose every right-hand side is a
+    full Gauss pass (vdr_assemble_rhs), to the solve tolerance."""
+    import torch
+    prob = vdr.problems.rotation_shear(12, 10, 8, seed=71)
+    prob.pdec[:] = 0.2
+    prob.robin_alpha = 0.4
+    dt = 10.0 / 12
+    aH, aM, cf, rM = 2.0, 3.0 / dt, 3.0, 3.0 / dt
+    steps, tol = 5, 1e-12
+    opts = vdr.Options(scatter=scatter, matrix_storage=store)
+    with vdr.Solver(prob, opts, aH=aH, aM=aM) as s:
+        t = torch.zeros(prob.mesh.nnode, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        masses, its, errs, st, done = s.time_steps_device(t, steps, cf, rM, tol=tol,
+                                                          itmax=5000)
+        torch.cuda.synchronize()
+        assert st == 0 and done == steps
+        t_loop = t.cpu().numpy()
+    with vdr.Solver(prob, opts, aH=aH, aM=aM) as s:
+        th = np.zeros(prob.mesh.nnode)
+        m_ref = []
+        for k in range(steps):
+            b = s.assemble_rhs(cf, rM, th)
+            th, it, err, st = s.solve(b, th, tol=tol, itmax=5000)
+            assert st == 0
+            m_ref.append(s.mass(th))
+    assert rel_l2(t_loop, th) < 1e-9
+    assert np.max(np.abs(masses - np.array(m_ref)) / np.abs(np.array(m_ref))) < 1e-9
+
+
 @pytest.mark.parametrize("restart", [1, 5, 20])
 def test_gcr_jacobi_matches_bicgstab(vdr, oracle, gpu_lib, restart):
     """Restarted GCR with Jacobi (the flexible solver of the learned path)

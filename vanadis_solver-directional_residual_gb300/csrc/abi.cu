@@ -152,6 +152,14 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
       ba.b = rhs->b;
       if ((e = cudaMemsetAsync(ba.b, 0, sizeof(double) * h.N, h.stream)))
         return cuda_fail(e, "memset rhs");
+      // time loop: keep M and F of this operator (double-float build only)
+      if (rhs->Mhi && !h.exact_build) {
+        ba.Mhi = rhs->Mhi;
+        ba.Mlo = rhs->Mlo;
+        ba.f = rhs->f;
+        if ((e = cudaMemsetAsync(ba.f, 0, sizeof(double) * h.N, h.stream)))
+          return cuda_fail(e, "memset f");
+      }
     }
     if (need_op) {
       if (stored && !df && (e = dalloc(&h.A64, (size_t)h.E * 32)))
@@ -181,7 +189,9 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
                              h.stream)) ||
         (e = cudaStreamSynchronize(h.stream)))
       return cuda_fail(e, "flag");
-    if (!bad) break;
+    // bit 3: the M store left its window (M is then not kept)
+    h.mass_valid = ba.Mhi && !(bad & 4) && !(bad & 3);
+    if (!(bad & 3)) break;
     if (bad & 2) h.exact_build = true;
     if ((bad & 1) && df) h.storage = VDR_STORE_FP64;
   }
@@ -231,6 +241,7 @@ int ensure_operator32(Handle &h) {
 
 void invalidate(Handle &h) {
   h.op64_valid = h.op32_valid = h.diag_valid = false;
+  h.mass_valid = false;
   h.aos_valid = h.phi_valid = false;
 }
 
@@ -278,6 +289,7 @@ void free_handle(Handle &h) {
   dfree(h.bk_f); dfree(h.bk_d);
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
   dfree(h.gcr_work); dfree(h.stage_d); dfree(h.drs); dfree(h.work32);
+  dfree(h.Mhi); dfree(h.Mlo); dfree(h.Fvec); dfree(h.rhs_tmp); dfree(h.massw);
   if (h.graph32) cudaGraphExecDestroy(h.graph32);
   if (h.gcr_graph) cudaGraphExecDestroy(h.gcr_graph);
   dfree(h.seg_d); dfree(h.seg_i); dfree(h.seg_ticket); dfree(h.seg_of_elem);
@@ -948,16 +960,38 @@ int vdr_time_steps(vdr_handle *H, int nsteps, double cf, double rM,
   }
   const int method = h.opt.solver == VDR_SOLVER_BICG ? VDR_SOLVER_BICG
                                                      : VDR_SOLVER_BICGSTAB;
+  // With the stored operator the first step keeps M and F; every later step
+  // (whose T_old is a solve's output, zero on Dirichlet nodes) forms
+  // b = cf F - (H - rM M) T_old from two applies instead of a Gauss pass.
+  const bool keep_mass = h.apply_mode == VDR_APPLY_STORED && h.aH != 0.0;
+  if (keep_mass &&
+      ((e = dalloc(&h.Mhi, (size_t)h.E * 16)) || (e = dalloc(&h.Mlo, (size_t)h.E * 16)) ||
+       (e = dalloc(&h.Fvec, h.N)) || (e = dalloc(&h.rhs_tmp, 2 * (size_t)h.N)))) {
+    if (dmass) cudaFree(dmass);
+    return cuda_fail(e, "vdr_time_steps: alloc");
+  }
   int status = VDR_OK, done = 0;
   for (int k = 0; k < nsteps; k++) {
-    BuildArgs rhs;
-    rhs.cf = cf;
-    rhs.rM = rM;
-    rhs.told = t;
-    rhs.b = b;
-    if ((st = build_operator(h, &rhs))) {
-      status = st;
-      break;
+    if (k > 0 && keep_mass && h.mass_valid && h.op64_valid) {
+      if ((e = launch_rhs_from_mass(h, cf, rM, t, b, h.stream))) {
+        status = cuda_fail(e, "rhs");
+        break;
+      }
+    } else {
+      BuildArgs rhs;
+      rhs.cf = cf;
+      rhs.rM = rM;
+      rhs.told = t;
+      rhs.b = b;
+      if (keep_mass) {
+        rhs.Mhi = h.Mhi;
+        rhs.Mlo = h.Mlo;
+        rhs.f = h.Fvec;
+      }
+      if ((st = build_operator(h, &rhs))) {
+        status = st;
+        break;
+      }
     }
     int it = 0;
     double err = 0.0;

@@ -589,6 +589,48 @@ cudaError_t launch_apply_both(const Handle &h, const double *x1, double *y1,
   return cudaGetLastError();
 }
 
+namespace {
+// b = cf F - a1 y1 + a2 y2 (y1 = A T, y2 = M T; F, y1, y2 are zero on
+// Dirichlet nodes, so b is too).
+__global__ void rhs_combine_kernel(const double *__restrict__ F,
+                                   const double *__restrict__ y1,
+                                   const double *__restrict__ y2, double cf,
+                                   double a1, double a2, double *__restrict__ b,
+                                   long N) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (long)gridDim.x * blockDim.x)
+    b[i] = cf * F[i] - a1 * y1[i] + a2 * y2[i];
+}
+}  // namespace
+
+cudaError_t launch_rhs_from_mass(Handle &h, double cf, double rM, const double *t,
+                                 double *b, cudaStream_t s) {
+  // H - rM M = A/aH - (aM/aH + rM) M
+  double *y1 = h.rhs_tmp, *y2 = h.rhs_tmp + h.N;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(h.rhs_tmp, 0, sizeof(double) * 2 * (size_t)h.N, s))) return e;
+  if ((e = launch_apply(h, false, t, y1, nullptr, nullptr, s))) return e;
+  const bool color = h.scatter == VDR_SCATTER_COLOR;
+  const int nranges = color ? h.ncolors : 1;
+  for (int r = 0; r < nranges; r++) {
+    const int p0 = color ? h.color_off[r] : 0;
+    const int p1 = color ? h.color_off[r + 1] : h.E;
+    if (p1 <= p0) continue;
+    const int grid = grid_for(p1 - p0, 256, 8);
+    if (color)
+      stored_apply_df<false, false><<<grid, 256, 0, s>>>(h.Mhi, h.Mlo, h.conn, h.E, p0, p1, t,
+                                                         y2, nullptr, nullptr, ElemGate{});
+    else
+      stored_apply_df<false, true><<<grid, 256, 0, s>>>(h.Mhi, h.Mlo, h.conn, h.E, p0, p1, t,
+                                                        y2, nullptr, nullptr, ElemGate{});
+    count_launches(1);
+  }
+  rhs_combine_kernel<<<grid_for(h.N, 256, 8), 256, 0, s>>>(
+      h.Fvec, y1, y2, cf, 1.0 / h.aH, h.aM / h.aH + rM, b, h.N);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 int apply_launches(const Handle &h) {
   if (h.apply_mode == VDR_APPLY_MATRIX_FREE || h.scatter != VDR_SCATTER_COLOR)
     return 1;

@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArg
     sm.rel[le][3 * lane8 + 1] = df_from_double_chk(yk - y0, range_bad);
     sm.rel[le][3 * lane8 + 2] = df_from_double_chk(zk - z0, range_bad);
     int tshift = 0;
-    if constexpr (SPLIT) {
+    if (SPLIT && ba.told) {
       const double tk = __ldg(ba.told + nk);
       int em = df_exp(tk);
       em = max(em, __shfl_xor_sync(FULL, em, 1));
@@ -708,11 +708,36 @@ __global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArg
       }
       if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, row[i]);
     }
+    if constexpr (SPLIT) {
+      if (ba.Mhi) {
+        // M row as its own double-float store (window as for A: bit 3)
+        Df2 rowm[8];
+        bool badm = false;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          rowm[j] = df_norm(accM[j % (SPLIT ? 8 : 1)]);
+          const unsigned eb = (__float_as_uint(rowm[j].h) >> 23) & 0xffu;
+          if (rowm[j].h != 0.0f && (eb < 27u || eb > 247u)) badm = true;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          ba.Mhi[(size_t)(2 * i + h) * E + p] =
+              make_float4(rowm[4 * h].h, rowm[4 * h + 1].h, rowm[4 * h + 2].h, rowm[4 * h + 3].h);
+          ba.Mlo[(size_t)(2 * i + h) * E + p] =
+              make_float4(rowm[4 * h].l, rowm[4 * h + 1].l, rowm[4 * h + 2].l, rowm[4 * h + 3].l);
+        }
+        if (badm) atomicOr(ba.bad, 4);
+      }
+    }
     if (ba.phi) ba.phi[(size_t)i * E + p] = df_to_double(fw.s, fw.c) / vol;
+    if (ba.f && ci >= 0) {
+      const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
+      atomicAdd(ba.f + ci, (qe / vol) * df_to_double(fw.s, fw.c));
+    }
     if (ba.b && ci >= 0) {
       const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
       double val = ba.cf * ((qe / vol) * df_to_double(fw.s, fw.c));
-      if constexpr (SPLIT) {
+      if (SPLIT && ba.told) {
         // (H - rM M) T_old in double-float on the scaled T_old, scaled back
         DfAcc ft{0.0f, 0.0f};
 #pragma unroll
@@ -816,6 +841,82 @@ __global__ void __launch_bounds__(256) mf_apply_kernel(
   }
 }
 
+// integrate_mass_hex8's per-element weights w_s = sum_q N_s(q) detJ_q
+// (2x2x2 Gauss, abscissa 1/sqrt(3), FP64), stored [8][E]: the geometry of a
+// handle is fixed, so they are formed once and every later integral is
+// sum_e sum_s w_s c_s (mass_dot_kernel).
+__global__ void __launch_bounds__(256) mass_weights_kernel(
+    const int *__restrict__ conn, int E, const double *__restrict__ xx,
+    const double *__restrict__ yy, const double *__restrict__ zz,
+    double *__restrict__ w) {
+  const double g = 1.0 / sqrt(3.0);
+  for (long p = (long)blockIdx.x * blockDim.x + threadIdx.x; p < E;
+       p += (long)gridDim.x * blockDim.x) {
+    double xe[8], ye[8], ze[8], ws[8];
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      const int n = __ldg(conn + (size_t)s * E + p) & NODE_BITS;
+      xe[s] = __ldg(xx + n);
+      ye[s] = __ldg(yy + n);
+      ze[s] = __ldg(zz + n);
+      ws[s] = 0.0;
+    }
+#pragma unroll 1
+    for (int q = 0; q < 8; q++) {
+      const double xi = ((q >> 2) & 1) ? g : -g;
+      const double eta = ((q >> 1) & 1) ? g : -g;
+      const double zeta = (q & 1) ? g : -g;
+      double n[8], d0[8], d1[8], d2[8];
+      shape_at<double>(xi, eta, zeta, n, d0, d1, d2);
+      double j11 = 0, j12 = 0, j13 = 0, j21 = 0, j22 = 0, j23 = 0, j31 = 0,
+             j32 = 0, j33 = 0;
+#pragma unroll
+      for (int s = 0; s < 8; s++) {
+        j11 += xe[s] * d0[s];
+        j12 += xe[s] * d1[s];
+        j13 += xe[s] * d2[s];
+        j21 += ye[s] * d0[s];
+        j22 += ye[s] * d1[s];
+        j23 += ye[s] * d2[s];
+        j31 += ze[s] * d0[s];
+        j32 += ze[s] * d1[s];
+        j33 += ze[s] * d2[s];
+      }
+      const double detj = j11 * (j22 * j33 - j23 * j32) -
+                          j12 * (j21 * j33 - j23 * j31) +
+                          j13 * (j21 * j32 - j22 * j31);
+#pragma unroll
+      for (int s = 0; s < 8; s++) ws[s] += n[s] * detj;
+    }
+#pragma unroll
+    for (int s = 0; s < 8; s++) w[(size_t)s * E + p] = ws[s];
+  }
+}
+
+// sum_e sum_s w_s c_s: one thread per element, block partials summed in
+// fixed order by the launcher's second kernel (deterministic).
+__global__ void __launch_bounds__(256) mass_dot_kernel(
+    const int *__restrict__ conn, int E, const double *__restrict__ w,
+    const double *__restrict__ c, double *__restrict__ partials) {
+  double acc = 0.0;
+  for (long p = (long)blockIdx.x * blockDim.x + threadIdx.x; p < E;
+       p += (long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      const int n = __ldg(conn + (size_t)s * E + p) & NODE_BITS;
+      acc += __ldg(w + (size_t)s * E + p) * __ldg(c + n);
+    }
+  }
+  __shared__ double sm[256];
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = 128; off > 0; off >>= 1) {
+    if (threadIdx.x < off) sm[threadIdx.x] += sm[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = sm[0];
+}
+
 // integrate_mass_hex8: one thread per element, 2x2x2 Gauss with
 // abscissa 1/sqrt(3); block partials summed in fixed order by the host
 // launcher's second kernel.
@@ -908,7 +1009,7 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
     }
     const int g2 = (int)std::min<long>(((long)a.E + 255) / 256, (long)sm_count() * 8);
     elem_dr_scalars_kernel<<<g2, 256, 0, s>>>(a, ba.drs);
-    if (ba.told)
+    if (ba.told || ba.Mhi)  // H and M apart
       elem_build_df_kernel<true><<<grid, 64, 0, s>>>(a, ba);
     else
       elem_build_df_kernel<false><<<grid, 64, 0, s>>>(a, ba);
@@ -939,10 +1040,24 @@ cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
   return cudaGetLastError();
 }
 
-cudaError_t launch_mass(const Handle &h, const double *c, double *partials,
+cudaError_t launch_mass(Handle &h, const double *c, double *partials,
                         double *out, cudaStream_t s) {
   const int grid = std::max(1, std::min((h.E + 255) / 256, sm_count() * 4));
-  mass_kernel<<<grid, 256, 0, s>>>(h.conn, h.E, h.xx, h.yy, h.zz, c, partials);
+  if (!h.massw) {  // per-element weights, once per handle (fixed geometry)
+    cudaError_t e = cudaMalloc(&h.massw, sizeof(double) * 8 * (size_t)std::max(h.E, 1));
+    if (e) {
+      h.massw = nullptr;
+      // no room for the weights: integrate directly
+      mass_kernel<<<grid, 256, 0, s>>>(h.conn, h.E, h.xx, h.yy, h.zz, c, partials);
+      sum_partials_kernel<<<1, 256, 0, s>>>(partials, grid, out);
+      count_launches(2);
+      cudaGetLastError();  // the allocation failure is not an error here
+      return cudaGetLastError();
+    }
+    mass_weights_kernel<<<grid, 256, 0, s>>>(h.conn, h.E, h.xx, h.yy, h.zz, h.massw);
+    count_launches(1);
+  }
+  mass_dot_kernel<<<grid, 256, 0, s>>>(h.conn, h.E, h.massw, c, partials);
   sum_partials_kernel<<<1, 256, 0, s>>>(partials, grid, out);
   count_launches(2);
   return cudaGetLastError();

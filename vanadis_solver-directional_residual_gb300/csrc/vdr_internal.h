@@ -140,6 +140,13 @@ struct Handle {
   size_t h_stage_bytes = 0;
   double *stage_d = nullptr;  // [3E] device staging of uploaded fields
   double *drs = nullptr;      // [5E] per-element DR scalars of the build
+  // time loop: the mass matrix M (double-float store) and the source vector
+  // F = sum_e f_e of the current fields, so that later steps form their
+  // right-hand side from two applies; rhs_tmp holds A T and M T
+  float4 *Mhi = nullptr, *Mlo = nullptr;
+  double *Fvec = nullptr, *rhs_tmp = nullptr;
+  bool mass_valid = false;
+  double *massw = nullptr;  // [8][E] integrate_mass weights (fixed geometry)
 
   vdr_solve_stats last{};
 
@@ -204,6 +211,9 @@ struct BuildArgs {
   bool exact_fp64 = false;  // H/M rows accumulated in FP64, not double-float
   double *phi = nullptr;     // [8][E] (1/vol) int W_i dOmega, per element
   double *drs = nullptr;     // [5][E] per-element DR scalars (double-float build)
+  // time loop: M kept as its own double-float store, and f = sum_e f_e
+  float4 *Mhi = nullptr, *Mlo = nullptr;
+  double *f = nullptr;
 };
 
 // ---- launchers (element.cu) ----
@@ -212,13 +222,17 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
 cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
                             const double *x, double *y, const int *skip,
                             const int *skip2, cudaStream_t s);
-cudaError_t launch_mass(const Handle &h, const double *c, double *partials,
+cudaError_t launch_mass(Handle &h, const double *c, double *partials,
                         double *out, cudaStream_t s);
 
 // ---- launchers (apply.cu) ----
 cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
                                 const double *x, double *y, const int *skip,
                                 const int *skip2, cudaStream_t s);
+// Time loop: b = cf F - (H - rM M) t from the stored A and M (t zero on
+// Dirichlet nodes), as b = cf F - (A t)/aH + (aM/aH + rM) M t.
+cudaError_t launch_rhs_from_mass(Handle &h, double cf, double rM, const double *t,
+                                 double *b, cudaStream_t s);
 // y1 += A x1 and y2 += A^T x2 in one pass (BiCG), when can_apply_both.
 bool can_apply_both(const Handle &h);
 cudaError_t launch_apply_both(const Handle &h, const double *x1, double *y1,
