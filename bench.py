@@ -561,12 +561,33 @@ def time_loop_section(vdr, s, prob, aH, aM, cf, rM):
         runs[n] = (time.perf_counter() - t0, [int(v) for v in its], int(st),
                    float(max(errs)))
     t1, t6 = runs[1][0], runs[6][0]
-    return {"steps_1_s": t1, "steps_6_s": t6, "later_step_s": (t6 - t1) / 5,
-            "iterations": runs[6][1], "status": runs[6][2],
-            "worst_rel_residual": runs[6][3],
-            "what": "vdr_time_steps from T = 0: first step = element build "
-                    "(A, M, F) + solve, later steps = RHS from two applies + "
-                    "solve; mass integral every step"}
+    out = {"steps_1_s": t1, "steps_6_s": t6, "later_step_s": (t6 - t1) / 5,
+           "iterations": runs[6][1], "status": runs[6][2],
+           "worst_rel_residual": runs[6][3],
+           "what": "vdr_time_steps from T = 0: first step = element build "
+                   "(A, M, F) + solve, later steps = RHS from two applies + "
+                   "solve; mass integral every step"}
+    # the same loop with Options(precision="mixed"): FP64 refinement around
+    # FP32-operator inner solves, same FP64 tolerance, on its own handle
+    sm = vdr.Solver(prob, vdr.Options(apply_mode="stored", precision="mixed"),
+                    aH=aH, aM=aM)
+    mruns = {}
+    for n in (1, 6, 1, 6):
+        t = torch.zeros(N, dtype=torch.float64, device="cuda")
+        sm.set_operator(aH, aM)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        masses, its, errs, st, done = sm.time_steps_device(t, n, cf, rM, tol=TOL,
+                                                           itmax=20000)
+        torch.cuda.synchronize()
+        mruns[n] = (time.perf_counter() - t0, [int(v) for v in its], int(st),
+                    float(max(errs)))
+    sm.close()
+    out["mixed"] = {"steps_1_s": mruns[1][0], "steps_6_s": mruns[6][0],
+                    "later_step_s": (mruns[6][0] - mruns[1][0]) / 5,
+                    "inner_iterations": mruns[6][1], "status": mruns[6][2],
+                    "worst_fp64_rel_residual": mruns[6][3]}
+    return out
 
 
 def learned_section(vdr, device, a):

@@ -80,6 +80,15 @@ extern "C" {
 #define VDR_SOLVER_BICGSTAB 0 /* Jacobi right-preconditioned BiCGStab */
 #define VDR_SOLVER_BICG 1     /* Jacobi BiCG, the reference's dbcg_simple */
 
+/* How vdr_solve, vdr_solve_device and vdr_time_steps reach their FP64
+ * tolerance: VDR_PRECISION_FP64 -- Krylov in FP64 on the FP64-accurate
+ * operator; VDR_PRECISION_MIXED -- FP64 iterative refinement around inner
+ * BiCGStab solves with the FP32 operator (as vdr_solve_mixed_device with
+ * inner_tol 1e-5): the same FP64 true-residual criterion, fewer bytes per
+ * iteration. */
+#define VDR_PRECISION_FP64 0
+#define VDR_PRECISION_MIXED 1
+
 typedef struct vdr_options {
   int dr_variant;      /* VDR_DR_* (default VDR_DR_VF) */
   int scatter;         /* VDR_SCATTER_* */
@@ -88,7 +97,8 @@ typedef struct vdr_options {
   int iters_per_graph; /* iterations per CUDA-graph launch (0 -> 8) */
   int device;          /* CUDA device ordinal */
   int matrix_storage;  /* VDR_STORE_* */
-  int reserved[9];
+  int precision;       /* VDR_PRECISION_* (default FP64) */
+  int reserved[8];
 } vdr_options;
 
 typedef struct vdr_handle vdr_handle;

@@ -86,3 +86,36 @@ def test_mixed_refinement_reaches_fp64_tolerance(vdr, gpu_lib, torch, solver,
         # error against the FP64 solution (itself within 1e-12 of the oracle
         # system): bounded by the residual times the conditioning seen here
         assert rel_l2(xm.cpu().numpy(), x64.cpu().numpy()) < 1e-8
+
+
+def test_precision_option_solve_and_time_loop(vdr, gpu_lib, torch):
+    """Options(precision="mixed") makes vdr_solve and vdr_time_steps run the
+    FP64 refinement around FP32 inner solves: the same FP64 true-residual
+    criterion, the same trajectory as the FP64 path to the solve
+    tolerance."""
+    prob = vdr.problems.rotation_shear(24, 20, 16, seed=35)
+    dt = 10.0 / 24
+    aH, aM, cf, rM = 2.0, 3.0 / dt, 3.0, 3.0 / dt
+    tol = 1e-11
+    out = {}
+    for precision in ("fp64", "mixed"):
+        opts = vdr.Options(precision=precision)
+        with vdr.Solver(prob, opts, aH=aH, aM=aM) as s:
+            b = s.assemble_rhs(cf, 0.0, None)
+            x, it, err, st = s.solve(b, tol=tol, itmax=5000)
+            assert st == 0 and err <= tol, (precision, it, err)
+            bd = torch.as_tensor(b, device="cuda")
+            xd = torch.as_tensor(x, device="cuda")
+            torch.cuda.synchronize()
+            assert s.true_residual_device(bd, xd) <= 1.5 * tol
+            t = torch.zeros(prob.mesh.nnode, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            masses, its, errs, st, done = s.time_steps_device(t, 4, cf, rM, tol=tol,
+                                                              itmax=5000)
+            torch.cuda.synchronize()
+            assert st == 0 and done == 4 and np.all(errs <= tol), (precision, errs)
+            out[precision] = (x, t.cpu().numpy(), masses)
+    assert rel_l2(out["mixed"][0], out["fp64"][0]) < 1e-8
+    assert rel_l2(out["mixed"][1], out["fp64"][1]) < 1e-8
+    assert np.max(np.abs(out["mixed"][2] - out["fp64"][2]) /
+                  np.abs(out["fp64"][2])) < 1e-8

@@ -20,14 +20,15 @@ SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOR = 0, 1, 2
 APPLY_AUTO, APPLY_STORED, APPLY_MATRIX_FREE = 0, 1, 2
 SOLVER_BICGSTAB, SOLVER_BICG = 0, 1
 STORE_AUTO, STORE_FP64, STORE_DF = 0, 1, 2
+PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 
 class VdrOptions(ctypes.Structure):
     _fields_ = [("dr_variant", ctypes.c_int), ("scatter", ctypes.c_int),
                 ("apply_mode", ctypes.c_int), ("solver", ctypes.c_int),
                 ("iters_per_graph", ctypes.c_int), ("device", ctypes.c_int),
-                ("matrix_storage", ctypes.c_int),
-                ("reserved", ctypes.c_int * 9)]
+                ("matrix_storage", ctypes.c_int), ("precision", ctypes.c_int),
+                ("reserved", ctypes.c_int * 8)]
 
 
 class VdrSolveStats(ctypes.Structure):

@@ -239,6 +239,22 @@ int ensure_operator32(Handle &h) {
   return VDR_OK;
 }
 
+// The solve of vdr_solve, vdr_solve_device and vdr_time_steps: FP64
+// Krylov, or (VDR_PRECISION_MIXED) FP64 refinement around FP32-operator
+// inner solves to the same FP64 tolerance; *iter counts inner iterations.
+int solve_by_option(Handle &h, int method, const double *b, double *x,
+                    double tol, int itmax, int *iter, double *err) {
+  if (h.opt.precision != VDR_PRECISION_MIXED)
+    return solve_device(h, method, b, x, tol, itmax, iter, err);
+  int st = ensure_operator32(h);
+  if (st) return st;
+  MixedStats ms;
+  st = solve_mixed_device(h, method, b, x, tol, 1e-5, 20, itmax, &ms);
+  if (iter) *iter = ms.inner;
+  if (err) *err = ms.err;
+  return st;
+}
+
 void invalidate(Handle &h) {
   h.op64_valid = h.op32_valid = h.diag_valid = false;
   h.mass_valid = false;
@@ -390,6 +406,10 @@ int vdr_create(vdr_handle **out, int nnode, int nelem, const double *xx,
   if (opt) o = *opt; else vdr_default_options(&o);
   if (o.dr_variant < VDR_DR_OT || o.dr_variant > VDR_DR_VF) {
     set_error("vdr_create: unknown dr_variant");
+    return VDR_BAD_ARGUMENT;
+  }
+  if (o.precision != VDR_PRECISION_FP64 && o.precision != VDR_PRECISION_MIXED) {
+    set_error("vdr_create: unknown precision");
     return VDR_BAD_ARGUMENT;
   }
   vdr_handle *H = new vdr_handle();
@@ -739,7 +759,7 @@ int vdr_solve_device(vdr_handle *H, const double *b, double *x, double tol,
   if (e) return cuda_fail(e, "rhs copy");
   const int method = h.opt.solver == VDR_SOLVER_BICG ? VDR_SOLVER_BICG
                                                      : VDR_SOLVER_BICGSTAB;
-  return solve_device(h, method, bm, x, tol, itmax, iter, err);
+  return solve_by_option(h, method, bm, x, tol, itmax, iter, err);
 }
 
 int vdr_solve_mixed_device(vdr_handle *H, const double *b, double *x,
@@ -995,7 +1015,7 @@ int vdr_time_steps(vdr_handle *H, int nsteps, double cf, double rM,
     }
     int it = 0;
     double err = 0.0;
-    st = solve_device(h, method, b, t, tol, itmax, &it, &err);
+    st = solve_by_option(h, method, b, t, tol, itmax, &it, &err);
     if (iters) iters[k] = it;
     if (errs) errs[k] = err;
     if (dmass && (e = launch_mass(h, t, H->mass_partials, dmass + k, h.stream))) {

@@ -27,11 +27,13 @@ module vdr_iso_c
   integer(c_int), parameter :: VDR_SOLVER_BICGSTAB = 0, VDR_SOLVER_BICG = 1
   integer(c_int), parameter :: VDR_STORE_AUTO = 0, VDR_STORE_FP64 = 1, &
        VDR_STORE_DF = 2
+  integer(c_int), parameter :: VDR_PRECISION_FP64 = 0, VDR_PRECISION_MIXED = 1
 
   type, bind(c) :: vdr_options
      integer(c_int) :: dr_variant, scatter, apply_mode, solver
      integer(c_int) :: iters_per_graph, device, matrix_storage
-     integer(c_int) :: reserved(9)
+     integer(c_int) :: precision
+     integer(c_int) :: reserved(8)
   end type vdr_options
 
   interface

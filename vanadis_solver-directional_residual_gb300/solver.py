@@ -98,6 +98,7 @@ class Options:
     iters_per_graph: int = 8
     device: int = 0
     matrix_storage: str = "auto"
+    precision: str = "fp64"      # "fp64" or "mixed" (FP64 refinement, FP32 inner)
 
     def to_c(self, default_variant: int) -> L.VdrOptions:
         o = L.VdrOptions()
@@ -112,6 +113,7 @@ class Options:
         o.iters_per_graph = int(self.iters_per_graph)
         o.device = int(self.device)
         o.matrix_storage = _STORE[self.matrix_storage]
+        o.precision = {"fp64": L.PRECISION_FP64, "mixed": L.PRECISION_MIXED}[self.precision]
         return o
 
 
