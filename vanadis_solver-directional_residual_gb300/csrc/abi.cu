@@ -1169,7 +1169,7 @@ int legacy_prepare(Legacy &L, int N, int E) {
       h.ev[k] = nullptr;
     }
     const size_t cN = std::max(N, L.capN), cE = std::max(E, L.capE);
-    if ((e = dalloc(&h.A64, cE * 32)) || (e = dalloc(&h.Ahi, cE * 16)) ||
+    if ((e = dalloc(&h.Ahi, cE * 16)) ||
         (e = dalloc(&h.Alo, cE * 16)) || (e = dalloc(&h.conn, cE * 8)) ||
         (e = dalloc(&h.diag, cN)) || (e = dalloc(&h.dinv, cN)) ||
         (e = dalloc(&h.mask, cN)) ||
@@ -1241,9 +1241,12 @@ void kernel_dbcg_simple_(int *Np, double *B, double *X, double *TOLp,
         (e = cudaMemcpyAsync(&bad, L.bad, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
       break;
-    // BB entries outside the double-float window: the FP64 store
+    // BB entries outside the double-float window: the FP64 store (allocated
+    // on first need, at the buffers' capacity)
     h.storage = (bad & 2) ? VDR_STORE_FP64 : VDR_STORE_DF;
-    if ((bad & 2) && (e = launch_legacy_bb(L.bb, (int)E, h.A64, s))) break;
+    if ((bad & 2) && ((e = dalloc(&h.A64, (size_t)L.capE * 32)) ||
+                      (e = launch_legacy_bb(L.bb, (int)E, h.A64, s))))
+      break;
   } while (0);
   if (e) {
     cuda_fail(e, "kernel_dbcg_simple_: upload");
