@@ -245,8 +245,9 @@ int vdr_apply_block_device(vdr_handle *h, int K, const void *d_X, void *d_Y,
 /* Solves A X = B for K columns (K = 16, 32 or 64): FP64 refinement per
  * column (residual with the FP64-accurate operator, FP64 update) around K
  * simultaneous FP32 Jacobi-BiCGStab inner solves with the tensor-core apply
- * (precision VDR_BLOCK_TF32 or VDR_BLOCK_TF32X3), each to inner_tol
- * relative to its column's residual; columns already at tol sit out.
+ * (precision VDR_BLOCK_TF32 or VDR_BLOCK_TF32X3), column k to
+ * max(inner_tol, 0.5 tol / err_k) relative to its residual (err_k its FP64
+ * relative residual); columns already at tol sit out.
  * d_X holds the initial guess.  Returns VDR_OK when every column's FP64
  * relative residual is <= tol.  errs: K host doubles (final per-column FP64
  * residuals) or NULL.  No counterpart in the reference, which solves one

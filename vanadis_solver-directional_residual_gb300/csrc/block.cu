@@ -548,6 +548,7 @@ struct BState {
 // per-column arrays, each of length K (kept in one device buffer)
 struct BCols {
   double *bnrm2, *err, *rho, *rho_old, *alpha, *omega, *snrm;
+  double *tol;  // the column's inner tolerance
   int *active, *sconv, *status;
 };
 
@@ -693,7 +694,7 @@ __global__ void __launch_bounds__(BT, 2) bb_start(BVec a) {
     a.c.sconv[k] = 0;
     const double err = bb > 0.0 ? sqrt(rr / bb) : 0.0;
     a.c.err[k] = err;
-    a.c.active[k] = (bb > 0.0 && err > a.st->tol &&
+    a.c.active[k] = (bb > 0.0 && err > a.c.tol[k] &&
                      !(a.outer_err && a.outer_err[k] <= a.outer_tol)) ? 1 : 0;
     a.c.status[k] = a.c.active[k] ? VDR_NOT_CONVERGED : VDR_OK;
   }
@@ -804,7 +805,7 @@ __global__ void __launch_bounds__(BT, 2) bb_s(BVec a) {
   if (col_grid_sum<1>(v, a, out)) {
     const double sn = a.c.bnrm2[k] > 0.0 ? sqrt(out[k] / a.c.bnrm2[k]) : 0.0;
     a.c.snrm[k] = sn;
-    a.c.sconv[k] = (a.c.active[k] && sn <= a.st->tol) ? 1 : 0;
+    a.c.sconv[k] = (a.c.active[k] && sn <= a.c.tol[k]) ? 1 : 0;
   }
 }
 
@@ -893,7 +894,7 @@ __global__ void __launch_bounds__(BT, 2) bb_xr(BVec a) {
       if (!(err == err)) {
         a.c.active[k] = 0;
         a.c.status[k] = VDR_BREAKDOWN;
-      } else if (err <= a.st->tol || sc) {
+      } else if (err <= a.c.tol[k] || sc) {
         a.c.active[k] = 0;
         a.c.status[k] = VDR_OK;
       } else if (out[a.K + k] == 0.0 || om == 0.f) {
@@ -1175,6 +1176,7 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
   double *mx = colsd + 8 * 64;      // 2 x 64
   double *scale = colsd + 10 * 64;
   int *colsi = reinterpret_cast<int *>(colsd + 11 * 64);  // 3 x 64 ints
+  a.c.tol = colsd + 13 * 64;
   a.c.active = colsi;
   a.c.sconv = colsi + 64;
   a.c.status = colsi + 128;
@@ -1233,7 +1235,7 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
   init.tol = inner_tol;
   init.itmax = inner_itmax;
   int total_inner = 0, outer = 0;
-  std::vector<double> herr(K, 0.0);
+  std::vector<double> herr(K, 0.0), htol(K, inner_tol);
   int status = VDR_NOT_CONVERGED;
   for (outer = 0;; outer++) {
     // FP64 residual of every column, its scale and relative norm
@@ -1263,8 +1265,14 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
       break;
     }
     if (outer >= max_outer) break;
-    // K simultaneous FP32 inner solves of A D = R / scale, D = 0
-    if ((e = cudaMemcpyAsync(st, &init, sizeof(BState), cudaMemcpyHostToDevice, s)) ||
+    // K simultaneous FP32 inner solves of A D = R / scale, D = 0; column k
+    // is solved to max(inner_tol, 0.5 tol / err_k): no further than its
+    // outer residual needs to reach tol
+    for (int k = 0; k < K; k++)
+      htol[k] = herr[k] > 0.0 ? std::max(inner_tol, 0.5 * tol / herr[k]) : inner_tol;
+    if ((e = cudaMemcpyAsync(a.c.tol, htol.data(), sizeof(double) * K,
+                             cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(st, &init, sizeof(BState), cudaMemcpyHostToDevice, s)) ||
         (e = cudaMemsetAsync(a.x, 0, sizeof(float) * n, s)) ||
         (e = cudaMemsetAsync(a.r, 0, sizeof(float) * n, s)))
       return cuda_fail(e, "inner reset");
