@@ -41,7 +41,7 @@ COURANT = 10.0
 TOL = 1e-8
 
 
-def args_parse():
+def args_parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -70,7 +70,7 @@ def args_parse():
                          "capture instead of the benchmark")
     ap.add_argument("--cpu-iters", type=int, default=4,
                     help="BiCGStab iterations timed in the CPU sample")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_info():
@@ -78,6 +78,17 @@ def dist_info():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def reduce_max_over_ranks(value, device):
+    """The largest of one float per rank (every rank gets it): the step time
+    of a replica run is the slowest rank's.  NCCL on the GPUs, gloo in the
+    CPU tests."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def workload_config(a, prob):
@@ -739,9 +750,7 @@ def run_native(a):
     launches = vdr.kernel_launch_count() - launches0
     clk = clocks.stop()
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = reduce_max_over_ranks(ms, "cuda")
     rel_true = s.true_residual_device(b, x)
     stats = s.stats()
 
