@@ -231,6 +231,11 @@ int vdr_time_steps(vdr_handle *h, int nsteps, double cf, double rM,
 #define VDR_BLOCK_APPLY_BULK 0
 #define VDR_BLOCK_APPLY_LSU 1
 int vdr_set_block_apply(vdr_handle *h, int variant);
+/* Diagnostic of the bounded device wait used by VDR_BLOCK_APPLY_BULK: one
+ * warp waits on an mbarrier that nothing completes, with a ~1 ms budget;
+ * the wait gives up, flags it and returns.  Returns VDR_TIMEOUT when that
+ * path works (the handle stays usable). */
+int vdr_diag_wait_timeout(vdr_handle *h);
 
 /* B[n*K + k] = cf * f(Q_k): the right-hand sides of K source fields at once.
  * d_Q is K x E (row k = per-element source of column k, kg/s, the caller's

@@ -105,6 +105,29 @@ def test_block_apply_tensor_core(vdr, oracle, gpu_lib, case, K, precision,
     assert np.all(Y[prob.bc == 1] == 0.0)
 
 
+def test_bounded_wait_times_out_and_recovers(vdr, oracle, gpu_lib, case):
+    """The bulk-copy block apply's device waits are bounded: a wait that
+    nothing completes gives up after its budget, the flag reaches the host
+    as VDR_TIMEOUT, and the handle keeps working (a bulk-copy block apply
+    afterwards matches the oracle)."""
+    import importlib
+    import torch
+    L = importlib.import_module(vdr.__name__ + "._lib")
+    prob, aH, aM, bb = case
+    N = prob.mesh.nnode
+    X = np.random.default_rng(9).standard_normal((N, 16)).astype(np.float32)
+    with vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=aH, aM=aM) as s:
+        assert s.lib.vdr_diag_wait_timeout(s.h) == L.TIMEOUT
+        s.set_block_apply("bulk")
+        Xd = to_dev(X, torch.float32)
+        Yd = torch.empty_like(Xd)
+        s.apply_block_device(Xd, Yd, "tf32x3")
+        torch.cuda.synchronize()
+        Y = Yd.cpu().numpy().astype(np.float64)
+    yref, _ = oracle.matvec0(prob.mesh.iss, bb, prob.bc, X[:, 0].astype(np.float64))
+    assert rel_l2(Y[:, 0], yref) < TF32_TOL["tf32x3"]
+
+
 def test_split_tf32_beats_tf32(vdr, oracle, gpu_lib, case):
     import torch
     prob, aH, aM, bb = case

@@ -870,6 +870,12 @@ int vdr_set_mixed_operator(vdr_handle *H, int mode) {
   return VDR_OK;
 }
 
+int vdr_diag_wait_timeout(vdr_handle *H) {
+  int st = check_handle(H);
+  if (st) return st;
+  return diag_wait_timeout(H->h);
+}
+
 int vdr_set_block_apply(vdr_handle *H, int variant) {
   int st = check_handle(H);
   if (st) return st;

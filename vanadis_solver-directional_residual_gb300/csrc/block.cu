@@ -228,13 +228,25 @@ __device__ __forceinline__ bool mbar_try(unsigned a, unsigned parity) {
       : "memory");
   return d != 0u;
 }
-// Warp-uniform bounded wait; false when the budget ran out.
-__device__ __forceinline__ bool mbar_wait(unsigned a, unsigned parity) {
+// Warp-uniform bounded wait; false when the budget (clock cycles) ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned a, unsigned parity,
+                                          long long budget = TMA_WAIT_CYCLES) {
   const long long t0 = clock64();
   while (!__all_sync(FULL, mbar_try(a, parity))) {
-    if (__any_sync(FULL, clock64() - t0 > TMA_WAIT_CYCLES)) return false;
+    if (__any_sync(FULL, clock64() - t0 > budget)) return false;
   }
   return true;
+}
+
+// The bounded wait's failure path on its own: one warp waits, with a short
+// budget, on an mbarrier that nothing arrives at (no copy is issued, so
+// nothing is in flight), sets *err when the budget runs out and returns.
+__global__ void __launch_bounds__(32) wait_timeout_kernel(int *err, long long budget) {
+  __shared__ __align__(8) unsigned long long bar;
+  const unsigned a = smem_u32(&bar);
+  if (threadIdx.x == 0) mbar_init(a);
+  __syncthreads();
+  if (!mbar_wait(a, 0u, budget) && threadIdx.x == 0) atomicOr(err, 1);
 }
 __device__ __forceinline__ void bulk_load(unsigned dst, const void *src, unsigned bytes,
                                           unsigned bar) {
@@ -1117,6 +1129,31 @@ constexpr int BK_COLS = 16 * 64;            // per-column doubles and ints
 constexpr int BK_PARTIALS = 2 * 64 * 2048;  // NQ x K x blocks
 constexpr int BK_MAX_GRID = 2048;
 }  // namespace
+
+// The bulk-copy wait's timeout path, end to end: VDR_TIMEOUT when a wait
+// that nothing completes ran out of its (about 1 ms) budget and the flag
+// reached the host; the context stays usable.
+int diag_wait_timeout(Handle &h) {
+  cudaError_t e;
+  if (!h.block_err && (e = cudaMalloc(&h.block_err, sizeof(int))))
+    return cuda_fail(e, "diag: alloc");
+  int flag = 0;
+  if ((e = cudaMemsetAsync(h.block_err, 0, sizeof(int), h.stream))) return cuda_fail(e, "diag");
+  wait_timeout_kernel<<<1, 32, 0, h.stream>>>(h.block_err, 2000000LL);
+  count_launches(1);
+  if ((e = cudaGetLastError()) ||
+      (e = cudaMemcpyAsync(&flag, h.block_err, sizeof(int), cudaMemcpyDeviceToHost,
+                           h.stream)) ||
+      (e = cudaMemsetAsync(h.block_err, 0, sizeof(int), h.stream)) ||
+      (e = cudaStreamSynchronize(h.stream)))
+    return cuda_fail(e, "diag");
+  if (!flag) {
+    set_error("diag: the wait completed although nothing arrived");
+    return VDR_CUDA_ERROR;
+  }
+  set_error("diag: the bounded wait ran out as designed");
+  return VDR_TIMEOUT;
+}
 
 // Block solve: FP64 refinement around K-column FP32 BiCGStab with the TF32
 // tensor-core apply.  B, X are N x K FP64 device arrays (node-major).
