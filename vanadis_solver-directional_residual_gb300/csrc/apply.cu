@@ -528,6 +528,22 @@ __global__ void mask_vec_kernel(double *__restrict__ v,
     if (m[i]) v[i] = 0.0;
 }
 
+// v = 0 on masked entries; *all_zero = 0 if any entry stays nonzero (every
+// writer stores the same 0).
+__global__ void mask_vec_flag_kernel(double *__restrict__ v,
+                                     const unsigned char *__restrict__ m, int N,
+                                     int *all_zero) {
+  bool nz = false;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (long)gridDim.x * blockDim.x) {
+    if (m && m[i])
+      v[i] = 0.0;
+    else if (v[i] != 0.0)
+      nz = true;
+  }
+  if (__syncthreads_or(nz) && threadIdx.x == 0) *all_zero = 0;
+}
+
 __global__ void bc_to_mask_kernel(const int *__restrict__ bc,
                                   unsigned char *__restrict__ m, int N) {
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
@@ -730,6 +746,13 @@ cudaError_t launch_mask_conn(int *conn, int E, const unsigned char *mask,
 cudaError_t launch_diag_fix(double *diag, double *dinv,
                             const unsigned char *mask, int N, cudaStream_t s) {
   diag_fix_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(diag, dinv, mask, N);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mask_vec_flag(double *v, const unsigned char *mask, int N,
+                                 int *all_zero, cudaStream_t s) {
+  mask_vec_flag_kernel<<<grid_for(N, 256, 8), 256, 0, s>>>(v, mask, N, all_zero);
   count_launches(1);
   return cudaGetLastError();
 }

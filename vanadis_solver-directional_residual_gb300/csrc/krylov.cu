@@ -556,16 +556,19 @@ int solve_device(Handle &h, int method, const double *b, double *x,
   init.itmax = itmax;
   init.best_err = INFINITY;
   init.stall_window = stall_window;
+  init.x_zero = 1;
   std::memcpy(&h.h_st[0], &init, sizeof(KState));
   if ((e = cudaMemcpyAsync(h.st, &h.h_st[0], sizeof(KState),
                            cudaMemcpyHostToDevice, s)))
     return cuda_fail(e, "state upload");
 
-  // x on Dirichlet nodes is zeroed in place, as matvec_0 does to its input.
-  if ((e = launch_mask_vec(x, h.mask, h.N, s))) return cuda_fail(e, "mask x");
+  // x on Dirichlet nodes is zeroed in place, as matvec_0 does to its input;
+  // A x is skipped when x is then zero (a cold start).
+  if ((e = launch_mask_vec_flag(x, h.mask, h.N, &h.st->x_zero, s)))
+    return cuda_fail(e, "mask x");
   if ((e = cudaMemsetAsync(a.r, 0, sizeof(double) * h.N, s)))
     return cuda_fail(e, "memset");
-  if ((e = launch_apply(h, false, x, a.r, nullptr, nullptr, s)))
+  if ((e = launch_apply(h, false, x, a.r, &h.st->x_zero, nullptr, s)))
     return cuda_fail(e, "initial apply");
   if (method == VDR_SOLVER_BICGSTAB)
     k_start<false><<<g, RED_THREADS, 0, s>>>(a);

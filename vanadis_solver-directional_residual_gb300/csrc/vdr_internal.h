@@ -31,6 +31,7 @@ struct KState {
   double best_err;   // lowest residual so far (stall detection)
   int iter, itmax, done, sconv, status, reason;  // reason: see vdr_solve_stats
   int since_best, stall_window;  // iterations without a 1% gain; 0 = off
+  int x_zero;  // the initial guess is zero (its apply is skipped)
   unsigned int ticket;
   unsigned int pad2;
 };
@@ -264,6 +265,9 @@ cudaError_t launch_legacy_conn(const int *iss_ref, int E, int N, const int *bc,
 // diag = 1 on Dirichlet nodes (when mask != null); dinv = 1/diag.
 cudaError_t launch_diag_fix(double *diag, double *dinv,
                             const unsigned char *mask, int N, cudaStream_t s);
+// Masks v and clears *all_zero when a nonzero entry remains.
+cudaError_t launch_mask_vec_flag(double *v, const unsigned char *mask, int N,
+                                 int *all_zero, cudaStream_t s);
 cudaError_t launch_mask_vec(double *v, const unsigned char *mask, int N,
                             cudaStream_t s);
 cudaError_t launch_bc_to_mask(const int *bc, unsigned char *mask, int N,
