@@ -1034,7 +1034,10 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
   const int g = red_grid(h.N);
   MixedStats st;
   int status = VDR_NOT_CONVERGED;
-  if ((e = launch_mask_vec(x, h.mask, h.N, s))) return cuda_fail(e, "mask x");
+  // x masked; the first residual's A x is skipped when x is then zero
+  if ((e = cudaMemsetAsync(&h.st->x_zero, 1, sizeof(int), s)) ||
+      (e = launch_mask_vec_flag(x, h.mask, h.N, &h.st->x_zero, s)))
+    return cuda_fail(e, "mask x");
   // The stored FP32 operator runs its inner BiCGStab on FP32 vectors.
   const bool f32v = h.apply_mode == VDR_APPLY_STORED && method == VDR_SOLVER_BICGSTAB;
   if (f32v && !h.dinv32 && (e = cudaMalloc(&h.dinv32, sizeof(float) * (size_t)h.N)))
@@ -1045,7 +1048,8 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
   for (int outer = 0; outer <= max_outer; outer++) {
     h.apply_fp32 = false;
     if ((e = cudaMemsetAsync(r, 0, sizeof(double) * h.N, s)) ||
-        (e = launch_apply(h, false, x, r, nullptr, nullptr, s)))
+        (e = launch_apply(h, false, x, r, outer == 0 ? &h.st->x_zero : nullptr,
+                          nullptr, s)))
       return cuda_fail(e, "outer residual");
     k_residual<<<g, RED_THREADS, 0, s>>>(a, r, scal);
     count_launches(1);
