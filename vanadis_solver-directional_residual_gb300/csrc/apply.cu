@@ -8,12 +8,14 @@
 // (vanadis_full_DR_OpenMP_timing.for:1837-1933) and MATVEC_C_cu /
 // MTTVEC_C_cu (src_v2026_2_1/cudatest.cu:184-227).
 //
-// Layout of the element-matrix store (GB300-first, not the reference's BB):
-// entry (i,j) of element p sits at pair index 4*i + j/2 of a double2 array
-// with stride E, i.e. A64[(4i + j/2)*E + p] -> every warp load is 32
-// consecutive elements' same entry pair: 512 contiguous bytes, streamed
-// once per apply with the evict-first (.cs) cache hint so that x and y
-// stay in the 129 MB L2.  FP32 copy: float4 A32[(2i + j/4)*E + p].
+// Layout of the element-matrix stores (GB300-first, not the reference's BB),
+// all slot-major with stride E so that every warp load is 32 consecutive
+// elements' same entries (512 contiguous bytes), streamed once per apply
+// with the evict-first (.cs) cache hint so that x and y stay in the 129 MB
+// L2: the default double-float store float4 Ahi/Alo[(2i + j/4)*E + p] (hi
+// and lo FP32 parts of entry (i,j); the hi parts are also the rounded FP32
+// operator), the FP64 store double2 A64[(4i + j/2)*E + p] (entries outside
+// the pair window), the recomputed FP32 store float4 A32[(2i + j/4)*E + p].
 //
 // Scatter: VDR_SCATTER_ATOMIC uses fp64 atomics (red.global.add.f64) in
 // natural element order; VDR_SCATTER_COLOR runs one pass per colour over a

@@ -1,23 +1,29 @@
 // element.cu -- per-element DR recompute kernels.
 //
-// Every kernel here maps one element onto 8 consecutive lanes; lane q
-// evaluates Gauss point q (the reference's point order: the node-sign
-// pattern of par_3d times 0.577350269189626) so the geometry, Jacobian
-// inverse and DR weight of the 8 points are computed in parallel in
-// registers.  What differs is what is done with them:
+// The build and apply kernels map one element onto 8 consecutive lanes;
+// lane q evaluates Gauss point q (the reference's point order: the
+// node-sign pattern of par_3d times 0.577350269189626) so the geometry,
+// Jacobian inverse and DR weight of the 8 points are computed in parallel
+// in registers.  What differs is what is done with them:
 //
-//   elem_rows_kernel<T,STORE>  C = c1*H + c2*M, row i kept by lane i, written
-//                              to the HBM-resident element-matrix store and
-//                              its diagonal scattered into the Jacobi diag
-//                              (el3d + sklad_wd + diag assembly,
-//                              vanadis_full_DR_OpenMP_timing.for:431-610,
-//                              691-737, 880-904)
-//   elem_rows_kernel<T,RHS>    b += cf*f - C . T_old   (przest3d :691-716)
-//   mf_apply_kernel<T,TRANS>   y += C x or C^T x without forming C: lane q
-//                              forms its point's contribution to all 8
-//                              outputs, then a 3-step shuffle reduce-scatter
-//                              leaves output i in lane i (matrix-free apply)
-//   mass_kernel                int c dOmega (integrate_mass_hex8 :2181-2285)
+//   elem_build_df_kernel<SPLIT>  (default) A_e = aH H + aM M, row i kept by
+//                                lane i, in double-float on the FP32 pipe,
+//                                written to the double-float store, with the
+//                                Jacobi diagonal, b += cf f - (H - rM M) T_old
+//                                and, for the time loop, M and F = sum f_e
+//                                (el3d + sklad_wd + diag assembly + przest3d,
+//                                vanadis_full_DR_OpenMP_timing.for:431-610,
+//                                676-740, 880-904); elem_dr_scalars_kernel
+//                                forms its per-element velocity scalars
+//   elem_build_kernel<T>         the same in plain FP64 (the range fallback)
+//                                or FP32 (the recomputed FP32 operator)
+//   mf_apply_kernel<T,TRANS>     y += C x or C^T x without forming C: lane q
+//                                forms its point's contribution to all 8
+//                                outputs, then a 3-step shuffle reduce-scatter
+//                                leaves output i in lane i (matrix-free apply)
+//   mass_weights_kernel,         int c dOmega (integrate_mass_hex8 :2181-2285)
+//   mass_dot_kernel, mass_kernel from per-element weights formed once, or
+//                                directly
 //
 // with H = int lambda gradN.gradN + int W (v.gradN) + P int W N
 //          + alpha int_{face 3} W N,  M = int W N,  f = (Q/vol) int W.
