@@ -331,7 +331,20 @@ namespace {
 std::atomic<long long> g_launches{0};
 }
 void count_launches(long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
+
+int device_sm_count() {
+  static std::atomic<int> cached{0};
+  int n = cached.load(std::memory_order_relaxed);
+  if (n > 0) return n;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  if (n <= 0) n = 1;
+  cached.store(n, std::memory_order_relaxed);
+  return n;
+}
 
 int cuda_fail(cudaError_t e, const char *what) {
   set_error(std::string(what) + ": " + cudaGetErrorString(e));

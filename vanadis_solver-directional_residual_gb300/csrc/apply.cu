@@ -31,16 +31,7 @@
 namespace vdr {
 namespace {
 
-int sm_count2() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
+int sm_count2() { return device_sm_count(); }
 
 template <bool TRANS, bool ATOMIC>
 __global__ void __launch_bounds__(256) stored_apply_f64(

@@ -21,6 +21,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "dfloat.cuh"
@@ -32,16 +33,7 @@ namespace {
 constexpr int BT = 512;  // threads per block of the block-vector kernels
 constexpr unsigned FULL = 0xffffffffu;
 
-int sm_count_b() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
+int sm_count_b() { return device_sm_count(); }
 
 // --------------------------------------------------------------- applies
 __device__ __forceinline__ unsigned to_tf32(float f) {
@@ -1005,6 +997,17 @@ __global__ void dinv_to_f32(const double *__restrict__ d, float *__restrict__ f,
     f[i] = (float)d[i];
 }
 
+// Resident blocks per SM of `kern`, queried once per instantiation.
+template <typename Kern>
+int cached_per_sm(std::atomic<int> &slot, Kern kern, int threads, int smem) {
+  int n = slot.load(std::memory_order_relaxed);
+  if (n > 0) return n;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem);
+  if (n < 1) n = 1;
+  slot.store(n, std::memory_order_relaxed);
+  return n;
+}
+
 int grid_n(long n, int threads, int per_sm) {
   const long need = (n + threads - 1) / threads;
   return (int)std::max<long>(1, std::min<long>(need, (long)sm_count_b() * per_sm));
@@ -1027,12 +1030,9 @@ int block_apply_launches_tf32(const Handle &h, int K, bool split,
   do {                                                                            \
     constexpr int KK = 16 * TILES;                                                \
     const int smem = TMA_WARPS * (TMA_S * 8 * (KK + 8) + 2 * 8 * (KK + 4)) * 4;   \
-    static int per_sm = 0;                                                        \
-    if (!per_sm) {                                                                \
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(                              \
-          &per_sm, block_apply_tma<SPLIT, TILES>, TMA_WARPS * 32, smem);          \
-      if (per_sm < 1) per_sm = 1;                                                 \
-    }                                                                             \
+    static std::atomic<int> slot{0};                                              \
+    const int per_sm = cached_per_sm(slot, block_apply_tma<SPLIT, TILES>,         \
+                                     TMA_WARPS * 32, smem);                       \
     block_apply_tma<SPLIT, TILES><<<grid_n((long)h.E * 32, TMA_WARPS * 32,        \
                                            per_sm),                               \
                                     TMA_WARPS * 32, smem, s>>>(                   \
@@ -1053,12 +1053,9 @@ int block_apply_launches_tf32(const Handle &h, int K, bool split,
   }
 #define VDR_BLOCK_APPLY(SPLIT, TILES)                                        \
   do {                                                                       \
-    static int per_sm = 0;                                                   \
-    if (!per_sm) {                                                           \
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(                         \
-          &per_sm, block_apply_tf32<SPLIT, TILES>, 256, 0);                  \
-      if (per_sm < 1) per_sm = 1;                                            \
-    }                                                                        \
+    static std::atomic<int> slot{0};                                         \
+    const int per_sm =                                                       \
+        cached_per_sm(slot, block_apply_tf32<SPLIT, TILES>, 256, 0);         \
     block_apply_tf32<SPLIT, TILES><<<grid_n((long)h.E * 32, 256, per_sm),    \
                                      256, 0, s>>>(A, h.conn, h.E, X, dscale, \
                                                   Y, skip);                  \

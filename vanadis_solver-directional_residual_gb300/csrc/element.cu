@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "dfloat.cuh"
 #include "dr_device.cuh"
@@ -981,16 +982,7 @@ __global__ void sum_partials_kernel(const double *__restrict__ partials, int n,
   if (threadIdx.x == 0) *out = sm[0];
 }
 
-int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
+int sm_count() { return device_sm_count(); }
 
 }  // namespace
 
@@ -1005,14 +997,13 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
     elem_build_kernel<double><<<grid, 64, 0, s>>>(a, ba);
   else {
     if (!ba.drs) return cudaErrorInvalidValue;
-    static bool carveout = false;  // 8 blocks of 27.5 KB need the full carveout
-    if (!carveout) {
+    static std::once_flag carveout;  // 8 blocks of 27.5 KB need the full carveout
+    std::call_once(carveout, [] {
       cudaFuncSetAttribute(elem_build_df_kernel<true>,
                            cudaFuncAttributePreferredSharedMemoryCarveout, 100);
       cudaFuncSetAttribute(elem_build_df_kernel<false>,
                            cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-      carveout = true;
-    }
+    });
     const int g2 = (int)std::min<long>(((long)a.E + 255) / 256, (long)sm_count() * 8);
     elem_dr_scalars_kernel<<<g2, 256, 0, s>>>(a, ba.drs);
     if (ba.told || ba.Mhi)  // H and M apart

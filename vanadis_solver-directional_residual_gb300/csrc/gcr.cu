@@ -31,16 +31,7 @@ namespace {
 constexpr int GT = 256;  // threads per block
 constexpr unsigned FULLG = 0xffffffffu;
 
-int sm_count_g() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
+int sm_count_g() { return device_sm_count(); }
 
 struct GcrArgs {
   long n;

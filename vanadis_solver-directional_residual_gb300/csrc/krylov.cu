@@ -31,16 +31,7 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-int sm_count3() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
+int sm_count3() { return device_sm_count(); }
 
 template <int NQ>
 __device__ __forceinline__ void block_sum(double (&v)[NQ]) {

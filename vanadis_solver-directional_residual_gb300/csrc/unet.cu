@@ -63,16 +63,7 @@ constexpr long layer_wsize(int l) {
   return l == L_HEAD ? 16 : 27L * DEFS[l].cout * (DEFS[l].cin1 + DEFS[l].cin2);
 }
 
-int sm_count_u() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
+int sm_count_u() { return device_sm_count(); }
 
 int grid_for(long n, int threads, int per_sm = 8) {
   const long need = (n + threads - 1) / threads;

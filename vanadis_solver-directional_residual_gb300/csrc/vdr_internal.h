@@ -190,6 +190,9 @@ struct Handle {
   long gcr_cycle_launches = 0;
 };
 
+// SM count of the current device, cached once (thread-safe).
+int device_sm_count();
+
 // Process-wide count of kernels launched by this library (graph nodes
 // included), for the benchmark's launch accounting.
 void count_launches(long n);
