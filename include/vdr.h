@@ -221,15 +221,20 @@ int vdr_time_steps(vdr_handle *h, int nsteps, double cf, double rM,
 #define VDR_BLOCK_TF32X3 2 /* FP32 vectors, split TF32 (three MMAs per
                               product: FP32-level accuracy) */
 
-/* Data movement of the tensor-core block apply: VDR_BLOCK_APPLY_LSU
- * (default, the faster by measurement) gathers X rows with 16-byte loads and
- * scatters with float4 atomics; VDR_BLOCK_APPLY_BULK moves each element's
+/* Data movement of the tensor-core block apply: VDR_BLOCK_APPLY_TILE
+ * (default) takes boxes of 8 x 2 x 2 elements of a mesh in the canonical
+ * structured numbering, reads each node row of a box once into shared
+ * memory and adds each result row once, one float4 atomic per 4 columns
+ * (other meshes, and colour-ordered storage, use the LSU variant);
+ * VDR_BLOCK_APPLY_LSU gathers X rows with 16-byte loads and scatters with
+ * float4 atomics, per element; VDR_BLOCK_APPLY_BULK moves each element's
  * K-wide node rows into shared memory with cp.async.bulk (mbarrier
  * completion, three elements ahead per warp) and scatters with
  * cp.reduce.async.bulk -- limited by the copy engine's per-operation cost
  * on 64-256-byte rows. */
 #define VDR_BLOCK_APPLY_BULK 0
 #define VDR_BLOCK_APPLY_LSU 1
+#define VDR_BLOCK_APPLY_TILE 2
 int vdr_set_block_apply(vdr_handle *h, int variant);
 /* Diagnostic of the bounded device wait used by VDR_BLOCK_APPLY_BULK: one
  * warp waits on an mbarrier that nothing completes, with a ~1 ms budget;
@@ -247,6 +252,11 @@ int vdr_assemble_rhs_block_device(vdr_handle *h, int K, const double *d_Q,
  * K = 16, 32 or 64). */
 int vdr_apply_block_device(vdr_handle *h, int K, const void *d_X, void *d_Y,
                            int precision);
+/* Y += P A P X, the same without zeroing Y first.  Both are ordered on the
+ * handle's stream without a host synchronisation (the bulk-copy variant
+ * synchronises to report a device wait that ran out). */
+int vdr_apply_block_accumulate_device(vdr_handle *h, int K, const void *d_X,
+                                      void *d_Y, int precision);
 /* Solves A X = B for K columns (K = 16, 32 or 64): FP64 refinement per
  * column (residual with the FP64-accurate operator, FP64 update) around K
  * simultaneous FP32 Jacobi-BiCGStab inner solves with the tensor-core apply

@@ -82,7 +82,7 @@ TF32_TOL = {"tf32": 5e-3, "tf32x3": 2e-5}
 
 @pytest.mark.parametrize("K", [16, 32, 64])
 @pytest.mark.parametrize("precision", ["tf32", "tf32x3"])
-@pytest.mark.parametrize("variant", ["bulk", "lsu"])
+@pytest.mark.parametrize("variant", ["bulk", "lsu", "tile"])
 def test_block_apply_tensor_core(vdr, oracle, gpu_lib, case, K, precision,
                                  variant):
     import torch
@@ -102,6 +102,76 @@ def test_block_apply_tensor_core(vdr, oracle, gpu_lib, case, K, precision,
                                  X[:, k].astype(np.float64))
         worst = max(worst, rel_l2(Y[:, k], yref))
     assert worst < TF32_TOL[precision], worst
+    assert np.all(Y[prob.bc == 1] == 0.0)
+
+
+@pytest.mark.parametrize("precision,K", [("fp64", 5), ("tf32x3", 64)])
+def test_block_apply_accumulate(vdr, oracle, gpu_lib, case, precision, K):
+    """vdr_apply_block_accumulate_device adds P A P X into Y without zeroing
+    it: two calls on a zero Y give twice the oracle's apply."""
+    import torch
+    prob, aH, aM, bb = case
+    N = prob.mesh.nnode
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    X = np.random.default_rng(55).standard_normal((N, K))
+    with vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=aH, aM=aM) as s:
+        Xd = to_dev(X, dt)
+        Yd = torch.zeros_like(Xd)
+        s.apply_block_accumulate_device(Xd, Yd, precision)
+        s.apply_block_accumulate_device(Xd, Yd, precision)
+        torch.cuda.synchronize()
+        Y = Yd.cpu().numpy().astype(np.float64)
+    tol = 1e-12 if precision == "fp64" else TF32_TOL[precision]
+    Xr = Xd.cpu().numpy().astype(np.float64)
+    for k in (0, K - 1):
+        yref, _ = oracle.matvec0(prob.mesh.iss, bb, prob.bc, Xr[:, k])
+        assert rel_l2(Y[:, k], 2.0 * yref) < tol, k
+
+
+def shuffled_elements(vdr, prob, seed):
+    """The same problem with its elements in a random order (the node
+    numbering is kept), so the mesh is no longer in the canonical structured
+    numbering."""
+    import dataclasses
+    m = prob.mesh
+    E = m.nelem
+    perm = np.random.default_rng(seed).permutation(E)
+    mesh = dataclasses.replace(
+        m, iss=np.ascontiguousarray(m.iss.reshape(8, E)[:, perm]).ravel(),
+        kod=np.ascontiguousarray(m.kod.reshape(6, E)[:, perm]).ravel())
+    return dataclasses.replace(
+        prob, mesh=mesh,
+        vel=np.ascontiguousarray(prob.vel.reshape(3, E)[:, perm]).ravel(),
+        lam=prob.lam[perm], pdec=prob.pdec[perm], q=prob.q[perm])
+
+
+@pytest.mark.parametrize("layout", ["shuffled", "color"])
+def test_block_apply_tile_request_off_the_structured_order(vdr, oracle, gpu_lib,
+                                                           case, layout):
+    """The node-tile variant needs the canonical structured numbering in
+    storage order; on a shuffled element order or the colour-ordered store
+    the request falls back to the per-element apply, with the same result."""
+    import torch
+    prob, aH, aM, bb = case
+    opts = vdr.Options(apply_mode="stored")
+    if layout == "shuffled":
+        prob = shuffled_elements(vdr, prob, seed=5)
+        bb = oracle_bb(oracle, prob, aH, aM)
+    else:
+        opts = vdr.Options(apply_mode="stored", scatter="color")
+    N = prob.mesh.nnode
+    X = np.random.default_rng(77).standard_normal((N, 32)).astype(np.float32)
+    with vdr.Solver(prob, opts, aH=aH, aM=aM) as s:
+        s.set_block_apply("tile")
+        Xd = to_dev(X, torch.float32)
+        Yd = torch.empty_like(Xd)
+        s.apply_block_device(Xd, Yd, "tf32x3")
+        torch.cuda.synchronize()
+        Y = Yd.cpu().numpy().astype(np.float64)
+    for k in (0, 31):
+        yref, _ = oracle.matvec0(prob.mesh.iss, bb, prob.bc,
+                                 X[:, k].astype(np.float64))
+        assert rel_l2(Y[:, k], yref) < TF32_TOL["tf32x3"], k
     assert np.all(Y[prob.bc == 1] == 0.0)
 
 
@@ -195,7 +265,9 @@ def column_residuals(oracle, prob, bb, B, X):
 
 @pytest.mark.parametrize("precision,variant", [("tf32x3", "bulk"),
                                                ("tf32", "bulk"),
-                                               ("tf32x3", "lsu")])
+                                               ("tf32x3", "lsu"),
+                                               ("tf32x3", "tile"),
+                                               ("tf32", "tile")])
 def test_block_solve_parity(vdr, oracle, gpu_lib, case, precision, variant):
     import torch
     prob, aH, aM, bb = case

@@ -823,8 +823,8 @@ int vdr_assemble_rhs_block_device(vdr_handle *H, int K, const double *Q,
   return e ? cuda_fail(e, "block rhs") : VDR_OK;
 }
 
-int vdr_apply_block_device(vdr_handle *H, int K, const void *X, void *Y,
-                           int precision) {
+static int apply_block(vdr_handle *H, int K, const void *X, void *Y,
+                       int precision, bool zero, const char *who) {
   int st = check_handle(H);
   if (st) return st;
   Handle &h = H->h;
@@ -833,7 +833,7 @@ int vdr_apply_block_device(vdr_handle *H, int K, const void *X, void *Y,
        precision != VDR_BLOCK_TF32X3) ||
       (precision != VDR_BLOCK_FP64 && K != 16 && K != 32 && K != 64) ||
       h.apply_mode != VDR_APPLY_STORED) {
-    set_error("vdr_apply_block_device: bad arguments (TF32 needs K = 16, 32 "
+    set_error(std::string(who) + ": bad arguments (TF32 needs K = 16, 32 "
               "or 64; block applies need the stored operator)");
     return VDR_BAD_ARGUMENT;
   }
@@ -841,14 +841,16 @@ int vdr_apply_block_device(vdr_handle *H, int K, const void *X, void *Y,
   cudaError_t e;
   if (precision != VDR_BLOCK_FP64) {
     float4 *Aaos = nullptr;
-    if ((e = ensure_aos(h, &Aaos))) return cuda_fail(e, "block operator copy");
-    if ((e = cudaMemsetAsync(Y, 0, sizeof(float) * h.N * (size_t)K, h.stream)))
+    if ((e = ensure_aos(h, false, &Aaos))) return cuda_fail(e, "block operator copy");
+    if (zero && (e = cudaMemsetAsync(Y, 0, sizeof(float) * h.N * (size_t)K, h.stream)))
       return cuda_fail(e, "memset");
     if (block_apply_launches_tf32(h, K, precision == VDR_BLOCK_TF32X3,
                                   static_cast<const float *>(X), nullptr,
                                   static_cast<float *>(Y), Aaos, nullptr,
                                   h.stream))
       return cuda_fail(cudaGetLastError(), "block apply");
+    if (!h.block_tma) return VDR_OK;
+    // the bulk-copy variant reports a device wait that ran out
     int tma_err = 0;
     if ((e = cudaMemcpyAsync(&tma_err, h.block_err, sizeof(int), cudaMemcpyDeviceToHost,
                              h.stream)) ||
@@ -861,11 +863,22 @@ int vdr_apply_block_device(vdr_handle *H, int K, const void *X, void *Y,
     }
     return VDR_OK;
   }
-  if ((e = cudaMemsetAsync(Y, 0, sizeof(double) * h.N * (size_t)K, h.stream)) ||
+  if ((zero && (e = cudaMemsetAsync(Y, 0, sizeof(double) * h.N * (size_t)K, h.stream))) ||
       (e = launch_block_apply64(h, K, static_cast<const double *>(X),
                                 static_cast<double *>(Y), h.stream)))
     return cuda_fail(e, "block apply");
   return VDR_OK;
+}
+
+int vdr_apply_block_device(vdr_handle *H, int K, const void *X, void *Y,
+                           int precision) {
+  return apply_block(H, K, X, Y, precision, true, "vdr_apply_block_device");
+}
+
+int vdr_apply_block_accumulate_device(vdr_handle *H, int K, const void *X,
+                                      void *Y, int precision) {
+  return apply_block(H, K, X, Y, precision, false,
+                     "vdr_apply_block_accumulate_device");
 }
 
 int vdr_set_mixed_operator(vdr_handle *H, int mode) {
@@ -892,12 +905,14 @@ int vdr_diag_wait_timeout(vdr_handle *H) {
 int vdr_set_block_apply(vdr_handle *H, int variant) {
   int st = check_handle(H);
   if (st) return st;
-  if (variant != VDR_BLOCK_APPLY_BULK && variant != VDR_BLOCK_APPLY_LSU) {
+  if (variant != VDR_BLOCK_APPLY_BULK && variant != VDR_BLOCK_APPLY_LSU &&
+      variant != VDR_BLOCK_APPLY_TILE) {
     set_error("vdr_set_block_apply: unknown variant");
     return VDR_BAD_ARGUMENT;
   }
   Handle &h = H->h;
   h.block_tma = variant == VDR_BLOCK_APPLY_BULK;
+  h.block_tile = variant == VDR_BLOCK_APPLY_TILE;
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
   h.bk_graph = nullptr;
   return VDR_OK;

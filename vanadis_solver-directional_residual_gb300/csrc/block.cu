@@ -1,13 +1,17 @@
 // block.cu -- many right-hand sides with one operator (K <= 64 columns).
 //
 // Block vectors are node-major, X[n*K + k], so the K values a node carries
-// are contiguous.  One warp handles one element at a time:
+// are contiguous.  The tensor-core applies compute Y^T (K x 8) += X_e^T
+// (K x 8) . A_e^T (8 x 8) per element with mma.sync m16n8k8 TF32 (one MMA
+// per 16 columns, three for split TF32) on FP32 vectors, A_e read from an
+// element-major FP32 copy (256 contiguous bytes per element), so the
+// element matrices stream once for all K columns:
 //
-//   block_apply_tf32  Y^T (K x 8) += X_e^T (K x 8) . A_e^T (8 x 8) on the
-//                     tensor cores, mma.sync m16n8k8 TF32 (one MMA per 16
-//                     columns); FP32 vectors; A_e read from an element-major
-//                     FP32 copy (256 contiguous bytes per element and warp),
-//                     so the element matrices stream once for all K columns.
+//   block_apply_tile  (default on the structured numbering) boxes of
+//                     8 x 2 x 2 elements, node rows staged once in shared
+//                     memory, results added there and sent once per node
+//   block_apply_tf32  one warp per element: row gathers and float4 atomics
+//   block_apply_tma   the same with bulk copies and bulk reductions
 //   block_apply_df    the FP64-accurate apply for the refinement residual:
 //                     lane = column, double-float contraction of the pair
 //                     store (FP32 pipe), FP64 vectors.
@@ -42,29 +46,38 @@ __device__ __forceinline__ unsigned to_tf32(float f) {
   return r;
 }
 
-// SoA pair store hi part -> element-major FP32 copy Aaos[p*64 + 8i + j].
-__global__ void aos_from_hi(const float4 *__restrict__ Ahi, int E,
-                            float4 *__restrict__ Aaos) {
+// Element-major FP32 copy of the operator for the tensor-core applies,
+// Aaos[p*64 + 8i + j] = A_e(i, j) * s(node j), with the rows and columns of
+// Dirichlet nodes zero; s is the FP32 inverse diagonal (the Jacobi
+// preconditioner of the block solve folded in) or 1.  From the hi parts of
+// the double-float store, or from the FP64 store.
+template <bool F64>
+__global__ void aos_build(const float4 *__restrict__ Ahi,
+                          const double2 *__restrict__ A64,
+                          const int *__restrict__ conn, int E,
+                          const float *__restrict__ colscale,
+                          float4 *__restrict__ Aaos) {
   const long total = (long)E * 16;
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long)gridDim.x * blockDim.x) {
     const long p = t >> 4;
-    const int chunk = (int)(t & 15);  // = 2i + h
-    Aaos[t] = Ahi[(size_t)chunk * E + p];
-  }
-}
-
-// SoA FP64 pair store -> element-major FP32 copy.
-__global__ void aos_from_f64(const double2 *__restrict__ A64, int E,
-                             float4 *__restrict__ Aaos) {
-  const long total = (long)E * 16;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long)gridDim.x * blockDim.x) {
-    const long p = t >> 4;
-    const int chunk = (int)(t & 15);
-    const double2 a = A64[(size_t)(2 * chunk) * E + p];
-    const double2 b = A64[(size_t)(2 * chunk + 1) * E + p];
-    Aaos[t] = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
+    const int chunk = (int)(t & 15);  // = 2i + h: row i, columns 4h..4h+3
+    float4 v;
+    if (F64) {
+      const double2 a = A64[(size_t)(2 * chunk) * E + p];
+      const double2 b = A64[(size_t)(2 * chunk + 1) * E + p];
+      v = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
+    } else {
+      v = Ahi[(size_t)chunk * E + p];
+    }
+    float sc[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int cj = __ldg(conn + (size_t)(4 * (chunk & 1) + q) * E + p);
+      sc[q] = cj < 0 ? 0.f : (colscale ? __ldg(colscale + (cj & NODE_BITS)) : 1.f);
+    }
+    if (__ldg(conn + (size_t)(chunk >> 1) * E + p) < 0) sc[0] = sc[1] = sc[2] = sc[3] = 0.f;
+    Aaos[t] = make_float4(v.x * sc[0], v.y * sc[1], v.z * sc[2], v.w * sc[3]);
   }
 }
 
@@ -182,6 +195,192 @@ __global__ void __launch_bounds__(256) block_apply_tf32(
     cl = cln;
     f0 = f0n;
     f1 = f1n;
+  }
+}
+
+// ------------------------------------------- node-tile variant (default)
+// On the canonical structured numbering (element (i, j, k), i fastest, has
+// nodes i + a j + a b k + {0, 1, 1 + a, a} and the same plus a b, on an
+// a x b x c node grid) a block takes a box of TILE_X x TY x TILE_Z
+// elements.  The (TILE_X + 1)(TY + 1)(TILE_Z + 1) node rows the box touches
+// (K contiguous floats per node) arrive once in shared memory by 16-byte
+// asynchronous copies, coalesced along x and zero-filled outside the mesh;
+// the elements' mma.sync contractions read their operands there and add
+// their results into a second shared tile (its rows enter the MMAs as the
+// accumulator), which then goes to Y with one float4 atomic per 4 columns
+// of each node.  Per element this reads and
+// adds about 2.5 node rows instead of 8 and 8.  The operator copy carries
+// the Dirichlet mask (zero rows and columns) and, in the block solve, the
+// Jacobi scale (see aos_build), so the kernel has no per-node work.  The
+// elements of a box are taken in the 8 parity classes of (i, j, k) (no two
+// elements of one class share a node), one element per warp per class with
+// a block barrier between classes, so the shared result tile needs no
+// atomics.  Shared rows are K + 8 floats apart (K + 24 for K = 16; 8 banks
+// mod 32) and x lines TILE_WP = 10 rows apart, which leaves every fragment
+// read and result update of a warp free of bank conflicts for TY + 1 odd.
+constexpr int TILE_X = 8, TILE_Y = 2, TILE_Z = 2, TILE_WP = 10;
+
+template <int K>
+__host__ __device__ constexpr int tile_row_stride() {
+  return K % 32 == 0 ? K + 8 : K + 24;
+}
+
+template <int TY, int KC>
+constexpr int tile_smem_bytes() {
+  return 2 * TILE_WP * (TY + 1) * (TILE_Z + 1) * tile_row_stride<KC>() * 4;
+}
+
+// Shared row offset of local node s (w_el order) of an element.
+template <int TY>
+__device__ __forceinline__ int tile_node_off(int s) {
+  const int s2 = s & 3;
+  const int dx = (s2 == 1 || s2 == 2) ? 1 : 0, dy = s2 >> 1, dz = s >> 2;
+  return dx + TILE_WP * (dy + (TY + 1) * dz);
+}
+
+// 16-byte global -> shared copy; bytes beyond src_bytes are zero-filled.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src,
+                                           unsigned src_bytes) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+               :: "r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+
+template <bool SPLIT, int TILES, int TY, int HALVES>
+__global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
+    const float *__restrict__ Aaos, int nax, int nay, int naz,
+    const float *__restrict__ X, float *__restrict__ Y, const int *skip) {
+  // KC columns per block (of the KR = HALVES * KC of a block-vector row)
+  constexpr int KC = 16 * TILES, KR = KC * HALVES;
+  constexpr int S = tile_row_stride<KC>(), C4 = KC / 4;
+  constexpr int LX = TILE_X + 1, HP = TY + 1, LZ = TILE_Z + 1;
+  constexpr int ROWS = TILE_WP * HP * LZ;
+  constexpr int NT = 64 * TY;            // threads: one warp per element of a class
+  constexpr int NV = LX * HP * LZ * C4;  // float4 slots of the node box
+  constexpr int PER = (NV + NT - 1) / NT;
+  static_assert(NT % C4 == 0, "a thread keeps its column chunk");
+  constexpr int RSTEP = NT / C4;         // box rows between a thread's slots
+  if (skip && *(volatile const int *)skip) return;
+  extern __shared__ __align__(16) float tile_sm[];
+  float *xs = tile_sm, *ys = tile_sm + ROWS * S;
+  const int nex = nax - 1, ney = nay - 1, nez = naz - 1;
+  const int ntx = (nex + TILE_X - 1) / TILE_X, nty = (ney + TY - 1) / TY;
+  const int bid = blockIdx.x / HALVES;
+  const int col0 = (blockIdx.x % HALVES) * KC;
+  X += col0;
+  Y += col0;
+  const int gx0 = (bid % ntx) * TILE_X, gy0 = ((bid / ntx) % nty) * TY,
+            gz0 = (bid / (ntx * nty)) * TILE_Z;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int c = threadIdx.x % C4, r0 = threadIdx.x / C4;
+
+  // Node rows of the box into shared memory; the result tile zeroed.
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int r = r0 + u * RSTEP;
+    if (r < LX * HP * LZ) {
+      const int li = r % LX, lj = (r / LX) % HP, lk = r / (LX * HP);
+      const int gx = gx0 + li, gy = gy0 + lj, gz = gz0 + lk;
+      const bool in = gx < nax && gy < nay && gz < naz;
+      const size_t n = in ? gx + (size_t)nax * (gy + (size_t)nay * gz) : 0;
+      const int row = li + TILE_WP * (lj + HP * lk);
+      cp_async16(xs + row * S + 4 * c, X + n * KR + 4 * c, in ? 16u : 0u);
+      *reinterpret_cast<float4 *>(ys + row * S + 4 * c) =
+          make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+
+  // This warp's element of each parity class and its operator fragment
+  // (B[j][i] = A_e[i][j]: lane (g, t) holds A_e[g][t] and A_e[g][t + 4]).
+  float fa[8][2];
+#pragma unroll
+  for (int ph = 0; ph < 8; ph++) {
+    const int gi = gx0 + (ph & 1) + 2 * (w & 3);
+    const int gj = gy0 + ((ph >> 1) & 1) + 2 * (w >> 2);
+    const int gk = gz0 + (ph >> 2);
+    fa[ph][0] = fa[ph][1] = 0.f;
+    if (gi < nex && gj < ney && gk < nez) {
+      const float *a =
+          Aaos + ((size_t)gi + (size_t)nex * (gj + (size_t)ney * gk)) * 64 + 8 * g + t;
+      fa[ph][0] = __ldg(a);
+      fa[ph][1] = __ldg(a + 4);
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  __syncthreads();
+
+  // The contractions, one parity class at a time.
+#pragma unroll
+  for (int ph = 0; ph < 8; ph++) {
+    const int ei = (ph & 1) + 2 * (w & 3), ej = ((ph >> 1) & 1) + 2 * (w >> 2),
+              ek = ph >> 2;
+    if (gx0 + ei < nex && gy0 + ej < ney && gz0 + ek < nez) {
+      const int rb = ei + TILE_WP * (ej + HP * ek);
+      const float *xl = xs + (rb + tile_node_off<TY>(t)) * S + g;
+      const float *xh = xs + (rb + tile_node_off<TY>(t + 4)) * S + g;
+      float *y0 = ys + (rb + tile_node_off<TY>(2 * t)) * S + g;
+      float *y1 = ys + (rb + tile_node_off<TY>(2 * t + 1)) * S + g;
+      const unsigned b0 = to_tf32(fa[ph][0]), b1 = to_tf32(fa[ph][1]);
+      unsigned c0 = 0u, c1 = 0u;
+      if (SPLIT) {
+        c0 = to_tf32(fa[ph][0] - __uint_as_float(b0));
+        c1 = to_tf32(fa[ph][1] - __uint_as_float(b1));
+      }
+#pragma unroll
+      for (int m = 0; m < TILES; m++) {
+        const float xa[4] = {xl[16 * m], xl[16 * m + 8], xh[16 * m], xh[16 * m + 8]};
+        unsigned ah[4], al[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          ah[u] = to_tf32(xa[u]);
+          al[u] = SPLIT ? to_tf32(xa[u] - __uint_as_float(ah[u])) : 0u;
+        }
+        // the result rows enter as the accumulator: D = X_e^T A_e^T + Y
+        float d0 = y0[16 * m], d1 = y1[16 * m], d2 = y0[16 * m + 8],
+              d3 = y1[16 * m + 8];
+        if (SPLIT) {
+          asm volatile(
+              "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+              "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+              : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
+              : "r"(al[0]), "r"(al[1]), "r"(al[2]), "r"(al[3]), "r"(b0), "r"(b1));
+          asm volatile(
+              "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+              "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+              : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
+              : "r"(ah[0]), "r"(ah[1]), "r"(ah[2]), "r"(ah[3]), "r"(c0), "r"(c1));
+        }
+        asm volatile(
+            "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+            "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+            : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
+            : "r"(ah[0]), "r"(ah[1]), "r"(ah[2]), "r"(ah[3]), "r"(b0), "r"(b1));
+        // D[k][i]: d0 (g, 2t), d1 (g, 2t+1), d2 (g+8, 2t), d3 (g+8, 2t+1)
+        y0[16 * m] = d0;
+        y1[16 * m] = d1;
+        y0[16 * m + 8] = d2;
+        y1[16 * m + 8] = d3;
+      }
+    }
+    __syncthreads();
+  }
+
+  // The result tile into Y.
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int r = r0 + u * RSTEP;
+    if (r < LX * HP * LZ) {
+      const int li = r % LX, lj = (r / LX) % HP, lk = r / (LX * HP);
+      const int gx = gx0 + li, gy = gy0 + lj, gz = gz0 + lk;
+      if (gx < nax && gy < nay && gz < naz) {
+        const int row = li + TILE_WP * (lj + HP * lk);
+        const size_t n = gx + (size_t)nax * (gy + (size_t)nay * gz);
+        atomicAdd(reinterpret_cast<float4 *>(Y + n * KR) + c,
+                  *reinterpret_cast<const float4 *>(ys + row * S + 4 * c));
+      }
+    }
   }
 }
 
@@ -1013,6 +1212,44 @@ int grid_n(long n, int threads, int per_sm) {
   return (int)std::max<long>(1, std::min<long>(need, (long)sm_count_b() * per_sm));
 }
 
+// One block per TILE_X x TY x TILE_Z box of elements and column half; the
+// dynamic shared memory above 48 KB is opted into once per device.
+template <bool SPLIT, int TILES, int TY, int HALVES>
+void launch_tile(const Handle &h, const float *A, const float *X, float *Y,
+                 const int *skip, cudaStream_t s) {
+  constexpr int smem = tile_smem_bytes<TY, 16 * TILES>();
+  static std::atomic<unsigned> opted{0u};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned bit = 1u << (dev & 31);
+  if (!(opted.load(std::memory_order_relaxed) & bit)) {
+    cudaFuncSetAttribute(block_apply_tile<SPLIT, TILES, TY, HALVES>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    opted.fetch_or(bit, std::memory_order_relaxed);
+  }
+  const long tiles = (long)((h.nax - 2) / TILE_X + 1) * ((h.nay - 2) / TY + 1) *
+                     ((h.naz - 2) / TILE_Z + 1);
+  block_apply_tile<SPLIT, TILES, TY, HALVES>
+      <<<(unsigned)(tiles * HALVES), 64 * TY, smem, s>>>(A, h.nax, h.nay, h.naz,
+                                                         X, Y, skip);
+}
+
+// K = 64 runs as two column halves of 32 (measured: more resident blocks
+// per SM beat the second operator-fragment load, 0.43 vs 0.51 ms per C4a
+// apply); TILE_Y = 2 (4 warps, 8 x 2 x 2 elements) measured ahead of 4.
+void launch_tile_k(const Handle &h, int K, bool split, const float *A,
+                   const float *X, float *Y, const int *skip, cudaStream_t s) {
+  if (split) {
+    if (K == 16) launch_tile<true, 1, TILE_Y, 1>(h, A, X, Y, skip, s);
+    else if (K == 32) launch_tile<true, 2, TILE_Y, 1>(h, A, X, Y, skip, s);
+    else launch_tile<true, 2, TILE_Y, 2>(h, A, X, Y, skip, s);
+  } else {
+    if (K == 16) launch_tile<false, 1, TILE_Y, 1>(h, A, X, Y, skip, s);
+    else if (K == 32) launch_tile<false, 2, TILE_Y, 1>(h, A, X, Y, skip, s);
+    else launch_tile<false, 2, TILE_Y, 2>(h, A, X, Y, skip, s);
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ host side
@@ -1021,6 +1258,16 @@ int block_apply_launches_tf32(const Handle &h, int K, bool split,
                               const float4 *Aaos, const int *skip,
                               cudaStream_t s) {
   const float *A = reinterpret_cast<const float *>(Aaos);
+  // The node-tile apply needs the canonical structured numbering in storage
+  // order (not the colour permutation), and any scale folded into the
+  // operator copy.
+  if (!h.block_tma && h.block_tile && h.nax > 1 && h.nay > 1 && h.naz > 1 &&
+      !h.perm_d && !dscale && !(reinterpret_cast<uintptr_t>(X) & 15) &&
+      !(reinterpret_cast<uintptr_t>(Y) & 15)) {
+    launch_tile_k(h, K, split, A, X, Y, skip, s);
+    count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? VDR_OK : VDR_CUDA_ERROR;
+  }
   // Bulk copies need 16-byte aligned rows (K * 4 bytes is a multiple of 16).
   const bool tma = h.block_tma && h.block_err &&
                    !(reinterpret_cast<uintptr_t>(X) & 15) &&
@@ -1095,8 +1342,10 @@ cudaError_t launch_block_rhs(const Handle &h, const double *phi, int K,
 }
 
 // Element-major FP32 copy of the operator for the tensor-core apply (and
-// the error flag of the bulk-copy block apply).
-cudaError_t ensure_aos(Handle &h, float4 **out) {
+// the error flag of the bulk-copy block apply); `scaled`: the Jacobi
+// preconditioner h.dinv32 folded into the columns (the block solve), else
+// the plain operator (the block apply of the C ABI).
+cudaError_t ensure_aos(Handle &h, bool scaled, float4 **out) {
   cudaError_t e;
   if (!h.block_err) {
     if ((e = cudaMalloc(&h.block_err, sizeof(int)))) return e;
@@ -1106,15 +1355,17 @@ cudaError_t ensure_aos(Handle &h, float4 **out) {
     if ((e = cudaMalloc(&h.Aaos, sizeof(float4) * 16 * (size_t)h.E))) return e;
     h.aos_valid = false;
   }
-  if (!h.aos_valid) {
+  if (!h.aos_valid || h.aos_scaled != scaled) {
     const int grid = grid_n((long)h.E * 16, 256, 16);
+    const float *cs = scaled ? h.dinv32 : nullptr;
     if (h.storage == VDR_STORE_DF && h.Ahi)
-      aos_from_hi<<<grid, 256, 0, h.stream>>>(h.Ahi, h.E, h.Aaos);
+      aos_build<false><<<grid, 256, 0, h.stream>>>(h.Ahi, nullptr, h.conn, h.E, cs, h.Aaos);
     else
-      aos_from_f64<<<grid, 256, 0, h.stream>>>(h.A64, h.E, h.Aaos);
+      aos_build<true><<<grid, 256, 0, h.stream>>>(nullptr, h.A64, h.conn, h.E, cs, h.Aaos);
     count_launches(1);
     if ((e = cudaGetLastError())) return e;
     h.aos_valid = true;
+    h.aos_scaled = scaled;
   }
   *out = h.Aaos;
   return cudaSuccess;
@@ -1170,8 +1421,6 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
   cudaError_t e;
   cudaStream_t s = h.stream;
   const long n = (long)h.N * K;
-  float4 *Aaos = nullptr;
-  if ((e = ensure_aos(h, &Aaos))) return cuda_fail(e, "block operator copy");
   if (h.bk_K != K || !h.bk_f) {
     if (h.bk_f) cudaFree(h.bk_f);
     if (h.bk_d) cudaFree(h.bk_d);
@@ -1230,6 +1479,10 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
 
   dinv_to_f32<<<grid_n(h.N, 256, 8), 256, 0, s>>>(h.dinv, h.dinv32, h.N);
   count_launches(1);
+  if ((e = cudaGetLastError())) return cuda_fail(e, "block setup");
+  // The apply's operator copy carries the Jacobi scale (A D^-1).
+  float4 *Aaos = nullptr;
+  if ((e = ensure_aos(h, true, &Aaos))) return cuda_fail(e, "block operator copy");
   const int gv = std::min(BK_MAX_GRID, grid_n(n, BT, 2));  // one wave
   const int gm = grid_n(n, 256, 8);
   bo_mask<<<gm, 256, 0, s>>>(n, a.kshift, X, h.mask);
@@ -1246,11 +1499,11 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
       return cuda_fail(e, "capture");
     for (int it = 0; it < KI; it++) {
       bb_p<<<gv, BT, 0, s>>>(a);
-      block_apply_launches_tf32(h, K, split, a.p, h.dinv32, a.v, Aaos,
+      block_apply_launches_tf32(h, K, split, a.p, nullptr, a.v, Aaos,
                                 &st->done, s);
       bb_alpha<<<gv, BT, 0, s>>>(a);
       bb_s<<<gv, BT, 0, s>>>(a);
-      block_apply_launches_tf32(h, K, split, a.s, h.dinv32, a.t, Aaos,
+      block_apply_launches_tf32(h, K, split, a.s, nullptr, a.t, Aaos,
                                 &st->done, s);
       bb_omega<<<gv, BT, 0, s>>>(a);
       bb_xr<<<gv, BT, 0, s>>>(a);

@@ -154,6 +154,7 @@ struct Handle {
   // many right-hand sides (block.cu)
   float4 *Aaos = nullptr;    // element-major FP32 copy [E][64] for the TF32 apply
   bool aos_valid = false;
+  bool aos_scaled = false;   // Aaos carries the Jacobi scale (block solve)
   double *phi = nullptr;     // [8][E] source weights (1/vol) int W_i
   bool want_phi = false, phi_valid = false;
   int *perm_d = nullptr;     // storage position -> caller element (colour mode)
@@ -163,7 +164,8 @@ struct Handle {
   double *bk_d = nullptr;
   cudaGraphExec_t bk_graph = nullptr;
   bool bk_graph_split = false;
-  bool block_tma = false;     // bulk-copy block apply (default: the LSU variant)
+  bool block_tma = false;     // bulk-copy block apply
+  bool block_tile = true;     // node-tile block apply on structured meshes (default)
   int *block_err = nullptr;   // set when a bulk-copy wait ran out
 
   // many meshes as segments (batch.cu)
@@ -323,7 +325,7 @@ int block_apply_launches_tf32(const Handle &h, int K, bool split,
 cudaError_t launch_block_rhs(const Handle &h, const double *phi, int K,
                              const double *Q, double cf, double *B,
                              cudaStream_t s);
-cudaError_t ensure_aos(Handle &h, float4 **out);
+cudaError_t ensure_aos(Handle &h, bool scaled, float4 **out);
 
 // ---- errors ----
 void set_error(const std::string &msg);

@@ -379,11 +379,14 @@ class Solver:
         L.check(self.lib.vdr_set_mixed_operator(self.h, {"rounded": 0, "recompute": 1}[mode]),
                 "vdr_set_mixed_operator")
 
-    def set_block_apply(self, variant="lsu"):
-        """Data movement of the tensor-core block apply: "lsu" (default) or
-        "bulk" (bulk copies and bulk reductions through shared memory)."""
-        L.check(self.lib.vdr_set_block_apply(self.h, {"bulk": 0, "lsu": 1}[variant]),
-                "vdr_set_block_apply")
+    def set_block_apply(self, variant="tile"):
+        """Data movement of the tensor-core block apply: "tile" (default:
+        node rows of 8 x 2 x 2-element boxes staged once in shared memory,
+        on meshes in the canonical structured numbering; "lsu" otherwise),
+        "lsu" (per-element row gathers and float4 atomics) or "bulk" (bulk
+        copies and bulk reductions through shared memory)."""
+        L.check(self.lib.vdr_set_block_apply(
+            self.h, {"bulk": 0, "lsu": 1, "tile": 2}[variant]), "vdr_set_block_apply")
 
     @_device_call
     def assemble_rhs_block_device(self, Q, B, cf=1.0):
@@ -402,6 +405,14 @@ class Solver:
         L.check(self.lib.vdr_apply_block_device(
             self.h, K, _ptr(X), _ptr(Y), self.BLOCK_PRECISION[precision]),
             "vdr_apply_block_device")
+
+    @_device_call
+    def apply_block_accumulate_device(self, X, Y, precision="fp64"):
+        """Y += P A P X (Y not zeroed first)."""
+        K = int(X.shape[1])
+        L.check(self.lib.vdr_apply_block_accumulate_device(
+            self.h, K, _ptr(X), _ptr(Y), self.BLOCK_PRECISION[precision]),
+            "vdr_apply_block_accumulate_device")
 
     @_device_call
     def solve_block_device(self, B, X, tol=None, inner_tol=1e-3,
