@@ -46,6 +46,7 @@ extern "C" {
 #define VDR_CUDA_ERROR 3
 #define VDR_BAD_ARGUMENT 4
 #define VDR_TIMEOUT 5
+#define VDR_IO_ERROR 6   /* a text output file could not be written */
 
 /* ---- DR variants (gauss_point_hex8DR) ----
  * VDR_DR_OT: vanadis_full_DR_OpenMP_timing.for:1567-1716 (axis lengths,
@@ -425,6 +426,29 @@ void *vdr_stream(vdr_handle *h);
 int vdr_destroy(vdr_handle *h);
 
 /* Message of the most recent failure in this thread ("" if none). */
+/* ---- text outputs of a time step (host arrays, host threads) ----
+ * The reference's result file T_sssss.TXT (vanadis_full_DR_OpenMP_timing
+ * .for:797-806): per node x, y, z, t * scale (the reference writes
+ * TNW2 * 1d6, kg/m^3 -> mg/m^3) in Fortran format (e12.5, 2x, e12.5, 2x,
+ * e12.5, 2x, e12.5), one node per 55-byte line ending in '\n', written
+ * as dir/T_sssss.TXT (the reference: output\T_sssss.TXT). */
+int vdr_write_result_txt(const char *dir, int step, long nnode,
+                         const double *xx, const double *yy, const double *zz,
+                         const double *t, double scale);
+/* The same text into buf (nnode * 55 bytes, no terminator). */
+int vdr_format_result_txt(char *buf, long nnode, const double *xx,
+                          const double *yy, const double *zz, const double *t,
+                          double scale);
+/* The 2-D slice files vanadis_files (vanadis_full_DR_OpenMP_timing.for:
+ * 1089-1184) splits from T_sssss.TXT on an nax x nay x naz node grid
+ * (x fastest): X_sssss_iii.TXT per x plane (y, z, s), Y_sssss_iii.TXT per
+ * y row (z, x, s), Z_sssss_iii.TXT per z plane (y, x, s), s = t * scale,
+ * format (e12.5, 2x, e12.5, 2x, e12.5); at most 999 nodes per axis (the
+ * names carry i3.3 numbers). */
+int vdr_write_slices_txt(const char *dir, int step, int nax, int nay, int naz,
+                         const double *xx, const double *yy, const double *zz,
+                         const double *t, double scale);
+
 const char *vdr_last_error(void);
 
 /* No counterpart in the reference.  The Jacobi BiCG solve of

@@ -10,9 +10,11 @@ Python host binding.
 from . import learned, problems
 from ._lib import (VdrError, build_library, last_error, library_path,
                    load_library)
-from .solver import (LearnedNet, Options, Solver, kernel_dbcg_simple,
-                     kernel_launch_count)
+from .solver import (LearnedNet, Options, Solver, format_result_txt,
+                     kernel_dbcg_simple, kernel_launch_count, write_result_txt,
+                     write_slices_txt)
 
 __all__ = ["problems", "learned", "Options", "Solver", "LearnedNet", "kernel_dbcg_simple",
-           "kernel_launch_count", "VdrError",
+           "kernel_launch_count", "VdrError", "format_result_txt",
+           "write_result_txt", "write_slices_txt",
            "build_library", "load_library", "library_path", "last_error"]

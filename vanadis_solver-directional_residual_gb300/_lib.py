@@ -11,9 +11,10 @@ from . import build as _build
 
 _lib = None
 
-OK, NOT_CONVERGED, BREAKDOWN, CUDA_ERROR, BAD_ARGUMENT, TIMEOUT = range(6)
+OK, NOT_CONVERGED, BREAKDOWN, CUDA_ERROR, BAD_ARGUMENT, TIMEOUT, IO_ERROR = range(7)
 STATUS_NAMES = {0: "ok", 1: "not converged", 2: "breakdown",
-                3: "cuda error", 4: "bad argument", 5: "timeout"}
+                3: "cuda error", 4: "bad argument", 5: "timeout",
+                6: "i/o error"}
 
 DR_OT, DR_GP, DR_VF = 0, 1, 2
 SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOR = 0, 1, 2
@@ -111,6 +112,11 @@ SIGNATURES = {
     "vdr_stream": (_P, [_P]),
     "vdr_destroy": (_i, [_P]),
     "vdr_last_error": (ctypes.c_char_p, []),
+    "vdr_write_result_txt": (_i, [ctypes.c_char_p, _i, ctypes.c_long, _P, _P,
+                                  _P, _P, _d]),
+    "vdr_format_result_txt": (_i, [_P, ctypes.c_long, _P, _P, _P, _P, _d]),
+    "vdr_write_slices_txt": (_i, [ctypes.c_char_p, _i, _i, _i, _i, _P, _P, _P,
+                                  _P, _d]),
     "kernel_dbcg_simple_": (None, [_I, _D, _D, _D, _I, _I, _D, _D, _I, _D,
                                    _I, _I, _I, _I]),
     "vdr_bicg_noalloc_device": (_i, [_i, _i, _i, _i, _P, _P, _d, _i, _P, _P,

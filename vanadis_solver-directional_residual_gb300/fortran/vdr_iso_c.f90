@@ -18,7 +18,8 @@ module vdr_iso_c
   implicit none
 
   integer(c_int), parameter :: VDR_OK = 0, VDR_NOT_CONVERGED = 1, &
-       VDR_BREAKDOWN = 2, VDR_CUDA_ERROR = 3, VDR_BAD_ARGUMENT = 4
+       VDR_BREAKDOWN = 2, VDR_CUDA_ERROR = 3, VDR_BAD_ARGUMENT = 4, &
+       VDR_TIMEOUT = 5, VDR_IO_ERROR = 6
   integer(c_int), parameter :: VDR_DR_OT = 0, VDR_DR_GP = 1, VDR_DR_VF = 2
   integer(c_int), parameter :: VDR_SCATTER_AUTO = 0, VDR_SCATTER_ATOMIC = 1, &
        VDR_SCATTER_COLOR = 2
@@ -136,5 +137,27 @@ module vdr_iso_c
        import :: c_int, c_ptr
        type(c_ptr), value :: h
      end function vdr_destroy
+
+     ! The step's T_sssss.TXT (scale 1d6 as the driver writes TNW2 * 1d6)
+     ! and the X/Y/Z slice files; dir is a NUL-terminated path, e.g.
+     ! 'output'//c_null_char.
+     integer(c_int) function vdr_write_result_txt(dir, step, nnode, xx, yy, &
+          zz, t, scale) bind(c, name="vdr_write_result_txt")
+       import :: c_int, c_long, c_double, c_char
+       character(kind=c_char), intent(in) :: dir(*)
+       integer(c_int), value :: step
+       integer(c_long), value :: nnode
+       real(c_double), intent(in) :: xx(*), yy(*), zz(*), t(*)
+       real(c_double), value :: scale
+     end function vdr_write_result_txt
+
+     integer(c_int) function vdr_write_slices_txt(dir, step, nax, nay, naz, &
+          xx, yy, zz, t, scale) bind(c, name="vdr_write_slices_txt")
+       import :: c_int, c_double, c_char
+       character(kind=c_char), intent(in) :: dir(*)
+       integer(c_int), value :: step, nax, nay, naz
+       real(c_double), intent(in) :: xx(*), yy(*), zz(*), t(*)
+       real(c_double), value :: scale
+     end function vdr_write_slices_txt
   end interface
 end module vdr_iso_c

@@ -659,3 +659,40 @@ def kernel_dbcg_simple(N, B, X, TOL, ITMAX, BB, ISS, DIAG, NAX, NAY, NAZ,
                             ctypes.byref(nax), ctypes.byref(nay),
                             ctypes.byref(naz), _ip(bc))
     return x, it.value, err.value
+
+
+def _host_f64(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(ctypes.c_void_p)
+
+
+def format_result_txt(xx, yy, zz, t, scale=1e6) -> bytes:
+    """The text of the reference's T_sssss.TXT for node arrays xx, yy, zz
+    and the field t: per node x, y, z, t * scale in Fortran format
+    (e12.5, 2x, e12.5, 2x, e12.5, 2x, e12.5), 55 bytes per line."""
+    lib = L.load_library()
+    arrs = [_host_f64(a) for a in (xx, yy, zz, t)]
+    n = arrs[0][0].size
+    buf = ctypes.create_string_buffer(55 * n)
+    L.check(lib.vdr_format_result_txt(buf, n, *(p for _, p in arrs), float(scale)),
+            "vdr_format_result_txt")
+    return buf.raw[:55 * n]
+
+
+def write_result_txt(directory, step, xx, yy, zz, t, scale=1e6):
+    """Writes directory/T_sssss.TXT as the reference's time step does."""
+    lib = L.load_library()
+    arrs = [_host_f64(a) for a in (xx, yy, zz, t)]
+    L.check(lib.vdr_write_result_txt(str(directory).encode(), int(step),
+                                     arrs[0][0].size, *(p for _, p in arrs),
+                                     float(scale)), "vdr_write_result_txt")
+
+
+def write_slices_txt(directory, step, nax, nay, naz, xx, yy, zz, t, scale=1e6):
+    """Writes the X_/Y_/Z_sssss_iii.TXT slice files that the reference's
+    vanadis_files splits from T_sssss.TXT (node grid nax x nay x naz)."""
+    lib = L.load_library()
+    arrs = [_host_f64(a) for a in (xx, yy, zz, t)]
+    L.check(lib.vdr_write_slices_txt(str(directory).encode(), int(step), int(nax),
+                                     int(nay), int(naz), *(p for _, p in arrs),
+                                     float(scale)), "vdr_write_slices_txt")
