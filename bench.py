@@ -60,6 +60,8 @@ def args_parse(argv=None):
                     help="skip the kernel_dbcg_simple_ section")
     ap.add_argument("--no-time-loop", action="store_true",
                     help="skip the device time-loop section")
+    ap.add_argument("--no-text", action="store_true",
+                    help="skip the text-output section")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-preconditioner section")
     ap.add_argument("--learn-steps", type=int, default=LEARN_STEPS)
@@ -557,6 +559,34 @@ def dropin_section(vdr, s, prob, cf, rM):
                     "A p / A^T p~ apply, X download"}
 
 
+def text_output_section(vdr, prob, x):
+    """The step's text output at the bench size: the T_sssss.TXT text of the
+    solution (x, y, z, T * 1e6 per node in Fortran e12.5 fields, 55 bytes a
+    line) formatted by the library's host threads into memory, then the
+    file written to a scratch directory (the disk's speed, for context)."""
+    import tempfile
+    import numpy as np
+    m = prob.mesh
+    t = x.cpu().numpy()
+    text = np.empty(55 * m.nnode, dtype=np.uint8)
+    fmt = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        vdr.format_result_txt(m.xx, m.yy, m.zz, t, 1e6, out=text)
+        fmt.append(time.perf_counter() - t0)
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        vdr.write_result_txt(d, 1, m.xx, m.yy, m.zz, t, 1e6)
+        t_write = time.perf_counter() - t0
+    t_fmt = min(fmt)
+    return {"nodes": int(m.nnode), "bytes": int(text.size), "format_s": t_fmt,
+            "format_mb_s": text.size / t_fmt / 1e6,
+            "format_lines_per_s": m.nnode / t_fmt,
+            "write_file_s": t_write, "host_threads": os.cpu_count(),
+            "what": "vdr_format_result_txt / vdr_write_result_txt: the "
+                    "reference's T_sssss.TXT (format 122) of one step"}
+
+
 def time_loop_section(vdr, s, prob, aH, aM, cf, rM):
     """The device time loop (vdr_time_steps) on the 256x256x128 rotation +
     shear theta step: per step the right-hand side from T, the solve to 1e-8
@@ -880,6 +910,7 @@ def run_native(a):
     learned = None if a.no_learned else learned_section(vdr, local, a)
     dropin = None if a.no_dropin else dropin_section(vdr, s, prob, cf, rM)
     tloop = None if a.no_time_loop else time_loop_section(vdr, s, prob, aH, aM, cf, rM)
+    text_out = None if a.no_text else text_output_section(vdr, prob, x)
 
     # ---- e2e through the C ABI with host buffers ----
     # The step's inputs (per-element fields) and outputs (right-hand side,
@@ -961,6 +992,7 @@ def run_native(a):
             "learned_preconditioner": learned,
             "dropin_bicg": dropin,
             "time_loop": tloop,
+            "text_output": text_out,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,

@@ -666,17 +666,21 @@ def _host_f64(a):
     return a, a.ctypes.data_as(ctypes.c_void_p)
 
 
-def format_result_txt(xx, yy, zz, t, scale=1e6) -> bytes:
+def format_result_txt(xx, yy, zz, t, scale=1e6, out=None):
     """The text of the reference's T_sssss.TXT for node arrays xx, yy, zz
     and the field t: per node x, y, z, t * scale in Fortran format
-    (e12.5, 2x, e12.5, 2x, e12.5, 2x, e12.5), 55 bytes per line."""
+    (e12.5, 2x, e12.5, 2x, e12.5, 2x, e12.5), 55 bytes per line.  Returns
+    bytes, or fills and returns `out` (a uint8 array of 55 * N bytes)."""
     lib = L.load_library()
     arrs = [_host_f64(a) for a in (xx, yy, zz, t)]
     n = arrs[0][0].size
-    buf = ctypes.create_string_buffer(55 * n)
-    L.check(lib.vdr_format_result_txt(buf, n, *(p for _, p in arrs), float(scale)),
+    buf = out if out is not None else np.empty(55 * n, dtype=np.uint8)
+    if buf.dtype != np.uint8 or buf.size != 55 * n or not buf.flags.c_contiguous:
+        raise ValueError("out must be a contiguous uint8 array of 55 * N bytes")
+    L.check(lib.vdr_format_result_txt(buf.ctypes.data_as(ctypes.c_void_p), n,
+                                      *(p for _, p in arrs), float(scale)),
             "vdr_format_result_txt")
-    return buf.raw[:55 * n]
+    return buf if out is not None else buf.tobytes()
 
 
 def write_result_txt(directory, step, xx, yy, zz, t, scale=1e6):
