@@ -11,7 +11,9 @@ the oracle assembled and solved on all host cores.
 * the mixed-precision step (FP32 inner solves) at the FP64 tolerance, its
   true residual recomputed by the oracle;
 * the 64-right-hand-side block solve at its full size (128 x 128 x 64):
-  every column's true residual recomputed by the oracle.
+  every column's true residual recomputed by the oracle;
+* the 256-mesh segmented solve at its full size (8.17M elements): every
+  mesh's true residual recomputed by the oracle.
 """
 import os
 
@@ -143,3 +145,37 @@ def test_fullsize_block_solve_residuals(oracle, gpu_lib, vdr):
         ax = oracle.matvec0_omp(m.iss, bb, prob.bc, ce, co, X[:, k], nthreads=nt)
         r = B[:, k] - ax
         assert np.linalg.norm(r) <= 1.01e-8 * np.linalg.norm(B[:, k]), k
+
+
+def test_fullsize_segmented_meshes_residuals(oracle, gpu_lib, vdr):
+    """The C4b form at full size: 256 cubes with edges of 8..48 elements
+    (8.17M elements in all) in one segmented solve to 1e-8; every mesh's
+    FP64 true residual, recomputed by the oracle on the union's BB, at
+    1e-8."""
+    import torch
+    P = vdr.problems
+    probs = P.cube_batch(256, seed=2001, nmin=8, nmax=48)
+    union = P.concat(probs)
+    m = union.mesh
+    aH, aM = 2.0, 3.0 / (COURANT / 32.0)
+    nt = os.cpu_count() or 1
+    with vdr.Solver(union, vdr.Options(apply_mode="stored"), aH=aH, aM=aM) as s:
+        s.set_segments(m.node_off)
+        b = torch.as_tensor(s.assemble_rhs(3.0, 0.0, None), device="cuda")
+        x = torch.zeros_like(b)
+        torch.cuda.synchronize()
+        its, errs, sts, st = s.solve_segmented_device(b, x, tol=1e-8, itmax=5000)
+        torch.cuda.synchronize()
+        X, B = x.cpu().numpy(), b.cpu().numpy()
+    assert st == 0 and np.all(sts == 0) and np.all(errs <= 1e-8)
+    bb, _, _ = oracle.assemble(union.variant, m.xx, m.yy, m.zz, m.iss, union.vel,
+                               union.lam, union.pdec, union.q, kod=m.kod,
+                               robin_alpha=union.robin_alpha, aH=aH, aM=aM,
+                               want_b=False, want_diag=False, nthreads=nt)
+    c, nc = oracle.greedy_colors(m.iss, m.nnode)
+    ce, co = oracle.color_lists(c, nc)
+    r = B - oracle.matvec0_omp(m.iss, bb, union.bc, ce, co, X, nthreads=nt)
+    off = m.node_off
+    for k in range(len(probs)):
+        rk, bk = r[off[k]:off[k + 1]], B[off[k]:off[k + 1]]
+        assert np.linalg.norm(rk) <= 1.01e-8 * np.linalg.norm(bk), k
