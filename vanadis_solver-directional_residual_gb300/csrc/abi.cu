@@ -196,7 +196,8 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
     if ((bad & 1) && df) h.storage = VDR_STORE_FP64;
   }
   if (need_op) {
-    if ((e = launch_diag_fix(h.diag, h.dinv, h.mask, h.N, h.stream)))
+    if ((e = launch_diag_fix(h.diag, h.dinv, h.mask, h.N, h.stream)) ||
+        (e = launch_emask(h)))
       return cuda_fail(e, "diag");
     h.op64_valid = true;
     h.diag_valid = true;
@@ -296,7 +297,7 @@ int upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
 void free_handle(Handle &h) {
   dfree(h.xx); dfree(h.yy); dfree(h.zz);
   dfree(h.xx32); dfree(h.yy32); dfree(h.zz32);
-  dfree(h.conn); dfree(h.mask);
+  dfree(h.conn); dfree(h.mask); dfree(h.emask);
   dfree(h.vel); dfree(h.lam); dfree(h.pdec); dfree(h.q);
   dfree(h.vel32); dfree(h.lam32); dfree(h.pdec32); dfree(h.robin);
   dfree(h.A64); dfree(h.A32); dfree(h.diag); dfree(h.dinv);

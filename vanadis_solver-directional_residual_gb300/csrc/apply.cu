@@ -4,7 +4,10 @@
 // y = P A P x with A = sum_e A_e (never assembled): one thread per element
 // gathers x at its 8 nodes (Dirichlet columns read as 0 through the sign
 // bit of the connectivity), multiplies by the element's 8x8 block and adds
-// the 8 results into y.  Same operation as matvec_0 / mttvec_0
+// the 8 results into y.  The FP32-vector apply and BiCG's fused pass form
+// the node numbers from the element number on the canonical structured
+// numbering (ConnView: 1 byte of Dirichlet bits per element instead of 32
+// bytes of connectivity).  Same operation as matvec_0 / mttvec_0
 // (vanadis_full_DR_OpenMP_timing.for:1837-1933) and MATVEC_C_cu /
 // MTTVEC_C_cu (src_v2026_2_1/cudatest.cu:184-227).
 //
@@ -143,22 +146,20 @@ __global__ void __launch_bounds__(256) stored_apply_f32(
 // y += A x with x gathered as float and the outputs scattered with FP32
 // atomics (or plain adds within a colour) -- no float<->double conversions,
 // which GB300 runs on its FP64 pipe.
-template <bool ATOMIC>
+template <bool ATOMIC, bool STRUCT>
 __global__ void __launch_bounds__(256) stored_apply_f32v(
-    const float4 *__restrict__ A, const int *__restrict__ conn, int E, int p0,
+    const float4 *__restrict__ A, const ConnView cv, int E, int p0,
     int p1, const float *__restrict__ x, float *__restrict__ y, const int *skip,
     const int *skip2) {
   if (skip && *(volatile const int *)skip) return;
   if (skip2 && *(volatile const int *)skip2) return;
   for (long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x; p < p1;
        p += (long)gridDim.x * blockDim.x) {
-    int c[8];
+    ElemNodes<STRUCT> c;
     float xv[8];
+    c.load(cv, E, p);
 #pragma unroll
-    for (int s = 0; s < 8; s++) {
-      c[s] = __ldg(conn + (size_t)s * E + p);
-      xv[s] = c[s] < 0 ? 0.f : __ldg(x + c[s]);
-    }
+    for (int s = 0; s < 8; s++) xv[s] = c[s] < 0 ? 0.f : __ldg(x + c[s]);
 #pragma unroll
     for (int i = 0; i < 8; i++) {
       const float4 a0 = __ldcs(A + (size_t)(2 * i) * E + p);
@@ -182,14 +183,13 @@ __global__ void __launch_bounds__(256) stored_apply_f32v(
 // drops from 64 FMA to 8 adds, so the kernel is bound by HBM.
 // Elements whose gathered x leaves the FP32 exponent range (|x| >= 2^128)
 // are redone here in FP64 from the merged pairs, gather and scatter included.
+template <typename Nodes>
 __device__ __noinline__ void df_element_fallback(
     const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
-    const int *__restrict__ conn, int E, long p, bool trans, bool atomic,
+    const Nodes &c, int E, long p, bool trans, bool atomic,
     const double *__restrict__ x, double *__restrict__ y) {
-  int c[8];
   double xv[8], out[8];
   for (int s = 0; s < 8; s++) {
-    c[s] = conn[(size_t)s * E + p];
     xv[s] = c[s] < 0 ? 0.0 : x[c[s]];
     out[s] = 0.0;
   }
@@ -216,10 +216,10 @@ __device__ __noinline__ void df_element_fallback(
     }
 }
 
-template <bool TRANS, bool ATOMIC>
+template <bool TRANS, bool ATOMIC, bool STRUCT>
 __global__ void __launch_bounds__(256, 4) stored_apply_df(
     const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
-    const int *__restrict__ conn, int E, int p0, int p1,
+    const ConnView cv, int E, int p0, int p1,
     const double *__restrict__ x, double *__restrict__ y, const int *skip,
     const int *skip2, ElemGate gate) {
   if (skip && *(volatile const int *)skip) return;
@@ -227,14 +227,14 @@ __global__ void __launch_bounds__(256, 4) stored_apply_df(
   for (long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x; p < p1;
        p += (long)gridDim.x * blockDim.x) {
     if (gate.active && !gate.active[__ldg(gate.eseg + p)]) continue;
-    int c[8];
+    ElemNodes<STRUCT> c;
     double xv[8];
     float xh[8], xl[8];
     bool bad = false;
     int emax = 0;
+    c.load(cv, E, p);
 #pragma unroll
     for (int s = 0; s < 8; s++) {
-      c[s] = __ldg(conn + (size_t)s * E + p);
       xv[s] = c[s] < 0 ? 0.0 : __ldg(x + c[s]);
       emax = max(emax, df_exp(xv[s]));
     }
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(256, 4) stored_apply_df(
 #pragma unroll
     for (int s = 0; s < 8; s++) df_split(xv[s], xh[s], xl[s], bad, shift);
     if (bad) {
-      df_element_fallback(Ahi, Alo, conn, E, p, TRANS, ATOMIC, x, y);
+      df_element_fallback(Ahi, Alo, c, E, p, TRANS, ATOMIC, x, y);
       continue;
     }
     if (!TRANS) {
@@ -318,25 +318,25 @@ __global__ void __launch_bounds__(256, 4) stored_apply_df(
 // of A x1 are scattered as they complete, the columns of A^T x2 accumulate
 // in registers.  Elements with an input outside the FP32 range take the
 // FP64 fallback for both products.
-template <bool ATOMIC>
+template <bool ATOMIC, bool STRUCT>
 __global__ void __launch_bounds__(256, 2) stored_apply_df_both(
     const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
-    const int *__restrict__ conn, int E, int p0, int p1,
+    const ConnView cv, int E, int p0, int p1,
     const double *__restrict__ x1, double *__restrict__ y1,
     const double *__restrict__ x2, double *__restrict__ y2, const int *skip) {
   if (skip && *(volatile const int *)skip) return;
   for (long p = p0 + (long)blockIdx.x * blockDim.x + threadIdx.x; p < p1;
        p += (long)gridDim.x * blockDim.x) {
-    int c[8];
+    ElemNodes<STRUCT> c;
     float ah[8], al[8], bh[8], bl[8];
     bool bad = false;
     int sa, sb;
     {
       double va[8], vb[8];
       int ea = 0, eb = 0;
+      c.load(cv, E, p);
 #pragma unroll
       for (int s = 0; s < 8; s++) {
-        c[s] = __ldg(conn + (size_t)s * E + p);
         va[s] = c[s] < 0 ? 0.0 : __ldg(x1 + c[s]);
         vb[s] = c[s] < 0 ? 0.0 : __ldg(x2 + c[s]);
         ea = max(ea, df_exp(va[s]));
@@ -351,8 +351,8 @@ __global__ void __launch_bounds__(256, 2) stored_apply_df_both(
       }
     }
     if (bad) {
-      df_element_fallback(Ahi, Alo, conn, E, p, false, ATOMIC, x1, y1);
-      df_element_fallback(Ahi, Alo, conn, E, p, true, ATOMIC, x2, y2);
+      df_element_fallback(Ahi, Alo, c, E, p, false, ATOMIC, x1, y1);
+      df_element_fallback(Ahi, Alo, c, E, p, true, ATOMIC, x2, y2);
       continue;
     }
     DfAcc acc2[8];
@@ -501,6 +501,19 @@ __global__ void mask_conn_kernel(int *__restrict__ conn, long total,
   }
 }
 
+// Per-element Dirichlet bits from the connectivity table's flags.
+__global__ void emask_kernel(const int *__restrict__ conn, int E,
+                             unsigned char *__restrict__ emask) {
+  for (long p = (long)blockIdx.x * blockDim.x + threadIdx.x; p < E;
+       p += (long)gridDim.x * blockDim.x) {
+    unsigned m = 0u;
+#pragma unroll
+    for (int s = 0; s < 8; s++)
+      if (__ldg(conn + (size_t)s * E + p) < 0) m |= 1u << s;
+    emask[p] = (unsigned char)m;
+  }
+}
+
 __global__ void diag_fix_kernel(double *__restrict__ d, double *__restrict__ dinv,
                                 const unsigned char *__restrict__ m, int N) {
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
@@ -555,6 +568,7 @@ cudaError_t launch_stored_apply32v(const Handle &h, const float *x, float *y,
                                    const int *skip, const int *skip2,
                                    cudaStream_t s) {
   const bool color = h.scatter == VDR_SCATTER_COLOR;
+  const ConnView cv = conn_view(h);
   const int nranges = color ? h.ncolors : 1;
   for (int r = 0; r < nranges; r++) {
     const int p0 = color ? h.color_off[r] : 0;
@@ -562,11 +576,14 @@ cudaError_t launch_stored_apply32v(const Handle &h, const float *x, float *y,
     if (p1 <= p0) continue;
     const int grid = grid_for(p1 - p0, 256, 8);
     if (color)
-      stored_apply_f32v<false><<<grid, 256, 0, s>>>(h.A32v, h.conn, h.E, p0, p1, x, y,
-                                                    skip, skip2);
+      stored_apply_f32v<false, false><<<grid, 256, 0, s>>>(h.A32v, cv, h.E, p0, p1, x, y,
+                                                           skip, skip2);
+    else if (cv.emask)
+      stored_apply_f32v<true, true><<<grid, 256, 0, s>>>(h.A32v, cv, h.E, p0, p1, x, y,
+                                                         skip, skip2);
     else
-      stored_apply_f32v<true><<<grid, 256, 0, s>>>(h.A32v, h.conn, h.E, p0, p1, x, y,
-                                                   skip, skip2);
+      stored_apply_f32v<true, false><<<grid, 256, 0, s>>>(h.A32v, cv, h.E, p0, p1, x, y,
+                                                          skip, skip2);
     count_launches(1);
   }
   return cudaGetLastError();
@@ -581,6 +598,7 @@ cudaError_t launch_apply_both(const Handle &h, const double *x1, double *y1,
                               const double *x2, double *y2, const int *skip,
                               cudaStream_t s) {
   const bool color = h.scatter == VDR_SCATTER_COLOR;
+  const ConnView cv = conn_view(h);
   const int nranges = color ? h.ncolors : 1;
   for (int r = 0; r < nranges; r++) {
     const int p0 = color ? h.color_off[r] : 0;
@@ -588,11 +606,14 @@ cudaError_t launch_apply_both(const Handle &h, const double *x1, double *y1,
     if (p1 <= p0) continue;
     const int grid = grid_for(p1 - p0, 256, 6);
     if (color)
-      stored_apply_df_both<false><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, h.conn, h.E, p0, p1,
-                                                       x1, y1, x2, y2, skip);
+      stored_apply_df_both<false, false><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, cv, h.E, p0,
+                                                              p1, x1, y1, x2, y2, skip);
+    else if (cv.emask)
+      stored_apply_df_both<true, true><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, cv, h.E, p0, p1,
+                                                            x1, y1, x2, y2, skip);
     else
-      stored_apply_df_both<true><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, h.conn, h.E, p0, p1,
-                                                      x1, y1, x2, y2, skip);
+      stored_apply_df_both<true, false><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, cv, h.E, p0,
+                                                             p1, x1, y1, x2, y2, skip);
     count_launches(1);
   }
   return cudaGetLastError();
@@ -620,6 +641,7 @@ cudaError_t launch_rhs_from_mass(Handle &h, double cf, double rM, const double *
   if ((e = cudaMemsetAsync(h.rhs_tmp, 0, sizeof(double) * 2 * (size_t)h.N, s))) return e;
   if ((e = launch_apply(h, false, t, y1, nullptr, nullptr, s))) return e;
   const bool color = h.scatter == VDR_SCATTER_COLOR;
+  const ConnView cv = conn_view(h);
   const int nranges = color ? h.ncolors : 1;
   for (int r = 0; r < nranges; r++) {
     const int p0 = color ? h.color_off[r] : 0;
@@ -627,11 +649,11 @@ cudaError_t launch_rhs_from_mass(Handle &h, double cf, double rM, const double *
     if (p1 <= p0) continue;
     const int grid = grid_for(p1 - p0, 256, 8);
     if (color)
-      stored_apply_df<false, false><<<grid, 256, 0, s>>>(h.Mhi, h.Mlo, h.conn, h.E, p0, p1, t,
-                                                         y2, nullptr, nullptr, ElemGate{});
+      stored_apply_df<false, false, false><<<grid, 256, 0, s>>>(
+          h.Mhi, h.Mlo, cv, h.E, p0, p1, t, y2, nullptr, nullptr, ElemGate{});
     else
-      stored_apply_df<false, true><<<grid, 256, 0, s>>>(h.Mhi, h.Mlo, h.conn, h.E, p0, p1, t,
-                                                        y2, nullptr, nullptr, ElemGate{});
+      stored_apply_df<false, true, false><<<grid, 256, 0, s>>>(
+          h.Mhi, h.Mlo, cv, h.E, p0, p1, t, y2, nullptr, nullptr, ElemGate{});
     count_launches(1);
   }
   rhs_combine_kernel<<<grid_for(h.N, 256, 8), 256, 0, s>>>(
@@ -652,6 +674,7 @@ cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
                                 const double *x, double *y, const int *skip,
                                 const int *skip2, cudaStream_t s) {
   const bool color = h.scatter == VDR_SCATTER_COLOR;
+  const ConnView cv = conn_view(h);
   const int nranges = color ? h.ncolors : 1;
   for (int r = 0; r < nranges; r++) {
     const int p0 = color ? h.color_off[r] : 0;
@@ -662,14 +685,18 @@ cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
   K<<<grid, 256, 0, s>>>(AP, h.conn, h.E, p0, p1, x, y, skip, skip2)
     if (!fp32 && h.storage == VDR_STORE_DF) {
 #define VDR_LAUNCH_DF(K)                                                      \
-  K<<<grid, 256, 0, s>>>(h.Ahi, h.Alo, h.conn, h.E, p0, p1, x, y, skip, skip2, \
+  K<<<grid, 256, 0, s>>>(h.Ahi, h.Alo, cv, h.E, p0, p1, x, y, skip, skip2,      \
                          ElemGate{h.gate_eseg, h.gate_active})
+      // The double-float apply reads the connectivity table even on the
+      // structured numbering: without its 32 B per element the kernel kept
+      // the same time (0.782 vs 0.786 ms at 8.4M elements) -- fewer bytes in
+      // flight per element, lower bandwidth -- while the FP32 applies gain.
       if (transpose) {
-        if (color) VDR_LAUNCH_DF((stored_apply_df<true, false>));
-        else VDR_LAUNCH_DF((stored_apply_df<true, true>));
+        if (color) VDR_LAUNCH_DF((stored_apply_df<true, false, false>));
+        else VDR_LAUNCH_DF((stored_apply_df<true, true, false>));
       } else {
-        if (color) VDR_LAUNCH_DF((stored_apply_df<false, false>));
-        else VDR_LAUNCH_DF((stored_apply_df<false, true>));
+        if (color) VDR_LAUNCH_DF((stored_apply_df<false, false, false>));
+        else VDR_LAUNCH_DF((stored_apply_df<false, true, false>));
       }
 #undef VDR_LAUNCH_DF
     } else if (!fp32) {
@@ -724,6 +751,34 @@ cudaError_t launch_legacy_conn(const int *iss_ref, int E, int N, const int *bc,
                                int *conn, int *bad, cudaStream_t s) {
   legacy_conn_kernel<<<grid_for((long)E * 8, 256, 16), 256, 0, s>>>(
       iss_ref, E, N, bc, conn, bad);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+ConnView conn_view(const Handle &h) {
+  ConnView v;
+  v.conn = h.conn;
+  if (h.emask && h.nax > 1 && h.nay > 1 && h.naz > 1 && !h.perm_d &&
+      h.scatter != VDR_SCATTER_COLOR) {
+    v.emask = h.emask;
+    v.nex = h.nax - 1;
+    v.ney = h.nay - 1;
+    v.nax = h.nax;
+    v.pl = h.nax * h.nay;
+  }
+  return v;
+}
+
+// The per-element Dirichlet bits of a mesh in the canonical structured
+// numbering (natural order), rebuilt with every operator build so that
+// they follow vdr_set_dirichlet.
+cudaError_t launch_emask(Handle &h) {
+  if (!(h.nax > 1 && h.nay > 1 && h.naz > 1) || h.perm_d ||
+      h.scatter == VDR_SCATTER_COLOR || !h.conn)
+    return cudaSuccess;
+  cudaError_t e;
+  if (!h.emask && (e = cudaMalloc(&h.emask, (size_t)h.E))) return e;
+  emask_kernel<<<grid_for(h.E, 256, 8), 256, 0, h.stream>>>(h.conn, h.E, h.emask);
   count_launches(1);
   return cudaGetLastError();
 }

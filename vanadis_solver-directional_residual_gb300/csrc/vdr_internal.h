@@ -56,6 +56,53 @@ struct ElemGate {
   const int *active = nullptr;
 };
 
+// Element connectivity as the stored applies read it: the table (8 ints per
+// element, Dirichlet flag in bit 31) or, on the canonical structured
+// numbering in natural storage order, node numbers computed from the
+// element number (element i + nex (j + ney k) has nodes i + nax j + pl k +
+// {0, 1, 1 + nax, nax} and the same plus pl) with one byte of Dirichlet
+// flags per element (bit s: local node s) -- 1 byte read instead of 32.
+struct ConnView {
+  const int *conn = nullptr;
+  const unsigned char *emask = nullptr;  // structured when set
+  int nex = 0, ney = 0, nax = 0, pl = 0;
+};
+
+// The 8 node numbers (| MASK_BIT on Dirichlet nodes) of one element:
+// loaded from the table, or (STRUCT) formed on use from the element's first
+// node and its Dirichlet bits, which keeps 4 registers live instead of 8.
+template <bool STRUCT>
+struct ElemNodes;
+template <>
+struct ElemNodes<false> {
+  int c[8];
+  __device__ __forceinline__ void load(const ConnView &cv, int E, long p) {
+#pragma unroll
+    for (int s = 0; s < 8; s++) c[s] = __ldg(cv.conn + (size_t)s * E + p);
+  }
+  __device__ __forceinline__ int operator[](int s) const { return c[s]; }
+};
+template <>
+struct ElemNodes<true> {
+  int base, nax, pl;
+  unsigned m;
+  __device__ __forceinline__ void load(const ConnView &cv, int E, long p) {
+    const unsigned u = (unsigned)p, nx = (unsigned)cv.nex;
+    const unsigned r = u / nx, i = u - r * nx;
+    const unsigned k = r / (unsigned)cv.ney, j = r - k * (unsigned)cv.ney;
+    nax = cv.nax;
+    pl = cv.pl;
+    base = (int)i + nax * (int)j + pl * (int)k;
+    m = __ldg(cv.emask + p);
+  }
+  __device__ __forceinline__ int operator[](int s) const {
+    const int s2 = s & 3;
+    const int n = base + ((s2 == 1 || s2 == 2) ? 1 : 0) + ((s2 >> 1) ? nax : 0) +
+                  ((s >> 2) ? pl : 0);
+    return ((m >> s) & 1u) ? (n | MASK_BIT) : n;
+  }
+};
+
 // Element-wise fields, device pointers in storage order.
 struct Fields {
   const double *vel = nullptr;   // [3][E]
@@ -93,6 +140,7 @@ struct Handle {
   double *xx = nullptr, *yy = nullptr, *zz = nullptr;
   float *xx32 = nullptr, *yy32 = nullptr, *zz32 = nullptr;
   int *conn = nullptr;               // [8][E] 0-based | MASK_BIT
+  unsigned char *emask = nullptr;    // [E] Dirichlet bits per element (structured)
   std::vector<int> perm;             // storage position -> element id
   std::vector<int> color_off;        // colour c occupies [off[c], off[c+1])
   int ncolors = 0;
@@ -191,6 +239,11 @@ struct Handle {
   const void *gcr_key = nullptr;
   long gcr_cycle_launches = 0;
 };
+
+// The connectivity view of the stored applies (structured when the mesh
+// is in the canonical numbering, natural order and emask is built).
+ConnView conn_view(const Handle &h);
+cudaError_t launch_emask(Handle &h);
 
 // SM count of the current device, cached once (thread-safe).
 int device_sm_count();
