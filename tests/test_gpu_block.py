@@ -128,6 +128,35 @@ def test_block_apply_accumulate(vdr, oracle, gpu_lib, case, precision, K):
         assert rel_l2(Y[:, k], 2.0 * yref) < tol, k
 
 
+@pytest.mark.parametrize("variant", ["tile", "lsu"])
+def test_block_apply_ignores_dirichlet_entries(vdr, oracle, gpu_lib, case,
+                                               variant):
+    """Dirichlet rows of X read as zero whatever they hold (NaN, inf) and
+    Dirichlet rows of Y receive nothing (the accumulating call leaves them
+    as they were)."""
+    import torch
+    prob, aH, aM, bb = case
+    N, K = prob.mesh.nnode, 64
+    d = prob.bc == 1
+    X = np.random.default_rng(31).standard_normal((N, K)).astype(np.float32)
+    X[d, 0::2] = np.nan
+    X[d, 1::2] = np.inf
+    Y0 = np.zeros((N, K), dtype=np.float32)
+    Y0[d] = 7.0
+    with vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=aH, aM=aM) as s:
+        s.set_block_apply(variant)
+        Xd = to_dev(X, torch.float32)
+        Yd = to_dev(Y0, torch.float32)
+        s.apply_block_accumulate_device(Xd, Yd, "tf32x3")
+        torch.cuda.synchronize()
+        Y = Yd.cpu().numpy().astype(np.float64)
+    assert np.all(Y[d] == 7.0)
+    Xz = np.where(d[:, None], 0.0, X.astype(np.float64))
+    for k in (0, 1, K - 1):
+        yref, _ = oracle.matvec0(prob.mesh.iss, bb, prob.bc, Xz[:, k])
+        assert rel_l2(np.where(d, 0.0, Y[:, k]), yref) < TF32_TOL["tf32x3"], k
+
+
 def shuffled_elements(vdr, prob, seed):
     """The same problem with its elements in a random order (the node
     numbering is kept), so the mesh is no longer in the canonical structured

@@ -211,7 +211,8 @@ __global__ void __launch_bounds__(256) block_apply_tf32(
 // of each node.  Per element this reads and
 // adds about 2.5 node rows instead of 8 and 8.  The operator copy carries
 // the Dirichlet mask (zero rows and columns) and, in the block solve, the
-// Jacobi scale (see aos_build), so the kernel has no per-node work.  The
+// Jacobi scale (see aos_build); the kernel reads one mask byte per node row
+// so that Dirichlet rows of X read as zero and of Y receive nothing.  The
 // elements of a box are taken in the 8 parity classes of (i, j, k) (no two
 // elements of one class share a node), one element per warp per class with
 // a block barrier between classes, so the shared result tile needs no
@@ -249,7 +250,8 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src,
 template <bool SPLIT, int TILES, int TY, int HALVES>
 __global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
     const float *__restrict__ Aaos, int nax, int nay, int naz,
-    const float *__restrict__ X, float *__restrict__ Y, const int *skip) {
+    const unsigned char *__restrict__ mask, const float *__restrict__ X,
+    float *__restrict__ Y, const int *skip) {
   // KC columns per block (of the KR = HALVES * KC of a block-vector row)
   constexpr int KC = 16 * TILES, KR = KC * HALVES;
   constexpr int S = tile_row_stride<KC>(), C4 = KC / 4;
@@ -259,6 +261,7 @@ __global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
   constexpr int NV = LX * HP * LZ * C4;  // float4 slots of the node box
   constexpr int PER = (NV + NT - 1) / NT;
   static_assert(NT % C4 == 0, "a thread keeps its column chunk");
+  static_assert(PER <= 32, "one bit per slot");
   constexpr int RSTEP = NT / C4;         // box rows between a thread's slots
   if (skip && *(volatile const int *)skip) return;
   extern __shared__ __align__(16) float tile_sm[];
@@ -276,6 +279,7 @@ __global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
   const int c = threadIdx.x % C4, r0 = threadIdx.x / C4;
 
   // Node rows of the box into shared memory; the result tile zeroed.
+  unsigned live = 0u;  // bit u: slot u's node is in the mesh and not Dirichlet
 #pragma unroll
   for (int u = 0; u < PER; u++) {
     const int r = r0 + u * RSTEP;
@@ -288,6 +292,7 @@ __global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
       cp_async16(xs + row * S + 4 * c, X + n * KR + 4 * c, in ? 16u : 0u);
       *reinterpret_cast<float4 *>(ys + row * S + 4 * c) =
           make_float4(0.f, 0.f, 0.f, 0.f);
+      if (in && !(mask && __ldg(mask + n))) live |= 1u << u;
     }
   }
   asm volatile("cp.async.commit_group;" ::: "memory");
@@ -309,6 +314,18 @@ __global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
     }
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
+  // Dirichlet rows read as zero whatever X holds there (each thread clears
+  // the chunks it copied itself, so the barrier below publishes them); the
+  // block solve passes no mask: its X is zero on those rows already.
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int r = r0 + u * RSTEP;
+    if (mask && r < LX * HP * LZ && !((live >> u) & 1u)) {
+      const int li = r % LX, lj = (r / LX) % HP, lk = r / (LX * HP);
+      *reinterpret_cast<float4 *>(xs + (li + TILE_WP * (lj + HP * lk)) * S + 4 * c) =
+          make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
   __syncthreads();
 
   // The contractions, one parity class at a time.
@@ -367,19 +384,17 @@ __global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
     __syncthreads();
   }
 
-  // The result tile into Y.
+  // The result tile into Y (Dirichlet nodes receive nothing).
 #pragma unroll
   for (int u = 0; u < PER; u++) {
     const int r = r0 + u * RSTEP;
-    if (r < LX * HP * LZ) {
+    if (r < LX * HP * LZ && ((live >> u) & 1u)) {
       const int li = r % LX, lj = (r / LX) % HP, lk = r / (LX * HP);
       const int gx = gx0 + li, gy = gy0 + lj, gz = gz0 + lk;
-      if (gx < nax && gy < nay && gz < naz) {
-        const int row = li + TILE_WP * (lj + HP * lk);
-        const size_t n = gx + (size_t)nax * (gy + (size_t)nay * gz);
-        atomicAdd(reinterpret_cast<float4 *>(Y + n * KR) + c,
-                  *reinterpret_cast<const float4 *>(ys + row * S + 4 * c));
-      }
+      const int row = li + TILE_WP * (lj + HP * lk);
+      const size_t n = gx + (size_t)nax * (gy + (size_t)nay * gz);
+      atomicAdd(reinterpret_cast<float4 *>(Y + n * KR) + c,
+                *reinterpret_cast<const float4 *>(ys + row * S + 4 * c));
     }
   }
 }
@@ -1216,7 +1231,7 @@ int grid_n(long n, int threads, int per_sm) {
 // dynamic shared memory above 48 KB is opted into once per device.
 template <bool SPLIT, int TILES, int TY, int HALVES>
 void launch_tile(const Handle &h, const float *A, const float *X, float *Y,
-                 const int *skip, cudaStream_t s) {
+                 const int *skip, const unsigned char *mask, cudaStream_t s) {
   constexpr int smem = tile_smem_bytes<TY, 16 * TILES>();
   static std::atomic<unsigned> opted{0u};
   int dev = 0;
@@ -1231,22 +1246,23 @@ void launch_tile(const Handle &h, const float *A, const float *X, float *Y,
                      ((h.naz - 2) / TILE_Z + 1);
   block_apply_tile<SPLIT, TILES, TY, HALVES>
       <<<(unsigned)(tiles * HALVES), 64 * TY, smem, s>>>(A, h.nax, h.nay, h.naz,
-                                                         X, Y, skip);
+                                                         mask, X, Y, skip);
 }
 
 // K = 64 runs as two column halves of 32 (measured: more resident blocks
 // per SM beat the second operator-fragment load, 0.43 vs 0.51 ms per C4a
 // apply); TILE_Y = 2 (4 warps, 8 x 2 x 2 elements) measured ahead of 4.
 void launch_tile_k(const Handle &h, int K, bool split, const float *A,
-                   const float *X, float *Y, const int *skip, cudaStream_t s) {
+                   const float *X, float *Y, const int *skip,
+                   const unsigned char *mask, cudaStream_t s) {
   if (split) {
-    if (K == 16) launch_tile<true, 1, TILE_Y, 1>(h, A, X, Y, skip, s);
-    else if (K == 32) launch_tile<true, 2, TILE_Y, 1>(h, A, X, Y, skip, s);
-    else launch_tile<true, 2, TILE_Y, 2>(h, A, X, Y, skip, s);
+    if (K == 16) launch_tile<true, 1, TILE_Y, 1>(h, A, X, Y, skip, mask, s);
+    else if (K == 32) launch_tile<true, 2, TILE_Y, 1>(h, A, X, Y, skip, mask, s);
+    else launch_tile<true, 2, TILE_Y, 2>(h, A, X, Y, skip, mask, s);
   } else {
-    if (K == 16) launch_tile<false, 1, TILE_Y, 1>(h, A, X, Y, skip, s);
-    else if (K == 32) launch_tile<false, 2, TILE_Y, 1>(h, A, X, Y, skip, s);
-    else launch_tile<false, 2, TILE_Y, 2>(h, A, X, Y, skip, s);
+    if (K == 16) launch_tile<false, 1, TILE_Y, 1>(h, A, X, Y, skip, mask, s);
+    else if (K == 32) launch_tile<false, 2, TILE_Y, 1>(h, A, X, Y, skip, mask, s);
+    else launch_tile<false, 2, TILE_Y, 2>(h, A, X, Y, skip, mask, s);
   }
 }
 
@@ -1256,7 +1272,7 @@ void launch_tile_k(const Handle &h, int K, bool split, const float *A,
 int block_apply_launches_tf32(const Handle &h, int K, bool split,
                               const float *X, const float *dscale, float *Y,
                               const float4 *Aaos, const int *skip,
-                              cudaStream_t s) {
+                              cudaStream_t s, bool x_clean) {
   const float *A = reinterpret_cast<const float *>(Aaos);
   // The node-tile apply needs the canonical structured numbering in storage
   // order (not the colour permutation), and any scale folded into the
@@ -1264,7 +1280,7 @@ int block_apply_launches_tf32(const Handle &h, int K, bool split,
   if (!h.block_tma && h.block_tile && h.nax > 1 && h.nay > 1 && h.naz > 1 &&
       !h.perm_d && !dscale && !(reinterpret_cast<uintptr_t>(X) & 15) &&
       !(reinterpret_cast<uintptr_t>(Y) & 15)) {
-    launch_tile_k(h, K, split, A, X, Y, skip, s);
+    launch_tile_k(h, K, split, A, X, Y, skip, x_clean ? nullptr : h.mask, s);
     count_launches(1);
     return cudaGetLastError() == cudaSuccess ? VDR_OK : VDR_CUDA_ERROR;
   }
@@ -1500,11 +1516,11 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
     for (int it = 0; it < KI; it++) {
       bb_p<<<gv, BT, 0, s>>>(a);
       block_apply_launches_tf32(h, K, split, a.p, nullptr, a.v, Aaos,
-                                &st->done, s);
+                                &st->done, s, true);
       bb_alpha<<<gv, BT, 0, s>>>(a);
       bb_s<<<gv, BT, 0, s>>>(a);
       block_apply_launches_tf32(h, K, split, a.s, nullptr, a.t, Aaos,
-                                &st->done, s);
+                                &st->done, s, true);
       bb_omega<<<gv, BT, 0, s>>>(a);
       bb_xr<<<gv, BT, 0, s>>>(a);
       bb_tail<<<1, 64, 0, s>>>(a);

@@ -86,14 +86,21 @@ void parallel_lines(long n, F &&line) {
   if ((long)nt > n) nt = n > 0 ? (unsigned)n : 1u;
   std::vector<std::thread> pool;
   const long chunk = (n + nt - 1) / nt;
+  long inline_from = n;  // chunks no thread could be started for
   for (unsigned k = 1; k < nt; k++) {
     const long i0 = k * chunk, i1 = std::min(n, i0 + chunk);
-    if (i0 < i1)
+    if (i0 >= i1) break;
+    try {
       pool.emplace_back([=, &line] {
         for (long i = i0; i < i1; i++) line(i);
       });
+    } catch (...) {
+      inline_from = i0;
+      break;
+    }
   }
   for (long i = 0; i < std::min(n, chunk); i++) line(i);
+  for (long i = inline_from; i < n; i++) line(i);
   for (auto &t : pool) t.join();
 }
 
@@ -158,7 +165,13 @@ int vdr_write_result_txt(const char *dir, int step, long nnode,
     set_error("vdr_write_result_txt: bad arguments (step 0..99999)");
     return VDR_BAD_ARGUMENT;
   }
-  std::vector<char> buf((size_t)nnode * LINE4);
+  std::vector<char> buf;
+  try {
+    buf.resize((size_t)nnode * LINE4);
+  } catch (...) {
+    set_error("vdr_write_result_txt: out of host memory");
+    return VDR_IO_ERROR;
+  }
   int st = vdr_format_result_txt(buf.data(), nnode, xx, yy, zz, t, scale);
   if (st) return st;
   char name[32];
@@ -177,6 +190,12 @@ int vdr_write_slices_txt(const char *dir, int step, int nax, int nay, int naz,
   }
   const long x = nax, y = nay, z = naz;
   std::vector<char> buf;
+  try {
+    buf.reserve((size_t)std::max(x * y, std::max(x * z, y * z)) * LINE3);
+  } catch (...) {
+    set_error("vdr_write_slices_txt: out of host memory");
+    return VDR_IO_ERROR;
+  }
   char name[32];
   // X_: plane j = 1..x, nodes x (i - 1) + j for i = 1..y z: (y, z, s)
   for (long j = 1; j <= x; j++) {

@@ -371,10 +371,12 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
                        double *errs_host);
 cudaError_t launch_block_apply64(const Handle &h, int K, const double *X,
                                  double *Y, cudaStream_t s);
+// x_clean: X is known to be zero on Dirichlet rows (the block solve's
+// vectors), so the node-tile apply skips its mask reads.
 int block_apply_launches_tf32(const Handle &h, int K, bool split,
                               const float *X, const float *dscale, float *Y,
                               const float4 *Aaos, const int *skip,
-                              cudaStream_t s);
+                              cudaStream_t s, bool x_clean = false);
 cudaError_t launch_block_rhs(const Handle &h, const double *phi, int K,
                              const double *Q, double cf, double *B,
                              cudaStream_t s);
