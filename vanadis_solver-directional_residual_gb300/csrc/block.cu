@@ -278,11 +278,14 @@ __global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
   const int g = lane >> 2, t = lane & 3;
   const int c = threadIdx.x % C4, r0 = threadIdx.x / C4;
 
-  // Node rows of the box into shared memory; the result tile zeroed.
-  unsigned live = 0u;  // bit u: slot u's node is in the mesh and not Dirichlet
+  // Node rows of the box into shared memory; the result tile zeroed; the
+  // slots' mask bytes loaded (all in flight before any is used).
+  unsigned inmesh = 0u;  // bit u: slot u's node is in the mesh
+  unsigned char mk[PER];
 #pragma unroll
   for (int u = 0; u < PER; u++) {
     const int r = r0 + u * RSTEP;
+    mk[u] = 0;
     if (r < LX * HP * LZ) {
       const int li = r % LX, lj = (r / LX) % HP, lk = r / (LX * HP);
       const int gx = gx0 + li, gy = gy0 + lj, gz = gz0 + lk;
@@ -292,7 +295,10 @@ __global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
       cp_async16(xs + row * S + 4 * c, X + n * KR + 4 * c, in ? 16u : 0u);
       *reinterpret_cast<float4 *>(ys + row * S + 4 * c) =
           make_float4(0.f, 0.f, 0.f, 0.f);
-      if (in && !(mask && __ldg(mask + n))) live |= 1u << u;
+      if (in) {
+        inmesh |= 1u << u;
+        if (mask) mk[u] = __ldg(mask + n);
+      }
     }
   }
   asm volatile("cp.async.commit_group;" ::: "memory");
@@ -313,6 +319,10 @@ __global__ void __launch_bounds__(64 * TY, 8 / TY) block_apply_tile(
       fa[ph][1] = __ldg(a + 4);
     }
   }
+  unsigned live = inmesh;  // bit u: in the mesh and not Dirichlet
+#pragma unroll
+  for (int u = 0; u < PER; u++)
+    if (mk[u]) live &= ~(1u << u);
   asm volatile("cp.async.wait_group 0;" ::: "memory");
   // Dirichlet rows read as zero whatever X holds there (each thread clears
   // the chunks it copied itself, so the barrier below publishes them); the
