@@ -490,8 +490,8 @@ LEARN_TILT = 0.5
 
 
 def dropin_section(vdr, s, prob, cf, rM):
-    """The reference's own solve entry at C2: kernel_dbcg_simple_ called with
-    host arrays as VANADIS.FOR:809 calls it -- B, X, BB (64E doubles, 4.3 GB),
+    """The reference's own solve entry on the 256x256x128 step:
+    kernel_dbcg_simple_ called with host arrays as VANADIS.FOR:809 calls it -- B, X, BB (64E doubles, 4.3 GB),
     ISS, DIAG and bc uploaded and X downloaded on every call -- on the
     GPU-built theta-step operator, exported once in the reference's BB layout
     (vdr_get_element_matrices); Jacobi-preconditioned BiCG, the reference's

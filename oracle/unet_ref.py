@@ -2,9 +2,9 @@
 INFRASTRUCTURE ONLY: the gradient and forward checks of the GPU kernels
 import it; the product never does).
 
-The network has no counterpart in the reference code base: it is this
-build's preconditioner for the reference's solve (north-star "learned
-parts").  This module restates it in float64 PyTorch on the CPU with
+The network has no counterpart in the reference code base: it is the
+library's learned preconditioner for the reference's solve (a 3-level 3-D
+U-Net, 16/32/64 channels).  This module restates it in float64 PyTorch on the CPU with
 autograd supplying the gradients, and emulates the GPU's BF16 storage
 (weights and every stored activation rounded to BF16, nearest-even), so
 that the only differences left are FP32 accumulation order and the BF16

@@ -94,7 +94,7 @@ def test_fullsize_linearity_and_adjoint(gpu_lib, full):
 
 
 def test_fullsize_mixed_precision_step(oracle, gpu_lib, vdr, full):
-    """The C3 form at full size: FP64 refinement around FP32 inner solves
+    """Mixed precision at full size: FP64 refinement around FP32 inner solves
     reaches the FP64 true residual 1e-8 as the oracle measures it (its
     matvec_0 on its own BB), next to the FP64 solution."""
     prob = full["prob"]
@@ -114,7 +114,7 @@ def test_fullsize_mixed_precision_step(oracle, gpu_lib, vdr, full):
 
 
 def test_fullsize_block_solve_residuals(oracle, gpu_lib, vdr):
-    """The C4a form at full size: 128 x 128 x 64 elements, K = 64 Gaussian
+    """Many right-hand sides at full size: 128 x 128 x 64 elements, K = 64 Gaussian
     sources, the refined block solve on the tensor-core block apply; every
     column's FP64 true residual, recomputed by the oracle, at 1e-8."""
     import torch
@@ -148,7 +148,7 @@ def test_fullsize_block_solve_residuals(oracle, gpu_lib, vdr):
 
 
 def test_fullsize_segmented_meshes_residuals(oracle, gpu_lib, vdr):
-    """The C4b form at full size: 256 cubes with edges of 8..48 elements
+    """Many meshes at full size: 256 cubes with edges of 8..48 elements
     (8.17M elements in all) in one segmented solve to 1e-8; every mesh's
     FP64 true residual, recomputed by the oracle on the union's BB, at
     1e-8."""

@@ -1260,8 +1260,9 @@ void launch_tile(const Handle &h, const float *A, const float *X, float *Y,
 }
 
 // K = 64 runs as two column halves of 32 (measured: more resident blocks
-// per SM beat the second operator-fragment load, 0.43 vs 0.51 ms per C4a
-// apply); TILE_Y = 2 (4 warps, 8 x 2 x 2 elements) measured ahead of 4.
+// per SM beat the second operator-fragment load, 0.43 vs 0.51 ms per
+// apply at 1M elements); TILE_Y = 2 (4 warps, 8 x 2 x 2 elements) measured
+// ahead of 4.
 void launch_tile_k(const Handle &h, int K, bool split, const float *A,
                    const float *X, float *Y, const int *skip,
                    const unsigned char *mask, cudaStream_t s) {
