@@ -4,10 +4,9 @@
 // y = P A P x with A = sum_e A_e (never assembled): one thread per element
 // gathers x at its 8 nodes (Dirichlet columns read as 0 through the sign
 // bit of the connectivity), multiplies by the element's 8x8 block and adds
-// the 8 results into y.  The FP32-vector apply and BiCG's fused pass form
-// the node numbers from the element number on the canonical structured
-// numbering (ConnView: 1 byte of Dirichlet bits per element instead of 32
-// bytes of connectivity).  Same operation as matvec_0 / mttvec_0
+// the 8 results into y.  The FP32-vector apply forms the node numbers from
+// the element number on the canonical structured numbering (ConnView: 1
+// byte of Dirichlet bits per element instead of 32 bytes of connectivity).  Same operation as matvec_0 / mttvec_0
 // (vanadis_full_DR_OpenMP_timing.for:1837-1933) and MATVEC_C_cu /
 // MTTVEC_C_cu (src_v2026_2_1/cudatest.cu:184-227).
 //
@@ -605,12 +604,10 @@ cudaError_t launch_apply_both(const Handle &h, const double *x1, double *y1,
     const int p1 = color ? h.color_off[r + 1] : h.E;
     if (p1 <= p0) continue;
     const int grid = grid_for(p1 - p0, 256, 6);
+    // the connectivity table, as the double-float single apply reads it
     if (color)
       stored_apply_df_both<false, false><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, cv, h.E, p0,
                                                               p1, x1, y1, x2, y2, skip);
-    else if (cv.emask)
-      stored_apply_df_both<true, true><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, cv, h.E, p0, p1,
-                                                            x1, y1, x2, y2, skip);
     else
       stored_apply_df_both<true, false><<<grid, 256, 0, s>>>(h.Ahi, h.Alo, cv, h.E, p0,
                                                              p1, x1, y1, x2, y2, skip);

@@ -241,7 +241,9 @@ struct Handle {
 };
 
 // The connectivity view of the stored applies (structured when the mesh
-// is in the canonical numbering, natural order and emask is built).
+// is in the canonical numbering, natural order and emask is built; the
+// FP32-vector apply uses the structured form, the double-float ones the
+// table).
 ConnView conn_view(const Handle &h);
 cudaError_t launch_emask(Handle &h);
 
