@@ -59,3 +59,28 @@ def test_reference_arm_nonzero_rank_exits_without_work(monkeypatch, capsys):
     monkeypatch.setenv("LOCAL_RANK", "1")
     assert bench.run_reference(bench.args_parse([])) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_json_line_small(monkeypatch, capsys):
+    """The reference arm on a small mesh, on the CPU: one JSON line with the
+    contract's keys, the CPU port as its baseline and no host-device bytes."""
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    a = bench.args_parse(["--impl", "reference", "--nex", "8", "--ney", "8",
+                          "--nez", "4", "--steps", "1", "--warmup", "1",
+                          "--cpu-iters", "2"])
+    assert bench.run_reference(a) == 0
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC
+    assert d["unit"] == "s" and d["value"] > 0 and d["higher_is_better"] is False
+    assert d["steps"] == 1 and d["warmup"] == 1 and d["n_gpus"] == 1
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": "s",
+                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert "workload" in d["config"] and d["reference_iterations"] > 0
