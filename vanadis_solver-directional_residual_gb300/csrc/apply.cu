@@ -33,8 +33,6 @@
 namespace vdr {
 namespace {
 
-int sm_count2() { return device_sm_count(); }
-
 template <bool TRANS, bool ATOMIC>
 __global__ void __launch_bounds__(256) stored_apply_f64(
     const double2 *__restrict__ A, const int *__restrict__ conn, int E, int p0,
@@ -558,7 +556,7 @@ __global__ void bc_to_mask_kernel(const int *__restrict__ bc,
 
 int grid_for(long n, int threads, int per_sm) {
   const long need = (n + threads - 1) / threads;
-  return (int)std::max<long>(1, std::min<long>(need, (long)sm_count2() * per_sm));
+  return (int)std::max<long>(1, std::min<long>(need, (long)device_sm_count() * per_sm));
 }
 
 }  // namespace

@@ -37,8 +37,6 @@ namespace {
 constexpr int BT = 512;  // threads per block of the block-vector kernels
 constexpr unsigned FULL = 0xffffffffu;
 
-int sm_count_b() { return device_sm_count(); }
-
 // --------------------------------------------------------------- applies
 __device__ __forceinline__ unsigned to_tf32(float f) {
   unsigned r;
@@ -1234,7 +1232,7 @@ int cached_per_sm(std::atomic<int> &slot, Kern kern, int threads, int smem) {
 
 int grid_n(long n, int threads, int per_sm) {
   const long need = (n + threads - 1) / threads;
-  return (int)std::max<long>(1, std::min<long>(need, (long)sm_count_b() * per_sm));
+  return (int)std::max<long>(1, std::min<long>(need, (long)device_sm_count() * per_sm));
 }
 
 // One block per TILE_X x TY x TILE_Z box of elements and column half; the

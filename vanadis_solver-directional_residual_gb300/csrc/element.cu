@@ -982,15 +982,13 @@ __global__ void sum_partials_kernel(const double *__restrict__ partials, int n,
   if (threadIdx.x == 0) *out = sm[0];
 }
 
-int sm_count() { return device_sm_count(); }
-
 }  // namespace
 
 cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
                          cudaStream_t s) {
   if (a.E <= 0) return cudaSuccess;
   const long blocks_needed = ((long)a.E + ROWS_EPB - 1) / ROWS_EPB;
-  const int grid = (int)std::min<long>(blocks_needed, (long)sm_count() * 32);
+  const int grid = (int)std::min<long>(blocks_needed, (long)device_sm_count() * 32);
   if (fp32)
     elem_build_kernel<float><<<grid, 64, 0, s>>>(a, ba);
   else if (ba.exact_fp64)
@@ -1004,7 +1002,7 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
       cudaFuncSetAttribute(elem_build_df_kernel<false>,
                            cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     });
-    const int g2 = (int)std::min<long>(((long)a.E + 255) / 256, (long)sm_count() * 8);
+    const int g2 = (int)std::min<long>(((long)a.E + 255) / 256, (long)device_sm_count() * 8);
     elem_dr_scalars_kernel<<<g2, 256, 0, s>>>(a, ba.drs);
     if (ba.told || ba.Mhi)  // H and M apart
       elem_build_df_kernel<true><<<grid, 64, 0, s>>>(a, ba);
@@ -1021,7 +1019,7 @@ cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
                             const int *skip2, cudaStream_t s) {
   if (a.E <= 0) return cudaSuccess;
   const long blocks_needed = ((long)a.E + 31) / 32;
-  const int grid = (int)std::min<long>(blocks_needed, (long)sm_count() * 8);
+  const int grid = (int)std::min<long>(blocks_needed, (long)device_sm_count() * 8);
   if (fp32) {
     if (transpose)
       mf_apply_kernel<float, true><<<grid, 256, 0, s>>>(a, (float)a.aH, (float)a.aM, x, y, skip, skip2);
@@ -1039,7 +1037,7 @@ cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
 
 cudaError_t launch_mass(Handle &h, const double *c, double *partials,
                         double *out, cudaStream_t s) {
-  const int grid = std::max(1, std::min((h.E + 255) / 256, sm_count() * 4));
+  const int grid = std::max(1, std::min((h.E + 255) / 256, device_sm_count() * 4));
   if (!h.massw) {  // per-element weights, once per handle (fixed geometry)
     cudaError_t e = cudaMalloc(&h.massw, sizeof(double) * 8 * (size_t)std::max(h.E, 1));
     if (e) {

@@ -31,8 +31,6 @@ namespace {
 constexpr int GT = 256;  // threads per block
 constexpr unsigned FULLG = 0xffffffffu;
 
-int sm_count_g() { return device_sm_count(); }
-
 struct GcrArgs {
   long n;
   int m;             // restart length
@@ -264,7 +262,7 @@ __global__ void __launch_bounds__(GT) g_xr(GcrArgs a, int k) {
 
 int gcr_grid(long n) {
   const long need = (n + GT - 1) / GT;
-  return (int)std::max<long>(1, std::min<long>(need, (long)sm_count_g() * 2));
+  return (int)std::max<long>(1, std::min<long>(need, (long)device_sm_count() * 2));
 }
 
 }  // namespace

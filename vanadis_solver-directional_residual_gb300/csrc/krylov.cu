@@ -31,8 +31,6 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-int sm_count3() { return device_sm_count(); }
-
 template <int NQ>
 __device__ __forceinline__ void block_sum(double (&v)[NQ]) {
   __shared__ double sm[RED_THREADS / 32][MAXQ];
@@ -422,7 +420,7 @@ __global__ void k_true_residual(Vec a, const double *ax, double *partials,
 
 int red_grid(int n) {
   const long need = ((long)n + RED_THREADS - 1) / RED_THREADS;
-  return (int)std::max<long>(1, std::min<long>(need, (long)sm_count3() * 8));
+  return (int)std::max<long>(1, std::min<long>(need, (long)device_sm_count() * 8));
 }
 
 Vec make_vec(Handle &h, const double *b, double *x) {

@@ -63,11 +63,9 @@ constexpr long layer_wsize(int l) {
   return l == L_HEAD ? 16 : 27L * DEFS[l].cout * (DEFS[l].cin1 + DEFS[l].cin2);
 }
 
-int sm_count_u() { return device_sm_count(); }
-
 int grid_for(long n, int threads, int per_sm = 8) {
   const long need = (n + threads - 1) / threads;
-  return (int)std::max<long>(1, std::min<long>(need, (long)sm_count_u() * per_sm));
+  return (int)std::max<long>(1, std::min<long>(need, (long)device_sm_count() * per_sm));
 }
 
 __device__ __forceinline__ bool skipped(const int *s1, const int *s2) {
@@ -919,7 +917,7 @@ cudaError_t wgrad_launch(const Net &n, WgArgs a, const float *dy, const bf16 *y,
   mask_transpose<COUT><<<grid_for(a.V * COUT, 256), 256, 0, s>>>(dy, y, n.dyt, a.V);
   a.dyt = n.dyt;
   const long nks = (long)a.H * a.D * ((a.W + 15) / 16);  // 16-voxel row segments
-  const long target = std::max<long>(1, (long)sm_count_u() * 8 / (27 * NGROUPS));
+  const long target = std::max<long>(1, (long)device_sm_count() * 8 / (27 * NGROUPS));
   long chunk = (nks + target - 1) / target;
   chunk = std::max<long>(16, ((chunk + 3) / 4) * 4);
   a.chunk = chunk;
