@@ -905,12 +905,24 @@ def run_native(a):
                   "iterations": cit, "status": cst}}
     sc.close()
 
-    batched = None if a.no_batched else batched_rhs_section(vdr, local)
-    meshes = None if a.no_meshes else batched_meshes_section(vdr, local)
-    learned = None if a.no_learned else learned_section(vdr, local, a)
-    dropin = None if a.no_dropin else dropin_section(vdr, s, prob, cf, rM)
-    tloop = None if a.no_time_loop else time_loop_section(vdr, s, prob, aH, aM, cf, rM)
-    text_out = None if a.no_text else text_output_section(vdr, prob, x)
+    def section(skip, fn, *args):
+        """An optional section; a failure is reported in its key (and on
+        stderr) instead of ending the run without the headline line."""
+        if skip:
+            return None
+        try:
+            return fn(*args)
+        except Exception as exc:  # noqa: BLE001 -- reported, not hidden
+            import traceback
+            traceback.print_exc()
+            return {"error": "%s: %s" % (type(exc).__name__, exc)}
+
+    batched = section(a.no_batched, batched_rhs_section, vdr, local)
+    meshes = section(a.no_meshes, batched_meshes_section, vdr, local)
+    learned = section(a.no_learned, learned_section, vdr, local, a)
+    dropin = section(a.no_dropin, dropin_section, vdr, s, prob, cf, rM)
+    tloop = section(a.no_time_loop, time_loop_section, vdr, s, prob, aH, aM, cf, rM)
+    text_out = section(a.no_text, text_output_section, vdr, prob, x)
 
     # ---- e2e through the C ABI with host buffers ----
     # The step's inputs (per-element fields) and outputs (right-hand side,
