@@ -183,44 +183,32 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def fp64_peak_tflops():
-    """Measured FP64 peak: cuBLAS DGEMM (torch.matmul, float64, 4096^3),
-    best of 3 -- the denominator for the FP64-pipe-bound element build."""
-    import torch
-    n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    torch.matmul(a, b)
-    torch.cuda.synchronize()
-    best = 1e30
-    for _ in range(3):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        torch.matmul(a, b)
-        e1.record()
-        torch.cuda.synchronize()
-        best = min(best, e0.elapsed_time(e1))
-    del a, b
-    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+def profile_value(name, key):
+    """A 'key: <number>' line of a committed ncu summary under profiles/."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith(key + ":"):
+                return float(line.split(":", 1)[1])
+    except (OSError, ValueError):
+        pass
+    return None
 
 
-# FP64 operations per element of elem_build_kernel<double>, from its
-# operation census (FMA = 2 FLOP): per Gauss point ~500 FLOP of geometry and
-# DR weight, ~780 FLOP of H/M row accumulation, ~30 FLOP of output; x 8.
-BUILD_FLOP_PER_ELEMENT = 10400.0
+# The element build is bound by instruction issue (FP32 pipe for the
+# double-float rows, FP64 for the DR scalars): its roofline is the SMs'
+# issue rate, 4 warp instructions per SM per clock, against the warp
+# instructions per element that ncu counted for the kernel.
+BUILD_PROFILE = "elem_build_df_rotation_shear_128x128x64.md"
+ISSUE_PER_SM_CLOCK = 4.0
 
 
 def profile_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (a line 'traffic_bytes_per_launch: <number>')."""
-    path = os.path.join(ROOT, "profiles", "stored_apply_df_rotation_shear.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1])
-    except OSError:
-        pass
-    return None
+    summary: a 1M-element capture's traffic scaled to the bench size by the
+    units processed (traffic grows in proportion to E and N)."""
+    return profile_value("stored_apply_df_rotation_shear.md",
+                         "traffic_bytes_per_launch")
 
 
 # --------------------------------------------------------------- CPU legs
@@ -287,6 +275,41 @@ def run_reference(a):
 
 
 # --------------------------------------------------------------- GPU arm
+def timed_steps(s, stream, b, x, aH, aM, cf, rM, solve, reps=3):
+    """One theta step on handle `s`, timed on its stream: the operator
+    invalidated, element matrices + Jacobi diagonal + right-hand side in one
+    element pass, then `solve()` from x = 0.  Returns the medians over
+    `reps` (after one untimed step) of (build + RHS, solve alone, whole
+    step) in seconds, and the last solve's return value."""
+    import torch
+    builds, solves, steps = [], [], []
+    out = None
+    for k in range(reps + 1):
+        with torch.cuda.stream(stream):
+            x.zero_()
+        s.set_operator(aH, aM)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        s.assemble_rhs_device(b, cf, rM, None)
+        e1.record(stream)
+        out = solve()
+        e2.record(stream)
+        torch.cuda.synchronize()
+        if k:
+            builds.append(e0.elapsed_time(e1) / 1e3)
+            solves.append(e1.elapsed_time(e2) / 1e3)
+            steps.append(e0.elapsed_time(e2) / 1e3)
+    return (statistics.median(builds), statistics.median(solves),
+            statistics.median(steps), out)
+
+
+def _r(v, n=4):
+    """v to n significant digits (short summary keys)."""
+    if v is None or not isinstance(v, (int, float)) or v != v:
+        return v
+    return float("%.*g" % (n, v))
+
+
 BATCH_MESH = (128, 128, 64)
 BATCH_K = 64
 
@@ -790,21 +813,12 @@ def run_native(a):
     rel_true = s.true_residual_device(b, x)
     stats = s.stats()
 
-    # ---- breakdown: element matrices vs Krylov (one extra step) ----
-    e_a, e_b, e_c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-    with torch.cuda.stream(stream):
-        x.zero_()
-    s.set_operator(aH, aM)
-    e_a.record(stream)
-    s.assemble_rhs_device(b, cf, rM, None)
+    # ---- step = element matrices + RHS, then the solve alone ----
+    t_build_s, t_krylov_s, step_s, fp64_out = timed_steps(
+        s, stream, b, x, aH, aM, cf, rM,
+        lambda: s.solve_device(b, x, tol=TOL, itmax=20000))
+    t_build, t_krylov = t_build_s * 1e3, t_krylov_s * 1e3
     y = torch.zeros_like(b)
-    s.apply_accumulate_device(x, y)     # triggers the element-matrix build
-    e_b.record(stream)
-    s.solve_device(b, x, tol=TOL, itmax=20000)
-    e_c.record(stream)
-    torch.cuda.synchronize()
-    t_build = e_a.elapsed_time(e_b)
-    t_krylov = e_b.elapsed_time(e_c)
 
     # ---- roofline of the dominant kernel: stored EBE apply ----
     xr = torch.randn(N, dtype=torch.float64, device="cuda")
@@ -824,9 +838,34 @@ def run_native(a):
     achieved = alg_bytes / (t_apply_ms * 1e-3) / 1e9
     traffic = profile_traffic()
 
-    # ---- FP64 element build: roofline against the measured FP64 peak ----
-    fp64_peak = fp64_peak_tflops()
-    build_tflops = BUILD_FLOP_PER_ELEMENT * E / (t_build * 1e-3) / 1e12
+    # ---- element build: roofline against the SMs' instruction issue rate ----
+    inst_per_elem = profile_value(BUILD_PROFILE, "warp_instructions_per_element")
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    issue_peak = n_sm * ISSUE_PER_SM_CLOCK * sm_mhz * 1e6 / 1e9   # G/s
+    build_issue = (inst_per_elem * E / (t_build * 1e-3) / 1e9
+                   if inst_per_elem else None)
+
+    # ---- the same step with the pure FP64 element-matrix store ----
+    s64 = vdr.Solver(prob, vdr.Options(apply_mode="stored",
+                                       matrix_storage="fp64",
+                                       solver="bicgstab", device=local),
+                     aH=aH, aM=aM)
+    st64 = torch.cuda.ExternalStream(s64.stream())
+    x64 = torch.zeros_like(b)
+    b64 = torch.zeros_like(b)
+    _, f64_solve, f64_step, f64_out = timed_steps(
+        s64, st64, b64, x64, aH, aM, cf, rM,
+        lambda: s64.solve_device(b64, x64, tol=TOL, itmax=20000))
+    fp64_store = {"step_s": f64_step, "solve_s": f64_solve,
+                  "iterations": f64_out[0], "rel_residual": f64_out[1],
+                  "status": f64_out[2],
+                  "rel_l2_vs_double_float_solution":
+                      float(torch.linalg.norm(x64 - x) / torch.linalg.norm(x)),
+                  "what": "element matrices kept as FP64 (512 B/element), "
+                          "contracted on the FP64 pipe"}
+    s64.close()
+    del x64, b64
 
     # ---- mixed precision (FP32 operator inside FP64 refinement) ----
     xm = torch.zeros_like(b)
@@ -839,21 +878,14 @@ def run_native(a):
 
     def mixed_step(op):
         s.set_mixed_operator(op)
-        times = []
-        for k in range(3):
-            with torch.cuda.stream(stream):
-                xm.zero_()
-            s.set_operator(aH, aM)
-            m0, m1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
-            m0.record(stream)
-            s.assemble_rhs_device(b, cf, rM, None)
-            mo, mi, merr, mst = s.solve_mixed_device(b, xm, tol=TOL, inner_tol=1e-5)
-            m1.record(stream)
-            torch.cuda.synchronize()
-            times.append(m0.elapsed_time(m1))
-        return {"value": statistics.mean(times[1:]) / 1e3, "unit": "s",
+        _, t_solve, t_step, out = timed_steps(
+            s, stream, b, xm, aH, aM, cf, rM,
+            lambda: s.solve_mixed_device(b, xm, tol=TOL, inner_tol=1e-5))
+        mo, mi, merr, mst = out
+        return {"value": t_step, "unit": "s", "solve_s": t_solve,
                 "outer_corrections": mo, "inner_iterations": mi,
                 "fp64_rel_residual": merr, "status": mst,
+                "true_rel_residual": s.true_residual_device(b, xm),
                 "rel_l2_vs_fp64_solution": float(torch.linalg.norm(xm - x) /
                                                  torch.linalg.norm(x))}
 
@@ -979,24 +1011,34 @@ def run_native(a):
             "true_rel_residual": rel_true, "status": st,
             "breakdown_ms": {"element_matrices_and_rhs": t_build,
                              "krylov": t_krylov,
-                             "per_iteration": t_krylov / max(1, iters[-1])},
+                             "per_iteration": t_krylov / max(1, fp64_out[0]),
+                             "step": step_s * 1e3},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic,
+                         "traffic_kind": "ncu DRAM bytes of a 1,048,576-"
+                                         "element capture scaled to this "
+                                         "size by elements and nodes "
+                                         "(profiles/stored_apply_df_"
+                                         "rotation_shear.md)",
                          "kernel": "stored_apply_df (EBE apply, double-float "
                                    "element matrices, atomic scatter)",
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "launch_ms": t_apply_ms, "peak_kind": peak_kind},
-            "roofline_build": {"bound": "fp64", "achieved": build_tflops,
-                               "peak": fp64_peak, "unit": "TFLOP/s",
-                               "frac": build_tflops / fp64_peak,
+            "roofline_build": {"bound": "issue", "achieved": build_issue,
+                               "peak": issue_peak,
+                               "unit": "G warp instructions/s",
+                               "frac": (build_issue / issue_peak
+                                        if build_issue else None),
                                "kernel": "elem_build_df_kernel (element "
                                          "matrices + diag + RHS; H/M rows "
-                                         "in double-float on the FP32 pipe, "
-                                         "so the FP64-equivalent rate can "
-                                         "exceed the FP64 peak)",
-                               "flop_per_element": BUILD_FLOP_PER_ELEMENT,
-                               "peak_kind": "measured live: cuBLAS DGEMM 4096^3"},
+                                         "in double-float on the FP32 pipe)",
+                               "warp_instructions_per_element": inst_per_elem,
+                               "peak_kind": "%d SMs x 4 warp instructions "
+                                            "per clock at the median SM "
+                                            "clock of the timed region" % n_sm,
+                               "instructions_from": "profiles/" + BUILD_PROFILE},
+            "fp64_store": fp64_store,
             "scatter_variants": scatter_variants,
             "mixed_precision": mixed,
             "batched_rhs": batched,
@@ -1012,11 +1054,54 @@ def run_native(a):
             "clocks": clk,
             "cpu_baseline": cpu,
         }
+        line["summary"] = summary_keys(line, ms / 1e3, t_krylov_s)
         print(json.dumps(line), flush=True)
     s.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def summary_keys(line, step_s, solve_s):
+    """The numbers of every section in a few short keys, placed last in the
+    JSON line: seconds per step and per solve (device-resident, to FP64
+    relative residual 1e-8) for each precision form, the speed-ups of the
+    batched and learned forms, and the apply's HBM fraction."""
+    def g(d, *ks):
+        for k in ks:
+            if not isinstance(d, dict):
+                return None
+            d = d.get(k)
+        return d
+
+    mp, f64 = line.get("mixed_precision") or {}, line.get("fp64_store") or {}
+    lp = line.get("learned_preconditioner") or {}
+    sv = line.get("scatter_variants") or {}
+    out = {
+        "fp64_step_s": _r(step_s), "fp64_solve_s": _r(solve_s),
+        "fp64_iters": line.get("iterations"),
+        "fp64store_step_s": _r(f64.get("step_s")),
+        "fp64store_solve_s": _r(f64.get("solve_s")),
+        "color_step_s": _r(g(sv, "color", "step_s")),
+        "mixed_step_s": _r(mp.get("value")), "mixed_solve_s": _r(mp.get("solve_s")),
+        "mixed_true_res": _r(mp.get("true_rel_residual"), 3),
+        "mixed_err_vs_fp64": _r(mp.get("rel_l2_vs_fp64_solution"), 3),
+        "mixed_solve_speedup": _r(solve_s / mp["solve_s"]) if mp.get("solve_s") else None,
+        "mixed_step_speedup": _r(step_s / mp["value"]) if mp.get("value") else None,
+        "c5_jacobi_s": _r(g(lp, "jacobi_bicgstab", "solve_s_total")),
+        "c5_learned_s": _r(g(lp, "learned_then_jacobi", "solve_s_total")),
+        "c5_learned_vs_jacobi_time": _r(lp.get("learned_vs_plain_time")),
+        "c4a_block_s": _r(g(line, "batched_rhs", "block_solve_s")),
+        "c4a_speedup": _r(g(line, "batched_rhs", "speedup_vs_sequential_fp64")),
+        "c4a_apply_frac": _r(g(line, "batched_rhs", "block_apply", "frac"), 3),
+        "c4b_s": _r(g(line, "batched_meshes", "segmented_solve_s")),
+        "c4b_speedup": _r(g(line, "batched_meshes", "speedup_vs_one_at_a_time")),
+        "apply_frac": _r(g(line, "roofline", "frac"), 3),
+        "build_ms": _r(g(line, "breakdown_ms", "element_matrices_and_rhs")),
+        "time_loop_later_s": _r(g(line, "time_loop", "later_step_s")),
+        "time_loop_mixed_later_s": _r(g(line, "time_loop", "mixed", "later_step_s")),
+    }
+    return {k: v for k, v in out.items() if v is not None}
 
 
 def run_case(a):

@@ -453,21 +453,28 @@ const char *vdr_last_error(void);
 
 /* No counterpart in the reference.  The Jacobi BiCG solve of
  * kernel_dbcg_simple_ for callers that cannot allocate device memory: a
- * program whose device memory is owned by someone else after start-up (a
- * framework's caching allocator, a fixed memory budget), or work about to be
- * captured into a CUDA graph, where cudaMalloc/cudaFree are not allowed.
- * This entry point calls no cudaMalloc, cudaFree or allocating library
- * routine.  Every pointer is a DEVICE pointer owned by the caller, with the
- * meaning of the kernel_dbcg_simple_ arguments below (b, x in/out, bb in the
- * BB[64e+8i+j] layout, iss(E,8) column-major 1-based, diag, bc or NULL);
- * sizes are passed by value; stream is a cudaStream_t (NULL = default).
- * Its work vectors live in one fixed device array inside the library, sized
- * for n <= VDR_NOALLOC_MAX_NODES (about 3 MB, held on every GPU that loads
- * the library until the process exits); larger n is rejected with
- * VDR_BAD_ARGUMENT.  The first call on a device looks up that array's
- * device address, so make that first call before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race.  Returns a
- * VDR_* status; *iter, *err as kernel_dbcg_simple_ reports them. */
+ * program whose device memory belongs to someone else after start-up (a
+ * framework's caching allocator that has reserved the device, a fixed
+ * memory budget set when the job starts), where a cudaMalloc would fail or
+ * would take memory another component counts on.  This entry point calls no
+ * cudaMalloc, cudaFree or allocating library routine.  Every pointer is a
+ * DEVICE pointer owned by the caller, with the meaning of the
+ * kernel_dbcg_simple_ arguments below (b, x in/out, bb in the BB[64e+8i+j]
+ * layout, iss(E,8) column-major 1-based, diag, bc or NULL); sizes are
+ * passed by value; stream is a cudaStream_t (NULL = default).  The call
+ * returns when the solve has ended: it waits on its stream while it
+ * iterates.  Its work vectors live in one fixed device array inside the
+ * library, sized for n <= VDR_NOALLOC_MAX_NODES (about 3 MB, held on every
+ * GPU that loads the library until the process exits); larger n is rejected
+ * with VDR_BAD_ARGUMENT.  The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress) and keeps it for the process, so
+ * make that first call before any stream capture, and do not call this entry
+ * point again after a cudaDeviceReset of that device.  All calls share the
+ * array and each clears what it needs at its start: calls that overlap on
+ * the GPU (two streams, two host threads) race.  An iss entry outside 1..n
+ * returns VDR_BAD_ARGUMENT before any iteration runs (x then only has its
+ * Dirichlet entries zeroed, as the solve masks its initial guess).  Returns
+ * a VDR_* status; *iter, *err as kernel_dbcg_simple_ reports them. */
 #define VDR_NOALLOC_MAX_NODES 65536
 int vdr_bicg_noalloc_device(int n, int nax, int nay, int naz, const double *b,
                             double *x, double tol, int itmax,

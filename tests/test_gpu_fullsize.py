@@ -3,9 +3,11 @@ theta step (8,388,608 elements, 8,520,321 nodes; the bench's step), against
 the oracle assembled and solved on all host cores.
 
 * operator apply and its transpose: GPU vs the oracle's colour-parallel
-  matvec_0 / mttvec_0 on the oracle's BB, 1e-12 relative L2;
+  matvec_0 / mttvec_0 on the oracle's BB, 1e-12 relative L2, with the
+  atomic scatter and with the colour-by-colour scatter;
 * Jacobi diagonal and right-hand side: 1e-12;
-* the solution of the step (both solved to 1e-12): 1e-9;
+* the solution of the step (both solved to 1e-12): 1e-9, with either
+  scatter;
 * size-independent identities on the GPU alone: linearity of the apply and
   the adjoint identity (A x, y) = (x, A^T y);
 * the mixed-precision step (FP32 inner solves) at the FP64 tolerance, its
@@ -75,6 +77,54 @@ def test_fullsize_solution_parity(oracle, gpu_lib, full):
                                         colors=full["colors"], nthreads=full["nt"])
     assert st == 0 and errr <= 1e-12
     x, it, err, st = s.solve(full["b"], tol=1e-12, itmax=20000)
+    assert st == 0 and err <= 1e-12
+    assert rel_l2(x, xr) < 1e-9
+    assert abs(it - itr) <= max(3, 0.1 * itr), (it, itr)
+
+
+@pytest.fixture(scope="module")
+def full_color(vdr, full):
+    """The same step on a handle with the colour-by-colour scatter (element
+    storage in parity-colour order, one launch per colour, no atomics)."""
+    s = vdr.Solver(full["prob"], vdr.Options(scatter="color"), aH=full["aH"],
+                   aM=full["aM"])
+    yield s
+    s.close()
+
+
+def test_fullsize_color_scatter_apply_parity(oracle, gpu_lib, full, full_color):
+    prob = full["prob"]
+    m = prob.mesh
+    x = np.random.default_rng(6).standard_normal(m.nnode)
+    ce, co = full["colors"]
+    for tr in (False, True):
+        yref = oracle.matvec0_omp(m.iss, full["bb"], prob.bc, ce, co, x,
+                                  transpose=tr, nthreads=full["nt"])
+        y = full_color.apply(x, transpose=tr)
+        assert rel_l2(y, yref) < 1e-12, tr
+        assert np.all(y[prob.bc == 1] == 0.0)
+
+
+def test_fullsize_color_scatter_solution_parity(oracle, gpu_lib, full,
+                                                full_color):
+    """The colour-scatter step solved to the bench's tolerance (1e-8) and
+    tightly (1e-12): its true residual recomputed by the oracle, and the
+    tight solution against the oracle's BiCGStab at 1e-12."""
+    prob = full["prob"]
+    m = prob.mesh
+    ce, co = full["colors"]
+    assert rel_l2(full_color.diag(), full["d"]) < 1e-12
+    assert rel_l2(full_color.assemble_rhs(3.0, full["aM"], None), full["b"]) < 1e-12
+    x8, it8, err8, st8 = full_color.solve(full["b"], tol=1e-8, itmax=20000)
+    assert st8 == 0 and err8 <= 1e-8
+    r = full["b"] - oracle.matvec0_omp(m.iss, full["bb"], prob.bc, ce, co, x8,
+                                       nthreads=full["nt"])
+    assert np.linalg.norm(r) <= 1.01e-8 * np.linalg.norm(full["b"])
+    xr, itr, errr, st = oracle.bicgstab(full["b"], np.zeros(m.nnode), full["bb"],
+                                        m.iss, full["d"], prob.bc, 1e-12, 20000,
+                                        colors=full["colors"], nthreads=full["nt"])
+    assert st == 0 and errr <= 1e-12
+    x, it, err, st = full_color.solve(full["b"], tol=1e-12, itmax=20000)
     assert st == 0 and err <= 1e-12
     assert rel_l2(x, xr) < 1e-9
     assert abs(it - itr) <= max(3, 0.1 * itr), (it, itr)

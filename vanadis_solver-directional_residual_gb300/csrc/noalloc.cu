@@ -3,20 +3,22 @@
 //
 // Who needs it: a host program that hands the solver buffers it already
 // owns and must not allocate afterwards -- e.g. a time loop running under a
-// memory budget fixed at start-up (a framework's caching allocator owns the
-// whole device), code that is about to be captured into a CUDA graph (a
-// cudaMalloc/cudaFree inside a capture is illegal and cudaFree synchronises
-// the device), or a Fortran driver whose every step would otherwise pay the
-// allocation and release the reference pays per call.
+// memory budget fixed at start-up, or next to a framework's caching
+// allocator that has reserved the whole device, where a cudaMalloc fails or
+// takes memory another part of the program counts on; or a Fortran driver
+// whose every step would otherwise pay the allocation and release the
+// reference pays per call.
 //
 // Scratch: the Krylov work vectors (r, rr, p, pp, z, zz), the per-block
 // reduction partials and the solver state live in one file-scope device
 // array, g_noalloc_scratch, sized for VDR_NOALLOC_MAX_NODES nodes (about
 // 3 MB on every GPU that loads the library, held until the process exits).
 // Its device address is taken once per device with cudaGetSymbolAddress on
-// the first call on that device.  Every call shares the array: calls that
-// overlap on the GPU (two streams, two host threads) race, and each call
-// clears the state it relies on before use.
+// the first call on that device and kept for the process (a cudaDeviceReset
+// of that device would leave it stale).  Every call shares the array: calls
+// that overlap on the GPU (two streams, two host threads) race, and each
+// call clears the state it relies on before use.  The call is synchronous:
+// it reads the solver state back every few iterations and waits for it.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -153,6 +155,11 @@ __global__ void na_start(NaArgs a) {
   double o[3];
   if (na_grid_sum<3>(v, a, o)) {
     NaState *st = a.st;
+    if (st->bad) {  // a bad ISS entry: no iteration may touch x
+      st->status = VDR_BAD_ARGUMENT;
+      st->done = 1;
+      return;
+    }
     st->bnrm2 = o[0];
     st->bknum = o[2];
     st->bkden = 1.0;
