@@ -182,17 +182,31 @@ int vdr_solve_device(vdr_handle *h, const double *d_b, double *d_x,
  * the outer residual needs to reach tol.  Stops when the FP64 true relative
  * residual ||b - A x||/||b|| <= tol or after max_outer corrections; *err is
  * that FP64 residual.  Device arrays. */
-/* The FP32 operator of vdr_apply32_device and of the mixed solve:
+/* The inner operator of the mixed solve (and the FP32 operator of
+ * vdr_apply32_device):
  * VDR_MIXED_ROUNDED (default) -- the FP64 element matrices rounded to FP32
  * (the hi parts of the double-float store; no second build);
- * VDR_MIXED_RECOMPUTE -- element Jacobians and DR terms recomputed in FP32. */
+ * VDR_MIXED_RECOMPUTE -- element Jacobians and DR terms recomputed in FP32;
+ * VDR_MIXED_HALF -- the Jacobi-scaled projected operator P A P D^-1 in
+ * binary16 with one power-of-two scale per element (128 B per element
+ * instead of 256), built from the FP64 element matrices when the operator
+ * changes; the inner BiCGStab then runs without preconditioner vectors and
+ * the correction is D^-1 of its solution.  Stored operator and BiCGStab
+ * only (elsewhere, and where an element's scale leaves the binary16 range,
+ * the rounded FP32 operator is used). */
 #define VDR_MIXED_ROUNDED 0
 #define VDR_MIXED_RECOMPUTE 1
+#define VDR_MIXED_HALF 2
 int vdr_set_mixed_operator(vdr_handle *h, int mode);
 int vdr_solve_mixed_device(vdr_handle *h, const double *d_b, double *d_x,
                            double tol, double inner_tol, int max_outer,
                            int inner_itmax, int *outer_iters, int *inner_iters,
                            double *err);
+
+/* y = A^ x with the binary16 inner operator A^ = P A P D^-1 of
+ * VDR_MIXED_HALF (FP32 device vectors of length N); builds the store if the
+ * operator changed.  For tests and measurement of that operator alone. */
+int vdr_apply_half_device(vdr_handle *h, const float *d_x, float *d_y);
 
 /* Device-resident time loop of the reference program (the do-while loop of
  * VANADIS.FOR:71-86 / vanadis_full_DR_OpenMP_timing.for:59-74 around

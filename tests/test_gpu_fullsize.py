@@ -163,6 +163,32 @@ def test_fullsize_mixed_precision_step(oracle, gpu_lib, vdr, full):
     assert rel_l2(x, x64) < 1e-6
 
 
+def test_fullsize_mixed_half_operator_step(oracle, gpu_lib, vdr, full):
+    """The same step with the binary16 inner operator (P A P D^-1 per element,
+    one power-of-two scale each): the FP64 true residual 1e-8 as the oracle
+    measures it, next to the FP64 solution."""
+    import torch
+    prob = full["prob"]
+    m = prob.mesh
+    with vdr.Solver(prob, vdr.Options(), aH=full["aH"], aM=full["aM"]) as sm:
+        sm.set_mixed_operator("half")
+        b = torch.as_tensor(full["b"], device="cuda")
+        x = torch.zeros_like(b)
+        torch.cuda.synchronize()
+        outer, inner, err, st = sm.solve_mixed_device(b, x, tol=1e-8,
+                                                      inner_tol=1e-3)
+        torch.cuda.synchronize()
+        x = x.cpu().numpy()
+    assert st == 0 and err <= 1e-8, (outer, inner, err)
+    ce, co = full["colors"]
+    ax = oracle.matvec0_omp(m.iss, full["bb"], prob.bc, ce, co, x,
+                            nthreads=full["nt"])
+    assert np.linalg.norm(full["b"] - ax) <= 1.01e-8 * np.linalg.norm(full["b"])
+    x64, _, _, st64 = full["s"].solve(full["b"], tol=1e-8, itmax=20000)
+    assert st64 == 0
+    assert rel_l2(x, x64) < 1e-6
+
+
 def test_fullsize_block_solve_residuals(oracle, gpu_lib, vdr):
     """Many right-hand sides at full size: 128 x 128 x 64 elements, K = 64 Gaussian
     sources, the refined block solve on the tensor-core block apply; every

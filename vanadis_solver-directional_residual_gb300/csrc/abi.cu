@@ -216,7 +216,25 @@ int ensure_operator32(Handle &h) {
     h.op32_valid = true;  // matrix-free: recomputed in FP32 at each apply
     return VDR_OK;
   }
-  if (h.mixed_op == VDR_MIXED_ROUNDED) {
+  h.use_half = false;
+  if (h.mixed_op == VDR_MIXED_HALF) {
+    // the binary16 Jacobi-scaled store for the FP32-vector inner solves;
+    // the rounded FP32 operator stays the one of FP64-vector inner solves
+    int st = ensure_operator(h);
+    if (st) return st;
+    cudaError_t e;
+    if (!h.flag && (e = cudaMalloc(&h.flag, sizeof(int))))
+      return cuda_fail(e, "flag");
+    int bad = 0;
+    if ((e = cudaMemsetAsync(h.flag, 0, sizeof(int), h.stream)) ||
+        (e = launch_half_store(h, h.flag, h.stream)) ||
+        (e = cudaMemcpyAsync(&bad, h.flag, sizeof(int), cudaMemcpyDeviceToHost,
+                             h.stream)) ||
+        (e = cudaStreamSynchronize(h.stream)))
+      return cuda_fail(e, "16-bit element matrices");
+    h.use_half = bad == 0;  // out of range: the rounded FP32 operator
+  }
+  if (h.mixed_op == VDR_MIXED_ROUNDED || h.mixed_op == VDR_MIXED_HALF) {
     // the hi parts of the double-float store are the FP64 element matrices
     // rounded to FP32, in the FP32 store's layout: no second build
     int st = ensure_operator(h);
@@ -249,8 +267,11 @@ int solve_by_option(Handle &h, int method, const double *b, double *x,
     return solve_device(h, method, b, x, tol, itmax, iter, err);
   int st = ensure_operator32(h);
   if (st) return st;
+  // each correction to 1e-5, or to 1e-3 with the binary16 operator, whose
+  // rounding (2^-11 per element) a tighter inner solve cannot get past
   MixedStats ms;
-  st = solve_mixed_device(h, method, b, x, tol, 1e-5, 20, itmax, &ms);
+  st = solve_mixed_device(h, method, b, x, tol, h.use_half ? 1e-3 : 1e-5, 20,
+                          itmax, &ms);
   if (iter) *iter = ms.inner;
   if (err) *err = ms.err;
   return st;
@@ -301,7 +322,7 @@ void free_handle(Handle &h) {
   dfree(h.vel); dfree(h.lam); dfree(h.pdec); dfree(h.q);
   dfree(h.vel32); dfree(h.lam32); dfree(h.pdec32); dfree(h.robin);
   dfree(h.A64); dfree(h.A32); dfree(h.diag); dfree(h.dinv);
-  dfree(h.Ahi); dfree(h.Alo); dfree(h.flag);
+  dfree(h.Ahi); dfree(h.Alo); dfree(h.flag); dfree(h.A16); dfree(h.e16);
   dfree(h.Aaos); dfree(h.phi); dfree(h.perm_d); dfree(h.dinv32); dfree(h.block_err);
   dfree(h.bk_f); dfree(h.bk_d);
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
@@ -805,6 +826,30 @@ int vdr_solve_mixed_device(vdr_handle *H, const double *b, double *x,
   return st;
 }
 
+int vdr_apply_half_device(vdr_handle *H, const float *x, float *y) {
+  int st = check_handle(H);
+  if (st) return st;
+  Handle &h = H->h;
+  if (!x || !y) {
+    set_error("vdr_apply_half_device: null vector");
+    return VDR_BAD_ARGUMENT;
+  }
+  if (h.apply_mode != VDR_APPLY_STORED || h.mixed_op != VDR_MIXED_HALF) {
+    set_error("vdr_apply_half_device: needs the stored operator and "
+              "vdr_set_mixed_operator(h, VDR_MIXED_HALF)");
+    return VDR_BAD_ARGUMENT;
+  }
+  if ((st = ensure_operator(h)) || (st = ensure_operator32(h))) return st;
+  if (!h.use_half) {
+    set_error("vdr_apply_half_device: an element scale is outside the "
+              "binary16 store's range");
+    return VDR_BAD_ARGUMENT;
+  }
+  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(float) * h.N, h.stream);
+  if (!e) e = launch_apply_half(h, x, y, nullptr, nullptr, h.stream);
+  return e ? cuda_fail(e, "apply half") : VDR_OK;
+}
+
 int vdr_assemble_rhs_block_device(vdr_handle *H, int K, const double *Q,
                                   double cf, double *B) {
   int st = check_handle(H);
@@ -885,7 +930,8 @@ int vdr_apply_block_accumulate_device(vdr_handle *H, int K, const void *X,
 int vdr_set_mixed_operator(vdr_handle *H, int mode) {
   int st = check_handle(H);
   if (st) return st;
-  if (mode != VDR_MIXED_ROUNDED && mode != VDR_MIXED_RECOMPUTE) {
+  if (mode != VDR_MIXED_ROUNDED && mode != VDR_MIXED_RECOMPUTE &&
+      mode != VDR_MIXED_HALF) {
     set_error("vdr_set_mixed_operator: unknown mode");
     return VDR_BAD_ARGUMENT;
   }

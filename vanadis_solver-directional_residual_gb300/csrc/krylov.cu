@@ -580,7 +580,12 @@ int solve_device(Handle &h, int method, const double *b, double *x,
                                    ((uintptr_t)h.scatter << 12) ^
                                    ((uintptr_t)h.storage << 16) ^
                                    ((uintptr_t)(prec ? prec->ctx : nullptr) << 3));
-  if (!h.graph_exec[slot] || h.graph_key[slot] != key) {
+  // the kernels' arguments carry N, E and the work-vector offsets, so a
+  // graph captured for other sizes (buffers reused by a smaller mesh) is
+  // captured again
+  const long long size_key = ((long long)h.N << 32) | (unsigned)h.E;
+  if (!h.graph_exec[slot] || h.graph_key[slot] != key ||
+      h.graph_size[slot] != size_key) {
     if (h.graph_exec[slot]) cudaGraphExecDestroy(h.graph_exec[slot]);
     h.graph_exec[slot] = nullptr;
     cudaGraph_t graph;
@@ -599,6 +604,7 @@ int solve_device(Handle &h, int method, const double *b, double *x,
     cudaGraphDestroy(graph);
     if (e) return cuda_fail(e, "graph instantiate");
     h.graph_key[slot] = key;
+    h.graph_size[slot] = size_key;
   }
   const long graph_nodes = launches_graph_nodes(h, method, prec);
 
@@ -740,6 +746,10 @@ __global__ void __launch_bounds__(RED_THREADS) k32_start(Vec32 a) {
 }
 
 // p = r + beta (p - omega v); ph = M^-1 p (0 on Dirichlet); v = 0.
+// JAC = false: the operator carries the Jacobi scale and the Dirichlet
+// projection (the binary16 store), so p itself is the apply's input and
+// neither ph nor the diagonal and mask are touched.
+template <bool JAC>
 __global__ void __launch_bounds__(RED_THREADS) b32_p(Vec32 a) {
   const KState *st = a.st;
   if (st->done) return;
@@ -750,11 +760,11 @@ __global__ void __launch_bounds__(RED_THREADS) b32_p(Vec32 a) {
   float rv[U], pv[U], vv[U], dv[U];
   unsigned char mv[U];
   VLOOP(rv[u] = ok ? a.r[i] : 0.f; pv[u] = (ok && !first) ? a.p[i] : 0.f;
-        vv[u] = (ok && !first) ? a.v[i] : 0.f; dv[u] = ok ? a.dinv[i] : 0.f;
-        mv[u] = ok ? a.m[i] : 1;,
+        vv[u] = (ok && !first) ? a.v[i] : 0.f;
+        dv[u] = (JAC && ok) ? a.dinv[i] : 0.f; mv[u] = (JAC && ok) ? a.m[i] : 1;,
         const float pi = first ? rv[u] : rv[u] + beta * (pv[u] - om * vv[u]);
         a.p[i] = pi;
-        a.ph[i] = mv[u] ? 0.f : pi * dv[u];
+        if (JAC) a.ph[i] = mv[u] ? 0.f : pi * dv[u];
         a.v[i] = 0.f;)
 }
 
@@ -779,7 +789,8 @@ __global__ void __launch_bounds__(RED_THREADS) b32_alpha(Vec32 a) {
   }
 }
 
-// s = r - alpha v; sh = M^-1 s; t = 0; ||s||.
+// s = r - alpha v; sh = M^-1 s (JAC only); t = 0; ||s||.
+template <bool JAC>
 __global__ void __launch_bounds__(RED_THREADS) b32_s(Vec32 a) {
   if (a.st->done) return;
   const float al = (float)a.st->alpha;
@@ -787,10 +798,10 @@ __global__ void __launch_bounds__(RED_THREADS) b32_s(Vec32 a) {
   float rv[U], vv[U], dv[U];
   unsigned char mv[U];
   VLOOP(rv[u] = ok ? a.r[i] : 0.f; vv[u] = ok ? a.v[i] : 0.f;
-        dv[u] = ok ? a.dinv[i] : 0.f; mv[u] = ok ? a.m[i] : 1;,
+        dv[u] = (JAC && ok) ? a.dinv[i] : 0.f; mv[u] = (JAC && ok) ? a.m[i] : 1;,
         const float si = rv[u] - al * vv[u];
         a.s[i] = si;
-        a.sh[i] = mv[u] ? 0.f : si * dv[u];
+        if (JAC) a.sh[i] = mv[u] ? 0.f : si * dv[u];
         a.t[i] = 0.f;
         dot_acc(n2, si, si);)
   double v[1] = {dot_val(n2)};
@@ -824,14 +835,18 @@ __global__ void __launch_bounds__(RED_THREADS) b32_omega(Vec32 a) {
   }
 }
 
-// x += alpha ph + omega sh; r = s - omega t; rho_new = (rh, r); ||r||.
+// x += alpha ph + omega sh (JAC = false: alpha p + omega s); r = s - omega t;
+// rho_new = (rh, r); ||r||.
+template <bool JAC>
 __global__ void __launch_bounds__(RED_THREADS) b32_xr(Vec32 a) {
   KState *stc = a.st;
   if (stc->done) return;
   const float al = (float)stc->alpha;
+  const float *ph = JAC ? a.ph : a.p;
+  const float *sh = JAC ? a.sh : a.s;
   if (stc->sconv) {
     float xv[U], pv[U], sv[U];
-    VLOOP(xv[u] = ok ? a.x[i] : 0.f; pv[u] = ok ? a.ph[i] : 0.f;
+    VLOOP(xv[u] = ok ? a.x[i] : 0.f; pv[u] = ok ? ph[i] : 0.f;
           sv[u] = ok ? a.s[i] : 0.f;,
           a.x[i] = xv[u] + al * pv[u];
           a.r[i] = sv[u];)
@@ -849,8 +864,8 @@ __global__ void __launch_bounds__(RED_THREADS) b32_xr(Vec32 a) {
   const float om = (float)stc->omega;
   DfAcc rr{0.f, 0.f}, hr{0.f, 0.f};
   float xv[U], pv[U], shv[U], sv[U], tv[U], hv[U];
-  VLOOP(xv[u] = ok ? a.x[i] : 0.f; pv[u] = ok ? a.ph[i] : 0.f;
-        shv[u] = ok ? a.sh[i] : 0.f; sv[u] = ok ? a.s[i] : 0.f;
+  VLOOP(xv[u] = ok ? a.x[i] : 0.f; pv[u] = ok ? ph[i] : 0.f;
+        shv[u] = ok ? sh[i] : 0.f; sv[u] = ok ? a.s[i] : 0.f;
         tv[u] = ok ? a.t[i] : 0.f; hv[u] = ok ? a.rh[i] : 0.f;,
         a.x[i] = xv[u] + al * pv[u] + om * shv[u];
         const float ri = sv[u] - om * tv[u];
@@ -884,22 +899,25 @@ __global__ void __launch_bounds__(RED_THREADS) b32_xr(Vec32 a) {
   }
 }
 
-// b32 = (float)(r * scale); dinv32 = (float)dinv.
+// b32 = (float)(r * scale); dinv32 = (float)dinv (when dinv32 is given).
 __global__ void __launch_bounds__(RED_THREADS) k32_in(Vec32 a, const double *r,
                                                       double scale, const double *dinv,
                                                       float *dinv32) {
   double rv[U], dv[U];
-  VLOOP(rv[u] = ok ? r[i] : 0.0; dv[u] = ok ? dinv[i] : 0.0;,
+  VLOOP(rv[u] = ok ? r[i] : 0.0; dv[u] = (ok && dinv32) ? dinv[i] : 0.0;,
         a.b[i] = (float)(rv[u] * scale);
-        dinv32[i] = (float)dv[u];)
+        if (dinv32) dinv32[i] = (float)dv[u];)
 }
 
-// x += scale * x32 (FP64 update).
-__global__ void __launch_bounds__(RED_THREADS) k32_out(Vec32 a, double *x, double scale) {
-  double xv[U];
+// x += scale * x32, or (dinv given: the inner solve ran on A D^-1) x +=
+// scale * dinv * x32 (FP64 update).
+__global__ void __launch_bounds__(RED_THREADS) k32_out(Vec32 a, double *x, double scale,
+                                                       const double *dinv) {
+  double xv[U], sv[U];
   float dv[U];
-  VLOOP(xv[u] = ok ? x[i] : 0.0; dv[u] = ok ? a.x[i] : 0.f;,
-        x[i] = xv[u] + scale * (double)dv[u];)
+  VLOOP(xv[u] = ok ? x[i] : 0.0; dv[u] = ok ? a.x[i] : 0.f;
+        sv[u] = (ok && dinv) ? dinv[i] : 1.0;,
+        x[i] = xv[u] + scale * sv[u] * (double)dv[u];)
 }
 
 Vec32 make_vec32(Handle &h) {
@@ -928,13 +946,23 @@ cudaError_t launch_iteration32(Handle &h, const Vec32 &a) {
   const int g = red_grid(h.N);
   cudaStream_t s = h.stream;
   cudaError_t e;
-  b32_p<<<g, RED_THREADS, 0, s>>>(a);
+  if (h.use_half) {  // A D^-1 in binary16: no preconditioner vectors
+    b32_p<false><<<g, RED_THREADS, 0, s>>>(a);
+    if ((e = launch_apply_half(h, a.p, a.v, &h.st->done, nullptr, s))) return e;
+    b32_alpha<<<g, RED_THREADS, 0, s>>>(a);
+    b32_s<false><<<g, RED_THREADS, 0, s>>>(a);
+    if ((e = launch_apply_half(h, a.s, a.t, &h.st->done, &h.st->sconv, s))) return e;
+    b32_omega<<<g, RED_THREADS, 0, s>>>(a);
+    b32_xr<false><<<g, RED_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  b32_p<true><<<g, RED_THREADS, 0, s>>>(a);
   if ((e = launch_stored_apply32v(h, a.ph, a.v, &h.st->done, nullptr, s))) return e;
   b32_alpha<<<g, RED_THREADS, 0, s>>>(a);
-  b32_s<<<g, RED_THREADS, 0, s>>>(a);
+  b32_s<true><<<g, RED_THREADS, 0, s>>>(a);
   if ((e = launch_stored_apply32v(h, a.sh, a.t, &h.st->done, &h.st->sconv, s))) return e;
   b32_omega<<<g, RED_THREADS, 0, s>>>(a);
-  b32_xr<<<g, RED_THREADS, 0, s>>>(a);
+  b32_xr<true><<<g, RED_THREADS, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -959,7 +987,9 @@ int solve32_inner(Handle &h, double tol, int itmax, int *iter, double *err) {
   if ((e = cudaGetLastError())) return cuda_fail(e, "start kernel");
   const int K = h.opt.iters_per_graph > 0 ? h.opt.iters_per_graph : 8;
   const void *key = (const void *)((uintptr_t)h.work32 ^ ((uintptr_t)h.A32v << 1) ^
-                                   (uintptr_t)K ^ ((uintptr_t)h.scatter << 12));
+                                   (uintptr_t)K ^ ((uintptr_t)h.scatter << 12) ^
+                                   ((uintptr_t)h.use_half << 20) ^
+                                   ((uintptr_t)h.A16 << 2));
   if (!h.graph32 || h.graph32_key != key) {
     if (h.graph32) cudaGraphExecDestroy(h.graph32);
     h.graph32 = nullptr;
@@ -977,7 +1007,7 @@ int solve32_inner(Handle &h, double tol, int itmax, int *iter, double *err) {
     if (e) return cuda_fail(e, "graph instantiate");
     h.graph32_key = key;
   }
-  const long nodes = 5 + 2 * apply_launches(h);
+  const long nodes = 5 + 2 * (h.use_half ? 1 : apply_launches(h));
   const int max_launches = (itmax + K - 1) / K + 1;
   bool finished = false;
   for (int c = 0; c < max_launches && !finished; c++) {
@@ -1065,13 +1095,15 @@ int solve_mixed_device(Handle &h, int method, const double *b, double *x,
       // d solves A32 d = r / ||r|| on FP32 vectors; x += ||r|| d in FP64
       if (!(1.0 / rr[1] < INFINITY)) break;  // ||r|| at the denormal floor
       Vec32 a32 = make_vec32(h);
-      k32_in<<<g, RED_THREADS, 0, s>>>(a32, r, 1.0 / rr[1], h.dinv, h.dinv32);
+      k32_in<<<g, RED_THREADS, 0, s>>>(a32, r, 1.0 / rr[1], h.dinv,
+                                       h.use_half ? nullptr : h.dinv32);
       count_launches(1);
       h.apply_fp32 = true;
       const int ist = solve32_inner(h, itol, inner_itmax, &it, &ierr);
       h.apply_fp32 = false;
       if (ist == VDR_CUDA_ERROR || ist == VDR_BAD_ARGUMENT) return ist;
-      k32_out<<<g, RED_THREADS, 0, s>>>(a32, x, rr[1]);
+      k32_out<<<g, RED_THREADS, 0, s>>>(a32, x, rr[1],
+                                        h.use_half ? h.dinv : nullptr);
       count_launches(1);
     } else {
       if ((e = cudaMemsetAsync(d, 0, sizeof(double) * h.N, s)))

@@ -161,6 +161,12 @@ struct Handle {
   float4 *A32 = nullptr;   // [16][E]
   const float4 *A32v = nullptr;  // the FP32 operator the FP32 apply reads (A32 or Ahi)
   int mixed_op = VDR_MIXED_ROUNDED;
+  // 16-bit inner operator of the mixed solve (half.cu): A^ = P A P D^-1 per
+  // element in binary16 rows, uint4 A16[i*E + p], with a power-of-two
+  // exponent per element; use_half once built and in range
+  uint4 *A16 = nullptr;
+  signed char *e16 = nullptr;
+  bool use_half = false;
   float4 *Ahi = nullptr;   // [16][E] double-float store: hi parts
   float4 *Alo = nullptr;   // [16][E] double-float store: lo parts
   int *flag = nullptr;     // device flag: an entry left the FP32 range
@@ -181,6 +187,7 @@ struct Handle {
   int red_blocks = 0;
   static constexpr int NGRAPH = 8;
   cudaGraphExec_t graph_exec[NGRAPH] = {};
+  long long graph_size[NGRAPH] = {};  // (N << 32) | E the graph was captured for
   const void *graph_key[NGRAPH] = {};
   cudaEvent_t ev[2] = {nullptr, nullptr};
 
@@ -332,6 +339,15 @@ cudaError_t launch_mask_vec(double *v, const unsigned char *mask, int N,
                             cudaStream_t s);
 cudaError_t launch_bc_to_mask(const int *bc, unsigned char *mask, int N,
                               cudaStream_t s);
+
+// ---- the 16-bit inner operator (half.cu) ----
+// Builds A^ = P A P D^-1 in the binary16 store from the current FP64
+// operator (hi parts of the double-float store, or the FP64 store) and the
+// Jacobi diagonal; bit 0 of *bad when an element's scale leaves the range.
+cudaError_t launch_half_store(Handle &h, int *bad, cudaStream_t s);
+// y += A^ x on FP32 vectors (x, y of length N).
+cudaError_t launch_apply_half(const Handle &h, const float *x, float *y,
+                              const int *skip, const int *skip2, cudaStream_t s);
 
 // ---- solvers (krylov.cu) ----
 int solve_device(Handle &h, int method, const double *b, double *x,

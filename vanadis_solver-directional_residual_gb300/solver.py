@@ -374,10 +374,20 @@ class Solver:
     BLOCK_PRECISION = {"fp64": 0, "tf32": 1, "tf32x3": 2}
 
     def set_mixed_operator(self, mode="rounded"):
-        """FP32 operator of the mixed solve: "rounded" (the FP64 element
-        matrices rounded to FP32) or "recompute" (DR terms in FP32)."""
-        L.check(self.lib.vdr_set_mixed_operator(self.h, {"rounded": 0, "recompute": 1}[mode]),
+        """Inner operator of the mixed solve: "rounded" (the FP64 element
+        matrices rounded to FP32), "recompute" (DR terms in FP32) or "half"
+        (the Jacobi-scaled operator P A P D^-1 in binary16 with one
+        power-of-two scale per element)."""
+        L.check(self.lib.vdr_set_mixed_operator(
+            self.h, {"rounded": 0, "recompute": 1, "half": 2}[mode]),
                 "vdr_set_mixed_operator")
+
+    @_device_call
+    def apply_half_device(self, x, y):
+        """y = A^ x with the binary16 inner operator A^ = P A P D^-1 (float32
+        device vectors); needs set_mixed_operator("half")."""
+        L.check(self.lib.vdr_apply_half_device(self.h, _ptr(x), _ptr(y)),
+                "vdr_apply_half_device")
 
     def set_block_apply(self, variant="tile"):
         """Data movement of the tensor-core block apply: "tile" (default:
