@@ -39,6 +39,7 @@ def problems(vdr):
 CASE_NAMES = ["const_adv_OT", "rotation_VF", "rotation_GP", "kat_VF_robin",
               "one_element", "ragged_2x1x3", "rotation_decay_robin"]
 MODES = [("stored", "atomic", "df"), ("stored", "color", "df"),
+         ("stored", "warp", "df"),
          ("stored", "atomic", "fp64"), ("stored", "color", "fp64"),
          ("matrix_free", "atomic", "auto"), ("matrix_free", "color", "auto")]
 

@@ -8,13 +8,14 @@ colouring.
 
 Checked against the oracle at this size:
 * the operator apply and its transpose in both scatter modes (atomic and
-  colour-by-colour), double-float and FP64 stores and the matrix-free
-  recompute: 1e-12 relative L2 (matvec_0 / mttvec_0, OT:1837-1933);
+  colour-by-colour) and with warp-aggregated atomics, double-float and FP64
+  stores and the matrix-free recompute: 1e-12 relative L2 (matvec_0 /
+  mttvec_0, OT:1837-1933);
 * the Jacobi diagonal and the right-hand side: 1e-12 (el3d + przest3d,
   OT:431-740);
 * the greedy colouring: bit-exact against the oracle's first-fit greedy and
   the reference's parity formula (cudatest_coloring_gtx1060_optimized.cu:50-74);
-* the solution of BiCGStab to 1e-10, both scatter modes: 1e-9 against the
+* the solution of BiCGStab to 1e-10, every scatter mode: 1e-9 against the
   oracle's BiCG (dbcg_simple, OT:906-984) converged to 1e-13, and the
   iteration count against the oracle's BiCGStab at 1e-10;
 * the reference's method (BiCG) on the GPU against the oracle's BiCG at 1e-10:
@@ -52,6 +53,7 @@ def c1(vdr, oracle):
 
 
 MODES = [("stored", "atomic", "df"), ("stored", "color", "df"),
+         ("stored", "warp", "df"),
          ("stored", "atomic", "fp64"), ("stored", "color", "fp64"),
          ("matrix_free", "atomic", "auto"), ("matrix_free", "color", "auto")]
 
@@ -92,7 +94,7 @@ def test_c1_greedy_colouring_bit_exact(vdr, oracle, gpu_lib, c1):
     assert np.array_equal(colors, (i & 1) + 2 * (j & 1) + 4 * (k & 1))
 
 
-@pytest.mark.parametrize("scatter", ["atomic", "color"])
+@pytest.mark.parametrize("scatter", ["atomic", "color", "warp"])
 def test_c1_bicgstab_solution(vdr, oracle, gpu_lib, c1, scatter):
     prob = c1["prob"]
     m = prob.mesh

@@ -25,6 +25,7 @@ def systems(vdr, oracle):
 @pytest.mark.parametrize("solver", ["bicgstab", "bicg"])
 @pytest.mark.parametrize("mode,scatter,store", [("stored", "atomic", "df"),
                                                 ("stored", "color", "df"),
+                                                ("stored", "warp", "df"),
                                                 ("stored", "atomic", "fp64"),
                                                 ("matrix_free", "atomic", "auto")])
 def test_solution_parity(vdr, gpu_lib, systems, name, solver, mode, scatter,

@@ -17,7 +17,7 @@ STATUS_NAMES = {0: "ok", 1: "not converged", 2: "breakdown",
                 6: "i/o error"}
 
 DR_OT, DR_GP, DR_VF = 0, 1, 2
-SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOR = 0, 1, 2
+SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOR, SCATTER_WARP = 0, 1, 2, 3
 APPLY_AUTO, APPLY_STORED, APPLY_MATRIX_FREE = 0, 1, 2
 SOLVER_BICGSTAB, SOLVER_BICG = 0, 1
 STORE_AUTO, STORE_FP64, STORE_DF = 0, 1, 2

@@ -454,6 +454,7 @@ int vdr_create(vdr_handle **out, int nnode, int nelem, const double *xx,
   h.opt = o;
   h.device = o.device;
   h.scatter = (o.scatter == VDR_SCATTER_COLOR) ? VDR_SCATTER_COLOR : VDR_SCATTER_ATOMIC;
+  h.warp_agg = o.scatter == VDR_SCATTER_WARP;
   h.apply_mode = (o.apply_mode == VDR_APPLY_MATRIX_FREE) ? VDR_APPLY_MATRIX_FREE
                                                          : VDR_APPLY_STORED;
   h.storage = (o.matrix_storage == VDR_STORE_FP64) ? VDR_STORE_FP64 : VDR_STORE_DF;

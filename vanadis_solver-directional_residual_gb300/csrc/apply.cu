@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) stored_apply_f32v(
 // Elements whose gathered x leaves the FP32 exponent range (|x| >= 2^128)
 // are redone here in FP64 from the merged pairs, gather and scatter included.
 template <typename Nodes>
-__device__ __noinline__ void df_element_fallback(
+__device__ __forceinline__ void df_element_fallback_core(
     const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
     const Nodes &c, int E, long p, bool trans, bool atomic,
     const double *__restrict__ x, double *__restrict__ y) {
@@ -211,6 +211,14 @@ __device__ __noinline__ void df_element_fallback(
       else
         y[c[s]] += out[s];
     }
+}
+
+template <typename Nodes>
+__device__ __noinline__ void df_element_fallback(
+    const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
+    const Nodes &c, int E, long p, bool trans, bool atomic,
+    const double *__restrict__ x, double *__restrict__ y) {
+  df_element_fallback_core(Ahi, Alo, c, E, p, trans, atomic, x, y);
 }
 
 template <bool TRANS, bool ATOMIC, bool STRUCT>
@@ -305,6 +313,127 @@ __global__ void __launch_bounds__(256, 4) stored_apply_df(
         else
           y[c[s]] += out[s];
       }
+    }
+  }
+}
+
+// The double-float apply with warp-aggregated atomics (VDR_SCATTER_WARP), on
+// the canonical structured numbering: lanes of a warp hold consecutive
+// elements, and element p and p + 1 of one x row share the four nodes of
+// their common face (local nodes 1,2,5,6 of p are 0,3,4,7 of p + 1).  Each
+// lane computes its 8 outputs, hands its +x face's four to the next lane
+// with shuffles, and issues four FP64 atomics instead of eight (lanes whose
+// right neighbour is not in the same row, not in the warp, gated off or
+// redone in FP64 issue all eight).  The loop runs whole warps so that every
+// shuffle sees all 32 lanes.
+template <bool TRANS>
+__global__ void __launch_bounds__(256, 3) stored_apply_df_warp(
+    const float4 *__restrict__ Ahi, const float4 *__restrict__ Alo,
+    const ConnView cv, int E, int p0, int p1,
+    const double *__restrict__ x, double *__restrict__ y, const int *skip,
+    const int *skip2, ElemGate gate) {
+  if (skip && *(volatile const int *)skip) return;
+  if (skip2 && *(volatile const int *)skip2) return;
+  const int lane = threadIdx.x & 31;
+  const unsigned FULLW = 0xffffffffu;
+  for (long w0 = p0 + (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); w0 < p1;
+       w0 += (long)gridDim.x * blockDim.x) {
+    const long p = w0 + lane;
+    bool normal = p < p1;
+    if (normal && gate.active && !gate.active[__ldg(gate.eseg + p)]) normal = false;
+    ElemNodes<true> c;
+    double out[8];
+#pragma unroll
+    for (int s = 0; s < 8; s++) out[s] = 0.0;
+    int ix = 0;
+    bool redo = false;  // x outside the FP32 range: the FP64 fallback
+    if (normal) {
+      c.load(cv, E, p);
+      ix = (int)(p % cv.nex);
+      double xv[8];
+      float xh[8], xl[8];
+      bool bad = false;
+      int emax = 0;
+#pragma unroll
+      for (int s = 0; s < 8; s++) {
+        xv[s] = c[s] < 0 ? 0.0 : __ldg(x + c[s]);
+        emax = max(emax, df_exp(xv[s]));
+      }
+      const int shift = emax - 1023;
+#pragma unroll
+      for (int s = 0; s < 8; s++) df_split(xv[s], xh[s], xl[s], bad, shift);
+      if (bad) {
+        redo = true;
+        normal = false;
+      } else if (TRANS) {
+        DfAcc acc[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[j] = DfAcc{0.0f, 0.0f};
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const float4 h0 = __ldcs(Ahi + (size_t)(2 * i) * E + p);
+          const float4 h1 = __ldcs(Ahi + (size_t)(2 * i + 1) * E + p);
+          const float4 l0 = __ldcs(Alo + (size_t)(2 * i) * E + p);
+          const float4 l1 = __ldcs(Alo + (size_t)(2 * i + 1) * E + p);
+          df_fma_acc(acc[0], h0.x, l0.x, xh[i], xl[i]);
+          df_fma_acc(acc[1], h0.y, l0.y, xh[i], xl[i]);
+          df_fma_acc(acc[2], h0.z, l0.z, xh[i], xl[i]);
+          df_fma_acc(acc[3], h0.w, l0.w, xh[i], xl[i]);
+          df_fma_acc(acc[4], h1.x, l1.x, xh[i], xl[i]);
+          df_fma_acc(acc[5], h1.y, l1.y, xh[i], xl[i]);
+          df_fma_acc(acc[6], h1.z, l1.z, xh[i], xl[i]);
+          df_fma_acc(acc[7], h1.w, l1.w, xh[i], xl[i]);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          out[j] = df_to_double(acc[j].s, acc[j].c);
+          if (!df_scale(out[j], shift)) out[j] = ldexp(out[j], shift);
+        }
+      } else {
+        // row by row: one accumulator pair live at a time
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const float4 h0 = __ldcs(Ahi + (size_t)(2 * i) * E + p);
+          const float4 h1 = __ldcs(Ahi + (size_t)(2 * i + 1) * E + p);
+          const float4 l0 = __ldcs(Alo + (size_t)(2 * i) * E + p);
+          const float4 l1 = __ldcs(Alo + (size_t)(2 * i + 1) * E + p);
+          DfAcc acc{0.0f, 0.0f};
+          df_fma_acc(acc, h0.x, l0.x, xh[0], xl[0]);
+          df_fma_acc(acc, h0.y, l0.y, xh[1], xl[1]);
+          df_fma_acc(acc, h0.z, l0.z, xh[2], xl[2]);
+          df_fma_acc(acc, h0.w, l0.w, xh[3], xl[3]);
+          df_fma_acc(acc, h1.x, l1.x, xh[4], xl[4]);
+          df_fma_acc(acc, h1.y, l1.y, xh[5], xl[5]);
+          df_fma_acc(acc, h1.z, l1.z, xh[6], xl[6]);
+          df_fma_acc(acc, h1.w, l1.w, xh[7], xl[7]);
+          out[i] = df_to_double(acc.s, acc.c);
+          if (!df_scale(out[i], shift)) out[i] = ldexp(out[i], shift);
+        }
+      }
+    }
+    // hand the +x face to the next lane where both are normal elements of
+    // one x row; masked outputs (Dirichlet rows) are never added
+    const unsigned nm = __ballot_sync(FULLW, normal);
+    const bool hand = normal && lane < 31 && ((nm >> (lane + 1)) & 1u) &&
+                      ix + 1 < cv.nex;
+    const unsigned hm = __ballot_sync(FULLW, hand);
+    const double r1 = __shfl_up_sync(FULLW, out[1], 1);
+    const double r2 = __shfl_up_sync(FULLW, out[2], 1);
+    const double r5 = __shfl_up_sync(FULLW, out[5], 1);
+    const double r6 = __shfl_up_sync(FULLW, out[6], 1);
+    if (redo) df_element_fallback_core(Ahi, Alo, c, E, p, TRANS, true, x, y);
+    if (!normal) continue;
+    if (lane > 0 && ((hm >> (lane - 1)) & 1u)) {
+      out[0] += r1;
+      out[3] += r2;
+      out[4] += r5;
+      out[7] += r6;
+    }
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      const bool plusx = (s == 1 || s == 2 || s == 5 || s == 6);
+      if (plusx && hand) continue;
+      if (c[s] >= 0) atomicAdd(y + c[s], out[s]);
     }
   }
 }
@@ -686,7 +815,10 @@ cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
       // structured numbering: without its 32 B per element the kernel kept
       // the same time (0.782 vs 0.786 ms at 8.4M elements) -- fewer bytes in
       // flight per element, lower bandwidth -- while the FP32 applies gain.
-      if (transpose) {
+      if (h.warp_agg && cv.emask) {
+        if (transpose) VDR_LAUNCH_DF((stored_apply_df_warp<true>));
+        else VDR_LAUNCH_DF((stored_apply_df_warp<false>));
+      } else if (transpose) {
         if (color) VDR_LAUNCH_DF((stored_apply_df<true, false, false>));
         else VDR_LAUNCH_DF((stored_apply_df<true, true, false>));
       } else {

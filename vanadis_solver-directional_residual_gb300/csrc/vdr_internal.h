@@ -130,7 +130,8 @@ struct Handle {
   int device = 0;
   cudaStream_t stream = nullptr;
   vdr_options opt{};
-  int scatter = VDR_SCATTER_ATOMIC;
+  int scatter = VDR_SCATTER_ATOMIC;  // ATOMIC or COLOR (WARP is ATOMIC + warp_agg)
+  bool warp_agg = false;  // warp-aggregated atomics on the structured numbering
   int apply_mode = VDR_APPLY_STORED;
   bool apply_fp32 = false;  // operator applies use the FP32 operator
   int storage = VDR_STORE_DF;  // element-matrix store (resolved, never AUTO)
@@ -160,7 +161,7 @@ struct Handle {
   double2 *A64 = nullptr;  // [32][E] stored element matrices (row-major pairs)
   float4 *A32 = nullptr;   // [16][E]
   const float4 *A32v = nullptr;  // the FP32 operator the FP32 apply reads (A32 or Ahi)
-  int mixed_op = VDR_MIXED_ROUNDED;
+  int mixed_op = VDR_MIXED_HALF;
   // 16-bit inner operator of the mixed solve (half.cu): A^ = P A P D^-1 per
   // element in binary16 rows, uint4 A16[i*E + p], with a power-of-two
   // exponent per element; use_half once built and in range

@@ -22,7 +22,7 @@ module vdr_iso_c
        VDR_TIMEOUT = 5, VDR_IO_ERROR = 6
   integer(c_int), parameter :: VDR_DR_OT = 0, VDR_DR_GP = 1, VDR_DR_VF = 2
   integer(c_int), parameter :: VDR_SCATTER_AUTO = 0, VDR_SCATTER_ATOMIC = 1, &
-       VDR_SCATTER_COLOR = 2
+       VDR_SCATTER_COLOR = 2, VDR_SCATTER_WARP = 3
   integer(c_int), parameter :: VDR_APPLY_AUTO = 0, VDR_APPLY_STORED = 1, &
        VDR_APPLY_MATRIX_FREE = 2
   integer(c_int), parameter :: VDR_SOLVER_BICGSTAB = 0, VDR_SOLVER_BICG = 1

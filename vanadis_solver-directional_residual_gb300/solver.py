@@ -82,7 +82,8 @@ def _device_call(fn):
 
 _VARIANTS = {"ot": L.DR_OT, "gp": L.DR_GP, "vf": L.DR_VF}
 _SCATTER = {"auto": L.SCATTER_AUTO, "atomic": L.SCATTER_ATOMIC,
-            "color": L.SCATTER_COLOR, "colour": L.SCATTER_COLOR}
+            "color": L.SCATTER_COLOR, "colour": L.SCATTER_COLOR,
+            "warp": L.SCATTER_WARP}
 _APPLY = {"auto": L.APPLY_AUTO, "stored": L.APPLY_STORED,
           "matrix_free": L.APPLY_MATRIX_FREE}
 _SOLVER = {"bicgstab": L.SOLVER_BICGSTAB, "bicg": L.SOLVER_BICG}
