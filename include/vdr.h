@@ -309,6 +309,19 @@ typedef struct vdr_net vdr_net;
  * network is bound to the handle (its stream, mask and operator). */
 int vdr_net_create(vdr_handle *h, unsigned long long seed, vdr_net **net);
 int vdr_net_destroy(vdr_net *net);
+/* The forward convolutions' kernels: VDR_NET_CONV_TCGEN05 (the default when
+ * the TMA tensor maps of the network's inputs can be made) -- implicit GEMM
+ * on the fifth-generation tensor cores (tcgen05.mma from TMA-loaded halo
+ * slabs, FP32 accumulators in tensor memory); VDR_NET_CONV_MMA -- the
+ * warp-level mma.sync kernels (the backward passes always use these).
+ * VDR_BAD_ARGUMENT for TCGEN05 when its maps could not be made. */
+#define VDR_NET_CONV_MMA 0
+#define VDR_NET_CONV_TCGEN05 1
+int vdr_net_set_conv(vdr_net *net, int mode);
+/* The mode in use (nullable) and VDR_TIMEOUT if a tcgen05 convolution gave
+ * up waiting for its operands since the last call (the flag is cleared);
+ * synchronises the handle's stream. */
+int vdr_net_conv_status(vdr_net *net, int *mode);
 int vdr_net_param_count(vdr_net *net, long long *count);
 /* FP32 master parameters / last gradients (host arrays of param_count). */
 int vdr_net_get_params(vdr_net *net, float *host);

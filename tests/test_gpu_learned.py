@@ -80,6 +80,76 @@ def test_forward_matches_cpu(small):
     assert rel_l2(out.cpu().numpy(), ref.numpy()) < 1e-2
 
 
+@pytest.fixture(scope="module")
+def mid(vdr, gpu_lib):
+    """A mesh whose coarsest level (11 x 19 x 3 nodes) still holds a whole
+    TMA box of the tensor-core convolution (10 x 18 x 3 voxels)."""
+    import torch
+    prob = vdr.problems.rotation_shear(40, 72, 10, seed=53)
+    s = vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=2.0, aM=30.0)
+    net = vdr.LearnedNet(s, seed=4)
+    feat = torch.empty((prob.mesh.nnode, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    net.update_features(feat)
+    yield prob, s, net, feat
+    net.close()
+    s.close()
+
+
+@pytest.mark.parametrize("mode", ["mma", "tcgen05"])
+def test_forward_modes_match_cpu(mid, mode):
+    """Both convolution paths -- tcgen05 (TMA halo slabs, TMEM accumulators)
+    and warp-level mma.sync -- against the CPU float64 reference, 1e-2."""
+    import torch
+    from oracle import unet_ref as U
+    prob, s, net, feat = mid
+    m = prob.mesh
+    N = m.nnode
+    p = random_params(U.layout(), net.nparam, 11)
+    net.set_params(p)
+    net.set_conv(mode)
+    rh = np.random.default_rng(12).standard_normal(N).astype(np.float32)
+    out = torch.empty(N, dtype=torch.float32, device="cuda")
+    net.forward(dev(rh), out)
+    torch.cuda.synchronize()
+    used, st = net.conv_status()
+    assert (used, st) == (mode, 0)
+    theta = torch.tensor(p.astype(np.float64))
+    ref = U.forward(theta, rh, feat.cpu().numpy(), m.nax, m.nay, m.naz)
+    assert rel_l2(out.cpu().numpy(), ref.numpy()) < 1e-2
+
+
+def test_tcgen05_forward_matches_mma_at_c5_size(vdr, gpu_lib):
+    """On the 128 x 128 x 64 mesh of the learned workload the tensor-core
+    forward pass equals the mma.sync one up to BF16 rounding of the
+    activations (both accumulate in FP32), and reports no timeout."""
+    import torch
+    from oracle import unet_ref as U
+    prob = vdr.problems.rotation_shear(128, 128, 64, seed=1005)
+    with vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=2.0,
+                    aM=30.0) as s:
+        net = vdr.LearnedNet(s, seed=5)
+        assert net.conv_status() == ("tcgen05", 0)   # the default
+        net.update_features(None)
+        net.set_params(random_params(U.layout(), net.nparam, 13))
+        N = prob.mesh.nnode
+        rh = dev(np.random.default_rng(14).standard_normal(N).astype(np.float32))
+        outs = {}
+        for mode in ("tcgen05", "mma", "tcgen05"):
+            net.set_conv(mode)
+            o = torch.empty(N, dtype=torch.float32, device="cuda")
+            net.forward(rh, o)
+            torch.cuda.synchronize()
+            assert net.conv_status() == (mode, 0)
+            if mode in outs:   # the same input twice: the same output
+                assert torch.equal(outs[mode], o)
+            outs[mode] = o
+        a, b = outs["tcgen05"].cpu().numpy(), outs["mma"].cpu().numpy()
+        assert np.all(np.isfinite(a))
+        assert rel_l2(a, b) < 1e-2
+        net.close()
+
+
 def test_gradients_match_cpu(small):
     import torch
     from oracle import unet_ref as U

@@ -96,6 +96,8 @@ SIGNATURES = {
     "vdr_net_train_step_device": (_i, [_P, _P, _P, _f, _D]),
     "vdr_net_precondition_device": (_i, [_P, _P, _P]),
     "vdr_net_set_smoothing": (_i, [_P, _i, _d]),
+    "vdr_net_set_conv": (_i, [_P, _i]),
+    "vdr_net_conv_status": (_i, [_P, _I]),
     "vdr_solve_learned_device": (_i, [_P, _P, _P, _P, _d, _i, _i, _I, _D, _I]),
     "vdr_solve_gcr_device": (_i, [_P, _P, _P, _P, _d, _i, _i, _i, _I, _D,
                                   _I]),

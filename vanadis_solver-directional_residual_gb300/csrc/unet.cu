@@ -29,6 +29,12 @@
 //                  mask of the layer output fused into the gather).
 //   conv3_wgrad    weight and bias gradients, FP32 (shared-memory tiles of
 //                  32 voxels per tap).
+//   conv3_tc_kernel (conv_tc.cuh) the forward convolutions on the fifth-
+//                  generation tensor cores: tcgen05.mma from TMA-staged
+//                  halo slabs into tensor memory (VDR_NET_CONV_TCGEN05,
+//                  the default where the tensor maps can be made); the
+//                  decoder's upsampled input is first copied to the fine
+//                  grid (upsample_bf16).
 //   pooling, head, loss, Adam, BF16 packing, features, normalisation.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -39,6 +45,7 @@
 #include <cstring>
 #include <vector>
 
+#include "conv_tc.cuh"
 #include "vdr_internal.h"
 
 namespace vdr {
@@ -560,7 +567,10 @@ __global__ void adam_kernel(float *th, const float *g, float *m, float *v, long 
 
 // BF16 copies of a conv layer's weights: wb (same layout) and wbt =
 // [27][CIN][COUT] with the tap flipped (the backward data pass).
-__global__ void pack_weights(const float *th, bf16 *wb, bf16 *wbt, int cin, int cout) {
+// wb[tap][co][ci] (forward), wbt[26 - tap][ci][co] (backward data pass) and
+// wtc[tap][ci/8][co][ci%8] (the tensor-core kernel's core-matrix order).
+__global__ void pack_weights(const float *th, bf16 *wb, bf16 *wbt, bf16 *wtc, int cin,
+                             int cout) {
   const long total = 27L * cin * cout;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (long)gridDim.x * blockDim.x) {
@@ -570,6 +580,28 @@ __global__ void pack_weights(const float *th, bf16 *wb, bf16 *wbt, int cin, int 
     const bf16 b = __float2bfloat16_rn(th[i]);
     wb[i] = b;
     wbt[((long)(26 - tap) * cin + ci) * cout + co] = b;
+    wtc[(((long)tap * (cin / 8) + ci / 8) * cout + co) * 8 + (ci & 7)] = b;
+  }
+}
+
+// Nearest upsampling of a coarse [Vc][C] BF16 tensor to the fine grid
+// (fine voxel (x, y, z) reads coarse (x/2, y/2, z/2)), 16 bytes a thread.
+__global__ void upsample_bf16(const bf16 *__restrict__ in, bf16 *__restrict__ out,
+                              int W, int H, long V, int Wc, int Hc, int C,
+                              const int *skip, const int *skip2) {
+  if (skipped(skip, skip2)) return;
+  const int c8 = C / 8;
+  const long total = V * c8;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long)gridDim.x * blockDim.x) {
+    const long v = i / c8;
+    const int k = (int)(i - v * c8);
+    const int x = (int)(v % W);
+    const long r = v / W;
+    const int y = (int)(r % H), z = (int)(r / H);
+    const long vc = (long)(x >> 1) + (long)Wc * ((long)(y >> 1) + (long)Hc * (z >> 1));
+    reinterpret_cast<uint4 *>(out)[v * c8 + k] =
+        __ldg(reinterpret_cast<const uint4 *>(in) + vc * c8 + k);
   }
 }
 
@@ -869,6 +901,14 @@ struct Net {
   int smooth_steps = 1;   // Jacobi post-smoothing steps after the network
   double smooth_omega = 1.0;
   bool features_set = false;
+  // tcgen05 forward convolutions: packed weights, the decoders' upsampled
+  // inputs on the fine grid, and per layer the TMA maps of its inputs
+  bf16 *wtc = nullptr;
+  bf16 *up0 = nullptr, *up1 = nullptr;  // up(u1) on level 0, up(b2) on level 1
+  int *tc_err = nullptr;                // bit 0: a tcgen05 kernel wait ran out
+  int conv_mode = VDR_NET_CONV_MMA;
+  bool tc_ok = false;                   // every map could be made
+  CUtensorMap tmap[NLAYER][2];
   std::vector<void *> allocs;
 };
 
@@ -974,10 +1014,134 @@ const bf16 *wf(const Net &n, int l) { return n.wb + n.woff[l]; }
 const bf16 *wt(const Net &n, int l) { return n.wbt + n.woff[l]; }
 const float *bs(const Net &n, int l) { return n.theta + n.boff[l]; }
 
-constexpr int FWD_LAUNCHES = 14;  // convs, pools, head
+// kernels of one forward pass: 10 convolutions, 2 pools, the head, and on
+// the tensor-core path the 2 upsampled copies
+int fwd_launches(const Net &n) {
+  return (n.conv_mode == VDR_NET_CONV_TCGEN05 && n.tc_ok) ? 15 : 13;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *,
+                                  const cuuint32_t *, const cuuint32_t *,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// The map of a channels-last [V][C] BF16 tensor on grid d: dimensions (C,
+// x, y, z), box (8 channels, 10 x 18 x 3 voxels) -- one 16-byte channel
+// chunk of a tile's halo slab; out-of-grid voxels read as zero.
+bool make_tmap(CUtensorMap *m, const bf16 *base, int C, const Dims &d) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !base) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)d.W, (cuuint64_t)d.H,
+                              (cuuint64_t)d.D};
+  const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)C * 2 * d.W,
+                                 (cuuint64_t)C * 2 * d.W * d.H};
+  const cuuint32_t box[4] = {8, convtc::SX, convtc::SY, 3};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(base), dims,
+            strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Every forward layer's input maps (in1, and the upsampled copy for the two
+// decoder layers that concatenate); false if any cannot be made.
+bool make_tmaps(Net &n) {
+  struct In {
+    int l;
+    const bf16 *in1, *in2;
+  };
+  const In ins[] = {{L_E0A, n.x0, nullptr}, {L_E0B, n.a0, nullptr},
+                    {L_E1A, n.p0, nullptr}, {L_E1B, n.a1, nullptr},
+                    {L_BTA, n.p1, nullptr}, {L_BTB, n.a2, nullptr},
+                    {L_D1A, n.s1, n.up1},   {L_D1B, n.a3, nullptr},
+                    {L_D0A, n.s0, n.up0},   {L_D0B, n.a4, nullptr}};
+  for (const In &i : ins) {
+    const Dims &d = n.d[DEFS[i.l].level];
+    if (!make_tmap(&n.tmap[i.l][0], i.in1, DEFS[i.l].cin1, d)) return false;
+    n.tmap[i.l][1] = n.tmap[i.l][0];
+    if (i.in2 && !make_tmap(&n.tmap[i.l][1], i.in2, DEFS[i.l].cin2, d)) return false;
+  }
+  return true;
+}
+
+template <int CIN1, int CIN2, int COUT>
+cudaError_t conv_tc_launch(const Net &n, int l, bf16 *out, const int *sk,
+                           const int *sk2, cudaStream_t s) {
+  using Sh = convtc::Shape<CIN1, CIN2, COUT>;
+  auto kern = convtc::conv3_tc_kernel<CIN1, CIN2, COUT>;
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Sh::SMEM);
+  if (attr) return attr;
+  const Dims &d = n.d[DEFS[l].level];
+  convtc::Args a;
+  a.W = d.W;
+  a.H = d.H;
+  a.D = d.D;
+  a.tiles_x = (d.W + convtc::TX - 1) / convtc::TX;
+  a.tiles_y = (d.H + convtc::TY - 1) / convtc::TY;
+  a.ntiles = a.tiles_x * a.tiles_y * d.D;
+  a.wpk = n.wtc + n.woff[l];
+  a.bias = n.theta + n.boff[l];
+  a.out = out;
+  a.relu = 1;
+  a.err = n.tc_err;
+  a.skip = sk;
+  a.skip2 = sk2;
+  const int grid = std::min(a.ntiles, device_sm_count());
+  kern<<<grid, convtc::THREADS, Sh::SMEM, s>>>(n.tmap[l][0], n.tmap[l][1], a);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+// The forward pass's ten convolutions on the tensor cores (tcgen05).
+cudaError_t net_forward_tc(Net &n, const int *sk, const int *sk2, cudaStream_t s) {
+  cudaError_t e;
+  const Dims &f0 = n.d[0], &f1 = n.d[1], &f2 = n.d[2];
+  if ((e = conv_tc_launch<16, 0, 16>(n, L_E0A, n.a0, sk, sk2, s)) ||
+      (e = conv_tc_launch<16, 0, 16>(n, L_E0B, n.s0, sk, sk2, s)))
+    return e;
+  pool_fwd<<<grid_for(f1.V * 16, 256), 256, 0, s>>>(n.s0, n.p0, f0, f1, 16, sk, sk2);
+  if ((e = conv_tc_launch<16, 0, 32>(n, L_E1A, n.a1, sk, sk2, s)) ||
+      (e = conv_tc_launch<32, 0, 32>(n, L_E1B, n.s1, sk, sk2, s)))
+    return e;
+  pool_fwd<<<grid_for(f2.V * 32, 256), 256, 0, s>>>(n.s1, n.p1, f1, f2, 32, sk, sk2);
+  if ((e = conv_tc_launch<32, 0, 64>(n, L_BTA, n.a2, sk, sk2, s)) ||
+      (e = conv_tc_launch<64, 0, 64>(n, L_BTB, n.b2, sk, sk2, s)))
+    return e;
+  upsample_bf16<<<grid_for(f1.V * 8, 256), 256, 0, s>>>(n.b2, n.up1, f1.W, f1.H, f1.V,
+                                                         f2.W, f2.H, 64, sk, sk2);
+  if ((e = conv_tc_launch<32, 64, 32>(n, L_D1A, n.a3, sk, sk2, s)) ||
+      (e = conv_tc_launch<32, 0, 32>(n, L_D1B, n.u1, sk, sk2, s)))
+    return e;
+  upsample_bf16<<<grid_for(f0.V * 4, 256), 256, 0, s>>>(n.u1, n.up0, f0.W, f0.H, f0.V,
+                                                         f1.W, f1.H, 32, sk, sk2);
+  if ((e = conv_tc_launch<16, 32, 16>(n, L_D0A, n.a4, sk, sk2, s)) ||
+      (e = conv_tc_launch<16, 0, 16>(n, L_D0B, n.u0, sk, sk2, s)))
+    return e;
+  head_fwd<<<grid_for(f0.V, 256), 256, 0, s>>>(n.u0, n.theta + n.woff[L_HEAD], n.c, f0.V,
+                                                sk, sk2);
+  count_launches(5);
+  return cudaGetLastError();
+}
 
 // Forward pass from the prepared input x0 to the head output c.
 cudaError_t net_forward(Net &n, const int *sk, const int *sk2, cudaStream_t s) {
+  if (n.conv_mode == VDR_NET_CONV_TCGEN05 && n.tc_ok) return net_forward_tc(n, sk, sk2, s);
   cudaError_t e;
 #define VDR_CONV(CI1, CI2, CO, LVL, IN1, IN2, L, OUT)                              \
   if ((e = conv_launch<CI1, CI2, CO, false, false>(                                \
@@ -1074,7 +1238,8 @@ cudaError_t pack_all(Net &n, cudaStream_t s) {
   for (int l = 0; l < L_HEAD; l++) {
     const int cin = DEFS[l].cin1 + DEFS[l].cin2, cout = DEFS[l].cout;
     pack_weights<<<grid_for(layer_wsize(l), 256), 256, 0, s>>>(
-        n.theta + n.woff[l], n.wb + n.woff[l], n.wbt + n.woff[l], cin, cout);
+        n.theta + n.woff[l], n.wb + n.woff[l], n.wbt + n.woff[l], n.wtc + n.woff[l], cin,
+        cout);
   }
   count_launches(L_HEAD);
   return cudaGetLastError();
@@ -1160,7 +1325,7 @@ cudaError_t net_enqueue(void *ctx, const double *in, double *out, const int *ski
 }
 
 int net_enqueue_launches(const Net &n) {
-  return FWD_LAUNCHES + 3 + n.smooth_steps * (1 + apply_launches(*n.h));
+  return fwd_launches(n) + 4 + n.smooth_steps * (1 + apply_launches(*n.h));
 }
 
 }  // namespace
@@ -1239,8 +1404,17 @@ extern "C" int vdr_net_create(vdr_handle *H, unsigned long long seed, vdr_net **
         (e = nalloc(n, &n.gbuf, V0)) || (e = nalloc(n, &n.dc, V0)) ||
         (e = nalloc(n, &n.dyt, std::max(V0 * 16, V1 * 32))) ||
         (e = nalloc(n, &n.scal, 8)) || (e = nalloc(n, &n.partials, 2L * n.red_grid)) ||
-        (e = nalloc(n, &n.ticket, 1))) {
+        (e = nalloc(n, &n.ticket, 1)) || (e = nalloc(n, &n.wtc, off)) ||
+        (e = nalloc(n, &n.up0, V0 * 32)) || (e = nalloc(n, &n.up1, V1 * 64)) ||
+        (e = nalloc(n, &n.tc_err, 1))) {
       st = cuda_fail(e, "network allocation");
+      break;
+    }
+    // the tensor-core path where every input's tensor map can be made
+    n.tc_ok = make_tmaps(n);
+    n.conv_mode = n.tc_ok ? VDR_NET_CONV_TCGEN05 : VDR_NET_CONV_MMA;
+    if ((e = cudaMemsetAsync(n.tc_err, 0, sizeof(int), h.stream))) {
+      st = cuda_fail(e, "network initialisation");
       break;
     }
     // Kaiming-normal weights (real fan-in), zero biases; the head starts at
@@ -1276,6 +1450,41 @@ extern "C" int vdr_net_create(vdr_handle *H, unsigned long long seed, vdr_net **
     return st;
   }
   *out = N;
+  return VDR_OK;
+}
+
+extern "C" int vdr_net_set_conv(vdr_net *N, int mode) {
+  int st = net_check(N);
+  if (st) return st;
+  Net &n = N->n;
+  if (mode != VDR_NET_CONV_MMA && mode != VDR_NET_CONV_TCGEN05) {
+    set_error("vdr_net_set_conv: unknown mode");
+    return VDR_BAD_ARGUMENT;
+  }
+  if (mode == VDR_NET_CONV_TCGEN05 && !n.tc_ok) {
+    set_error("vdr_net_set_conv: the tensor maps of the tcgen05 path could not be made");
+    return VDR_BAD_ARGUMENT;
+  }
+  n.conv_mode = mode;
+  return VDR_OK;
+}
+
+extern "C" int vdr_net_conv_status(vdr_net *N, int *mode) {
+  int st = net_check(N);
+  if (st) return st;
+  Net &n = N->n;
+  if (mode) *mode = (n.conv_mode == VDR_NET_CONV_TCGEN05 && n.tc_ok) ? VDR_NET_CONV_TCGEN05
+                                                                       : VDR_NET_CONV_MMA;
+  int err = 0;
+  cudaError_t e = cudaMemcpyAsync(&err, n.tc_err, sizeof(int), cudaMemcpyDeviceToHost,
+                                  n.h->stream);
+  if (!e) e = cudaStreamSynchronize(n.h->stream);
+  if (!e) e = cudaMemsetAsync(n.tc_err, 0, sizeof(int), n.h->stream);
+  if (e) return cuda_fail(e, "vdr_net_conv_status");
+  if (err) {
+    set_error("a tcgen05 convolution gave up waiting for its operands");
+    return VDR_TIMEOUT;
+  }
   return VDR_OK;
 }
 

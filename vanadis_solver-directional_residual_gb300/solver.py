@@ -527,6 +527,22 @@ class LearnedNet:
                 "vdr_net_param_count")
         self.nparam = n.value
 
+    CONV = {"mma": 0, "tcgen05": 1}
+
+    def set_conv(self, mode: str):
+        """Forward convolutions on "tcgen05" (fifth-generation tensor cores,
+        TMA-staged operands, TMEM accumulators; the default where available)
+        or "mma" (warp-level mma.sync)."""
+        L.check(self.lib.vdr_net_set_conv(self.h, self.CONV[mode]), "vdr_net_set_conv")
+
+    def conv_status(self):
+        """(mode in use, status): status VDR_TIMEOUT (5) if a tcgen05
+        convolution gave up waiting for its operands since the last call."""
+        m = ctypes.c_int(-1)
+        st = self.lib.vdr_net_conv_status(self.h, ctypes.byref(m))
+        L.check(st, "vdr_net_conv_status", allow=(L.OK, L.TIMEOUT))
+        return {0: "mma", 1: "tcgen05"}[m.value], st
+
     def get_params(self) -> np.ndarray:
         out = np.empty(self.nparam, dtype=np.float32)
         L.check(self.lib.vdr_net_get_params(self.h, out.ctypes.data_as(_FP)),
