@@ -67,7 +67,8 @@ def args_parse(argv=None):
     ap.add_argument("--learn-steps", type=int, default=LEARN_STEPS)
     ap.add_argument("--learn-epochs", type=int, default=1)
     ap.add_argument("--case", default=None,
-                    choices=["apply", "block_apply", "bicg", "mixed", "unet_train"],
+                    choices=["apply", "block_apply", "bicg", "mixed", "unet_train",
+                             "unet_forward"],
                     help="run one small fixed workload for a profiler "
                          "capture instead of the benchmark")
     ap.add_argument("--cpu-iters", type=int, default=4,
@@ -660,6 +661,52 @@ def time_loop_section(vdr, s, prob, aH, aM, cf, rM):
     return out
 
 
+# FLOPs of one forward pass of the network (3x3x3 convolutions, 2 per
+# multiply-add) per level-0 voxel: sum over layers of 27 cin cout x (voxels
+# of the layer's level / voxels of level 0), with levels 1 and 2 holding
+# ~1/8 and ~1/64 of the voxels (computed exactly from the grid below).
+def network_flops(dims):
+    layers = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2),
+              (64, 64, 2), (96, 32, 1), (32, 32, 1), (48, 16, 0), (16, 16, 0)]
+    return sum(2.0 * 27 * ci * co * dims[l] for ci, co, l in layers)
+
+
+def network_forward_times(vdr, net, run, reps=10):
+    """One forward pass of the network on the workload's grid, per
+    convolution path, timed with CUDA events on the library's stream; the
+    rate counts the convolutions' FLOPs (the pools, upsampled copies and
+    head are in the time, not in the count)."""
+    import torch
+    m = run.prob.mesh
+    n0 = (m.nax, m.nay, m.naz)
+    n1 = tuple((v + 1) // 2 for v in n0)
+    n2 = tuple((v + 1) // 2 for v in n1)
+    vox = [n0[0] * n0[1] * n0[2], n1[0] * n1[1] * n1[2], n2[0] * n2[1] * n2[2]]
+    flops = network_flops(vox)
+    net.update_features(None)
+    st = torch.cuda.ExternalStream(run.s.stream())
+    rh = torch.randn(m.nnode, dtype=torch.float32, device="cuda")
+    out = torch.empty_like(rh)
+    torch.cuda.synchronize()
+    res = {"gflop": flops / 1e9}
+    for mode in ("tcgen05", "mma"):
+        net.set_conv(mode)
+        for _ in range(3):
+            net.forward(rh, out)
+        e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(reps):
+            net.forward(rh, out)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        res[mode] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12}
+    net.set_conv("tcgen05")
+    res["speedup"] = res["mma"]["ms"] / res["tcgen05"]["ms"]
+    return res
+
+
 def learned_section(vdr, device, a):
     """The learned preconditioner on the tilting-axis transient problem
     (128x128x64, theta-step at Courant 10, rotation axis tilting 0.5 degrees
@@ -679,6 +726,7 @@ def learned_section(vdr, device, a):
                        tilt_deg=LEARN_TILT, device=device)
     net = vdr.LearnedNet(run.s, seed=5)
     net.set_smoothing(0)
+    fwd = network_forward_times(vdr, net, run)
     steps_train = list(range(LEARN_TRAIN_STEPS))
     total = a.learn_steps
     t0 = time.perf_counter()
@@ -728,7 +776,10 @@ def learned_section(vdr, device, a):
                     "relative residual %g" % (nx, ny, nz, total, COURANT,
                                               LEARN_TILT, TOL),
         "network": "3-level 3D U-Net 16/32/64 channels, 3^3 kernels, BF16 "
-                   "weights/activations, FP32 accumulate (mma.sync m16n8k16)",
+                   "weights/activations, FP32 accumulate; forward convolutions "
+                   "on tcgen05 (TMA halo slabs, TMEM accumulators), backward "
+                   "passes on mma.sync m16n8k16",
+        "network_forward": fwd,
         "training": {"pairs": int(data["rhat"].shape[0]),
                      "pairs_from_learned_solves": int(more["rhat"].shape[0]),
                      "epochs": a.learn_epochs, "loss": "residual",
@@ -1110,6 +1161,8 @@ def summary_keys(line, step_s, solve_s):
         "c5_jacobi_s": _r(g(lp, "jacobi_bicgstab", "solve_s_total")),
         "c5_learned_s": _r(g(lp, "learned_then_jacobi", "solve_s_total")),
         "c5_learned_vs_jacobi_time": _r(lp.get("learned_vs_plain_time")),
+        "net_fwd_tc_ms": _r(g(lp, "network_forward", "tcgen05", "ms")),
+        "net_fwd_mma_ms": _r(g(lp, "network_forward", "mma", "ms")),
         "c4a_block_s": _r(g(line, "batched_rhs", "block_solve_s")),
         "c4a_speedup": _r(g(line, "batched_rhs", "speedup_vs_sequential_fp64")),
         "c4a_apply_frac": _r(g(line, "batched_rhs", "block_apply", "frac"), 3),
@@ -1167,6 +1220,20 @@ def run_case(a):
         s.assemble_rhs_device(b, 3.0, 0.0, None)
         x = torch.zeros_like(b)
         s.solve_mixed_device(b, x, tol=TOL, inner_tol=1e-5)
+    elif a.case == "unet_forward":
+        # three forward passes of the network per convolution path
+        run = vdr.learned.TiltingRun(a.nex, a.ney, a.nez, seed=1005, courant=COURANT,
+                                     tol=TOL, tilt_deg=LEARN_TILT)
+        net = vdr.LearnedNet(run.s, seed=11)
+        net.update_features(None)
+        rh = torch.randn(prob.mesh.nnode, dtype=torch.float32, device="cuda")
+        out = torch.empty_like(rh)
+        torch.cuda.synchronize()
+        for mode in ("tcgen05", "mma"):
+            net.set_conv(mode)
+            for _ in range(3):
+                net.forward(rh, out)
+        torch.cuda.synchronize()
     elif a.case == "unet_train":
         L = vdr.learned
         run = L.TiltingRun(a.nex, a.ney, a.nez, seed=1005, courant=COURANT,
