@@ -95,6 +95,21 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   d |= (uint64_t)1 << 46;
   return d;
 }
+// Swizzled K-major descriptor (layout 2 = 128B, 4 = 64B, 6 = 32B swizzle):
+// rows of the swizzle width, consecutive 8-row groups `sbo` bytes apart;
+// the leading offset is unused (an MMA's K extent lies within one row).
+// The swizzle is applied to absolute shared-memory address bits, as the TMA
+// unit applies it, so the start may lie anywhere on a 16-byte boundary
+// inside a slab the TMA unit wrote with the same mode (base offset 0).
+__device__ __forceinline__ uint64_t smem_desc_sw(uint32_t addr, uint32_t sbo, int layout) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)(layout & 7) << 61;
+  return d;
+}
 // Instruction descriptor of kind::f16 with BF16 A and B, FP32 accumulator,
 // both operands K-major: D format (1 = F32) in bits 4-5, A format (1 =
 // BF16) in 7-9, B format in 10-12, N >> 3 in 17-22, M >> 4 in 24-28.

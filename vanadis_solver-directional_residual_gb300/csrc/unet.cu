@@ -1041,19 +1041,24 @@ EncodeTiledFn encode_tiled() {
 }
 
 // The map of a channels-last [V][C] BF16 tensor on grid d: dimensions (C,
-// x, y, z), box (8 channels, 10 x 18 x 3 voxels) -- one 16-byte channel
-// chunk of a tile's halo slab; out-of-grid voxels read as zero.
-bool make_tmap(CUtensorMap *m, const bf16 *base, int C, const Dims &d) {
+// x, y, z), box (C channels, 10 x 18 x `planes` voxels) -- a tile's halo
+// slab, swizzled for the tensor cores by its row width 2C; out-of-grid
+// voxels read as zero.
+bool make_tmap(CUtensorMap *m, const bf16 *base, int C, int planes, const Dims &d) {
   EncodeTiledFn fn = encode_tiled();
   if (!fn || !base) return false;
+  if (C != 16 && C != 32 && C != 64) return false;
   const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)d.W, (cuuint64_t)d.H,
                               (cuuint64_t)d.D};
   const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)C * 2 * d.W,
                                  (cuuint64_t)C * 2 * d.W * d.H};
-  const cuuint32_t box[4] = {8, convtc::SX, convtc::SY, 3};
+  const cuuint32_t box[4] = {(cuuint32_t)C, convtc::SX, convtc::SY, (cuuint32_t)planes};
   const cuuint32_t es[4] = {1, 1, 1, 1};
+  const CUtensorMapSwizzle sw = C == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                        : (C == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                                   : CU_TENSOR_MAP_SWIZZLE_32B);
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(base), dims,
-            strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -1071,10 +1076,12 @@ bool make_tmaps(Net &n) {
                     {L_D1A, n.s1, n.up1},   {L_D1B, n.a3, nullptr},
                     {L_D0A, n.s0, n.up0},   {L_D0B, n.a4, nullptr}};
   for (const In &i : ins) {
-    const Dims &d = n.d[DEFS[i.l].level];
-    if (!make_tmap(&n.tmap[i.l][0], i.in1, DEFS[i.l].cin1, d)) return false;
+    const LayerDef &L = DEFS[i.l];
+    const Dims &d = n.d[L.level];
+    const int planes = convtc::group_of(L.cin1, L.cin2, L.cout) + 2;  // G + halo
+    if (!make_tmap(&n.tmap[i.l][0], i.in1, L.cin1, planes, d)) return false;
     n.tmap[i.l][1] = n.tmap[i.l][0];
-    if (i.in2 && !make_tmap(&n.tmap[i.l][1], i.in2, DEFS[i.l].cin2, d)) return false;
+    if (i.in2 && !make_tmap(&n.tmap[i.l][1], i.in2, L.cin2, planes, d)) return false;
   }
   return true;
 }
@@ -1094,7 +1101,7 @@ cudaError_t conv_tc_launch(const Net &n, int l, bf16 *out, const int *sk,
   a.D = d.D;
   a.tiles_x = (d.W + convtc::TX - 1) / convtc::TX;
   a.tiles_y = (d.H + convtc::TY - 1) / convtc::TY;
-  a.ntiles = a.tiles_x * a.tiles_y * d.D;
+  a.ntiles = a.tiles_x * a.tiles_y * ((d.D + Sh::G - 1) / Sh::G);
   a.wpk = n.wtc + n.woff[l];
   a.bias = n.theta + n.boff[l];
   a.out = out;
