@@ -79,7 +79,10 @@ __host__ __device__ constexpr int fit_group(int cin1, int cin2, int cout, int ns
   return 0;
 }
 // Double-buffered slabs when they allow G >= 2 (or as large a G as one
-// stage would), else one stage with the larger G.
+// stage would), else one stage with the larger G.  Measured: double
+// buffering matters more than a larger G (G = 4 with one stage instead of
+// G = 2 with two took the [16 | 32] -> 16 layer from 157 to 227 us, G = 8
+// with one stage the 32 -> 32 layer from 22.6 to 30.7 us).
 __host__ __device__ constexpr int stages_of(int cin1, int cin2, int cout) {
   return (fit_group(cin1, cin2, cout, 2) >= 2 ||
           fit_group(cin1, cin2, cout, 2) >= fit_group(cin1, cin2, cout, 1))
