@@ -410,6 +410,8 @@ def batched_rhs_section(vdr, device):
                            "ms": t_apply, "achieved_gbs": ach,
                            "algorithmic_bytes": alg, "peak": peak,
                            "frac": ach / peak, "peak_kind": peak_kind}}
+    out["block_apply"]["tuning"] = {k: v for k, v in s.apply_tuning().items()
+                                    if k.startswith("block")}
     s.close()
     return out
 
@@ -897,6 +899,9 @@ def run_native(a):
     build_issue = (inst_per_elem * E / (t_build * 1e-3) / 1e9
                    if inst_per_elem else None)
 
+    # ---- the launch shapes the handle chose by measurement ----
+    tuning = s.apply_tuning()
+
     # ---- the same step with the pure FP64 element-matrix store ----
     s64 = vdr.Solver(prob, vdr.Options(apply_mode="stored",
                                        matrix_storage="fp64",
@@ -1102,6 +1107,7 @@ def run_native(a):
                                             "clock of the timed region" % n_sm,
                                "instructions_from": "profiles/" + BUILD_PROFILE},
             "fp64_store": fp64_store,
+            "apply_tuning": tuning,
             "scatter_variants": scatter_variants,
             "mixed_precision": mixed,
             "batched_rhs": batched,
@@ -1169,6 +1175,8 @@ def summary_keys(line, step_s, solve_s):
         "c4b_s": _r(g(line, "batched_meshes", "segmented_solve_s")),
         "c4b_speedup": _r(g(line, "batched_meshes", "speedup_vs_one_at_a_time")),
         "apply_frac": _r(g(line, "roofline", "frac"), 3),
+        "apply_per_sm": g(line, "apply_tuning", "apply_blocks_per_sm"),
+        "half_per_sm": g(line, "apply_tuning", "half_blocks_per_sm"),
         "build_ms": _r(g(line, "breakdown_ms", "element_matrices_and_rhs")),
         "time_loop_later_s": _r(g(line, "time_loop", "later_step_s")),
         "time_loop_mixed_later_s": _r(g(line, "time_loop", "mixed", "later_step_s")),

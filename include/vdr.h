@@ -420,6 +420,24 @@ int vdr_solve_segmented_device(vdr_handle *h, const double *d_b, double *d_x,
                                double *errs, int *statuses);
 int vdr_segment_tuning(vdr_handle *h, int *tile_nodes, int *threads);
 
+/* Launch shapes of the operator applies, chosen by measurement on the
+ * handle's own operator (no counterpart in the reference): the first build
+ * of the stored operator times the stored apply's grid at 2, 4, 8, 16 and
+ * 32 resident blocks per SM and keeps the fastest, the first build of the
+ * binary16 inner operator does the same for its apply, and the first
+ * 64-column block solve times the node-tile block apply's (box height,
+ * column halves) at (2, 2), (2, 1) and (4, 2).  Meshes below 65,536
+ * elements keep the defaults (8 blocks per SM; (2, 2)) and report zero
+ * times.  Choices are cached per element-count octave for the process. */
+typedef struct vdr_apply_tuning_info {
+  int apply_blocks_per_sm, half_blocks_per_sm;
+  int block_tile_y, block_halves;
+  int grid_candidates[5];  /* blocks per SM tried, in the order of the times */
+  float apply_ms[5], half_ms[5];  /* time per apply of each candidate */
+  float block_ms[3];              /* (2,2), (2,1), (4,2) */
+} vdr_apply_tuning_info;
+int vdr_apply_tuning(vdr_handle *h, vdr_apply_tuning_info *info);
+
 /* Statistics of the handle's most recent solve. */
 typedef struct vdr_solve_stats {
   int iterations;      /* Krylov iterations done */

@@ -32,6 +32,15 @@ class VdrOptions(ctypes.Structure):
                 ("reserved", ctypes.c_int * 8)]
 
 
+class VdrApplyTuning(ctypes.Structure):
+    _fields_ = [("apply_blocks_per_sm", ctypes.c_int),
+                ("half_blocks_per_sm", ctypes.c_int),
+                ("block_tile_y", ctypes.c_int), ("block_halves", ctypes.c_int),
+                ("grid_candidates", ctypes.c_int * 5),
+                ("apply_ms", ctypes.c_float * 5), ("half_ms", ctypes.c_float * 5),
+                ("block_ms", ctypes.c_float * 3)]
+
+
 class VdrSolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("status", ctypes.c_int),
                 ("graph_launches", ctypes.c_int),
@@ -79,6 +88,7 @@ SIGNATURES = {
     "vdr_set_segments": (_i, [_P, _i, _I]),
     "vdr_solve_segmented_device": (_i, [_P, _P, _P, _d, _i, _I, _D, _I]),
     "vdr_segment_tuning": (_i, [_P, _I, _I]),
+    "vdr_apply_tuning": (_i, [_P, ctypes.POINTER(VdrApplyTuning)]),
     "vdr_net_create": (_i, [_P, ctypes.c_ulonglong, ctypes.POINTER(_P)]),
     "vdr_net_destroy": (_i, [_P]),
     "vdr_net_param_count": (_i, [_P, ctypes.POINTER(ctypes.c_longlong)]),

@@ -202,6 +202,10 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
     h.op64_valid = true;
     h.diag_valid = true;
     h.phi_valid = h.want_phi;
+    if (stored) {  // the apply's launch shape, once per handle
+      const int st = tune_stored_apply(h);
+      if (st) return st;
+    }
   }
   return VDR_OK;
 }
@@ -233,6 +237,10 @@ int ensure_operator32(Handle &h) {
         (e = cudaStreamSynchronize(h.stream)))
       return cuda_fail(e, "16-bit element matrices");
     h.use_half = bad == 0;  // out of range: the rounded FP32 operator
+    if (h.use_half) {
+      const int st = tune_half_apply(h);
+      if (st) return st;
+    }
   }
   if (h.mixed_op == VDR_MIXED_ROUNDED || h.mixed_op == VDR_MIXED_HALF) {
     // the hi parts of the double-float store are the FP64 element matrices

@@ -700,7 +700,7 @@ cudaError_t launch_stored_apply32v(const Handle &h, const float *x, float *y,
     const int p0 = color ? h.color_off[r] : 0;
     const int p1 = color ? h.color_off[r + 1] : h.E;
     if (p1 <= p0) continue;
-    const int grid = grid_for(p1 - p0, 256, 8);
+    const int grid = grid_for(p1 - p0, 256, h.apply_per_sm);
     if (color)
       stored_apply_f32v<false, false><<<grid, 256, 0, s>>>(h.A32v, cv, h.E, p0, p1, x, y,
                                                            skip, skip2);
@@ -804,7 +804,7 @@ cudaError_t launch_stored_apply(const Handle &h, bool fp32, bool transpose,
     const int p0 = color ? h.color_off[r] : 0;
     const int p1 = color ? h.color_off[r + 1] : h.E;
     if (p1 <= p0) continue;
-    const int grid = grid_for(p1 - p0, 256, 8);
+    const int grid = grid_for(p1 - p0, 256, h.apply_per_sm);
 #define VDR_LAUNCH(K, AP)                                                     \
   K<<<grid, 256, 0, s>>>(AP, h.conn, h.E, p0, p1, x, y, skip, skip2)
     if (!fp32 && h.storage == VDR_STORE_DF) {

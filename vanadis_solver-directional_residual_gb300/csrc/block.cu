@@ -1257,21 +1257,29 @@ void launch_tile(const Handle &h, const float *A, const float *X, float *Y,
                                                          mask, X, Y, skip);
 }
 
-// K = 64 runs as two column halves of 32 (measured: more resident blocks
-// per SM beat the second operator-fragment load, 0.43 vs 0.51 ms per
-// apply at 1M elements); TILE_Y = 2 (4 warps, 8 x 2 x 2 elements) measured
-// ahead of 4.
+// K = 64: the box height (TILE_Y = 2 or 4 element rows) and whether the 64
+// columns run as two blocks of 32 or one block of 64 are chosen by
+// measurement (tune_block_apply; two halves of 32 at TILE_Y = 2 measured
+// 0.43 vs 0.51 ms per apply at 1M elements when this was fixed by hand).
+template <bool SPLIT>
+void launch_tile_64(const Handle &h, const float *A, const float *X, float *Y,
+                    const int *skip, const unsigned char *mask, cudaStream_t s) {
+  if (h.blk_ty == 4) launch_tile<SPLIT, 2, 4, 2>(h, A, X, Y, skip, mask, s);
+  else if (h.blk_halves == 1) launch_tile<SPLIT, 4, TILE_Y, 1>(h, A, X, Y, skip, mask, s);
+  else launch_tile<SPLIT, 2, TILE_Y, 2>(h, A, X, Y, skip, mask, s);
+}
+
 void launch_tile_k(const Handle &h, int K, bool split, const float *A,
                    const float *X, float *Y, const int *skip,
                    const unsigned char *mask, cudaStream_t s) {
   if (split) {
     if (K == 16) launch_tile<true, 1, TILE_Y, 1>(h, A, X, Y, skip, mask, s);
     else if (K == 32) launch_tile<true, 2, TILE_Y, 1>(h, A, X, Y, skip, mask, s);
-    else launch_tile<true, 2, TILE_Y, 2>(h, A, X, Y, skip, mask, s);
+    else launch_tile_64<true>(h, A, X, Y, skip, mask, s);
   } else {
     if (K == 16) launch_tile<false, 1, TILE_Y, 1>(h, A, X, Y, skip, mask, s);
     else if (K == 32) launch_tile<false, 2, TILE_Y, 1>(h, A, X, Y, skip, mask, s);
-    else launch_tile<false, 2, TILE_Y, 2>(h, A, X, Y, skip, mask, s);
+    else launch_tile_64<false>(h, A, X, Y, skip, mask, s);
   }
 }
 
@@ -1370,6 +1378,51 @@ cudaError_t launch_block_rhs(const Handle &h, const double *phi, int K,
 // the error flag of the bulk-copy block apply); `scaled`: the Jacobi
 // preconditioner h.dinv32 folded into the columns (the block solve), else
 // the plain operator (the block apply of the C ABI).
+int tune_block_apply(Handle &h, const float *X, float *Y, const float4 *Aaos) {
+  if (h.blk_tuned) return VDR_OK;
+  h.blk_tuned = true;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h.stream, &cs) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusNone || h.E < 65536 || !h.block_tile ||
+      h.block_tma || !(h.nax > 1 && h.nay > 1 && h.naz > 1) || h.perm_d)
+    return VDR_OK;
+  const int ty[TUNE_TILES] = {2, 2, 4}, halves[TUNE_TILES] = {2, 1, 2};
+  cudaEvent_t e0, e1;
+  cudaError_t e;
+  if ((e = cudaEventCreate(&e0))) return cuda_fail(e, "tune events");
+  if ((e = cudaEventCreate(&e1))) {
+    cudaEventDestroy(e0);
+    return cuda_fail(e, "tune events");
+  }
+  float best = 1e30f;
+  int bi = 0;
+  const float *A = reinterpret_cast<const float *>(Aaos);
+  for (int c = 0; c < TUNE_TILES && !e; c++) {
+    h.blk_ty = ty[c];
+    h.blk_halves = halves[c];
+    launch_tile_k(h, 64, true, A, X, Y, nullptr, nullptr, h.stream);  // warm
+    cudaEventRecord(e0, h.stream);
+    for (int rep = 0; rep < 3; rep++)
+      launch_tile_k(h, 64, true, A, X, Y, nullptr, nullptr, h.stream);
+    cudaEventRecord(e1, h.stream);
+    count_launches(4);
+    if ((e = cudaEventSynchronize(e1))) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    h.blk_tune_ms[c] = ms / 3.f;
+    if (ms < best) {
+      best = ms;
+      bi = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e) return cuda_fail(e, "block apply tuning");
+  h.blk_ty = ty[bi];
+  h.blk_halves = halves[bi];
+  return VDR_OK;
+}
+
 cudaError_t ensure_aos(Handle &h, bool scaled, float4 **out) {
   cudaError_t e;
   if (!h.block_err) {
@@ -1508,6 +1561,14 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
   // The apply's operator copy carries the Jacobi scale (A D^-1).
   float4 *Aaos = nullptr;
   if ((e = ensure_aos(h, true, &Aaos))) return cuda_fail(e, "block operator copy");
+  if (K == 64 && !h.blk_tuned) {  // launch shape by measurement, before capture
+    if ((e = cudaMemsetAsync(a.p, 0, sizeof(float) * 2 * n, s)))
+      return cuda_fail(e, "block tuning");
+    const int tst = tune_block_apply(h, a.p, a.v, Aaos);
+    if (tst) return tst;
+    if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
+    h.bk_graph = nullptr;
+  }
   const int gv = std::min(BK_MAX_GRID, grid_n(n, BT, 2));  // one wave
   const int gm = grid_n(n, 256, 8);
   bo_mask<<<gm, 256, 0, s>>>(n, a.kshift, X, h.mask);

@@ -266,7 +266,7 @@ cudaError_t launch_apply_half(const Handle &h, const float *x, float *y,
   const ConnView cv = conn_view(h);
   if (cv.emask) {
     // whole warps of elements: the grid covers E rounded up to 32
-    const int grid = grid_for(h.E, 256, 8);
+    const int grid = grid_for(h.E, 256, h.half_per_sm);
     apply_half_struct<<<grid, 256, 0, s>>>(h.A16, h.e16, h.E, cv.nex, cv.ney,
                                            cv.nax, cv.pl, x, y, skip, skip2);
     count_launches(1);
@@ -278,7 +278,7 @@ cudaError_t launch_apply_half(const Handle &h, const float *x, float *y,
     const int p0 = color ? h.color_off[r] : 0;
     const int p1 = color ? h.color_off[r + 1] : h.E;
     if (p1 <= p0) continue;
-    const int grid = grid_for(p1 - p0, 256, 8);
+    const int grid = grid_for(p1 - p0, 256, h.half_per_sm);
     if (color)
       apply_half_table<false><<<grid, 256, 0, s>>>(h.A16, h.e16, h.conn, h.E, p0,
                                                    p1, x, y, skip, skip2);

@@ -124,12 +124,26 @@ struct OpArgs {
   double aH = 1.0, aM = 0.0;
 };
 
+// Candidate launch shapes of the apply tuner (tune.cu).
+constexpr int TUNE_GRIDS = 5;   // resident blocks per SM: 2, 4, 8, 16, 32
+constexpr int TUNE_TILES = 3;   // block apply (box height, column halves): (2,2) (2,1) (4,2)
+constexpr int TUNE_GRID_PER_SM[TUNE_GRIDS] = {2, 4, 8, 16, 32};
+
 struct Handle {
   int N = 0, E = 0;
   int nax = 0, nay = 0, naz = 0;  // > 0 when the mesh is the canonical structured numbering
   int device = 0;
   cudaStream_t stream = nullptr;
   vdr_options opt{};
+  // launch shapes chosen by measurement (tune.cu): resident blocks per SM
+  // of the stored single-product applies' grids and of the binary16 apply,
+  // the node-tile block apply's box height and column split (K = 64)
+  int apply_per_sm = 8, half_per_sm = 8;
+  bool apply_tuned = false, half_tuned = false;
+  float apply_tune_ms[TUNE_GRIDS] = {}, half_tune_ms[TUNE_GRIDS] = {};
+  int blk_ty = 2, blk_halves = 2;
+  bool blk_tuned = false;
+  float blk_tune_ms[TUNE_TILES] = {};
   int scatter = VDR_SCATTER_ATOMIC;  // ATOMIC or COLOR (WARP is ATOMIC + warp_agg)
   bool warp_agg = false;  // warp-aggregated atomics on the structured numbering
   int apply_mode = VDR_APPLY_STORED;
@@ -349,6 +363,17 @@ cudaError_t launch_half_store(Handle &h, int *bad, cudaStream_t s);
 // y += A^ x on FP32 vectors (x, y of length N).
 cudaError_t launch_apply_half(const Handle &h, const float *x, float *y,
                               const int *skip, const int *skip2, cudaStream_t s);
+
+// ---- launch-shape tuning (tune.cu) ----
+// Times the stored apply's grid candidates on the current operator and keeps
+// the fastest in h.apply_per_sm (once per handle; not while the stream is
+// being captured; meshes below 65,536 elements keep the default).
+int tune_stored_apply(Handle &h);
+// The same for the binary16 inner operator's apply (h.half_per_sm).
+int tune_half_apply(Handle &h);
+// The node-tile block apply's (box height, column halves) for K = 64, timed
+// on X -> Y scratch columns of N x 64 floats (h.blk_ty, h.blk_halves).
+int tune_block_apply(Handle &h, const float *X, float *Y, const float4 *Aaos);
 
 // ---- solvers (krylov.cu) ----
 int solve_device(Handle &h, int method, const double *b, double *x,

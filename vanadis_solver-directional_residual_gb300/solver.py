@@ -277,6 +277,22 @@ class Solver:
                 "vdr_segment_tuning")
         return t.value, th.value
 
+    def apply_tuning(self) -> dict:
+        """The applies' launch shapes chosen by measurement
+        (vdr_apply_tuning): blocks per SM of the stored and binary16 applies
+        with the time per apply of each candidate, and the block apply's box
+        height and column halves with the times of (2,2), (2,1), (4,2)."""
+        t = L.VdrApplyTuning()
+        L.check(self.lib.vdr_apply_tuning(self.h, ctypes.byref(t)), "vdr_apply_tuning")
+        grid = list(t.grid_candidates)
+        return {"apply_blocks_per_sm": t.apply_blocks_per_sm,
+                "apply_ms": dict(zip(grid, [round(v, 4) for v in t.apply_ms])),
+                "half_blocks_per_sm": t.half_blocks_per_sm,
+                "half_ms": dict(zip(grid, [round(v, 4) for v in t.half_ms])),
+                "block_tile_y": t.block_tile_y, "block_halves": t.block_halves,
+                "block_ms": dict(zip(["2x2", "2x1", "4x2"],
+                                     [round(v, 4) for v in t.block_ms]))}
+
     @_device_call
     def solve_learned_device(self, net, b, x, tol=None, itmax=1000,
                              stall_window=20):
