@@ -899,9 +899,6 @@ def run_native(a):
     build_issue = (inst_per_elem * E / (t_build * 1e-3) / 1e9
                    if inst_per_elem else None)
 
-    # ---- the launch shapes the handle chose by measurement ----
-    tuning = s.apply_tuning()
-
     # ---- the same step with the pure FP64 element-matrix store ----
     s64 = vdr.Solver(prob, vdr.Options(apply_mode="stored",
                                        matrix_storage="fp64",
@@ -1004,6 +1001,10 @@ def run_native(a):
         "FP64 atomics after neighbouring lanes add their shared x-face nodes "
         "by shuffles (4 instead of 8 atomics per element)")
     scatter_variants["color"]["what"] = "8 launches per apply, no atomics"
+
+    # ---- the launch shapes the handle chose by measurement (the binary16
+    # apply's after the mixed steps above) ----
+    tuning = s.apply_tuning()
 
     def section(skip, fn, *args):
         """An optional section; a failure is reported in its key (and on

@@ -428,7 +428,8 @@ int vdr_segment_tuning(vdr_handle *h, int *tile_nodes, int *threads);
  * 64-column block solve times the node-tile block apply's (box height,
  * column halves) at (2, 2), (2, 1) and (4, 2).  Meshes below 65,536
  * elements keep the defaults (8 blocks per SM; (2, 2)) and report zero
- * times.  Choices are cached per element-count octave for the process. */
+ * times.  Choices are cached per scatter form, store and element-count
+ * octave for the process. */
 typedef struct vdr_apply_tuning_info {
   int apply_blocks_per_sm, half_blocks_per_sm;
   int block_tile_y, block_halves;

@@ -8,8 +8,8 @@
 // the first time the operator is built -- before any solve captures an
 // iteration into a CUDA graph -- and keeps the fastest; the binary16 inner
 // operator's apply is tuned the same way when its store is first built.
-// The results are cached per (storage, element-count octave) for the
-// process, so handles of similar size reuse them.  Meshes below 65,536
+// The results are cached per (scatter form, storage, element-count octave)
+// for the process, so handles of similar size reuse them.  Meshes below 65,536
 // elements, where the launch is too short to time, keep the default of 8.
 // vdr_apply_tuning reports the choices and the measured times.
 #include <cuda_runtime.h>
@@ -26,7 +26,7 @@ namespace {
 constexpr int TUNE_MIN_ELEMENTS = 65536;
 
 std::mutex g_tune_mu;
-// (device, kind, storage, floor(log2 E)) -> (blocks per SM, times)
+// (device, kind, scatter form, storage, floor(log2 E)) -> (blocks per SM, times)
 struct TuneEntry {
   int per_sm;
   float ms[TUNE_GRIDS];
@@ -53,8 +53,10 @@ template <typename F>
 int time_grids(Handle &h, int *per_sm, float *ms_out, long key_kind, F launch) {
   int dev = 0;
   cudaGetDevice(&dev);
+  // the scatter form changes the kernel (and its resident blocks per SM)
+  const long form = (long)h.scatter * 2 + (h.warp_agg ? 1 : 0);
   const std::pair<long, long> key{((long)dev << 8) | key_kind,
-                                  ((long)h.storage << 8) | ilog2(h.E)};
+                                  (form << 16) | ((long)h.storage << 8) | ilog2(h.E)};
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_tune_cache.find(key);
