@@ -67,8 +67,8 @@ def args_parse(argv=None):
     ap.add_argument("--learn-steps", type=int, default=LEARN_STEPS)
     ap.add_argument("--learn-epochs", type=int, default=1)
     ap.add_argument("--case", default=None,
-                    choices=["apply", "block_apply", "bicg", "mixed", "unet_train",
-                             "unet_forward"],
+                    choices=["apply", "block_apply", "block_apply_tc", "bicg", "mixed",
+                             "unet_train", "unet_forward"],
                     help="run one small fixed workload for a profiler "
                          "capture instead of the benchmark")
     ap.add_argument("--cpu-iters", type=int, default=4,
@@ -315,6 +315,15 @@ BATCH_MESH = (128, 128, 64)
 BATCH_K = 64
 
 
+BLOCK_TILE_KERNEL = ("block_apply_tile<split> (8x2x2-element boxes, node rows "
+                     "staged in shared memory by cp.async, mma.sync m16n8k8 TF32 "
+                     "x3, one float4 atomic per node and 4 columns)")
+BLOCK_TC_KERNEL = ("block_apply_tc_kernel<split> (4x4x4-element boxes: box "
+                   "operator assembled in TMEM, node rows by 4-D TMA, split and "
+                   "transposed in shared memory, tcgen05.mma kind::tf32 x3 "
+                   "M=128 N=128+64 K=128, float4 atomics)")
+
+
 def batched_rhs_section(vdr, device):
     """Many right-hand sides with one operator: the 128x128x64 rotation +
     shear mesh (same theta-step operator at Courant 10), K = 64 seeded
@@ -375,15 +384,25 @@ def batched_rhs_section(vdr, device):
     Yf = torch.zeros_like(Xf)
     for _ in range(3):
         s.apply_block_accumulate_device(Xf, Yf, "tf32x3")
-    r0, r1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
-    torch.cuda.synchronize()
-    r0.record(st)
-    reps = 20
-    for _ in range(reps):
-        s.apply_block_accumulate_device(Xf, Yf, "tf32x3")
-    r1.record(st)
-    torch.cuda.synchronize()
-    t_apply = r0.elapsed_time(r1) / reps
+    def time_apply(reps=20):
+        r0, r1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+        torch.cuda.synchronize()
+        r0.record(st)
+        for _ in range(reps):
+            s.apply_block_accumulate_device(Xf, Yf, "tf32x3")
+        r1.record(st)
+        torch.cuda.synchronize()
+        return r0.elapsed_time(r1) / reps
+    t_apply = time_apply()
+    tuning = {k: v for k, v in s.apply_tuning().items() if k.startswith("block")}
+    # both K = 64 forms on their own (the solve above used the measured choice)
+    form_ms = {}
+    for form in ("tile", "tcgen05"):
+        s.set_block_apply(form)
+        for _ in range(3):
+            s.apply_block_accumulate_device(Xf, Yf, "tf32x3")
+        form_ms[form] = time_apply()
+    s.set_block_apply("auto")
     # FP32 element matrix (256 B) per element (the node-tile kernel forms
     # node numbers from the structured numbering: no connectivity read); X
     # read once and Y read + written once (4 B per column per node)
@@ -401,17 +420,15 @@ def batched_rhs_section(vdr, device):
            "sequential_fp64_iterations_max": max(its),
            "sequential_worst_rel_residual": worst_single,
            "speedup_vs_sequential_fp64": t_single / t_block,
-           "block_apply": {"kernel": "block_apply_tile<split> (8x2x2-element "
-                                     "boxes, node rows staged in shared "
-                                     "memory by cp.async, mma.sync m16n8k8 "
-                                     "TF32 x3, one float4 atomic per node "
-                                     "and 4 columns; K = 64 as two column "
-                                     "halves)",
+           "block_apply": {"kernel": BLOCK_TC_KERNEL if tuning["block_tcgen05"]
+                                     else BLOCK_TILE_KERNEL,
                            "ms": t_apply, "achieved_gbs": ach,
                            "algorithmic_bytes": alg, "peak": peak,
-                           "frac": ach / peak, "peak_kind": peak_kind}}
-    out["block_apply"]["tuning"] = {k: v for k, v in s.apply_tuning().items()
-                                    if k.startswith("block")}
+                           "frac": ach / peak, "peak_kind": peak_kind,
+                           "form_ms": form_ms,
+                           "form_frac": {f: alg / (ms * 1e-3) / 1e9 / peak
+                                         for f, ms in form_ms.items()}}}
+    out["block_apply"]["tuning"] = tuning
     s.close()
     return out
 
@@ -1173,6 +1190,8 @@ def summary_keys(line, step_s, solve_s):
         "c4a_block_s": _r(g(line, "batched_rhs", "block_solve_s")),
         "c4a_speedup": _r(g(line, "batched_rhs", "speedup_vs_sequential_fp64")),
         "c4a_apply_frac": _r(g(line, "batched_rhs", "block_apply", "frac"), 3),
+        "c4a_tile_ms": _r(g(line, "batched_rhs", "block_apply", "form_ms", "tile"), 4),
+        "c4a_tcgen05_ms": _r(g(line, "batched_rhs", "block_apply", "form_ms", "tcgen05"), 4),
         "c4b_s": _r(g(line, "batched_meshes", "segmented_solve_s")),
         "c4b_speedup": _r(g(line, "batched_meshes", "speedup_vs_one_at_a_time")),
         "apply_frac": _r(g(line, "roofline", "frac"), 3),
@@ -1188,7 +1207,8 @@ def summary_keys(line, step_s, solve_s):
 def run_case(a):
     """Small fixed workloads for profiler captures (not benchmarks): the
     stored double-float apply (--case apply), the K=64 block solve
-    (--case block_apply), a BiCG solve (--case bicg, fused A/A^T apply), a
+    (--case block_apply), four K=64 block applies on the tcgen05 box form
+    (--case block_apply_tc), a BiCG solve (--case bicg, fused A/A^T apply), a
     mixed-precision solve (--case mixed, FP32-vector inner apply) and
     learned-network training steps (--case unet_train), each on the
     --nex x --ney x --nez mesh."""
@@ -1214,6 +1234,15 @@ def run_case(a):
         s.assemble_rhs_block_device(Q, B, 3.0)
         X = torch.zeros_like(B)
         s.solve_block_device(B, X, tol=TOL, inner_tol=1e-3, precision="tf32x3")
+    elif a.case == "block_apply_tc":
+        # four 64-column accumulating block applies on the tcgen05 form
+        s = vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=2.0, aM=3.0 / dt)
+        s.set_block_apply("tcgen05")
+        X = torch.randn((prob.mesh.nnode, BATCH_K), dtype=torch.float32, device="cuda")
+        Y = torch.zeros_like(X)
+        torch.cuda.synchronize()
+        for _ in range(4):
+            s.apply_block_accumulate_device(X, Y, "tf32x3")
     elif a.case == "bicg":
         # BiCG: the fused A p / A^T p~ apply over the double-float store
         s = vdr.Solver(prob, vdr.Options(apply_mode="stored", solver="bicg"),

@@ -242,11 +242,18 @@ int vdr_time_steps(vdr_handle *h, int nsteps, double cf, double rM,
 #define VDR_BLOCK_TF32X3 2 /* FP32 vectors, split TF32 (three MMAs per
                               product: FP32-level accuracy) */
 
-/* Data movement of the tensor-core block apply: VDR_BLOCK_APPLY_TILE
- * (default) takes boxes of 8 x 2 x 2 elements of a mesh in the canonical
- * structured numbering, reads each node row of a box once into shared
- * memory and adds each result row once, one float4 atomic per 4 columns
- * (other meshes, and colour-ordered storage, use the LSU variant);
+/* Data movement of the tensor-core block apply: VDR_BLOCK_APPLY_AUTO
+ * (default) is the node tile below, or for K = 64 the tcgen05 box apply
+ * when the handle's first 64-column block solve measured it faster;
+ * VDR_BLOCK_APPLY_TCGEN05 takes, for K = 64, boxes of 4 x 4 x 4 elements,
+ * assembles each box's 125 x 125 operator in tensor memory and multiplies
+ * it with the box's node rows on the fifth-generation tensor cores
+ * (tcgen05.mma kind::tf32, node rows by TMA; other K use the node tile);
+ * VDR_BLOCK_APPLY_TILE takes boxes of 8 x 2 x 2 elements of a mesh in the
+ * canonical structured numbering, reads each node row of a box once into
+ * shared memory and adds each result row once, one float4 atomic per 4
+ * columns (mma.sync; other meshes, and colour-ordered storage, use the LSU
+ * variant, as do the two forms above);
  * VDR_BLOCK_APPLY_LSU gathers X rows with 16-byte loads and scatters with
  * float4 atomics, per element; VDR_BLOCK_APPLY_BULK moves each element's
  * K-wide node rows into shared memory with cp.async.bulk (mbarrier
@@ -256,8 +263,11 @@ int vdr_time_steps(vdr_handle *h, int nsteps, double cf, double rM,
 #define VDR_BLOCK_APPLY_BULK 0
 #define VDR_BLOCK_APPLY_LSU 1
 #define VDR_BLOCK_APPLY_TILE 2
+#define VDR_BLOCK_APPLY_TCGEN05 3
+#define VDR_BLOCK_APPLY_AUTO 4
 int vdr_set_block_apply(vdr_handle *h, int variant);
-/* Diagnostic of the bounded device wait used by VDR_BLOCK_APPLY_BULK: one
+/* Diagnostic of the bounded device wait used by VDR_BLOCK_APPLY_BULK (the
+ * tcgen05 box apply bounds its waits the same way): one
  * warp waits on an mbarrier that nothing completes, with a ~1 ms budget;
  * the wait gives up, flags it and returns.  Returns VDR_TIMEOUT when that
  * path works (the handle stays usable). */
@@ -426,16 +436,18 @@ int vdr_segment_tuning(vdr_handle *h, int *tile_nodes, int *threads);
  * 32 resident blocks per SM and keeps the fastest, the first build of the
  * binary16 inner operator does the same for its apply, and the first
  * 64-column block solve times the node-tile block apply's (box height,
- * column halves) at (2, 2), (2, 1) and (4, 2).  Meshes below 65,536
- * elements keep the defaults (8 blocks per SM; (2, 2)) and report zero
- * times.  Choices are cached per scatter form, store and element-count
- * octave for the process. */
+ * column halves) at (2, 2), (2, 1) and (4, 2) and the tcgen05 box apply.
+ * Meshes below 65,536 elements keep the defaults (8 blocks per SM; node
+ * tile (2, 2)) and report zero times.  The stored and binary16 choices are
+ * cached per scatter form, store and element-count octave for the process;
+ * the block apply's per handle. */
 typedef struct vdr_apply_tuning_info {
   int apply_blocks_per_sm, half_blocks_per_sm;
   int block_tile_y, block_halves;
   int grid_candidates[5];  /* blocks per SM tried, in the order of the times */
   float apply_ms[5], half_ms[5];  /* time per apply of each candidate */
-  float block_ms[3];              /* (2,2), (2,1), (4,2) */
+  float block_ms[4];              /* node tile (2,2), (2,1), (4,2); tcgen05 */
+  int block_tcgen05;              /* 1: the tcgen05 box apply was chosen */
 } vdr_apply_tuning_info;
 int vdr_apply_tuning(vdr_handle *h, vdr_apply_tuning_info *info);
 

@@ -82,7 +82,7 @@ TF32_TOL = {"tf32": 5e-3, "tf32x3": 2e-5}
 
 @pytest.mark.parametrize("K", [16, 32, 64])
 @pytest.mark.parametrize("precision", ["tf32", "tf32x3"])
-@pytest.mark.parametrize("variant", ["bulk", "lsu", "tile"])
+@pytest.mark.parametrize("variant", ["bulk", "lsu", "tile", "tcgen05"])
 def test_block_apply_tensor_core(vdr, oracle, gpu_lib, case, K, precision,
                                  variant):
     import torch
@@ -128,7 +128,7 @@ def test_block_apply_accumulate(vdr, oracle, gpu_lib, case, precision, K):
         assert rel_l2(Y[:, k], 2.0 * yref) < tol, k
 
 
-@pytest.mark.parametrize("variant", ["tile", "lsu"])
+@pytest.mark.parametrize("variant", ["tile", "lsu", "tcgen05"])
 def test_block_apply_ignores_dirichlet_entries(vdr, oracle, gpu_lib, case,
                                                variant):
     """Dirichlet rows of X read as zero whatever they hold (NaN, inf) and

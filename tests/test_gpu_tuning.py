@@ -1,8 +1,9 @@
 """Launch shapes chosen by measurement (vdr_apply_tuning): on a mesh large
 enough to be tuned (64 x 64 x 32 = 131,072 elements) the stored apply, the
-binary16 inner apply and the 64-column block apply each pick one of their
-candidates with measured times, and the operator keeps its parity with the
-oracle under the chosen shapes; a small mesh keeps the defaults."""
+binary16 inner apply and the 64-column block apply (node-tile shapes and the
+tcgen05 box apply) each pick one of their candidates with measured times,
+and the operator keeps its parity with the oracle under the chosen shapes; a
+small mesh keeps the defaults."""
 import numpy as np
 import pytest
 
@@ -58,6 +59,10 @@ def test_tuned_shapes_and_parity(vdr, oracle, gpu_lib):
         t = s.apply_tuning()
         assert (t["block_tile_y"], t["block_halves"]) in [(2, 2), (2, 1), (4, 2)]
         assert all(v > 0 for v in t["block_ms"].values())
+        assert set(t["block_ms"]) == {"2x2", "2x1", "4x2", "tcgen05"}
+        # the tcgen05 box apply is chosen exactly when it timed fastest
+        fastest = min(t["block_ms"], key=t["block_ms"].get)
+        assert t["block_tcgen05"] == (fastest == "tcgen05")
 
 
 def test_small_mesh_keeps_defaults(vdr, gpu_lib):
@@ -66,5 +71,5 @@ def test_small_mesh_keeps_defaults(vdr, gpu_lib):
         s.apply(np.ones(prob.mesh.nnode))
         t = s.apply_tuning()
     assert t["apply_blocks_per_sm"] == 8 and t["half_blocks_per_sm"] == 8
-    assert (t["block_tile_y"], t["block_halves"]) == (2, 2)
+    assert (t["block_tile_y"], t["block_halves"]) == (2, 2) and not t["block_tcgen05"]
     assert all(v == 0 for v in t["apply_ms"].values())

@@ -38,7 +38,7 @@ class VdrApplyTuning(ctypes.Structure):
                 ("block_tile_y", ctypes.c_int), ("block_halves", ctypes.c_int),
                 ("grid_candidates", ctypes.c_int * 5),
                 ("apply_ms", ctypes.c_float * 5), ("half_ms", ctypes.c_float * 5),
-                ("block_ms", ctypes.c_float * 3)]
+                ("block_ms", ctypes.c_float * 4), ("block_tcgen05", ctypes.c_int)]
 
 
 class VdrSolveStats(ctypes.Structure):

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libvdr.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["element.cu", "apply.cu", "half.cu", "krylov.cu", "abi.cu", "noalloc.cu",
-           "block.cu", "unet.cu", "gcr.cu", "batch.cu", "tune.cu", "txtio.cpp"]
+           "block.cu", "block_tc.cu", "unet.cu", "gcr.cu", "batch.cu", "tune.cu", "txtio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-Wall", "--expt-relaxed-constexpr"]

@@ -962,13 +962,16 @@ int vdr_set_block_apply(vdr_handle *H, int variant) {
   int st = check_handle(H);
   if (st) return st;
   if (variant != VDR_BLOCK_APPLY_BULK && variant != VDR_BLOCK_APPLY_LSU &&
-      variant != VDR_BLOCK_APPLY_TILE) {
+      variant != VDR_BLOCK_APPLY_TILE && variant != VDR_BLOCK_APPLY_TCGEN05 &&
+      variant != VDR_BLOCK_APPLY_AUTO) {
     set_error("vdr_set_block_apply: unknown variant");
     return VDR_BAD_ARGUMENT;
   }
   Handle &h = H->h;
   h.block_tma = variant == VDR_BLOCK_APPLY_BULK;
-  h.block_tile = variant == VDR_BLOCK_APPLY_TILE;
+  h.block_tile = variant == VDR_BLOCK_APPLY_TILE || variant == VDR_BLOCK_APPLY_TCGEN05 ||
+                 variant == VDR_BLOCK_APPLY_AUTO;
+  h.blk_tc_mode = variant == VDR_BLOCK_APPLY_TCGEN05 ? 1 : (variant == VDR_BLOCK_APPLY_AUTO ? -1 : 0);
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
   h.bk_graph = nullptr;
   return VDR_OK;

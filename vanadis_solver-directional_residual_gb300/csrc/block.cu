@@ -1297,6 +1297,10 @@ int block_apply_launches_tf32(const Handle &h, int K, bool split,
   if (!h.block_tma && h.block_tile && h.nax > 1 && h.nay > 1 && h.naz > 1 &&
       !h.perm_d && !dscale && !(reinterpret_cast<uintptr_t>(X) & 15) &&
       !(reinterpret_cast<uintptr_t>(Y) & 15)) {
+    // K = 64: the tcgen05 box apply when requested or measured fastest
+    if (K == 64 && (h.blk_tc_mode == 1 || (h.blk_tc_mode < 0 && h.blk_use_tc)) &&
+        block_tc_supported(h))
+      return launch_block_tc(h, split, A, X, Y, skip, x_clean ? nullptr : h.mask, s);
     launch_tile_k(h, K, split, A, X, Y, skip, x_clean ? nullptr : h.mask, s);
     count_launches(1);
     return cudaGetLastError() == cudaSuccess ? VDR_OK : VDR_CUDA_ERROR;
@@ -1374,10 +1378,10 @@ cudaError_t launch_block_rhs(const Handle &h, const double *phi, int K,
   return cudaGetLastError();
 }
 
-// Element-major FP32 copy of the operator for the tensor-core apply (and
-// the error flag of the bulk-copy block apply); `scaled`: the Jacobi
-// preconditioner h.dinv32 folded into the columns (the block solve), else
-// the plain operator (the block apply of the C ABI).
+// The K = 64 block apply's form by measurement, once per handle and
+// before any capture: the node tile at (box height, column halves) (2, 2),
+// (2, 1), (4, 2) and the tcgen05 box apply, each timed over 3 applies of X
+// into the scratch Y after one warm-up; the fastest is kept.
 int tune_block_apply(Handle &h, const float *X, float *Y, const float4 *Aaos) {
   if (h.blk_tuned) return VDR_OK;
   h.blk_tuned = true;
@@ -1386,7 +1390,9 @@ int tune_block_apply(Handle &h, const float *X, float *Y, const float4 *Aaos) {
       cs != cudaStreamCaptureStatusNone || h.E < 65536 || !h.block_tile ||
       h.block_tma || !(h.nax > 1 && h.nay > 1 && h.naz > 1) || h.perm_d)
     return VDR_OK;
-  const int ty[TUNE_TILES] = {2, 2, 4}, halves[TUNE_TILES] = {2, 1, 2};
+  // candidates 0-2: node-tile shapes; 3: the tcgen05 box apply
+  const int ty[TUNE_TILES] = {2, 2, 4, 2}, halves[TUNE_TILES] = {2, 1, 2, 2};
+  const int ncand = (block_tc_supported(h) && h.blk_tc_mode != 0) ? TUNE_TILES : TUNE_TILES - 1;
   cudaEvent_t e0, e1;
   cudaError_t e;
   if ((e = cudaEventCreate(&e0))) return cuda_fail(e, "tune events");
@@ -1397,16 +1403,22 @@ int tune_block_apply(Handle &h, const float *X, float *Y, const float4 *Aaos) {
   float best = 1e30f;
   int bi = 0;
   const float *A = reinterpret_cast<const float *>(Aaos);
-  for (int c = 0; c < TUNE_TILES && !e; c++) {
+  int st = VDR_OK;
+  for (int c = 0; c < ncand && !e && !st; c++) {
     h.blk_ty = ty[c];
     h.blk_halves = halves[c];
-    launch_tile_k(h, 64, true, A, X, Y, nullptr, nullptr, h.stream);  // warm
-    cudaEventRecord(e0, h.stream);
-    for (int rep = 0; rep < 3; rep++)
+    auto launch = [&]() {
+      if (c == TUNE_TILES - 1)
+        return launch_block_tc(h, true, A, X, Y, nullptr, nullptr, h.stream);
       launch_tile_k(h, 64, true, A, X, Y, nullptr, nullptr, h.stream);
+      count_launches(1);
+      return VDR_OK;
+    };
+    if ((st = launch())) break;  // warm
+    cudaEventRecord(e0, h.stream);
+    for (int rep = 0; rep < 3 && !st; rep++) st = launch();
     cudaEventRecord(e1, h.stream);
-    count_launches(4);
-    if ((e = cudaEventSynchronize(e1))) break;
+    if (st || (e = cudaEventSynchronize(e1))) break;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     h.blk_tune_ms[c] = ms / 3.f;
@@ -1417,12 +1429,18 @@ int tune_block_apply(Handle &h, const float *X, float *Y, const float4 *Aaos) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (st) return st;
   if (e) return cuda_fail(e, "block apply tuning");
+  h.blk_use_tc = bi == TUNE_TILES - 1;
   h.blk_ty = ty[bi];
   h.blk_halves = halves[bi];
   return VDR_OK;
 }
 
+// Element-major FP32 copy of the operator for the tensor-core applies (and
+// the error flag of their bounded waits); `scaled`: the Jacobi
+// preconditioner h.dinv32 folded into the columns (the block solve), else
+// the plain operator (the block apply of the C ABI).
 cudaError_t ensure_aos(Handle &h, bool scaled, float4 **out) {
   cudaError_t e;
   if (!h.block_err) {
@@ -1672,7 +1690,7 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
     return cuda_fail(e, "block solve");
   if (tma_err) {
     cudaMemset(h.block_err, 0, sizeof(int));
-    set_error("block solve: a bulk-copy wait ran out of time");
+    set_error("block solve: a bounded device wait of the block apply ran out of time");
     return VDR_TIMEOUT;
   }
   if (outer_iters) *outer_iters = outer;

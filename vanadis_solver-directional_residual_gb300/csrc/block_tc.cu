@@ -1,0 +1,585 @@
+// block_tc.cu -- the 64-column block apply Y += A X on the fifth-generation
+// tensor cores, for meshes in the canonical structured numbering.
+//
+// The mma.sync applies of block.cu contract each 8 x 8 element matrix with
+// its 8 node rows; they are bound by the instructions that gather, split
+// and scatter per element.  Here a CTA takes a box of 4 x 4 x 4 elements
+// and its 5 x 5 x 5 = 125 node rows, assembles the box operator A_box
+// (125 x 125: the couplings of the box's own elements) in tensor memory,
+// and computes D = A_box X_box for all 64 columns with tcgen05.mma
+// (kind::tf32, M = 128 rows = box nodes, K = 128 box nodes, FP32
+// accumulators in TMEM):
+//
+//   X_box   the 125 node rows (64 floats each) arrive by two 4-D TMA boxes
+//           (32 columns x 5 x 5 x 5 nodes, 128-byte swizzle) from the
+//           node-major block vector viewed as (64, nax, nay, naz); nodes
+//           outside the mesh arrive as zeros.  TF32 operands must be
+//           K-major (an MN-major TF32 B operand measured all zeros), so the
+//           split pass writes B transposed: row n = column n of X, the 125
+//           box nodes along K (lane = node: each store of a warp fills one
+//           128-byte row, no bank conflicts).
+//   A_box   thread r of the four assembly warps owns box node r: it sums
+//           node r's rows of the (up to 8) box elements around it into its
+//           27 stencil couplings, writes them into its row of a shared
+//           staging buffer at columns r + dx + 5 dy + 25 dz (the other
+//           columns of the row stay zero), reads back the columns its warp
+//           covers and stores them to TMEM lane r (tcgen05.st) as TF32 head
+//           and tail.  The MMAs read A from TMEM.
+//   split   D = A_hi [X_hi | X_lo] (one N = 128 MMA per K step: head and
+//           tail of X side by side in B) + A_lo X_hi (N = 64): the three
+//           products of split TF32, FP32-level accuracy.  Plain TF32 issues
+//           A_hi X_hi alone.
+//   Y       the epilogue adds the two halves of D and sends each node row
+//           with 16 float4 atomics; nodes on box faces receive one add per
+//           box that shares them.
+//
+// The element matrices come from the element-major FP32 copy
+// Aaos[p*64 + 8i + j] (Jacobi scale folded into the columns, Dirichlet rows
+// and columns zero), each 32-byte row read once.
+//
+// Warp roles (448 threads, one CTA per SM, boxes strided over the grid):
+// warp 0 = TMA producer, warp 1 = TMEM owner and MMA issuer, warps 2-5 = A
+// assembly (element rows loaded one box ahead), warps 6-9 = X split and
+// transpose (one 32-node K atom each), warps 10-13 = epilogue; warp w
+// reaches TMEM lanes 32 (w % 4) .. 32 (w % 4) + 31.  The TMA stages and D
+// are double-buffered, so the load of box i+1 and the epilogue of box i-1
+// overlap the MMAs of box i.  A (256 of the 512 TMEM columns) and B are
+// single and handed over in two halves of K: box i's MMAs release the first
+// half while the second half multiplies, and box i+1's first half (its A
+// columns and its B atoms) is written meanwhile.
+// Every mbarrier wait is bounded; a wait that runs out sets *err, the
+// roles stop, outstanding copies and MMAs are drained (bounded too) and the
+// TMEM is released before the kernel returns.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+#include "tc_ptx.cuh"
+#include "vdr_internal.h"
+
+namespace vdr {
+namespace blocktc {
+
+constexpr int BE = 4, BN = 5, ROWS = BN * BN * BN;  // box: 4^3 elements, 125 nodes
+// warps: 0 TMA producer, 1 MMA issuer, 2-5 A assembly, 6-9 X split, 10-13
+// epilogue
+constexpr int W_ASM = 2, W_SPL = 6, W_EPI = 10;
+constexpr int THREADS = 32 * (W_EPI + 4);
+constexpr int XREG = 16384;         // 128 rows x 128 bytes: 32 columns of the TMA stage
+constexpr int XSTAGE = 2 * XREG;    // node rows as the TMA lands them
+constexpr int XBYTES = 2 * 32 * 4 * ROWS;  // bytes the two TMA boxes land
+constexpr int KATOM = 16384;        // B: 128 rows (columns of X) x 32 nodes x 4 bytes
+constexpr int BSTAGE = 4 * KATOM;   // B: rows 0-63 head, 64-127 tail; K = 128 nodes
+                                    // (atoms 0-1: first half of K, 2-3: second)
+constexpr int SPITCH = 100;         // staging row pitch (floats): conflict-free rows
+constexpr int STAGING = 128 * SPITCH * 4;
+constexpr int NBAR = 13;
+constexpr int SMEM = 1024 + 2 * XSTAGE + BSTAGE + STAGING + NBAR * 8 + 8;
+constexpr int TMEM_COLS = 512;
+constexpr uint32_t A_HI = 0, A_LO = 128, D_BASE = 256;  // TMEM columns
+constexpr long long WAIT_LIMIT = 2000000000LL;         // ~1 s of clocks per wait
+// barrier indices
+// AFULL / AFREE: one per half of K, covering that half's A columns (TMEM)
+// and B rows' K atoms (shared memory)
+constexpr int B_XFULL = 0, B_XEMPTY = 2, B_AFULL = 4, B_AFREE = 6, B_DFULL = 8,
+              B_DEMPTY = 10, B_DRAIN = 12;
+
+struct Args {
+  const float *A;             // Aaos, [E][64]
+  float *Y;                   // [N][64], accumulated
+  const unsigned char *mask;  // optional: Dirichlet rows of X read as zero, of Y get nothing
+  int nax, nay, naz;          // nodes per direction
+  int nbx, nby, nbox;         // boxes in x, y; all boxes
+  const int *skip;            // nonzero: return at once (a finished inner solve)
+  int *err;                   // bit 0: a wait ran out
+};
+
+// Instruction descriptor of kind::tf32: FP32 accumulator (bits 4-5), A and
+// B TF32 (format 2 in bits 7-9 and 10-12), both K-major, N >> 3 in bits
+// 17-22, M >> 4 in 24-28.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+// D[tmem] (+)= A[tmem] * B[desc]^T, kind::tf32, one CTA, issued by one thread.
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d, uint32_t a, uint64_t bdesc,
+                                            uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, q;\n}\n" ::"r"(d),
+      "r"(a), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// Whole warp: 16 consecutive 32-bit columns of the warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
+      "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]),
+      "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t tf32_rna(float f) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(f));
+  return r;
+}
+// Local index of the HEX8 corner (x, y, z): 0 (0,0,0), 1 (1,0,0), 2 (1,1,0),
+// 3 (0,1,0), and + 4 at z = 1.
+__host__ __device__ constexpr int corner(int x, int y, int z) {
+  return 4 * z + (y ? (x ? 2 : 3) : (x ? 1 : 0));
+}
+__host__ __device__ constexpr int cx(int j) { return ((j & 3) == 1 || (j & 3) == 2) ? 1 : 0; }
+__host__ __device__ constexpr int cy(int j) { return (j & 3) >> 1; }
+__host__ __device__ constexpr int cz(int j) { return j >> 2; }
+
+template <bool SPLIT>
+__global__ void __launch_bounds__(THREADS, 1)
+    block_apply_tc_kernel(const __grid_constant__ CUtensorMap xmap, Args a) {
+  if (a.skip && *(volatile const int *)a.skip) return;
+  extern __shared__ unsigned char dsm[];
+  unsigned char *base =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(dsm) + 1023) &
+                                        ~static_cast<uintptr_t>(1023));
+  unsigned char *xst = base;                // two TMA stages: node rows
+  unsigned char *bst = base + 2 * XSTAGE;   // B (transposed, split)
+  float *staging = reinterpret_cast<float *>(bst + BSTAGE);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(bst + BSTAGE + STAGING);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + NBAR);
+  auto bar = [&](int i) { return tc::smem_u32(bars + i); };
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nex = a.nax - 1, ney = a.nay - 1, nez = a.naz - 1;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 2; i++) {
+      tc::mbar_init(bar(B_XFULL + i), 1);
+      tc::mbar_init(bar(B_XEMPTY + i), 4);
+      tc::mbar_init(bar(B_AFULL + i), 4 + 2);  // A assembly warps + split warps of the half
+      tc::mbar_init(bar(B_AFREE + i), 1);
+      tc::mbar_init(bar(B_DFULL + i), 1);
+      tc::mbar_init(bar(B_DEMPTY + i), 4);
+    }
+    tc::mbar_init(bar(B_DRAIN), 1);
+    tc::mbar_init_fence();
+  }
+  if (warp == 1) tc::tmem_alloc(tc::smem_u32(tslot), TMEM_COLS);
+  if (warp >= W_ASM && warp < W_ASM + 4) {
+    // staging rows zero (only a row's stencil columns are ever written)
+    const int r = 32 * (warp & 3) + lane;
+    float4 *srow = reinterpret_cast<float4 *>(staging + r * SPITCH);
+    for (int i = 0; i < SPITCH / 4; i++) srow[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  } else if (warp >= W_SPL && warp < W_SPL + 4) {
+    // K positions 124..127 of every B row zero: 125..127 are never written
+    // and the MMA reads them (times zero columns of A)
+    const int row = threadIdx.x - 32 * W_SPL;
+    *reinterpret_cast<float4 *>(bst + 3 * KATOM + row * 128 + ((7 ^ (row & 7)) << 4)) =
+        make_float4(0.f, 0.f, 0.f, 0.f);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0) {
+    // ------------------------------------------------ producer
+    if (lane == 0) {
+      tc::prefetch_tensormap(&xmap);
+      bool ok = true;
+      int it = 0;
+      for (int b = blockIdx.x; b < a.nbox; b += gridDim.x, it++) {
+        // the split of the box two back has read the stage
+        const int s = it & 1;
+        if (!tc::mbar_wait(bar(B_XEMPTY + s), ((uint32_t)(it >> 1) & 1u) ^ 1u, WAIT_LIMIT)) {
+          ok = false;
+          break;
+        }
+        const int bx = b % a.nbx, by = (b / a.nbx) % a.nby, bz = b / (a.nbx * a.nby);
+        tc::mbar_arrive_expect_tx(bar(B_XFULL + s), XBYTES);
+        const uint32_t dst = tc::smem_u32(xst + s * XSTAGE);
+        tc::tma_load_4d(dst, &xmap, 0, BE * bx, BE * by, BE * bz, bar(B_XFULL + s));
+        tc::tma_load_4d(dst + XREG, &xmap, 32, BE * bx, BE * by, BE * bz, bar(B_XFULL + s));
+      }
+      if (!ok) atomicOr(a.err, 1);
+      // drain: every copy issued has landed before the block may exit
+      for (int k = (it > 2 ? it - 2 : 0); k < it; k++)
+        tc::mbar_wait(bar(B_XFULL + (k & 1)), (uint32_t)(k >> 1) & 1u, WAIT_LIMIT);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t IDESC_N = idesc_tf32(128, SPLIT ? 128 : 64);
+      constexpr uint32_t IDESC_64 = idesc_tf32(128, 64);
+      bool ok = true;
+      int it = 0;
+      for (int b = blockIdx.x; b < a.nbox && ok; b += gridDim.x, it++) {
+        const int s = it & 1;
+        const uint32_t ph = (uint32_t)(it >> 1) & 1u;
+        if (!tc::mbar_wait(bar(B_DEMPTY + s), ph ^ 1u, WAIT_LIMIT)) {
+          ok = false;
+          break;
+        }
+        const uint32_t dtm = tmem + D_BASE + 128u * (uint32_t)s;
+        // K step k (box nodes 8k .. 8k+7): 32 bytes into K atom k / 4; the
+        // 8-row groups of B (columns of X) are 1 KB apart
+        const uint64_t b0 = tc::smem_desc_sw(tc::smem_u32(bst), 1024, 2);
+        // A and B in two halves of K: the first half is released (and
+        // refilled with the next box) while the second half multiplies
+#pragma unroll 1
+        for (int hf = 0; hf < 2; hf++) {
+          if (!tc::mbar_wait(bar(B_AFULL + hf), (uint32_t)it & 1u, WAIT_LIMIT)) {
+            ok = false;
+            break;
+          }
+          tc::fence_after();
+#pragma unroll
+          for (int k = 8 * hf; k < 8 * hf + 8; k++)
+            mma_tf32_ts(dtm, tmem + A_HI + 8 * k,
+                        b0 + (uint64_t)(((k >> 2) * KATOM + (k & 3) * 32) >> 4), IDESC_N,
+                        k > 0 ? 1u : 0u);
+          if (SPLIT) {
+#pragma unroll
+            for (int k = 8 * hf; k < 8 * hf + 8; k++)
+              mma_tf32_ts(dtm, tmem + A_LO + 8 * k,
+                          b0 + (uint64_t)(((k >> 2) * KATOM + (k & 3) * 32) >> 4), IDESC_64,
+                          1u);
+          }
+          tc::commit(bar(B_AFREE + hf));
+        }
+        if (!ok) break;
+        tc::commit(bar(B_DFULL + s));
+      }
+      if (!ok) atomicOr(a.err, 1);
+      // drain: every MMA issued has completed before the TMEM is released
+      tc::commit(bar(B_DRAIN));
+      tc::mbar_wait(bar(B_DRAIN), 0u, WAIT_LIMIT);
+    }
+    __syncwarp();
+  } else if (warp < W_ASM + 4) {
+    // ------------------------------------------------ A assembly
+    const int q = warp & 3;        // TMEM lanes 32q .. 32q + 31
+    const int r = 32 * q + lane;   // box node of this thread
+    const bool rv = r < ROWS;
+    const int lx = r % BN, ly = (r / BN) % BN, lz = r / (BN * BN);
+    // chunks of 16 columns this warp's rows reach: rows 32q .. 32q+31 couple
+    // to columns 32q - 31 .. 32q + 62
+    const int c_lo = q == 0 ? 0 : (q == 1 ? 0 : (q == 2 ? 2 : 4));
+    const int c_hi = q == 0 ? 4 : (q == 1 ? 6 : 8);
+    float *srow = staging + r * SPITCH - 16 * c_lo;  // srow[column]
+    const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    // in-box couplings of this node: bit (dx+1) + 3 (dy+1) + 9 (dz+1)
+    unsigned inb = 0u;
+#pragma unroll
+    for (int o = 0; o < 27; o++) {
+      const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = o / 9 - 1;
+      if (rv && lx + dx >= 0 && lx + dx < BN && ly + dy >= 0 && ly + dy < BN &&
+          lz + dz >= 0 && lz + dz < BN)
+        inb |= 1u << o;
+    }
+    // the A region of TMEM starts zero: columns outside a warp's window are
+    // never written again
+    {
+      uint32_t z[16];
+#pragma unroll
+      for (int i = 0; i < 16; i++) z[i] = 0u;
+#pragma unroll 1
+      for (int c = 0; c < 256; c += 16) tmem_st16(lane_base + (uint32_t)c, z);
+      tmem_wait_st();
+    }
+    // node r's rows of the box elements around it: element (lx-1+e0,
+    // ly-1+e1, lz-1+e2) holds the node at its corner (1-e0, 1-e1, 1-e2);
+    // loaded one box ahead
+    float4 ld[8][2];
+    auto load_box = [&](int b) {
+      const int bx = b % a.nbx, by = (b / a.nbx) % a.nby, bz = b / (a.nbx * a.nby);
+      const int ox = BE * bx, oy = BE * by, oz = BE * bz;
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const int e0 = e & 1, e1 = (e >> 1) & 1, e2 = e >> 2;
+        const int ex = lx - 1 + e0, ey = ly - 1 + e1, ez = lz - 1 + e2;
+        const bool in = b < a.nbox && rv && ex >= 0 && ex < BE && ey >= 0 && ey < BE &&
+                        ez >= 0 && ez < BE && ox + ex < nex && oy + ey < ney && oz + ez < nez;
+        ld[e][0] = ld[e][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (in) {
+          const size_t p =
+              (size_t)(ox + ex) + (size_t)nex * ((size_t)(oy + ey) + (size_t)ney * (oz + ez));
+          const float4 *src = reinterpret_cast<const float4 *>(a.A + p * 64) +
+                              2 * corner(1 - e0, 1 - e1, 1 - e2);
+          ld[e][0] = __ldg(src);
+          ld[e][1] = __ldg(src + 1);
+        }
+      }
+    };
+    load_box(blockIdx.x);
+    bool ok = true;
+    int it = 0;
+    for (int b = blockIdx.x; b < a.nbox; b += gridDim.x, it++) {
+      // the 27 stencil sums: element (e0, e1, e2)'s input node j sits at
+      // offset (e0 - 1 + x_j, e1 - 1 + y_j, e2 - 1 + z_j) from node r
+      float sten[27];
+#pragma unroll
+      for (int o = 0; o < 27; o++) sten[o] = 0.f;
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const float v8[8] = {ld[e][0].x, ld[e][0].y, ld[e][0].z, ld[e][0].w,
+                             ld[e][1].x, ld[e][1].y, ld[e][1].z, ld[e][1].w};
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int o = ((e & 1) + cx(j)) + 3 * (((e >> 1) & 1) + cy(j)) + 9 * ((e >> 2) + cz(j));
+          sten[o] += v8[j];
+        }
+      }
+      load_box(b + gridDim.x);  // the next box's rows, in flight meanwhile
+      // into this node's staging row (fixed positions: the rest stays zero)
+#pragma unroll
+      for (int o = 0; o < 27; o++)
+        if ((inb >> o) & 1u)
+          srow[r + (o % 3 - 1) + BN * ((o / 3) % 3 - 1) + BN * BN * (o / 9 - 1)] = sten[o];
+      // head and tail into TMEM, K half by K half as the previous box's
+      // MMAs release them
+#pragma unroll 1
+      for (int hf = 0; hf < 2; hf++) {
+        const bool freed =
+            tc::mbar_wait(bar(B_AFREE + hf), ((uint32_t)it & 1u) ^ 1u, WAIT_LIMIT);
+        if (!__all_sync(0xffffffffu, freed)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after();
+        const int c0 = c_lo > 4 * hf ? c_lo : 4 * hf;
+        const int c1 = c_hi < 4 * hf + 4 ? c_hi : 4 * hf + 4;
+#pragma unroll 1
+        for (int c = c0; c < c1; c++) {
+          const float4 *src = reinterpret_cast<const float4 *>(srow + 16 * c);
+          uint32_t hi[16], lo[16];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const float4 v = src[u];
+            const float f[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+              hi[4 * u + k] = tf32_rna(f[k]);
+              lo[4 * u + k] = SPLIT ? tf32_rna(f[k] - __uint_as_float(hi[4 * u + k])) : 0u;
+            }
+          }
+          tmem_st16(lane_base + A_HI + 16u * (uint32_t)c, hi);
+          if (SPLIT) tmem_st16(lane_base + A_LO + 16u * (uint32_t)c, lo);
+        }
+        tmem_wait_st();
+        tc::fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(bar(B_AFULL + hf));
+      }
+      if (!ok) break;
+    }
+    if (!ok && lane == 0) atomicOr(a.err, 1);
+  } else if (warp < W_SPL + 4) {
+    // ------------------------------------------------ X split
+    // warp q: box nodes 32q .. 32q + 31 (K atom q, in half q / 2 of K); this
+    // thread's node row of the TMA stage, 16 chunks of 4 columns, to K
+    // position r of B rows n (head) and 64 + n (tail); Dirichlet rows zero
+    // when masked
+    const int q = warp - W_SPL, hf = q >> 1;
+    const int r = 32 * q + lane;
+    const bool rv = r < ROWS;
+    const int lx = r % BN, ly = (r / BN) % BN, lz = r / (BN * BN);
+    // byte offset of this lane's word in a B row n, by n % 8 (the swizzle)
+    uint32_t woff[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) woff[k] = (((uint32_t)(lane >> 2) ^ (uint32_t)k) << 4) + (lane & 3) * 4;
+    unsigned char *bq = bst + q * KATOM;
+    bool ok = true;
+    int it = 0;
+    for (int b = blockIdx.x; b < a.nbox; b += gridDim.x, it++) {
+      const int s = it & 1;
+      bool zero = !rv;
+      if (a.mask && rv) {
+        const int bx = b % a.nbx, by = (b / a.nbx) % a.nby, bz = b / (a.nbx * a.nby);
+        const int gx = BE * bx + lx, gy = BE * by + ly, gz = BE * bz + lz;
+        zero = gx < a.nax && gy < a.nay && gz < a.naz &&
+               __ldg(a.mask + (size_t)gx + (size_t)a.nax * ((size_t)gy + (size_t)a.nay * gz));
+      }
+      const bool landed =
+          tc::mbar_wait(bar(B_XFULL + s), (uint32_t)(it >> 1) & 1u, WAIT_LIMIT);
+      const bool bfree = tc::mbar_wait(bar(B_AFREE + hf), ((uint32_t)it & 1u) ^ 1u, WAIT_LIMIT);
+      if (!__all_sync(0xffffffffu, landed && bfree)) {
+        ok = false;
+        break;
+      }
+      const unsigned char *xr = xst + s * XSTAGE + r * 128;
+      if (rv) {
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+          float4 v = *reinterpret_cast<const float4 *>(xr + (c >> 3) * XREG +
+                                                       (((c & 7) ^ (r & 7)) << 4));
+          if (zero) v = make_float4(0.f, 0.f, 0.f, 0.f);
+          const float f[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            const int n = 4 * c + i;
+            const uint32_t h = tf32_rna(f[i]);
+            *reinterpret_cast<uint32_t *>(bq + n * 128 + woff[n & 7]) = h;
+            if (SPLIT)
+              *reinterpret_cast<uint32_t *>(bq + (64 + n) * 128 + woff[n & 7]) =
+                  tf32_rna(f[i] - __uint_as_float(h));
+          }
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) {
+        tc::mbar_arrive(bar(B_XEMPTY + s));
+        tc::mbar_arrive(bar(B_AFULL + hf));
+      }
+    }
+    if (!ok && lane == 0) atomicOr(a.err, 1);
+  } else {
+    // ------------------------------------------------ epilogue
+    const int q = warp & 3;
+    const int r = 32 * q + lane;
+    const bool rv = r < ROWS;
+    const int lx = r % BN, ly = (r / BN) % BN, lz = r / (BN * BN);
+    const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    bool ok = true;
+    int it = 0;
+    for (int b = blockIdx.x; b < a.nbox; b += gridDim.x, it++) {
+      const int d = it & 1;
+      const bool got = tc::mbar_wait(bar(B_DFULL + d), (uint32_t)(it >> 1) & 1u, WAIT_LIMIT);
+      if (!__all_sync(0xffffffffu, got)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after();
+      float y[64];
+#pragma unroll
+      for (int c0 = 0; c0 < 64; c0 += 16) {
+        uint32_t r1[16], r2[16];
+        tc::tmem_ld16(lane_base + D_BASE + 128u * (uint32_t)d + (uint32_t)c0, r1);
+        if (SPLIT) tc::tmem_ld16(lane_base + D_BASE + 128u * (uint32_t)d + 64u + (uint32_t)c0, r2);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+          y[c0 + k] = __uint_as_float(r1[k]) + (SPLIT ? __uint_as_float(r2[k]) : 0.f);
+      }
+      tc::fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(bar(B_DEMPTY + d));
+      const int bx = b % a.nbx, by = (b / a.nbx) % a.nby, bz = b / (a.nbx * a.nby);
+      const int gx = BE * bx + lx, gy = BE * by + ly, gz = BE * bz + lz;
+      if (rv && gx < a.nax && gy < a.nay && gz < a.naz) {
+        const size_t n = (size_t)gx + (size_t)a.nax * ((size_t)gy + (size_t)a.nay * gz);
+        if (!a.mask || !__ldg(a.mask + n)) {
+          float4 *dst = reinterpret_cast<float4 *>(a.Y + n * 64);
+#pragma unroll
+          for (int c4 = 0; c4 < 16; c4++)
+            atomicAdd(dst + c4, make_float4(y[4 * c4], y[4 * c4 + 1], y[4 * c4 + 2],
+                                            y[4 * c4 + 3]));
+        }
+      }
+    }
+    if (!ok && lane == 0) atomicOr(a.err, 1);
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                   CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// The map of a node-major [N][64] FP32 block vector on the structured node
+// grid: dimensions (64, nax, nay, naz), box (32 columns, 5 x 5 x 5 nodes),
+// 128-byte swizzle, nodes outside the grid read as zero.
+bool make_xmap(CUtensorMap *m, const float *X, int nax, int nay, int naz) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !X || (reinterpret_cast<uintptr_t>(X) & 15)) return false;
+  const cuuint64_t dims[4] = {64, (cuuint64_t)nax, (cuuint64_t)nay, (cuuint64_t)naz};
+  const cuuint64_t strides[3] = {256, 256 * (cuuint64_t)nax,
+                                 256 * (cuuint64_t)nax * (cuuint64_t)nay};
+  const cuuint32_t box[4] = {32, BN, BN, BN};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float *>(X), dims, strides, box,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
+}  // namespace blocktc
+
+bool block_tc_supported(const Handle &h) {
+  return h.nax > 1 && h.nay > 1 && h.naz > 1 && !h.perm_d && h.block_err &&
+         blocktc::encode_tiled() != nullptr;
+}
+
+int launch_block_tc(const Handle &h, bool split, const float *A, const float *X, float *Y,
+                    const int *skip, const unsigned char *mask, cudaStream_t s) {
+  using namespace blocktc;
+  if (!block_tc_supported(h) || (reinterpret_cast<uintptr_t>(Y) & 15)) {
+    set_error("tcgen05 block apply: needs the structured numbering and 16-byte aligned vectors");
+    return VDR_BAD_ARGUMENT;
+  }
+  CUtensorMap map;
+  if (!make_xmap(&map, X, h.nax, h.nay, h.naz)) {
+    set_error("tcgen05 block apply: tensor map of X could not be made");
+    return VDR_CUDA_ERROR;
+  }
+  static std::atomic<unsigned> opted{0u};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned bit = 1u << (dev & 31);
+  if (!(opted.load(std::memory_order_relaxed) & bit)) {
+    cudaError_t e1 = cudaFuncSetAttribute(block_apply_tc_kernel<true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    cudaError_t e2 = cudaFuncSetAttribute(block_apply_tc_kernel<false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    if (e1 || e2) return cuda_fail(e1 ? e1 : e2, "tcgen05 block apply");
+    opted.fetch_or(bit, std::memory_order_relaxed);
+  }
+  Args a;
+  a.A = A;
+  a.Y = Y;
+  a.mask = mask;
+  a.nax = h.nax;
+  a.nay = h.nay;
+  a.naz = h.naz;
+  a.nbx = (h.nax - 2) / BE + 1;
+  a.nby = (h.nay - 2) / BE + 1;
+  const int nbz = (h.naz - 2) / BE + 1;
+  a.nbox = a.nbx * a.nby * nbz;
+  a.skip = skip;
+  a.err = h.block_err;
+  const int grid = a.nbox < device_sm_count() ? a.nbox : device_sm_count();
+  if (split)
+    block_apply_tc_kernel<true><<<grid, THREADS, SMEM, s>>>(map, a);
+  else
+    block_apply_tc_kernel<false><<<grid, THREADS, SMEM, s>>>(map, a);
+  count_launches(1);
+  const cudaError_t e = cudaGetLastError();
+  return e ? cuda_fail(e, "tcgen05 block apply") : VDR_OK;
+}
+
+}  // namespace vdr

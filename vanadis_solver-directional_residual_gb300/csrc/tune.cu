@@ -165,5 +165,6 @@ extern "C" int vdr_apply_tuning(vdr_handle *H, vdr_apply_tuning_info *info) {
     info->half_ms[c] = h.half_tune_ms[c];
   }
   for (int c = 0; c < TUNE_TILES; c++) info->block_ms[c] = h.blk_tune_ms[c];
+  info->block_tcgen05 = h.blk_use_tc ? 1 : 0;
   return VDR_OK;
 }

@@ -126,7 +126,8 @@ struct OpArgs {
 
 // Candidate launch shapes of the apply tuner (tune.cu).
 constexpr int TUNE_GRIDS = 5;   // resident blocks per SM: 2, 4, 8, 16, 32
-constexpr int TUNE_TILES = 3;   // block apply (box height, column halves): (2,2) (2,1) (4,2)
+constexpr int TUNE_TILES = 4;   // block apply: node tile (box height, column halves) (2,2)
+                                // (2,1) (4,2), and the tcgen05 box apply
 constexpr int TUNE_GRID_PER_SM[TUNE_GRIDS] = {2, 4, 8, 16, 32};
 
 struct Handle {
@@ -142,6 +143,7 @@ struct Handle {
   bool apply_tuned = false, half_tuned = false;
   float apply_tune_ms[TUNE_GRIDS] = {}, half_tune_ms[TUNE_GRIDS] = {};
   int blk_ty = 2, blk_halves = 2;
+  bool blk_use_tc = false;  // the tcgen05 box apply measured fastest (K = 64)
   bool blk_tuned = false;
   float blk_tune_ms[TUNE_TILES] = {};
   int scatter = VDR_SCATTER_ATOMIC;  // ATOMIC or COLOR (WARP is ATOMIC + warp_agg)
@@ -236,7 +238,8 @@ struct Handle {
   bool bk_graph_split = false;
   bool block_tma = false;     // bulk-copy block apply
   bool block_tile = true;     // node-tile block apply on structured meshes (default)
-  int *block_err = nullptr;   // set when a bulk-copy wait ran out
+  int blk_tc_mode = -1;       // K = 64 on the tile path: -1 by measurement, 0 node tile, 1 tcgen05
+  int *block_err = nullptr;   // set when a bounded device wait ran out
 
   // many meshes as segments (batch.cu)
   std::vector<int> seg_off;  // node offsets, nseg + 1
@@ -374,6 +377,12 @@ int tune_half_apply(Handle &h);
 // The node-tile block apply's (box height, column halves) for K = 64, timed
 // on X -> Y scratch columns of N x 64 floats (h.blk_ty, h.blk_halves).
 int tune_block_apply(Handle &h, const float *X, float *Y, const float4 *Aaos);
+// The tcgen05 box block apply (block_tc.cu): K = 64, Y += A X with boxes of
+// 4 x 4 x 4 elements; needs the structured numbering, the error flag and
+// the driver's tensor-map encoder.
+bool block_tc_supported(const Handle &h);
+int launch_block_tc(const Handle &h, bool split, const float *A, const float *X, float *Y,
+                    const int *skip, const unsigned char *mask, cudaStream_t s);
 
 // ---- solvers (krylov.cu) ----
 int solve_device(Handle &h, int method, const double *b, double *x,

@@ -281,7 +281,8 @@ class Solver:
         """The applies' launch shapes chosen by measurement
         (vdr_apply_tuning): blocks per SM of the stored and binary16 applies
         with the time per apply of each candidate, and the block apply's box
-        height and column halves with the times of (2,2), (2,1), (4,2)."""
+        height and column halves with the times of (2,2), (2,1), (4,2) and
+        of the tcgen05 box apply, and whether that one was chosen."""
         t = L.VdrApplyTuning()
         L.check(self.lib.vdr_apply_tuning(self.h, ctypes.byref(t)), "vdr_apply_tuning")
         grid = list(t.grid_candidates)
@@ -290,8 +291,9 @@ class Solver:
                 "half_blocks_per_sm": t.half_blocks_per_sm,
                 "half_ms": dict(zip(grid, [round(v, 4) for v in t.half_ms])),
                 "block_tile_y": t.block_tile_y, "block_halves": t.block_halves,
-                "block_ms": dict(zip(["2x2", "2x1", "4x2"],
-                                     [round(v, 4) for v in t.block_ms]))}
+                "block_ms": dict(zip(["2x2", "2x1", "4x2", "tcgen05"],
+                                     [round(v, 4) for v in t.block_ms])),
+                "block_tcgen05": bool(t.block_tcgen05)}
 
     @_device_call
     def solve_learned_device(self, net, b, x, tol=None, itmax=1000,
@@ -406,14 +408,19 @@ class Solver:
         L.check(self.lib.vdr_apply_half_device(self.h, _ptr(x), _ptr(y)),
                 "vdr_apply_half_device")
 
-    def set_block_apply(self, variant="tile"):
-        """Data movement of the tensor-core block apply: "tile" (default:
-        node rows of 8 x 2 x 2-element boxes staged once in shared memory,
-        on meshes in the canonical structured numbering; "lsu" otherwise),
-        "lsu" (per-element row gathers and float4 atomics) or "bulk" (bulk
-        copies and bulk reductions through shared memory)."""
+    def set_block_apply(self, variant="auto"):
+        """Data movement of the tensor-core block apply: "auto" (default:
+        the node tile, or for 64 columns the tcgen05 box apply when the
+        first 64-column block solve measured it faster), "tcgen05" (64
+        columns: 4 x 4 x 4-element box operators in tensor memory times the
+        boxes' node rows on tcgen05), "tile" (node rows of 8 x 2 x 2-element
+        boxes staged once in shared memory, mma.sync), all three on meshes
+        in the canonical structured numbering ("lsu" otherwise), "lsu"
+        (per-element row gathers and float4 atomics) or "bulk" (bulk copies
+        and bulk reductions through shared memory)."""
         L.check(self.lib.vdr_set_block_apply(
-            self.h, {"bulk": 0, "lsu": 1, "tile": 2}[variant]), "vdr_set_block_apply")
+            self.h, {"bulk": 0, "lsu": 1, "tile": 2, "tcgen05": 3, "auto": 4}[variant]),
+            "vdr_set_block_apply")
 
     @_device_call
     def assemble_rhs_block_device(self, Q, B, cf=1.0):
