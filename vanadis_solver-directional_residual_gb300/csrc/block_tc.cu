@@ -29,9 +29,12 @@
 //           tail of X side by side in B) + A_lo X_hi (N = 64): the three
 //           products of split TF32, FP32-level accuracy.  Plain TF32 issues
 //           A_hi X_hi alone.
-//   Y       the epilogue adds the two halves of D and sends each node row
-//           with 16 float4 atomics; nodes on box faces receive one add per
-//           box that shares them.
+//   Y       the epilogue adds the two halves of D into a shared tile laid
+//           out as the TMA box, and one thread adds the tile to Y with two
+//           tensor reduces (cp.reduce.async.bulk.tensor .add.f32: element-
+//           wise atomic adds by the TMA unit; nodes outside the mesh are
+//           skipped); nodes on box faces receive one add per box sharing
+//           them.
 //
 // The element matrices come from the element-major FP32 copy
 // Aaos[p*64 + 8i + j] (Jacobi scale folded into the columns, Dirichlet rows
@@ -75,8 +78,9 @@ constexpr int BSTAGE = 4 * KATOM;   // B: rows 0-63 head, 64-127 tail; K = 128 n
                                     // (atoms 0-1: first half of K, 2-3: second)
 constexpr int SPITCH = 100;         // staging row pitch (floats): conflict-free rows
 constexpr int STAGING = 128 * SPITCH * 4;
+constexpr int YSTAGE = 2 * XREG;    // the D tile in the TMA box layout, for the reduce
 constexpr int NBAR = 13;
-constexpr int SMEM = 1024 + 2 * XSTAGE + BSTAGE + STAGING + NBAR * 8 + 8;
+constexpr int SMEM = 1024 + 2 * XSTAGE + BSTAGE + STAGING + YSTAGE + NBAR * 8 + 8;
 constexpr int TMEM_COLS = 512;
 constexpr uint32_t A_HI = 0, A_LO = 128, D_BASE = 256;  // TMEM columns
 constexpr long long WAIT_LIMIT = 2000000000LL;         // ~1 s of clocks per wait
@@ -122,6 +126,40 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16
       "r"(r[14]), "r"(r[15])
       : "memory");
 }
+// Element-wise atomic add of a shared-memory box into the 4-D tensor (out
+// of range elements are skipped), tracked by the issuing thread's bulk group.
+__device__ __forceinline__ void tma_reduce_add_4d(const CUtensorMap *map, uint32_t src, int c0,
+                                                  int c1, int c2, int c3) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.4d.global.shared::cta.add.tile.bulk_group"
+      " [%0, {%2, %3, %4, %5}], [%1];" ::"l"((uint64_t)map),
+      "r"(src), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// Waits until the bulk operations this thread committed have read their
+// shared-memory sources.
+__device__ __forceinline__ void bulk_wait_read0() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// Named barrier 1 over the four epilogue warps; the _or form returns
+// whether `pred` held for any of their threads (so that a timeout seen by
+// one warp stops all four at the same point).
+__device__ __forceinline__ void epi_sync() {
+  asm volatile("bar.sync 1, 128;" ::: "memory");
+}
+__device__ __forceinline__ bool epi_sync_or(bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, 128, p;\n"
+      " selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)pred)
+      : "memory");
+  return r != 0;
+}
 __device__ __forceinline__ void tmem_wait_st() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
@@ -141,7 +179,8 @@ __host__ __device__ constexpr int cz(int j) { return j >> 2; }
 
 template <bool SPLIT>
 __global__ void __launch_bounds__(THREADS, 1)
-    block_apply_tc_kernel(const __grid_constant__ CUtensorMap xmap, Args a) {
+    block_apply_tc_kernel(const __grid_constant__ CUtensorMap xmap,
+                          const __grid_constant__ CUtensorMap ymap, Args a) {
   if (a.skip && *(volatile const int *)a.skip) return;
   extern __shared__ unsigned char dsm[];
   unsigned char *base =
@@ -150,7 +189,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   unsigned char *xst = base;                // two TMA stages: node rows
   unsigned char *bst = base + 2 * XSTAGE;   // B (transposed, split)
   float *staging = reinterpret_cast<float *>(bst + BSTAGE);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(bst + BSTAGE + STAGING);
+  unsigned char *yst = bst + BSTAGE + STAGING;  // D tile for the TMA reduce
+  uint64_t *bars = reinterpret_cast<uint64_t *>(yst + YSTAGE);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + NBAR);
   auto bar = [&](int i) { return tc::smem_u32(bars + i); };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -441,48 +481,73 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (!ok && lane == 0) atomicOr(a.err, 1);
   } else {
     // ------------------------------------------------ epilogue
+    // D (head + tail halves) of box node r into its row of the shared Y
+    // tile, laid out as the TMA box (128-byte swizzle), then one thread
+    // adds the tile to Y with two tensor reduces; Dirichlet rows under a
+    // mask send zeros, rows outside the mesh are skipped by the TMA unit
     const int q = warp & 3;
     const int r = 32 * q + lane;
     const bool rv = r < ROWS;
     const int lx = r % BN, ly = (r / BN) % BN, lz = r / (BN * BN);
+    const bool issuer = warp == W_EPI && lane == 0;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    if (issuer) tc::prefetch_tensormap(&ymap);
     bool ok = true;
     int it = 0;
     for (int b = blockIdx.x; b < a.nbox; b += gridDim.x, it++) {
       const int d = it & 1;
+      const int bx = b % a.nbx, by = (b / a.nbx) % a.nby, bz = b / (a.nbx * a.nby);
+      bool zero = false;
+      if (a.mask && rv) {
+        const int gx = BE * bx + lx, gy = BE * by + ly, gz = BE * bz + lz;
+        zero = gx < a.nax && gy < a.nay && gz < a.naz &&
+               __ldg(a.mask + (size_t)gx + (size_t)a.nax * ((size_t)gy + (size_t)a.nay * gz));
+      }
       const bool got = tc::mbar_wait(bar(B_DFULL + d), (uint32_t)(it >> 1) & 1u, WAIT_LIMIT);
-      if (!__all_sync(0xffffffffu, got)) {
+      // the previous box's reduces have read the tile; every epilogue
+      // thread got this box's D, or all four warps stop here
+      if (issuer) bulk_wait_read0();
+      if (epi_sync_or(!got)) {
         ok = false;
         break;
       }
       tc::fence_after();
-      float y[64];
+      // four passes of 16 columns: TMEM -> registers -> the tile
+      unsigned char *yr = yst + r * 128;
 #pragma unroll
       for (int c0 = 0; c0 < 64; c0 += 16) {
         uint32_t r1[16], r2[16];
         tc::tmem_ld16(lane_base + D_BASE + 128u * (uint32_t)d + (uint32_t)c0, r1);
         if (SPLIT) tc::tmem_ld16(lane_base + D_BASE + 128u * (uint32_t)d + 64u + (uint32_t)c0, r2);
         tc::tmem_wait_ld();
+        if (rv) {
 #pragma unroll
-        for (int k = 0; k < 16; k++)
-          y[c0 + k] = __uint_as_float(r1[k]) + (SPLIT ? __uint_as_float(r2[k]) : 0.f);
+          for (int u = 0; u < 4; u++) {
+            const int c = c0 / 4 + u;  // 16-byte chunk of the row
+            float v[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+              v[k] = zero ? 0.f
+                          : __uint_as_float(r1[4 * u + k]) +
+                                (SPLIT ? __uint_as_float(r2[4 * u + k]) : 0.f);
+            *reinterpret_cast<float4 *>(yr + (c >> 3) * XREG + (((c & 7) ^ (r & 7)) << 4)) =
+                make_float4(v[0], v[1], v[2], v[3]);
+          }
+        }
       }
       tc::fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(bar(B_DEMPTY + d));
-      const int bx = b % a.nbx, by = (b / a.nbx) % a.nby, bz = b / (a.nbx * a.nby);
-      const int gx = BE * bx + lx, gy = BE * by + ly, gz = BE * bz + lz;
-      if (rv && gx < a.nax && gy < a.nay && gz < a.naz) {
-        const size_t n = (size_t)gx + (size_t)a.nax * ((size_t)gy + (size_t)a.nay * gz);
-        if (!a.mask || !__ldg(a.mask + n)) {
-          float4 *dst = reinterpret_cast<float4 *>(a.Y + n * 64);
-#pragma unroll
-          for (int c4 = 0; c4 < 16; c4++)
-            atomicAdd(dst + c4, make_float4(y[4 * c4], y[4 * c4 + 1], y[4 * c4 + 2],
-                                            y[4 * c4 + 3]));
-        }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      epi_sync();
+      if (issuer) {
+        const uint32_t src = tc::smem_u32(yst);
+        tma_reduce_add_4d(&ymap, src, 0, BE * bx, BE * by, BE * bz);
+        tma_reduce_add_4d(&ymap, src + XREG, 32, BE * bx, BE * by, BE * bz);
+        bulk_commit();
       }
     }
+    if (issuer) bulk_wait_read0();
     if (!ok && lane == 0) atomicOr(a.err, 1);
   }
   tc::fence_before();
@@ -513,7 +578,8 @@ EncodeTiledFn encode_tiled() {
 
 // The map of a node-major [N][64] FP32 block vector on the structured node
 // grid: dimensions (64, nax, nay, naz), box (32 columns, 5 x 5 x 5 nodes),
-// 128-byte swizzle, nodes outside the grid read as zero.
+// 128-byte swizzle; loads read nodes outside the grid as zero, reduces skip
+// them.
 bool make_xmap(CUtensorMap *m, const float *X, int nax, int nay, int naz) {
   EncodeTiledFn fn = encode_tiled();
   if (!fn || !X || (reinterpret_cast<uintptr_t>(X) & 15)) return false;
@@ -542,9 +608,9 @@ int launch_block_tc(const Handle &h, bool split, const float *A, const float *X,
     set_error("tcgen05 block apply: needs the structured numbering and 16-byte aligned vectors");
     return VDR_BAD_ARGUMENT;
   }
-  CUtensorMap map;
-  if (!make_xmap(&map, X, h.nax, h.nay, h.naz)) {
-    set_error("tcgen05 block apply: tensor map of X could not be made");
+  CUtensorMap xmap, ymap;
+  if (!make_xmap(&xmap, X, h.nax, h.nay, h.naz) || !make_xmap(&ymap, Y, h.nax, h.nay, h.naz)) {
+    set_error("tcgen05 block apply: tensor maps of X and Y could not be made");
     return VDR_CUDA_ERROR;
   }
   static std::atomic<unsigned> opted{0u};
@@ -574,9 +640,9 @@ int launch_block_tc(const Handle &h, bool split, const float *A, const float *X,
   a.err = h.block_err;
   const int grid = a.nbox < device_sm_count() ? a.nbox : device_sm_count();
   if (split)
-    block_apply_tc_kernel<true><<<grid, THREADS, SMEM, s>>>(map, a);
+    block_apply_tc_kernel<true><<<grid, THREADS, SMEM, s>>>(xmap, ymap, a);
   else
-    block_apply_tc_kernel<false><<<grid, THREADS, SMEM, s>>>(map, a);
+    block_apply_tc_kernel<false><<<grid, THREADS, SMEM, s>>>(xmap, ymap, a);
   count_launches(1);
   const cudaError_t e = cudaGetLastError();
   return e ? cuda_fail(e, "tcgen05 block apply") : VDR_OK;
