@@ -17,7 +17,8 @@
 //           K-major (an MN-major TF32 B operand measured all zeros), so the
 //           split pass writes B transposed: row n = column n of X, the 125
 //           box nodes along K (lane = node: each store of a warp fills one
-//           128-byte row, no bank conflicts).
+//           128-byte row, no bank conflicts).  Heads are truncated to TF32
+//           (top 10 mantissa bits), tails are the exact FP32 remainders.
 //   A_box   thread r of the four assembly warps owns box node r: it sums
 //           node r's rows of the (up to 8) box elements around it into its
 //           27 stencil couplings, writes them into its row of a shared
@@ -38,7 +39,7 @@
 //
 // The element matrices come from the element-major FP32 copy
 // Aaos[p*64 + 8i + j] (Jacobi scale folded into the columns, Dirichlet rows
-// and columns zero), each 32-byte row read once.
+// and columns zero), a box's 64 elements by two TMA boxes per box.
 //
 // Warp roles (448 threads, one CTA per SM, boxes strided over the grid):
 // warp 0 = TMA producer, warp 1 = TMEM owner and MMA issuer, warps 2-5 = A
@@ -77,10 +78,13 @@ constexpr int KATOM = 16384;        // B: 128 rows (columns of X) x 32 nodes x 4
 constexpr int BSTAGE = 4 * KATOM;   // B: rows 0-63 head, 64-127 tail; K = 128 nodes
                                     // (atoms 0-1: first half of K, 2-3: second)
 constexpr int SPITCH = 100;         // staging row pitch (floats): conflict-free rows
-constexpr int STAGING = 128 * SPITCH * 4;
+constexpr int STAGING = ROWS * SPITCH * 4;
+constexpr int ETILE = 64 * 128;     // element matrices: 64 box elements x 32 floats
+constexpr int ESTAGE = 2 * ETILE;   // [rows 0-3 | rows 4-7] of every box element
 constexpr int YSTAGE = 2 * XREG;    // the D tile in the TMA box layout, for the reduce
-constexpr int NBAR = 13;
-constexpr int SMEM = 1024 + 2 * XSTAGE + BSTAGE + STAGING + YSTAGE + NBAR * 8 + 8;
+constexpr int NBAR = 15;
+constexpr int SMEM = 1024 + 2 * XSTAGE + BSTAGE + YSTAGE + ESTAGE + STAGING + NBAR * 8 + 8;
+static_assert(SMEM <= 232448, "shared memory per block");
 constexpr int TMEM_COLS = 512;
 constexpr uint32_t A_HI = 0, A_LO = 128, D_BASE = 256;  // TMEM columns
 constexpr long long WAIT_LIMIT = 2000000000LL;         // ~1 s of clocks per wait
@@ -88,7 +92,7 @@ constexpr long long WAIT_LIMIT = 2000000000LL;         // ~1 s of clocks per wai
 // AFULL / AFREE: one per half of K, covering that half's A columns (TMEM)
 // and B rows' K atoms (shared memory)
 constexpr int B_XFULL = 0, B_XEMPTY = 2, B_AFULL = 4, B_AFREE = 6, B_DFULL = 8,
-              B_DEMPTY = 10, B_DRAIN = 12;
+              B_DEMPTY = 10, B_DRAIN = 12, B_EFULL = 13, B_EEMPTY = 14;
 
 struct Args {
   const float *A;             // Aaos, [E][64]
@@ -163,10 +167,14 @@ __device__ __forceinline__ bool epi_sync_or(bool pred) {
 __device__ __forceinline__ void tmem_wait_st() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
-__device__ __forceinline__ uint32_t tf32_rna(float f) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(f));
-  return r;
+// Split TF32 by truncation: the head keeps the top 10 mantissa bits (an
+// exact TF32 value), the tail v - head is exact in FP32 and loses at most
+// 2^-10 of itself (under 2^-20 of v) when the tensor core reads it as TF32.
+__device__ __forceinline__ uint32_t tf32_head(float f) {
+  return __float_as_uint(f) & 0xFFFFE000u;
+}
+__device__ __forceinline__ uint32_t tf32_tail(float f, uint32_t head) {
+  return __float_as_uint(f - __uint_as_float(head));
 }
 // Local index of the HEX8 corner (x, y, z): 0 (0,0,0), 1 (1,0,0), 2 (1,1,0),
 // 3 (0,1,0), and + 4 at z = 1.
@@ -180,7 +188,8 @@ __host__ __device__ constexpr int cz(int j) { return j >> 2; }
 template <bool SPLIT>
 __global__ void __launch_bounds__(THREADS, 1)
     block_apply_tc_kernel(const __grid_constant__ CUtensorMap xmap,
-                          const __grid_constant__ CUtensorMap ymap, Args a) {
+                          const __grid_constant__ CUtensorMap ymap,
+                          const __grid_constant__ CUtensorMap amap, Args a) {
   if (a.skip && *(volatile const int *)a.skip) return;
   extern __shared__ unsigned char dsm[];
   unsigned char *base =
@@ -188,13 +197,13 @@ __global__ void __launch_bounds__(THREADS, 1)
                                         ~static_cast<uintptr_t>(1023));
   unsigned char *xst = base;                // two TMA stages: node rows
   unsigned char *bst = base + 2 * XSTAGE;   // B (transposed, split)
-  float *staging = reinterpret_cast<float *>(bst + BSTAGE);
-  unsigned char *yst = bst + BSTAGE + STAGING;  // D tile for the TMA reduce
-  uint64_t *bars = reinterpret_cast<uint64_t *>(yst + YSTAGE);
+  unsigned char *yst = bst + BSTAGE;        // D tile for the TMA reduce
+  unsigned char *est = yst + YSTAGE;        // element matrices of a box (TMA)
+  float *staging = reinterpret_cast<float *>(est + ESTAGE);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(est + ESTAGE + STAGING);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + NBAR);
   auto bar = [&](int i) { return tc::smem_u32(bars + i); };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nex = a.nax - 1, ney = a.nay - 1, nez = a.naz - 1;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < 2; i++) {
@@ -206,14 +215,18 @@ __global__ void __launch_bounds__(THREADS, 1)
       tc::mbar_init(bar(B_DEMPTY + i), 4);
     }
     tc::mbar_init(bar(B_DRAIN), 1);
+    tc::mbar_init(bar(B_EFULL), 1);
+    tc::mbar_init(bar(B_EEMPTY), 4);
     tc::mbar_init_fence();
   }
   if (warp == 1) tc::tmem_alloc(tc::smem_u32(tslot), TMEM_COLS);
   if (warp >= W_ASM && warp < W_ASM + 4) {
     // staging rows zero (only a row's stencil columns are ever written)
     const int r = 32 * (warp & 3) + lane;
-    float4 *srow = reinterpret_cast<float4 *>(staging + r * SPITCH);
-    for (int i = 0; i < SPITCH / 4; i++) srow[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (r < ROWS) {
+      float4 *srow = reinterpret_cast<float4 *>(staging + r * SPITCH);
+      for (int i = 0; i < SPITCH / 4; i++) srow[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
   } else if (warp >= W_SPL && warp < W_SPL + 4) {
     // K positions 124..127 of every B row zero: 125..127 are never written
     // and the MMA reads them (times zero columns of A)
@@ -236,7 +249,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int b = blockIdx.x; b < a.nbox; b += gridDim.x, it++) {
         // the split of the box two back has read the stage
         const int s = it & 1;
-        if (!tc::mbar_wait(bar(B_XEMPTY + s), ((uint32_t)(it >> 1) & 1u) ^ 1u, WAIT_LIMIT)) {
+        if (!tc::mbar_wait_sleep(bar(B_XEMPTY + s), ((uint32_t)(it >> 1) & 1u) ^ 1u, WAIT_LIMIT)) {
           ok = false;
           break;
         }
@@ -249,7 +262,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!ok) atomicOr(a.err, 1);
       // drain: every copy issued has landed before the block may exit
       for (int k = (it > 2 ? it - 2 : 0); k < it; k++)
-        tc::mbar_wait(bar(B_XFULL + (k & 1)), (uint32_t)(k >> 1) & 1u, WAIT_LIMIT);
+        tc::mbar_wait_sleep(bar(B_XFULL + (k & 1)), (uint32_t)(k >> 1) & 1u, WAIT_LIMIT);
     }
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
@@ -261,7 +274,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int b = blockIdx.x; b < a.nbox && ok; b += gridDim.x, it++) {
         const int s = it & 1;
         const uint32_t ph = (uint32_t)(it >> 1) & 1u;
-        if (!tc::mbar_wait(bar(B_DEMPTY + s), ph ^ 1u, WAIT_LIMIT)) {
+        if (!tc::mbar_wait_sleep(bar(B_DEMPTY + s), ph ^ 1u, WAIT_LIMIT)) {
           ok = false;
           break;
         }
@@ -273,7 +286,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         // refilled with the next box) while the second half multiplies
 #pragma unroll 1
         for (int hf = 0; hf < 2; hf++) {
-          if (!tc::mbar_wait(bar(B_AFULL + hf), (uint32_t)it & 1u, WAIT_LIMIT)) {
+          if (!tc::mbar_wait_sleep(bar(B_AFULL + hf), (uint32_t)it & 1u, WAIT_LIMIT)) {
             ok = false;
             break;
           }
@@ -298,7 +311,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!ok) atomicOr(a.err, 1);
       // drain: every MMA issued has completed before the TMEM is released
       tc::commit(bar(B_DRAIN));
-      tc::mbar_wait(bar(B_DRAIN), 0u, WAIT_LIMIT);
+      tc::mbar_wait_sleep(bar(B_DRAIN), 0u, WAIT_LIMIT);
     }
     __syncwarp();
   } else if (warp < W_ASM + 4) {
@@ -332,50 +345,74 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int c = 0; c < 256; c += 16) tmem_st16(lane_base + (uint32_t)c, z);
       tmem_wait_st();
     }
-    // node r's rows of the box elements around it: element (lx-1+e0,
-    // ly-1+e1, lz-1+e2) holds the node at its corner (1-e0, 1-e1, 1-e2);
-    // loaded one box ahead
-    float4 ld[8][2];
-    auto load_box = [&](int b) {
+    // The box's element matrices arrive by two TMA boxes of Aaos viewed as
+    // (64 floats, nex, ney, nez): (32 floats, 4 x 4 x 4 elements) each, rows
+    // 0-3 and rows 4-7 of every element; box element le = ex + 4 ey + 16 ez
+    // is the 128-byte row le of each tile, its 16-byte chunks permuted by
+    // the 128-byte swizzle (le % 8), so the lanes of a warp reading the same
+    // corner of different elements hit different banks.  Elements outside
+    // the mesh arrive as zeros.  Warp W_ASM issues the next box's copies
+    // once all four warps have read the stage.
+    auto load_elements = [&](int b) {
       const int bx = b % a.nbx, by = (b / a.nbx) % a.nby, bz = b / (a.nbx * a.nby);
-      const int ox = BE * bx, oy = BE * by, oz = BE * bz;
-#pragma unroll
-      for (int e = 0; e < 8; e++) {
-        const int e0 = e & 1, e1 = (e >> 1) & 1, e2 = e >> 2;
-        const int ex = lx - 1 + e0, ey = ly - 1 + e1, ez = lz - 1 + e2;
-        const bool in = b < a.nbox && rv && ex >= 0 && ex < BE && ey >= 0 && ey < BE &&
-                        ez >= 0 && ez < BE && ox + ex < nex && oy + ey < ney && oz + ez < nez;
-        ld[e][0] = ld[e][1] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (in) {
-          const size_t p =
-              (size_t)(ox + ex) + (size_t)nex * ((size_t)(oy + ey) + (size_t)ney * (oz + ez));
-          const float4 *src = reinterpret_cast<const float4 *>(a.A + p * 64) +
-                              2 * corner(1 - e0, 1 - e1, 1 - e2);
-          ld[e][0] = __ldg(src);
-          ld[e][1] = __ldg(src + 1);
-        }
-      }
+      tc::mbar_arrive_expect_tx(bar(B_EFULL), ESTAGE);
+      tc::tma_load_4d(tc::smem_u32(est), &amap, 0, BE * bx, BE * by, BE * bz, bar(B_EFULL));
+      tc::tma_load_4d(tc::smem_u32(est + ETILE), &amap, 32, BE * bx, BE * by, BE * bz,
+                      bar(B_EFULL));
     };
-    load_box(blockIdx.x);
+    const bool eissuer = warp == W_ASM && lane == 0;
+    if (eissuer) {
+      tc::prefetch_tensormap(&amap);
+      load_elements(blockIdx.x);
+    }
+    int issued = 1;  // element copies issued (box it lands in phase it)
     bool ok = true;
     int it = 0;
     for (int b = blockIdx.x; b < a.nbox; b += gridDim.x, it++) {
-      // the 27 stencil sums: element (e0, e1, e2)'s input node j sits at
-      // offset (e0 - 1 + x_j, e1 - 1 + y_j, e2 - 1 + z_j) from node r
+      const bool landed = tc::mbar_wait_sleep(bar(B_EFULL), (uint32_t)it & 1u, WAIT_LIMIT);
+      if (!__all_sync(0xffffffffu, landed)) {
+        ok = false;
+        break;
+      }
+      // the 27 stencil sums: element (e0, e1, e2) around node r (local
+      // (lx-1+e0, ly-1+e1, lz-1+e2)) holds the node at its corner (1-e0,
+      // 1-e1, 1-e2), row s of its matrix; its input node j sits at offset
+      // (e0 - 1 + x_j, e1 - 1 + y_j, e2 - 1 + z_j) from node r
       float sten[27];
 #pragma unroll
       for (int o = 0; o < 27; o++) sten[o] = 0.f;
 #pragma unroll
       for (int e = 0; e < 8; e++) {
-        const float v8[8] = {ld[e][0].x, ld[e][0].y, ld[e][0].z, ld[e][0].w,
-                             ld[e][1].x, ld[e][1].y, ld[e][1].z, ld[e][1].w};
+        const int e0 = e & 1, e1 = (e >> 1) & 1, e2 = e >> 2;
+        const int ex = lx - 1 + e0, ey = ly - 1 + e1, ez = lz - 1 + e2;
+        const bool in = rv && ex >= 0 && ex < BE && ey >= 0 && ey < BE && ez >= 0 && ez < BE;
+        if (in) {
+          const int le = ex + BE * (ey + BE * ez);
+          const int sc = corner(1 - e0, 1 - e1, 1 - e2);  // row of the element matrix
+          const unsigned char *row = est + (sc >> 2) * ETILE + le * 128;
+          const int c0 = 2 * (sc & 3);  // its two 16-byte chunks
+          const float4 va = *reinterpret_cast<const float4 *>(row + (((c0 ^ le) & 7) << 4));
+          const float4 vb = *reinterpret_cast<const float4 *>(row + ((((c0 + 1) ^ le) & 7) << 4));
+          const float v8[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const int o = ((e & 1) + cx(j)) + 3 * (((e >> 1) & 1) + cy(j)) + 9 * ((e >> 2) + cz(j));
-          sten[o] += v8[j];
+          for (int j = 0; j < 8; j++) {
+            const int o = (e0 + cx(j)) + 3 * (e1 + cy(j)) + 9 * (e2 + cz(j));
+            sten[o] += v8[j];
+          }
         }
       }
-      load_box(b + gridDim.x);  // the next box's rows, in flight meanwhile
+      // the stage is read: the next box's copies may overwrite it
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(bar(B_EEMPTY));
+      if (warp == W_ASM && b + (int)gridDim.x < a.nbox) {
+        const bool read = tc::mbar_wait_sleep(bar(B_EEMPTY), (uint32_t)it & 1u, WAIT_LIMIT);
+        if (!__all_sync(0xffffffffu, read)) {
+          ok = false;
+          break;
+        }
+        if (eissuer) load_elements(b + gridDim.x);
+        issued++;
+      }
       // into this node's staging row (fixed positions: the rest stays zero)
 #pragma unroll
       for (int o = 0; o < 27; o++)
@@ -386,7 +423,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll 1
       for (int hf = 0; hf < 2; hf++) {
         const bool freed =
-            tc::mbar_wait(bar(B_AFREE + hf), ((uint32_t)it & 1u) ^ 1u, WAIT_LIMIT);
+            tc::mbar_wait_sleep(bar(B_AFREE + hf), ((uint32_t)it & 1u) ^ 1u, WAIT_LIMIT);
         if (!__all_sync(0xffffffffu, freed)) {
           ok = false;
           break;
@@ -404,8 +441,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             const float f[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-              hi[4 * u + k] = tf32_rna(f[k]);
-              lo[4 * u + k] = SPLIT ? tf32_rna(f[k] - __uint_as_float(hi[4 * u + k])) : 0u;
+              hi[4 * u + k] = tf32_head(f[k]);
+              lo[4 * u + k] = SPLIT ? tf32_tail(f[k], hi[4 * u + k]) : 0u;
             }
           }
           tmem_st16(lane_base + A_HI + 16u * (uint32_t)c, hi);
@@ -418,6 +455,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       if (!ok) break;
     }
+    // drain: an element copy issued for a box never reached has landed
+    if (eissuer && issued > it)
+      tc::mbar_wait_sleep(bar(B_EFULL), (uint32_t)(issued - 1) & 1u, WAIT_LIMIT);
     if (!ok && lane == 0) atomicOr(a.err, 1);
   } else if (warp < W_SPL + 4) {
     // ------------------------------------------------ X split
@@ -446,8 +486,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                __ldg(a.mask + (size_t)gx + (size_t)a.nax * ((size_t)gy + (size_t)a.nay * gz));
       }
       const bool landed =
-          tc::mbar_wait(bar(B_XFULL + s), (uint32_t)(it >> 1) & 1u, WAIT_LIMIT);
-      const bool bfree = tc::mbar_wait(bar(B_AFREE + hf), ((uint32_t)it & 1u) ^ 1u, WAIT_LIMIT);
+          tc::mbar_wait_sleep(bar(B_XFULL + s), (uint32_t)(it >> 1) & 1u, WAIT_LIMIT);
+      const bool bfree = tc::mbar_wait_sleep(bar(B_AFREE + hf), ((uint32_t)it & 1u) ^ 1u, WAIT_LIMIT);
       if (!__all_sync(0xffffffffu, landed && bfree)) {
         ok = false;
         break;
@@ -463,11 +503,11 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
           for (int i = 0; i < 4; i++) {
             const int n = 4 * c + i;
-            const uint32_t h = tf32_rna(f[i]);
+            const uint32_t h = tf32_head(f[i]);
             *reinterpret_cast<uint32_t *>(bq + n * 128 + woff[n & 7]) = h;
             if (SPLIT)
               *reinterpret_cast<uint32_t *>(bq + (64 + n) * 128 + woff[n & 7]) =
-                  tf32_rna(f[i] - __uint_as_float(h));
+                  tf32_tail(f[i], h);
           }
         }
       }
@@ -503,7 +543,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         zero = gx < a.nax && gy < a.nay && gz < a.naz &&
                __ldg(a.mask + (size_t)gx + (size_t)a.nax * ((size_t)gy + (size_t)a.nay * gz));
       }
-      const bool got = tc::mbar_wait(bar(B_DFULL + d), (uint32_t)(it >> 1) & 1u, WAIT_LIMIT);
+      const bool got = tc::mbar_wait_sleep(bar(B_DFULL + d), (uint32_t)(it >> 1) & 1u, WAIT_LIMIT);
       // the previous box's reduces have read the tile; every epilogue
       // thread got this box's D, or all four warps stop here
       if (issuer) bulk_wait_read0();
@@ -594,6 +634,24 @@ bool make_xmap(CUtensorMap *m, const float *X, int nax, int nay, int naz) {
          CUDA_SUCCESS;
 }
 
+// The map of the element-major FP32 operator copy [E][64] on the structured
+// element grid: dimensions (64, nex, ney, nez), box (32 floats = 4 rows of
+// an element matrix, 4 x 4 x 4 elements), 128-byte swizzle, elements outside
+// the grid read as zero.
+bool make_amap(CUtensorMap *m, const float *A, int nex, int ney, int nez) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !A || (reinterpret_cast<uintptr_t>(A) & 15)) return false;
+  const cuuint64_t dims[4] = {64, (cuuint64_t)nex, (cuuint64_t)ney, (cuuint64_t)nez};
+  const cuuint64_t strides[3] = {256, 256 * (cuuint64_t)nex,
+                                 256 * (cuuint64_t)nex * (cuuint64_t)ney};
+  const cuuint32_t box[4] = {32, BE, BE, BE};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float *>(A), dims, strides, box,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
 }  // namespace blocktc
 
 bool block_tc_supported(const Handle &h) {
@@ -608,9 +666,10 @@ int launch_block_tc(const Handle &h, bool split, const float *A, const float *X,
     set_error("tcgen05 block apply: needs the structured numbering and 16-byte aligned vectors");
     return VDR_BAD_ARGUMENT;
   }
-  CUtensorMap xmap, ymap;
-  if (!make_xmap(&xmap, X, h.nax, h.nay, h.naz) || !make_xmap(&ymap, Y, h.nax, h.nay, h.naz)) {
-    set_error("tcgen05 block apply: tensor maps of X and Y could not be made");
+  CUtensorMap xmap, ymap, amap;
+  if (!make_xmap(&xmap, X, h.nax, h.nay, h.naz) || !make_xmap(&ymap, Y, h.nax, h.nay, h.naz) ||
+      !make_amap(&amap, A, h.nax - 1, h.nay - 1, h.naz - 1)) {
+    set_error("tcgen05 block apply: tensor maps of X, Y and the operator could not be made");
     return VDR_CUDA_ERROR;
   }
   static std::atomic<unsigned> opted{0u};
@@ -640,9 +699,9 @@ int launch_block_tc(const Handle &h, bool split, const float *A, const float *X,
   a.err = h.block_err;
   const int grid = a.nbox < device_sm_count() ? a.nbox : device_sm_count();
   if (split)
-    block_apply_tc_kernel<true><<<grid, THREADS, SMEM, s>>>(xmap, ymap, a);
+    block_apply_tc_kernel<true><<<grid, THREADS, SMEM, s>>>(xmap, ymap, amap, a);
   else
-    block_apply_tc_kernel<false><<<grid, THREADS, SMEM, s>>>(xmap, ymap, a);
+    block_apply_tc_kernel<false><<<grid, THREADS, SMEM, s>>>(xmap, ymap, amap, a);
   count_launches(1);
   const cudaError_t e = cudaGetLastError();
   return e ? cuda_fail(e, "tcgen05 block apply") : VDR_OK;

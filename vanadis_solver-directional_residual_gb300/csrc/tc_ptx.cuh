@@ -45,6 +45,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// try_wait with a suspend-time hint: the thread sleeps until the phase
+// completes or about `hint_ns` nanoseconds pass, instead of returning at
+// once, so that waiting warps leave the issue slots to the working ones.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parity,
+                                                    uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+// Waits as mbar_wait below, sleeping in the try_wait between checks of the
+// clock (each sleep at most `hint_ns`, far below the limit).
+__device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity, long long limit,
+                                                uint32_t hint_ns = 20000u) {
+  if (mbar_try_wait_sleep(bar, parity, hint_ns)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait_sleep(bar, parity, hint_ns))
+    if (clock64() - t0 > limit) return false;
+  return true;
+}
 // Waits until the phase with the given parity has completed, at most
 // `limit` cycles; false when it gave up.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
