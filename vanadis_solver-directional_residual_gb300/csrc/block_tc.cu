@@ -41,10 +41,10 @@
 // Aaos[p*64 + 8i + j] (Jacobi scale folded into the columns, Dirichlet rows
 // and columns zero), a box's 64 elements by two TMA boxes per box.
 //
-// Warp roles (448 threads, one CTA per SM, boxes strided over the grid):
+// Warp roles (576 threads, one CTA per SM, boxes strided over the grid):
 // warp 0 = TMA producer, warp 1 = TMEM owner and MMA issuer, warps 2-5 = A
-// assembly (element rows loaded one box ahead), warps 6-9 = X split and
-// transpose (one 32-node K atom each), warps 10-13 = epilogue; warp w
+// assembly, warps 6-13 = X split and transpose (a 32-node K atom and 32
+// columns each), warps 14-17 = epilogue; warp w
 // reaches TMEM lanes 32 (w % 4) .. 32 (w % 4) + 31.  The TMA stages and D
 // are double-buffered, so the load of box i+1 and the epilogue of box i-1
 // overlap the MMAs of box i.  A (256 of the 512 TMEM columns) and B are
@@ -67,9 +67,9 @@ namespace vdr {
 namespace blocktc {
 
 constexpr int BE = 4, BN = 5, ROWS = BN * BN * BN;  // box: 4^3 elements, 125 nodes
-// warps: 0 TMA producer, 1 MMA issuer, 2-5 A assembly, 6-9 X split, 10-13
+// warps: 0 TMA producer, 1 MMA issuer, 2-5 A assembly, 6-13 X split, 14-17
 // epilogue
-constexpr int W_ASM = 2, W_SPL = 6, W_EPI = 10;
+constexpr int W_ASM = 2, W_SPL = 6, W_EPI = 14;
 constexpr int THREADS = 32 * (W_EPI + 4);
 constexpr int XREG = 16384;         // 128 rows x 128 bytes: 32 columns of the TMA stage
 constexpr int XSTAGE = 2 * XREG;    // node rows as the TMA lands them
@@ -208,8 +208,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (threadIdx.x == 0) {
     for (int i = 0; i < 2; i++) {
       tc::mbar_init(bar(B_XFULL + i), 1);
-      tc::mbar_init(bar(B_XEMPTY + i), 4);
-      tc::mbar_init(bar(B_AFULL + i), 4 + 2);  // A assembly warps + split warps of the half
+      tc::mbar_init(bar(B_XEMPTY + i), 8);
+      tc::mbar_init(bar(B_AFULL + i), 4 + 4);  // A assembly warps + split warps of the half
       tc::mbar_init(bar(B_AFREE + i), 1);
       tc::mbar_init(bar(B_DFULL + i), 1);
       tc::mbar_init(bar(B_DEMPTY + i), 4);
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   } else if (warp >= W_SPL && warp < W_SPL + 4) {
     // K positions 124..127 of every B row zero: 125..127 are never written
     // and the MMA reads them (times zero columns of A)
-    const int row = threadIdx.x - 32 * W_SPL;
+    const int row = threadIdx.x - 32 * W_SPL;  // 0 .. 127
     *reinterpret_cast<float4 *>(bst + 3 * KATOM + row * 128 + ((7 ^ (row & 7)) << 4)) =
         make_float4(0.f, 0.f, 0.f, 0.f);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -459,13 +459,13 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (eissuer && issued > it)
       tc::mbar_wait_sleep(bar(B_EFULL), (uint32_t)(issued - 1) & 1u, WAIT_LIMIT);
     if (!ok && lane == 0) atomicOr(a.err, 1);
-  } else if (warp < W_SPL + 4) {
+  } else if (warp < W_SPL + 8) {
     // ------------------------------------------------ X split
-    // warp q: box nodes 32q .. 32q + 31 (K atom q, in half q / 2 of K); this
-    // thread's node row of the TMA stage, 16 chunks of 4 columns, to K
-    // position r of B rows n (head) and 64 + n (tail); Dirichlet rows zero
-    // when masked
-    const int q = warp - W_SPL, hf = q >> 1;
+    // warp g: box nodes 32 (g / 2) .. + 31 (K atom g / 2, in half g / 4 of
+    // K), columns 32 (g % 2) .. + 31 (one region of the TMA stage); this
+    // thread's node row, 8 chunks of 4 columns, to K position r of B rows n
+    // (head) and 64 + n (tail); Dirichlet rows zero when masked
+    const int g = warp - W_SPL, q = g >> 1, hf = g >> 2, ch = g & 1;
     const int r = 32 * q + lane;
     const bool rv = r < ROWS;
     const int lx = r % BN, ly = (r / BN) % BN, lz = r / (BN * BN);
@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     uint32_t woff[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) woff[k] = (((uint32_t)(lane >> 2) ^ (uint32_t)k) << 4) + (lane & 3) * 4;
-    unsigned char *bq = bst + q * KATOM;
+    unsigned char *bq = bst + q * KATOM + ch * 32 * 128;  // rows n from 32 ch
     bool ok = true;
     int it = 0;
     for (int b = blockIdx.x; b < a.nbox; b += gridDim.x, it++) {
@@ -492,17 +492,16 @@ __global__ void __launch_bounds__(THREADS, 1)
         ok = false;
         break;
       }
-      const unsigned char *xr = xst + s * XSTAGE + r * 128;
+      const unsigned char *xr = xst + s * XSTAGE + ch * XREG + r * 128;
       if (rv) {
 #pragma unroll
-        for (int c = 0; c < 16; c++) {
-          float4 v = *reinterpret_cast<const float4 *>(xr + (c >> 3) * XREG +
-                                                       (((c & 7) ^ (r & 7)) << 4));
+        for (int c = 0; c < 8; c++) {
+          float4 v = *reinterpret_cast<const float4 *>(xr + ((c ^ (r & 7)) << 4));
           if (zero) v = make_float4(0.f, 0.f, 0.f, 0.f);
           const float f[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
           for (int i = 0; i < 4; i++) {
-            const int n = 4 * c + i;
+            const int n = 4 * c + i;  // column 32 ch + n
             const uint32_t h = tf32_head(f[i]);
             *reinterpret_cast<uint32_t *>(bq + n * 128 + woff[n & 7]) = h;
             if (SPLIT)
