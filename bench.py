@@ -318,10 +318,11 @@ BATCH_K = 64
 BLOCK_TILE_KERNEL = ("block_apply_tile<split> (8x2x2-element boxes, node rows "
                      "staged in shared memory by cp.async, mma.sync m16n8k8 TF32 "
                      "x3, one float4 atomic per node and 4 columns)")
-BLOCK_TC_KERNEL = ("block_apply_tc_kernel<split> (4x4x4-element boxes: box "
-                   "operator assembled in TMEM, node rows by 4-D TMA, split and "
-                   "transposed in shared memory, tcgen05.mma kind::tf32 x3 "
-                   "M=128 N=128+64 K=128, float4 atomics)")
+BLOCK_TC_KERNEL = ("block_apply_tc_kernel<split> (4x4x4-element boxes: element "
+                   "matrices and node rows by 4-D TMA, box operator assembled "
+                   "in TMEM, node rows split and transposed in shared memory, "
+                   "tcgen05.mma kind::tf32 x3 M=128 N=128+64 K=128, Y by two "
+                   "TMA tensor reduces per box)")
 
 
 def batched_rhs_section(vdr, device):
