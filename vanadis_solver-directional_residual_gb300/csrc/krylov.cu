@@ -21,6 +21,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 
 #include "dfloat.cuh"
@@ -899,6 +900,271 @@ __global__ void __launch_bounds__(RED_THREADS) b32_xr(Vec32 a) {
   }
 }
 
+// ---- the FP32 inner iteration as two persistent, fused vector kernels ----
+// With the binary16 operator (which carries the Jacobi scale and the
+// Dirichlet projection) an inner iteration is apply(p -> v), fused alpha +
+// s, apply(s -> t), fused omega + x, r + the next p: two cooperative
+// kernels instead of five launches, and the vectors a phase re-reads after
+// a grid-wide reduction (v, t, s, r, p; 4 bytes a node) mostly come back
+// from L2.  Between the phases of one kernel the grid meets at a barrier;
+// every block then adds all blocks' partial sums in the same fixed order,
+// so every block holds the same scalars (bit-identical) and block 0 writes
+// them to KState.  The launch is cooperative (all blocks resident), and the
+// barrier's wait is bounded: a block whose wait runs out marks the solve
+// VDR_TIMEOUT (reason 7) and returns.
+constexpr long long BAR_LIMIT = 2000000000LL;  // ~1 s of clocks
+
+__device__ bool grid_barrier(KState *st) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = &st->bar_gen;
+    const unsigned g0 = *gen;  // cannot advance before this block arrives
+    __threadfence();
+    bool ok = true;
+    if (atomicAdd(&st->bar_count, 1u) == gridDim.x - 1) {
+      atomicExch(&st->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&st->bar_gen, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*gen == g0) {
+        if (clock64() - t0 > BAR_LIMIT) {
+          ok = false;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+__device__ void barrier_timeout(KState *st) {
+  if (threadIdx.x == 0) {
+    st->status = VDR_TIMEOUT;
+    st->reason = 7;
+    st->done = 1;
+  }
+}
+
+// This block's sums of NQ quantities into partials[q * gridDim.x + block].
+template <int NQ>
+__device__ __forceinline__ void put_partials(double (&v)[NQ], double *partials) {
+  block_sum<NQ>(v);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) partials[q * gridDim.x + blockIdx.x] = v[q];
+}
+// After a barrier: the grid totals, added in a fixed order, in every thread.
+template <int NQ>
+__device__ __forceinline__ void all_sum(const double *partials, double (&out)[NQ]) {
+  __shared__ double res[NQ];
+  double w[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    w[q] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+      w[q] += __ldcg(partials + q * gridDim.x + b);
+  }
+  block_sum<NQ>(w);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) res[q] = w[q];
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NQ; q++) out[q] = res[q];
+}
+
+// alpha = rho / (rh, v); s = r - alpha v; t = 0; ||s||.
+__global__ void __launch_bounds__(RED_THREADS, 4) b32f_alpha_s(Vec32 a) {
+  KState *st = a.st;
+  if (st->done) return;
+  double *pa = a.partials, *pb = a.partials + MAXQ * gridDim.x;
+  const double rho = st->rho;
+  {
+    DfAcc d{0.f, 0.f};
+    float hv[U], vv[U];
+    VLOOP(hv[u] = ok ? a.rh[i] : 0.f; vv[u] = ok ? a.v[i] : 0.f;,
+          dot_acc(d, hv[u], vv[u]);)
+    double v[1] = {dot_val(d)};
+    put_partials<1>(v, pa);
+  }
+  if (!grid_barrier(st)) {
+    barrier_timeout(st);
+    return;
+  }
+  double o[1];
+  all_sum<1>(pa, o);
+  if (o[0] == 0.0 || !finite(o[0])) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->status = VDR_BREAKDOWN;
+      st->reason = 2;
+      st->done = 1;
+    }
+    return;
+  }
+  const double alpha = rho / o[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->alpha = alpha;
+  const float al = (float)alpha;
+  DfAcc n2{0.f, 0.f};
+  float rv[U], vv[U];
+  VLOOP(rv[u] = ok ? a.r[i] : 0.f; vv[u] = ok ? a.v[i] : 0.f;,
+        const float si = rv[u] - al * vv[u];
+        a.s[i] = si;
+        a.t[i] = 0.f;
+        dot_acc(n2, si, si);)
+  double v[1] = {dot_val(n2)};
+  double o2[1];
+  if (grid_sum<1>(v, pb, &st->ticket, o2)) {
+    st->snrm = sqrt(o2[0]) / sqrt(st->bnrm2);
+    if (st->snrm <= st->tol) st->sconv = 1;
+  }
+}
+
+// omega = (t, s) / (t, t); x += alpha p + omega s; r = s - omega t; rho =
+// (rh, r), ||r||, convergence; then, unless done, the next iteration's
+// p = r + beta (p - omega v), v = 0.
+__global__ void __launch_bounds__(RED_THREADS, 3) b32f_omega_xr_p(Vec32 a) {
+  KState *st = a.st;
+  if (st->done) return;
+  const float al = (float)st->alpha;
+  if (st->sconv) {  // s met the tolerance: x += alpha p, r = s
+    float xv[U], pv[U], sv[U];
+    VLOOP(xv[u] = ok ? a.x[i] : 0.f; pv[u] = ok ? a.p[i] : 0.f;
+          sv[u] = ok ? a.s[i] : 0.f;,
+          a.x[i] = xv[u] + al * pv[u];
+          a.r[i] = sv[u];)
+    double v[1] = {0.0};
+    double o[1];
+    if (grid_sum<1>(v, a.partials, &st->ticket, o)) {
+      st->iter += 1;
+      st->err = st->snrm;
+      st->status = VDR_OK;
+      st->done = 1;
+    }
+    return;
+  }
+  double *pa = a.partials, *pb = a.partials + MAXQ * gridDim.x;
+  // everything read from KState before block 0 writes it
+  const double rho0 = st->rho, alpha = st->alpha, bnrm2 = st->bnrm2, tol = st->tol;
+  const int iter0 = st->iter, itmax = st->itmax;
+  {
+    DfAcc ts{0.f, 0.f}, tt{0.f, 0.f};
+    float tv[U], sv[U];
+    VLOOP(tv[u] = ok ? a.t[i] : 0.f; sv[u] = ok ? a.s[i] : 0.f;,
+          dot_acc(ts, tv[u], sv[u]);
+          dot_acc(tt, tv[u], tv[u]);)
+    double v[2] = {dot_val(ts), dot_val(tt)};
+    put_partials<2>(v, pa);
+  }
+  if (!grid_barrier(st)) {
+    barrier_timeout(st);
+    return;
+  }
+  double o[2];
+  all_sum<2>(pa, o);
+  if (o[1] == 0.0 || !finite(o[1]) || !finite(o[0])) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->status = VDR_BREAKDOWN;
+      st->reason = 3;
+      st->done = 1;
+    }
+    return;
+  }
+  const double omega = o[0] / o[1];
+  const float om = (float)omega;
+  {
+    DfAcc rr{0.f, 0.f}, hr{0.f, 0.f};
+    float xv[U], pv[U], sv[U], tv[U], hv[U];
+    VLOOP(xv[u] = ok ? a.x[i] : 0.f; pv[u] = ok ? a.p[i] : 0.f; sv[u] = ok ? a.s[i] : 0.f;
+          tv[u] = ok ? a.t[i] : 0.f; hv[u] = ok ? a.rh[i] : 0.f;,
+          a.x[i] = xv[u] + al * pv[u] + om * sv[u];
+          const float ri = sv[u] - om * tv[u];
+          a.r[i] = ri;
+          dot_acc(rr, ri, ri);
+          dot_acc(hr, hv[u], ri);)
+    double v[2] = {dot_val(rr), dot_val(hr)};
+    put_partials<2>(v, pb);
+  }
+  if (!grid_barrier(st)) {
+    barrier_timeout(st);
+    return;
+  }
+  double o2[2];
+  all_sum<2>(pb, o2);
+  // the convergence decision, identical in every block
+  const double err = sqrt(o2[0]) / sqrt(bnrm2);
+  const int iter = iter0 + 1;
+  int status = VDR_NOT_CONVERGED, reason = 0;
+  bool done = true;
+  if (!(err == err) || !finite(o2[1])) {
+    status = VDR_BREAKDOWN;
+    reason = 5;
+  } else if (err <= tol) {
+    status = VDR_OK;
+  } else if (o2[1] == 0.0 || omega == 0.0) {
+    status = VDR_BREAKDOWN;
+    reason = o2[1] == 0.0 ? 1 : 4;
+  } else if (iter >= itmax) {
+    status = VDR_NOT_CONVERGED;
+  } else {
+    done = false;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->omega = omega;
+    st->iter = iter;
+    st->rho_old = rho0;
+    st->rho = o2[1];
+    st->err = err;
+    if (done) {
+      st->status = status;
+      if (reason) st->reason = reason;
+      st->done = 1;
+    }
+  }
+  if (done) return;
+  // the next iteration's search direction (r and p just passed through L2)
+  const float beta = (float)((o2[1] / rho0) * (alpha / omega));
+  float rv[U], pv[U], vv[U];
+  VLOOP(rv[u] = ok ? a.r[i] : 0.f; pv[u] = ok ? a.p[i] : 0.f; vv[u] = ok ? a.v[i] : 0.f;,
+        a.p[i] = rv[u] + beta * (pv[u] - om * vv[u]);
+        a.v[i] = 0.f;)
+}
+
+// The cooperative grid of a fused kernel: at most the blocks that fit on
+// the device at once (its own resident blocks per SM, cached in `slot`).
+template <typename Kern>
+int fused_grid(Kern kern, std::atomic<int> &slot, int n) {
+  int per_sm = slot.load(std::memory_order_relaxed);
+  if (per_sm <= 0) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RED_THREADS, 0);
+    if (per_sm < 1) per_sm = 1;
+    slot.store(per_sm, std::memory_order_relaxed);
+  }
+  const long need = ((long)n + RED_THREADS - 1) / RED_THREADS;
+  return (int)std::max<long>(1, std::min<long>(need, (long)device_sm_count() * std::min(per_sm, 8)));
+}
+std::atomic<int> g_occ_alpha_s{0}, g_occ_omega_xr_p{0};
+
+template <typename Kern>
+cudaError_t launch_cooperative(Kern kern, int grid, const Vec32 &a, cudaStream_t s) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(RED_THREADS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, a);
+}
+
 // b32 = (float)(r * scale); dinv32 = (float)dinv (when dinv32 is given).
 __global__ void __launch_bounds__(RED_THREADS) k32_in(Vec32 a, const double *r,
                                                       double scale, const double *dinv,
@@ -946,6 +1212,15 @@ cudaError_t launch_iteration32(Handle &h, const Vec32 &a) {
   const int g = red_grid(h.N);
   cudaStream_t s = h.stream;
   cudaError_t e;
+  if (h.use_half && h.fused32) {  // p formed by the previous iteration's fused kernel
+    if ((e = launch_apply_half(h, a.p, a.v, &h.st->done, nullptr, s))) return e;
+    if ((e = launch_cooperative(b32f_alpha_s, fused_grid(b32f_alpha_s, g_occ_alpha_s, h.N), a,
+                                s)))
+      return e;
+    if ((e = launch_apply_half(h, a.s, a.t, &h.st->done, &h.st->sconv, s))) return e;
+    return launch_cooperative(b32f_omega_xr_p,
+                              fused_grid(b32f_omega_xr_p, g_occ_omega_xr_p, h.N), a, s);
+  }
   if (h.use_half) {  // A D^-1 in binary16: no preconditioner vectors
     b32_p<false><<<g, RED_THREADS, 0, s>>>(a);
     if ((e = launch_apply_half(h, a.p, a.v, &h.st->done, nullptr, s))) return e;
@@ -986,11 +1261,13 @@ int solve32_inner(Handle &h, double tol, int itmax, int *iter, double *err) {
   count_launches(1);
   if ((e = cudaGetLastError())) return cuda_fail(e, "start kernel");
   const int K = h.opt.iters_per_graph > 0 ? h.opt.iters_per_graph : 8;
-  const void *key = (const void *)((uintptr_t)h.work32 ^ ((uintptr_t)h.A32v << 1) ^
-                                   (uintptr_t)K ^ ((uintptr_t)h.scatter << 12) ^
-                                   ((uintptr_t)h.use_half << 20) ^
-                                   ((uintptr_t)h.A16 << 2));
-  if (!h.graph32 || h.graph32_key != key) {
+  for (int attempt = 0; attempt < 2; attempt++) {
+    const bool fused = h.use_half && h.fused32;
+    const void *key = (const void *)((uintptr_t)h.work32 ^ ((uintptr_t)h.A32v << 1) ^
+                                     (uintptr_t)K ^ ((uintptr_t)h.scatter << 12) ^
+                                     ((uintptr_t)h.use_half << 20) ^
+                                     ((uintptr_t)h.A16 << 2) ^ ((uintptr_t)fused << 21));
+    if (h.graph32 && h.graph32_key == key) break;
     if (h.graph32) cudaGraphExecDestroy(h.graph32);
     h.graph32 = nullptr;
     cudaGraph_t graph;
@@ -1000,14 +1277,34 @@ int solve32_inner(Handle &h, double tol, int itmax, int *iter, double *err) {
     for (int k = 0; k < K && !e; k++) e = launch_iteration32(h, a);
     count_launches(before - launches_so_far());  // captured, not launched
     cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (!e && !e2) {
+      e = cudaGraphInstantiate(&h.graph32, graph, 0);
+      cudaGraphDestroy(graph);
+      if (!e) {
+        h.graph32_key = key;
+        break;
+      }
+      h.graph32 = nullptr;
+    } else if (!e2) {
+      cudaGraphDestroy(graph);
+    }
+    // a cooperative launch that the capture or the graph refuses: the
+    // unfused kernels instead
+    if (fused) {
+      cudaGetLastError();
+      h.fused32 = false;
+      e = cudaSuccess;
+      continue;
+    }
     if (e) return cuda_fail(e, "capture");
     if (e2) return cuda_fail(e2, "end capture");
-    e = cudaGraphInstantiate(&h.graph32, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e) return cuda_fail(e, "graph instantiate");
-    h.graph32_key = key;
   }
-  const long nodes = 5 + 2 * (h.use_half ? 1 : apply_launches(h));
+  if (h.use_half && h.fused32) {  // the first search direction p = r, v = 0
+    b32_p<false><<<g, RED_THREADS, 0, s>>>(a);
+    count_launches(1);
+    if ((e = cudaGetLastError())) return cuda_fail(e, "first direction");
+  }
+  const long nodes = (h.use_half && h.fused32) ? 4 : 5 + 2 * (h.use_half ? 1 : apply_launches(h));
   const int max_launches = (itmax + K - 1) / K + 1;
   bool finished = false;
   for (int c = 0; c < max_launches && !finished; c++) {

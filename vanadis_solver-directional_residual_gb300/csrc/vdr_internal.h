@@ -34,6 +34,7 @@ struct KState {
   int x_zero;  // the initial guess is zero (its apply is skipped)
   unsigned int ticket;
   unsigned int pad2;
+  unsigned int bar_count, bar_gen;  // grid barrier of the fused inner kernels
 };
 
 // A right preconditioner for BiCGStab beyond Jacobi: `enqueue` adds
@@ -198,6 +199,9 @@ struct Handle {
   float *work32 = nullptr;
   cudaGraphExec_t graph32 = nullptr;
   const void *graph32_key = nullptr;
+  // the FP32 inner iteration with the binary16 operator as two fused
+  // cooperative vector kernels (krylov.cu); off after a failed capture
+  bool fused32 = true;
   KState *st = nullptr;
   KState *h_st = nullptr;  // pinned mirror
   double *partials = nullptr;
