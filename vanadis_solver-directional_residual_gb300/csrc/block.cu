@@ -1206,10 +1206,15 @@ __global__ void bo_update(long n, int K, double *X, const float *D,
     X[i] += (double)D[i] * scale[i & (K - 1)];
 }
 
-__global__ void bo_mask(long n, int kshift, double *X, const unsigned char *m) {
+// X = 0 on Dirichlet rows; *nonzero set when any entry is left nonzero.
+__global__ void bo_mask(long n, int kshift, double *X, const unsigned char *m, int *nonzero) {
+  bool nz = false;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long)gridDim.x * blockDim.x)
+       i += (long)gridDim.x * blockDim.x) {
     if (m[i >> kshift]) X[i] = 0.0;
+    else if (X[i] != 0.0) nz = true;
+  }
+  if (__any_sync(FULL, nz) && (threadIdx.x & 31) == 0) atomicOr(nonzero, 1);
 }
 
 __global__ void dinv_to_f32(const double *__restrict__ d, float *__restrict__ f,
@@ -1554,7 +1559,7 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
   double *outer_err = colsd + 7 * 64;
   double *mx = colsd + 8 * 64;      // 2 x 64
   double *scale = colsd + 10 * 64;
-  int *colsi = reinterpret_cast<int *>(colsd + 11 * 64);  // 3 x 64 ints
+  int *colsi = reinterpret_cast<int *>(colsd + 11 * 64);  // 3 x 64 ints + a flag
   a.c.tol = colsd + 13 * 64;
   a.c.active = colsi;
   a.c.sconv = colsi + 64;
@@ -1589,9 +1594,16 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
   }
   const int gv = std::min(BK_MAX_GRID, grid_n(n, BT, 2));  // one wave
   const int gm = grid_n(n, 256, 8);
-  bo_mask<<<gm, 256, 0, s>>>(n, a.kshift, X, h.mask);
+  // the initial guess masked; a zero one makes the first residual B itself
+  int *x_nonzero = colsi + 3 * 64;
+  int x_nz_host = 1;
+  if ((e = cudaMemsetAsync(x_nonzero, 0, sizeof(int), s))) return cuda_fail(e, "block setup");
+  bo_mask<<<gm, 256, 0, s>>>(n, a.kshift, X, h.mask, x_nonzero);
   count_launches(1);
-  if ((e = cudaGetLastError())) return cuda_fail(e, "block setup");
+  if ((e = cudaGetLastError()) ||
+      (e = cudaMemcpyAsync(&x_nz_host, x_nonzero, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaStreamSynchronize(s)))
+    return cuda_fail(e, "block setup");
 
   // KI inner iterations per graph launch (8 kernels each)
   constexpr int KI = 4;
@@ -1631,7 +1643,7 @@ int solve_block_device(Handle &h, int K, int precision, const double *B,
   for (outer = 0;; outer++) {
     // FP64 residual of every column, its scale and relative norm
     if ((e = cudaMemsetAsync(R, 0, sizeof(double) * n, s)) ||
-        (e = launch_block_apply64(h, K, X, R, s)) ||
+        ((outer > 0 || x_nz_host) && (e = launch_block_apply64(h, K, X, R, s))) ||
         (e = cudaMemsetAsync(st, 0, sizeof(BState), s)))
       return cuda_fail(e, "block residual");
     bo_residual<<<gv, BT, 0, s>>>(a, B, R, mx);
