@@ -871,46 +871,83 @@ __device__ __forceinline__ double dot_val(const DfAcc &acc) {
   return df_to_double(acc.s, acc.c);
 }
 
-// Grid-stride loops over the N*K block entries, four entries per thread
-// per trip (all loads issued before use).  The stride is a multiple of K,
-// so a thread's column k = threadIdx.x % K never changes.
+// Grid-stride loops.  BLOOP: over the N*K block entries, one per thread per
+// trip (the FP64 glue kernels below).  ULOOP: over units of four
+// consecutive columns 4g .. 4g+3 of one node row (unit j = node * K/4 + g,
+// float4 loads and stores); the stride is a multiple of K/4, so a thread's
+// column group g = threadIdx.x % (K/4) never changes.
 #define BSTRIDE ((long)gridDim.x * blockDim.x)
 #define BLOOP(i)                                                      \
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; \
        i += BSTRIDE)
-#define BLOOP4(i0) \
-  for (long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x; i0 < a.n; \
-       i0 += 4 * BSTRIDE)
+#define ULOOP(j)                                                           \
+  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < (a.n >> 2); \
+       j += BSTRIDE)
+
+__device__ __forceinline__ float4 ld4(const float *p, long j) {
+  return reinterpret_cast<const float4 *>(p)[j];
+}
+__device__ __forceinline__ void st4(float *p, long j, float4 v) {
+  reinterpret_cast<float4 *>(p)[j] = v;
+}
+__device__ __forceinline__ float f4(const float4 &v, int c) {
+  return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
+}
+
+// col_grid_sum for threads that own four columns: each block first adds,
+// per column 4g + c, the values of its threads with column group g, then
+// the last block combines the blocks as col_grid_sum does.
+template <int NQ>
+__device__ __forceinline__ bool col_grid_sum4(double (&v)[NQ][4], const BVec &a,
+                                              double *out /* [NQ][K] */) {
+  __shared__ double sm4[NQ][4][BT];
+  const int K = a.K, Q = K >> 2;
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int q = 0; q < NQ; q++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) sm4[q][c][tid] = v[q][c];
+  __syncthreads();
+  double w[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) w[q] = 0.0;
+  if (tid < K) {
+    const int g = tid >> 2, c = tid & 3;
+#pragma unroll
+    for (int q = 0; q < NQ; q++)
+      for (int t = g; t < BT; t += Q) w[q] += sm4[q][c][t];
+  }
+  // the block's per-column sums now sit in threads tid < K: hand them to the
+  // one-column-per-thread reduction (threads tid >= K contribute zero)
+  return col_grid_sum<NQ>(w, a, out);
+}
 
 // r = b - r (r holds A x); rh = r; per-column norms; columns with b = 0 are
 // inactive from the start.
 __global__ void __launch_bounds__(BT, 2) bb_start(BVec a) {
-  const int k = threadIdx.x & (a.K - 1);
-  DfAcc d0{0.f, 0.f}, d1{0.f, 0.f};
-  BLOOP4(i0) {
-    float bv[4], rv[4];
+  DfAcc d0[4], d1[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      const bool ok = i < a.n;
-      bv[u] = ok ? a.b[i] : 0.f;
-      rv[u] = ok ? a.r[i] : 0.f;
-    }
+  for (int c = 0; c < 4; c++) d0[c] = d1[c] = DfAcc{0.f, 0.f};
+  ULOOP(j) {
+    const float4 bv = ld4(a.b, j), rv = ld4(a.r, j);
+    const float4 ri = make_float4(bv.x - rv.x, bv.y - rv.y, bv.z - rv.z, bv.w - rv.w);
+    st4(a.r, j, ri);
+    st4(a.rh, j, ri);
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      const float ri = bv[u] - rv[u];
-      if (i < a.n) {
-        a.r[i] = ri;
-        a.rh[i] = ri;
-      }
-      dot_acc(d0, bv[u], bv[u]);
-      dot_acc(d1, ri, ri);
+    for (int c = 0; c < 4; c++) {
+      dot_acc(d0[c], f4(bv, c), f4(bv, c));
+      dot_acc(d1[c], f4(ri, c), f4(ri, c));
     }
   }
-  double v[2] = {dot_val(d0), dot_val(d1)};
+  double v[2][4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    v[0][c] = dot_val(d0[c]);
+    v[1][c] = dot_val(d1[c]);
+  }
   __shared__ double out[2 * 64];
-  if (col_grid_sum<2>(v, a, out)) {
+  if (col_grid_sum4<2>(v, a, out)) {
+    const int k = threadIdx.x;
     const double bb = out[k], rr = out[a.K + k];
     a.c.bnrm2[k] = bb;
     a.c.rho[k] = rr;
@@ -938,55 +975,54 @@ __global__ void bb_finish_start(BVec a) {  // one block: any column active?
   }
 }
 
-// p = r + beta (p - omega v) (p = r on the first iteration); v = 0.
+// p = r + beta (p - omega v) (p = r on the first iteration); v = 0;
+// inactive columns get p = 0.
 __global__ void __launch_bounds__(BT, 2) bb_p(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x & (a.K - 1);
-  const bool act = a.c.active[k];
+  const int k0 = 4 * (threadIdx.x & ((a.K >> 2) - 1));
   const bool first = a.st->iter == 0;
-  const float beta = first ? 0.f
-      : (float)((a.c.rho[k] / a.c.rho_old[k]) * (a.c.alpha[k] / a.c.omega[k]));
-  const float om = (float)a.c.omega[k];
-  BLOOP4(i0) {
-    float rv[4], pv[4], vv[4];
+  float beta[4], om[4];
+  bool on[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      const bool ok = i < a.n && act;
-      rv[u] = ok ? a.r[i] : 0.f;
-      pv[u] = (ok && !first) ? a.p[i] : 0.f;
-      vv[u] = (ok && !first) ? a.v[i] : 0.f;
-    }
+  for (int c = 0; c < 4; c++) {
+    const int k = k0 + c;
+    on[c] = a.c.active[k] != 0;
+    beta[c] = first ? 0.f
+        : (float)((a.c.rho[k] / a.c.rho_old[k]) * (a.c.alpha[k] / a.c.omega[k]));
+    om[c] = (float)a.c.omega[k];
+  }
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  ULOOP(j) {
+    const float4 rv = ld4(a.r, j);
+    const float4 pv = first ? z4 : ld4(a.p, j);
+    const float4 vv = first ? z4 : ld4(a.v, j);
+    float o[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      if (i < a.n) {
-        a.p[i] = first ? rv[u] : rv[u] + beta * (pv[u] - om * vv[u]);
-        a.v[i] = 0.f;
-      }
+    for (int c = 0; c < 4; c++) {
+      const float r = f4(rv, c), p = f4(pv, c), v = f4(vv, c);
+      o[c] = on[c] ? (first ? r : r + beta[c] * (p - om[c] * v)) : 0.f;
     }
+    st4(a.p, j, make_float4(o[0], o[1], o[2], o[3]));
+    st4(a.v, j, z4);
   }
 }
 
 __global__ void __launch_bounds__(BT, 2) bb_alpha(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x & (a.K - 1);
-  DfAcc d0{0.f, 0.f};
-  BLOOP4(i0) {
-    float hv[4], vv[4];
+  DfAcc d0[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      const bool ok = i < a.n;
-      hv[u] = ok ? a.rh[i] : 0.f;
-      vv[u] = ok ? a.v[i] : 0.f;
-    }
+  for (int c = 0; c < 4; c++) d0[c] = DfAcc{0.f, 0.f};
+  ULOOP(j) {
+    const float4 hv = ld4(a.rh, j), vv = ld4(a.v, j);
 #pragma unroll
-    for (int u = 0; u < 4; u++) dot_acc(d0, hv[u], vv[u]);
+    for (int c = 0; c < 4; c++) dot_acc(d0[c], f4(hv, c), f4(vv, c));
   }
-  double v[1] = {dot_val(d0)};
+  double v[1][4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) v[0][c] = dot_val(d0[c]);
   __shared__ double out[64];
-  if (col_grid_sum<1>(v, a, out)) {
+  if (col_grid_sum4<1>(v, a, out)) {
+    const int k = threadIdx.x;
     if (a.c.active[k]) {
       const double rv = out[k];
       if (rv == 0.0 || !isfinite(rv)) {
@@ -1003,32 +1039,31 @@ __global__ void __launch_bounds__(BT, 2) bb_alpha(BVec a) {
 // s = r - alpha v; t = 0; ||s|| per column.
 __global__ void __launch_bounds__(BT, 2) bb_s(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x & (a.K - 1);
-  const float al = a.c.active[k] ? (float)a.c.alpha[k] : 0.f;
-  DfAcc d0{0.f, 0.f};
-  BLOOP4(i0) {
-    float rv[4], vv[4];
+  const int k0 = 4 * (threadIdx.x & ((a.K >> 2) - 1));
+  float al[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      const bool ok = i < a.n;
-      rv[u] = ok ? a.r[i] : 0.f;
-      vv[u] = ok ? a.v[i] : 0.f;
-    }
+  for (int c = 0; c < 4; c++)
+    al[c] = a.c.active[k0 + c] ? (float)a.c.alpha[k0 + c] : 0.f;
+  DfAcc d0[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      const float si = rv[u] - al * vv[u];
-      if (i < a.n) {
-        a.s[i] = si;
-        a.t[i] = 0.f;
-      }
-      dot_acc(d0, si, si);
+  for (int c = 0; c < 4; c++) d0[c] = DfAcc{0.f, 0.f};
+  ULOOP(j) {
+    const float4 rv = ld4(a.r, j), vv = ld4(a.v, j);
+    float sv[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      sv[c] = f4(rv, c) - al[c] * f4(vv, c);
+      dot_acc(d0[c], sv[c], sv[c]);
     }
+    st4(a.s, j, make_float4(sv[0], sv[1], sv[2], sv[3]));
+    st4(a.t, j, make_float4(0.f, 0.f, 0.f, 0.f));
   }
-  double v[1] = {dot_val(d0)};
+  double v[1][4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) v[0][c] = dot_val(d0[c]);
   __shared__ double out[64];
-  if (col_grid_sum<1>(v, a, out)) {
+  if (col_grid_sum4<1>(v, a, out)) {
+    const int k = threadIdx.x;
     const double sn = a.c.bnrm2[k] > 0.0 ? sqrt(out[k] / a.c.bnrm2[k]) : 0.0;
     a.c.snrm[k] = sn;
     a.c.sconv[k] = (a.c.active[k] && sn <= a.c.tol[k]) ? 1 : 0;
@@ -1037,26 +1072,26 @@ __global__ void __launch_bounds__(BT, 2) bb_s(BVec a) {
 
 __global__ void __launch_bounds__(BT, 2) bb_omega(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x & (a.K - 1);
-  DfAcc d0{0.f, 0.f}, d1{0.f, 0.f};
-  BLOOP4(i0) {
-    float tv[4], sv[4];
+  DfAcc d0[4], d1[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      const bool ok = i < a.n;
-      tv[u] = ok ? a.t[i] : 0.f;
-      sv[u] = ok ? a.s[i] : 0.f;
-    }
+  for (int c = 0; c < 4; c++) d0[c] = d1[c] = DfAcc{0.f, 0.f};
+  ULOOP(j) {
+    const float4 tv = ld4(a.t, j), sv = ld4(a.s, j);
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      dot_acc(d0, tv[u], sv[u]);
-      dot_acc(d1, tv[u], tv[u]);
+    for (int c = 0; c < 4; c++) {
+      dot_acc(d0[c], f4(tv, c), f4(sv, c));
+      dot_acc(d1[c], f4(tv, c), f4(tv, c));
     }
   }
-  double v[2] = {dot_val(d0), dot_val(d1)};
+  double v[2][4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    v[0][c] = dot_val(d0[c]);
+    v[1][c] = dot_val(d1[c]);
+  }
   __shared__ double out[2 * 64];
-  if (col_grid_sum<2>(v, a, out)) {
+  if (col_grid_sum4<2>(v, a, out)) {
+    const int k = threadIdx.x;
     if (a.c.active[k] && !a.c.sconv[k]) {
       const double ts = out[k], tt = out[a.K + k];
       if (tt == 0.0 || !isfinite(tt) || !isfinite(ts)) {
@@ -1070,49 +1105,68 @@ __global__ void __launch_bounds__(BT, 2) bb_omega(BVec a) {
 
 // x += D^-1 (alpha p + omega s) (Dirichlet entries stay); r = s - omega t
 // (r = s when s already met the tolerance); norms for the next iteration.
+// Inactive columns keep x and r.
 __global__ void __launch_bounds__(BT, 2) bb_xr(BVec a) {
   if (a.st->done) return;
-  const int k = threadIdx.x & (a.K - 1);
-  const bool act = a.c.active[k];
-  const bool sc = a.c.sconv[k];
-  const float al = act ? (float)a.c.alpha[k] : 0.f;
-  const float om = (act && !sc) ? (float)a.c.omega[k] : 0.f;
-  DfAcc d0{0.f, 0.f}, d1{0.f, 0.f};
-  BLOOP4(i0) {
-    float xv[4], pv[4], sv[4], tv[4], hv[4], rv[4], dn[4];
+  const int k0 = 4 * (threadIdx.x & ((a.K >> 2) - 1));
+  const int qshift = a.kshift - 2;  // units per node row = 1 << qshift
+  bool act[4];
+  float al[4], om[4];
+  bool any_act = false;
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      const bool ok = i < a.n;
-      const bool oa = ok && act;
-      const long node = i >> a.kshift;
-      xv[u] = oa ? a.x[i] : 0.f;
-      pv[u] = oa ? a.p[i] : 0.f;
-      sv[u] = oa ? a.s[i] : 0.f;
-      tv[u] = (oa && !sc) ? a.t[i] : 0.f;
-      rv[u] = (ok && !act) ? a.r[i] : 0.f;
-      hv[u] = ok ? a.rh[i] : 0.f;
-      dn[u] = (oa && !a.m[node]) ? a.dinv[node] : 0.f;
+  for (int c = 0; c < 4; c++) {
+    const int k = k0 + c;
+    act[c] = a.c.active[k] != 0;
+    const bool sc = a.c.sconv[k] != 0;
+    al[c] = act[c] ? (float)a.c.alpha[k] : 0.f;
+    om[c] = (act[c] && !sc) ? (float)a.c.omega[k] : 0.f;
+    any_act |= act[c];
+  }
+  DfAcc d0[4], d1[4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) d0[c] = d1[c] = DfAcc{0.f, 0.f};
+  ULOOP(j) {
+    const long node = j >> qshift;
+    const float4 hv = ld4(a.rh, j), rv = ld4(a.r, j);
+    float4 xv = make_float4(0.f, 0.f, 0.f, 0.f), pv = xv, sv = xv, tv = xv;
+    float dn = 0.f;
+    if (any_act) {
+      xv = ld4(a.x, j);
+      pv = ld4(a.p, j);
+      sv = ld4(a.s, j);
+      tv = ld4(a.t, j);
+      dn = a.m[node] ? 0.f : a.dinv[node];
     }
+    float xo[4], ro[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const long i = i0 + u * BSTRIDE;
-      float ri = rv[u];
-      if (act) {
-        ri = sv[u] - om * tv[u];
-        if (i < a.n) {
-          a.x[i] = xv[u] + dn[u] * (al * pv[u] + om * sv[u]);
-          a.r[i] = ri;
-        }
+    for (int c = 0; c < 4; c++) {
+      float ri = f4(rv, c), xi = f4(xv, c);
+      if (act[c]) {
+        ri = f4(sv, c) - om[c] * f4(tv, c);
+        xi = xi + dn * (al[c] * f4(pv, c) + om[c] * f4(sv, c));
       }
-      dot_acc(d0, ri, ri);
-      dot_acc(d1, hv[u], ri);
+      xo[c] = xi;
+      ro[c] = ri;
+      dot_acc(d0[c], ri, ri);
+      dot_acc(d1[c], f4(hv, c), ri);
+    }
+    if (any_act) {
+      st4(a.x, j, make_float4(xo[0], xo[1], xo[2], xo[3]));
+      st4(a.r, j, make_float4(ro[0], ro[1], ro[2], ro[3]));
     }
   }
-  double v[2] = {dot_val(d0), dot_val(d1)};
+  double v[2][4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    v[0][c] = dot_val(d0[c]);
+    v[1][c] = dot_val(d1[c]);
+  }
   __shared__ double out[2 * 64];
-  if (col_grid_sum<2>(v, a, out)) {
-    if (act) {
+  if (col_grid_sum4<2>(v, a, out)) {
+    const int k = threadIdx.x;
+    if (a.c.active[k]) {
+      const bool sc = a.c.sconv[k] != 0;
+      const double omk = a.c.omega[k];
       a.c.rho_old[k] = a.c.rho[k];
       a.c.rho[k] = out[a.K + k];
       const double err = sqrt(out[k] / a.c.bnrm2[k]);
@@ -1123,7 +1177,7 @@ __global__ void __launch_bounds__(BT, 2) bb_xr(BVec a) {
       } else if (err <= a.c.tol[k] || sc) {
         a.c.active[k] = 0;
         a.c.status[k] = VDR_OK;
-      } else if (out[a.K + k] == 0.0 || om == 0.f) {
+      } else if (out[a.K + k] == 0.0 || (float)omk == 0.f) {
         a.c.active[k] = 0;
         a.c.status[k] = VDR_BREAKDOWN;
       }
