@@ -272,6 +272,12 @@ int vdr_set_block_apply(vdr_handle *h, int variant);
  * the wait gives up, flags it and returns.  Returns VDR_TIMEOUT when that
  * path works (the handle stays usable). */
 int vdr_diag_wait_timeout(vdr_handle *h);
+/* Diagnostic of the bounded grid barrier of the mixed solve's fused inner
+ * kernels (cooperative launches): one block of a two-block launch never
+ * arrives, the other waits with a ~1 ms budget, gives up and marks the solve
+ * state.  Returns VDR_TIMEOUT when that path works (the handle stays
+ * usable). */
+int vdr_diag_barrier_timeout(vdr_handle *h);
 
 /* B[n*K + k] = cf * f(Q_k): the right-hand sides of K source fields at once.
  * d_Q is K x E (row k = per-element source of column k, kg/s, the caller's

@@ -173,3 +173,26 @@ def test_precision_option_solve_and_time_loop(vdr, gpu_lib, torch, op):
     assert rel_l2(out["mixed"][1], out["fp64"][1]) < 1e-8
     assert np.max(np.abs(out["mixed"][2] - out["fp64"][2]) /
                   np.abs(out["fp64"][2])) < 1e-8
+
+
+def test_fused_inner_barrier_times_out_and_recovers(vdr, gpu_lib, torch):
+    """The grid barrier of the fused inner vector kernels (binary16 operator)
+    is bounded: a cooperative launch whose second block never arrives makes
+    the waiting block give up after its ~1 ms budget, VDR_TIMEOUT reaches the
+    host, and a mixed solve on the same handle afterwards (through the fused
+    kernels) still reaches its FP64 tolerance."""
+    import importlib
+    L = importlib.import_module(vdr.__name__ + "._lib")
+    prob = vdr.problems.rotation_shear(32, 32, 16, seed=35)
+    dt = 10.0 / 32
+    with vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=2.0, aM=3.0 / dt) as s:
+        assert s.lib.vdr_diag_barrier_timeout(s.h) == L.TIMEOUT
+        s.set_mixed_operator("half")
+        b = torch.empty(prob.mesh.nnode, dtype=torch.float64, device="cuda")
+        s.assemble_rhs_device(b, 3.0, 3.0 / dt, None)
+        x = torch.zeros_like(b)
+        torch.cuda.synchronize()
+        outer, inner, err, st = s.solve_mixed_device(b, x, tol=1e-10, inner_tol=1e-3)
+        torch.cuda.synchronize()
+        assert st == 0 and err <= 1e-10, (outer, inner, err, st)
+        assert s.true_residual_device(b, x) <= 1.5e-10

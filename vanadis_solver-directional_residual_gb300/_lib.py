@@ -78,6 +78,7 @@ SIGNATURES = {
     "vdr_assemble_rhs_block_device": (_i, [_P, _i, _P, _d, _P]),
     "vdr_set_block_apply": (_i, [_P, _i]),
     "vdr_diag_wait_timeout": (_i, [_P]),
+    "vdr_diag_barrier_timeout": (_i, [_P]),
     "vdr_set_mixed_operator": (_i, [_P, _i]),
     "vdr_apply_half_device": (_i, [_P, _P, _P]),
     "vdr_apply_block_device": (_i, [_P, _i, _P, _P, _i]),

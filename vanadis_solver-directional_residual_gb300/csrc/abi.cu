@@ -958,6 +958,12 @@ int vdr_diag_wait_timeout(vdr_handle *H) {
   return diag_wait_timeout(H->h);
 }
 
+int vdr_diag_barrier_timeout(vdr_handle *H) {
+  int st = check_handle(H);
+  if (st) return st;
+  return diag_barrier_timeout(H->h);
+}
+
 int vdr_set_block_apply(vdr_handle *H, int variant) {
   int st = check_handle(H);
   if (st) return st;

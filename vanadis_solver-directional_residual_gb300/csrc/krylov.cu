@@ -914,7 +914,7 @@ __global__ void __launch_bounds__(RED_THREADS) b32_xr(Vec32 a) {
 // VDR_TIMEOUT (reason 7) and returns.
 constexpr long long BAR_LIMIT = 2000000000LL;  // ~1 s of clocks
 
-__device__ bool grid_barrier(KState *st) {
+__device__ bool grid_barrier(KState *st, long long limit = BAR_LIMIT) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -929,7 +929,7 @@ __device__ bool grid_barrier(KState *st) {
     } else {
       const long long t0 = clock64();
       while (*gen == g0) {
-        if (clock64() - t0 > BAR_LIMIT) {
+        if (clock64() - t0 > limit) {
           ok = false;
           break;
         }
@@ -949,6 +949,14 @@ __device__ void barrier_timeout(KState *st) {
     st->reason = 7;
     st->done = 1;
   }
+}
+
+// The barrier's failure path on its own: block 1 of a two-block cooperative
+// launch returns at once and never arrives, block 0 waits with a short
+// limit, gives up and marks the state VDR_TIMEOUT.
+__global__ void barrier_timeout_kernel(KState *st, long long limit) {
+  if (blockIdx.x != 0) return;
+  if (!grid_barrier(st, limit)) barrier_timeout(st);
 }
 
 // This block's sums of NQ quantities into partials[q * gridDim.x + block].
@@ -1241,6 +1249,41 @@ cudaError_t launch_iteration32(Handle &h, const Vec32 &a) {
   return cudaGetLastError();
 }
 
+}  // namespace
+
+// The fused kernels' barrier timeout, end to end: VDR_TIMEOUT when the wait
+// that nothing completes ran out of its (about 1 ms) budget and the state
+// said so; the handle stays usable (the next solve resets the state).
+int diag_barrier_timeout(Handle &h) {
+  cudaError_t e = ensure_solver_workspace(h, 8);
+  if (e) return cuda_fail(e, "diag");
+  cudaStream_t s = h.stream;
+  if ((e = cudaMemsetAsync(h.st, 0, sizeof(KState), s))) return cuda_fail(e, "diag");
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(2);
+  cfg.blockDim = dim3(32);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if ((e = cudaLaunchKernelEx(&cfg, barrier_timeout_kernel, h.st, 2000000LL)))
+    return cuda_fail(e, "diag launch");
+  count_launches(1);
+  KState fin;
+  if ((e = cudaMemcpyAsync(&fin, h.st, sizeof(KState), cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaStreamSynchronize(s)))
+    return cuda_fail(e, "diag");
+  if (fin.done && fin.status == VDR_TIMEOUT && fin.reason == 7) {
+    set_error("diag: the grid barrier's wait ran out (as intended)");
+    return VDR_TIMEOUT;
+  }
+  set_error("diag: the grid barrier did not report its timeout");
+  return VDR_CUDA_ERROR;
+}
+
+namespace {
 // Inner solve A32 x32 = b32 (FP32 vectors in work32, x32 from zero) to `tol`
 // relative residual; graph-captured like solve_device.
 int solve32_inner(Handle &h, double tol, int itmax, int *iter, double *err) {

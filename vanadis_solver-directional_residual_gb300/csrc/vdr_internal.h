@@ -331,6 +331,8 @@ cudaError_t launch_apply_both(const Handle &h, const double *x1, double *y1,
 // Runs a one-warp mbarrier wait that nothing completes with a short budget:
 // VDR_TIMEOUT when the bound tripped and was reported (block.cu).
 int diag_wait_timeout(Handle &h);
+// The same for the grid barrier of the fused inner kernels (krylov.cu).
+int diag_barrier_timeout(Handle &h);
 // The FP32 operator (A32v) on FP32 vectors, y += A x (stored mode only).
 cudaError_t launch_stored_apply32v(const Handle &h, const float *x, float *y,
                                    const int *skip, const int *skip2,
