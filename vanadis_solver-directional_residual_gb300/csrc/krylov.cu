@@ -451,11 +451,16 @@ Vec make_vec(Handle &h, const double *b, double *x) {
   return a;
 }
 
+// The fused FP64 BiCGStab iteration (defined below with the fused kernels).
+cudaError_t launch_fused64_iteration(Handle &h, const Vec &a, cudaStream_t s);
+
 cudaError_t launch_iteration(Handle &h, int method, const Vec &a,
                              const Precond *prec) {
   const int g = red_grid(h.N);
   cudaStream_t s = h.stream;
   cudaError_t e;
+  if (method == VDR_SOLVER_BICGSTAB && !prec && h.fused64)
+    return launch_fused64_iteration(h, a, s);
   if (method == VDR_SOLVER_BICGSTAB) {
     bs_p<<<g, RED_THREADS, 0, s>>>(a);
     if (prec && (e = prec->enqueue(prec->ctx, a.p, a.ph, &h.st->done, nullptr, s)))
@@ -515,6 +520,7 @@ cudaError_t ensure_solver_workspace(Handle &h, int nvec) {
 
 // Kernels of one captured iteration.
 long launches_graph_nodes(Handle &h, int method, const Precond *prec) {
+  if (method == VDR_SOLVER_BICGSTAB && !prec && h.fused64) return 2 + 2 * apply_launches(h);
   long n = (method == VDR_SOLVER_BICGSTAB ? 5 : 3) +
            (method != VDR_SOLVER_BICGSTAB && can_apply_both(h) ? 1 : 2) *
                apply_launches(h);
@@ -585,8 +591,12 @@ int solve_device(Handle &h, int method, const double *b, double *x,
   // graph captured for other sizes (buffers reused by a smaller mesh) is
   // captured again
   const long long size_key = ((long long)h.N << 32) | (unsigned)h.E;
-  if (!h.graph_exec[slot] || h.graph_key[slot] != key ||
-      h.graph_size[slot] != size_key) {
+  const bool fusable = method == VDR_SOLVER_BICGSTAB && !prec;
+  for (int attempt = 0; attempt < 2; attempt++) {
+    const bool fused = fusable && h.fused64;
+    const void *fkey = (const void *)((uintptr_t)key ^ ((uintptr_t)fused << 20));
+    if (h.graph_exec[slot] && h.graph_key[slot] == fkey && h.graph_size[slot] == size_key)
+      break;
     if (h.graph_exec[slot]) cudaGraphExecDestroy(h.graph_exec[slot]);
     h.graph_exec[slot] = nullptr;
     cudaGraph_t graph;
@@ -599,13 +609,33 @@ int solve_device(Handle &h, int method, const double *b, double *x,
     }
     count_launches(before - launches_so_far());  // captured, not launched
     cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (!e && !e2) {
+      e = cudaGraphInstantiate(&h.graph_exec[slot], graph, 0);
+      cudaGraphDestroy(graph);
+      if (!e) {
+        h.graph_key[slot] = fkey;
+        h.graph_size[slot] = size_key;
+        break;
+      }
+      h.graph_exec[slot] = nullptr;
+    } else if (!e2) {
+      cudaGraphDestroy(graph);
+    }
+    // a cooperative launch that the capture or the graph refuses: the
+    // five-kernel iteration instead
+    if (fused) {
+      cudaGetLastError();
+      h.fused64 = false;
+      e = cudaSuccess;
+      continue;
+    }
     if (e) return cuda_fail(e, "capture");
-    if (e2) return cuda_fail(e2, "end capture");
-    e = cudaGraphInstantiate(&h.graph_exec[slot], graph, 0);
-    cudaGraphDestroy(graph);
-    if (e) return cuda_fail(e, "graph instantiate");
-    h.graph_key[slot] = key;
-    h.graph_size[slot] = size_key;
+    return cuda_fail(e2 ? e2 : cudaErrorUnknown, "end capture");
+  }
+  if (fusable && h.fused64) {  // the first search direction p = r, p^ = D^-1 r, v = 0
+    bs_p<<<g, RED_THREADS, 0, s>>>(a);
+    count_launches(1);
+    if ((e = cudaGetLastError())) return cuda_fail(e, "first direction");
   }
   const long graph_nodes = launches_graph_nodes(h, method, prec);
 
@@ -1171,6 +1201,204 @@ cudaError_t launch_cooperative(Kern kern, int grid, const Vec32 &a, cudaStream_t
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, kern, a);
+}
+
+// The FP64 Jacobi-BiCGStab iteration in the same two-kernel form (right
+// preconditioned: p^ = D^-1 p and s^ = D^-1 s, zero on Dirichlet nodes, are
+// the applies' inputs): apply(p^ -> v), fused alpha + s + s^, apply(s^ ->
+// t), fused omega + x, r + next p + p^.
+__global__ void __launch_bounds__(RED_THREADS, 2) bsf_alpha_s(Vec a) {
+  KState *st = a.st;
+  if (st->done) return;
+  double *pa = a.partials, *pb = a.partials + MAXQ * gridDim.x;
+  const double rho = st->rho;
+  {
+    double v[1] = {0.0};
+    double hv[U], vv[U];
+    VLOOP(hv[u] = ok ? a.rh[i] : 0.0; vv[u] = ok ? a.v[i] : 0.0;, v[0] += hv[u] * vv[u];)
+    put_partials<1>(v, pa);
+  }
+  if (!grid_barrier(st)) {
+    barrier_timeout(st);
+    return;
+  }
+  double o[1];
+  all_sum<1>(pa, o);
+  if (o[0] == 0.0 || !finite(o[0])) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->status = VDR_BREAKDOWN;
+      st->reason = 2;
+      st->done = 1;
+    }
+    return;
+  }
+  const double al = rho / o[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->alpha = al;
+  double v[1] = {0.0};
+  double rv[U], vv[U], dv[U];
+  unsigned char mv[U];
+  VLOOP(rv[u] = ok ? a.r[i] : 0.0; vv[u] = ok ? a.v[i] : 0.0;
+        dv[u] = ok ? a.dinv[i] : 0.0; mv[u] = ok ? a.m[i] : 1;,
+        const double si = rv[u] - al * vv[u];
+        a.s[i] = si;
+        a.sh[i] = mv[u] ? 0.0 : si * dv[u];
+        a.t[i] = 0.0;
+        v[0] += si * si;)
+  double o2[1];
+  if (grid_sum<1>(v, pb, &st->ticket, o2)) {
+    st->snrm = sqrt(o2[0]) / sqrt(st->bnrm2);
+    if (st->snrm <= st->tol) st->sconv = 1;
+  }
+}
+
+__global__ void __launch_bounds__(RED_THREADS, 2) bsf_omega_xr_p(Vec a) {
+  KState *st = a.st;
+  if (st->done) return;
+  const double al = st->alpha;
+  if (st->sconv) {  // s met the tolerance: x += alpha p^, r = s
+    double xv[U], pv[U], sv[U];
+    VLOOP(xv[u] = ok ? a.x[i] : 0.0; pv[u] = ok ? a.ph[i] : 0.0;
+          sv[u] = ok ? a.s[i] : 0.0;,
+          a.x[i] = xv[u] + al * pv[u];
+          a.r[i] = sv[u];)
+    double v[1] = {0.0};
+    double o[1];
+    if (grid_sum<1>(v, a.partials, &st->ticket, o)) {
+      st->iter += 1;
+      st->err = st->snrm;
+      st->status = VDR_OK;
+      st->done = 1;
+    }
+    return;
+  }
+  double *pa = a.partials, *pb = a.partials + MAXQ * gridDim.x;
+  // everything read from KState before block 0 writes it
+  const double rho0 = st->rho, bnrm2 = st->bnrm2, tol = st->tol, best0 = st->best_err;
+  const int iter0 = st->iter, itmax = st->itmax, window = st->stall_window,
+            since0 = st->since_best;
+  {
+    double v[2] = {0.0, 0.0};
+    double tv[U], sv[U];
+    VLOOP(tv[u] = ok ? a.t[i] : 0.0; sv[u] = ok ? a.s[i] : 0.0;,
+          v[0] += tv[u] * sv[u];
+          v[1] += tv[u] * tv[u];)
+    put_partials<2>(v, pa);
+  }
+  if (!grid_barrier(st)) {
+    barrier_timeout(st);
+    return;
+  }
+  double o[2];
+  all_sum<2>(pa, o);
+  if (o[1] == 0.0 || !finite(o[1]) || !finite(o[0])) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->status = VDR_BREAKDOWN;
+      st->reason = 3;
+      st->done = 1;
+    }
+    return;
+  }
+  const double om = o[0] / o[1];
+  {
+    double v[2] = {0.0, 0.0};
+    double xv[U], pv[U], shv[U], sv[U], tv[U], hv[U];
+    VLOOP(xv[u] = ok ? a.x[i] : 0.0; pv[u] = ok ? a.ph[i] : 0.0;
+          shv[u] = ok ? a.sh[i] : 0.0; sv[u] = ok ? a.s[i] : 0.0;
+          tv[u] = ok ? a.t[i] : 0.0; hv[u] = ok ? a.rh[i] : 0.0;,
+          a.x[i] = xv[u] + al * pv[u] + om * shv[u];
+          const double ri = sv[u] - om * tv[u];
+          a.r[i] = ri;
+          v[0] += ri * ri;
+          v[1] += hv[u] * ri;)
+    put_partials<2>(v, pb);
+  }
+  if (!grid_barrier(st)) {
+    barrier_timeout(st);
+    return;
+  }
+  double o2[2];
+  all_sum<2>(pb, o2);
+  // the convergence decision, identical in every block
+  const double err = sqrt(o2[0]) / sqrt(bnrm2);
+  const int iter = iter0 + 1;
+  int status = VDR_NOT_CONVERGED, reason = 0;
+  bool done = true;
+  double best = best0;
+  int since = since0;
+  if (!(err == err) || !finite(o2[1])) {
+    status = VDR_BREAKDOWN;
+    reason = 5;
+  } else if (err <= tol) {
+    status = VDR_OK;
+  } else if (o2[1] == 0.0 || om == 0.0) {
+    status = VDR_BREAKDOWN;
+    reason = o2[1] == 0.0 ? 1 : 4;
+  } else if (iter >= itmax) {
+    status = VDR_NOT_CONVERGED;
+  } else {
+    done = false;
+    if (window > 0) {
+      if (err < 0.99 * best) {
+        best = err;
+        since = 0;
+      } else if (++since >= window) {
+        status = VDR_NOT_CONVERGED;
+        reason = 6;  // stalled
+        done = true;
+      }
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->omega = om;
+    st->iter = iter;
+    st->rho_old = rho0;
+    st->rho = o2[1];
+    st->err = err;
+    st->best_err = best;
+    st->since_best = since;
+    if (done) {
+      st->status = status;
+      if (reason) st->reason = reason;
+      st->done = 1;
+    }
+  }
+  if (done) return;
+  // the next iteration's search direction and its Jacobi image
+  const double beta = (o2[1] / rho0) * (al / om);
+  double rv[U], pv[U], vv[U], dv[U];
+  unsigned char mv[U];
+  VLOOP(rv[u] = ok ? a.r[i] : 0.0; pv[u] = ok ? a.p[i] : 0.0; vv[u] = ok ? a.v[i] : 0.0;
+        dv[u] = ok ? a.dinv[i] : 0.0; mv[u] = ok ? a.m[i] : 1;,
+        const double pi = rv[u] + beta * (pv[u] - om * vv[u]);
+        a.p[i] = pi;
+        a.ph[i] = mv[u] ? 0.0 : pi * dv[u];
+        a.v[i] = 0.0;)
+}
+
+template <typename Kern>
+cudaError_t launch_cooperative64(Kern kern, int grid, const Vec &a, cudaStream_t s) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(RED_THREADS);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, a);
+}
+std::atomic<int> g_occ_bsf_alpha_s{0}, g_occ_bsf_omega_xr_p{0};
+
+cudaError_t launch_fused64_iteration(Handle &h, const Vec &a, cudaStream_t s) {
+  cudaError_t e;
+  if ((e = launch_apply(h, false, a.ph, a.v, &h.st->done, nullptr, s))) return e;
+  if ((e = launch_cooperative64(bsf_alpha_s, fused_grid(bsf_alpha_s, g_occ_bsf_alpha_s, h.N),
+                                a, s)))
+    return e;
+  if ((e = launch_apply(h, false, a.sh, a.t, &h.st->done, &h.st->sconv, s))) return e;
+  return launch_cooperative64(bsf_omega_xr_p,
+                              fused_grid(bsf_omega_xr_p, g_occ_bsf_omega_xr_p, h.N), a, s);
 }
 
 // b32 = (float)(r * scale); dinv32 = (float)dinv (when dinv32 is given).

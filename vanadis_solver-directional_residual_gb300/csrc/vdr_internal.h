@@ -199,9 +199,10 @@ struct Handle {
   float *work32 = nullptr;
   cudaGraphExec_t graph32 = nullptr;
   const void *graph32_key = nullptr;
-  // the FP32 inner iteration with the binary16 operator as two fused
-  // cooperative vector kernels (krylov.cu); off after a failed capture
-  bool fused32 = true;
+  // the FP32 inner iteration with the binary16 operator, and the FP64
+  // Jacobi-BiCGStab iteration, as two fused cooperative vector kernels each
+  // (krylov.cu); off after a failed capture
+  bool fused32 = true, fused64 = true;
   KState *st = nullptr;
   KState *h_st = nullptr;  // pinned mirror
   double *partials = nullptr;
