@@ -1,6 +1,6 @@
 """CPU oracle for the Vanadis EBE HEX8 directional-residual solve.
 
-TEST INFRASTRUCTURE ONLY.  This package is the checker: the test suite, the
+TEST INFRASTRUCTURE ONLY.  This package is the oracle: the test suite, the
 smoke check and the CPU-baseline leg of the benchmark import it; the product
 library (``libvdr.so`` and its Python host module) never does.  The numerics
 live in ``vdr_oracle.c`` (a plain-C restatement of the reference's CPU build

@@ -1,6 +1,6 @@
 """CPU restatement of the reference's text outputs of a time step.
 
-TEST INFRASTRUCTURE ONLY: the checker of the library's text writers
+TEST INFRASTRUCTURE ONLY: the oracle of the library's text writers
 (``vdr_write_result_txt``, ``vdr_write_slices_txt``); the product never
 imports it.
 

@@ -2,7 +2,8 @@
  * vdr_oracle.h -- CPU oracle for the Vanadis EBE HEX8 directional-residual
  * (DR) solve.  TEST INFRASTRUCTURE ONLY: the product library never links,
  * loads or calls anything declared here.  Only the test suite, the smoke
- * check and the CPU-baseline leg of the benchmark use it, as the checker.
+ * check and the CPU-baseline leg of the benchmark use it, to check the
+ * product against.
  *
  * Every function restates, from its mathematics, one routine of the
  * reference Fortran CPU build `src_updates/vanadis_full_DR_OpenMP_timing.for`

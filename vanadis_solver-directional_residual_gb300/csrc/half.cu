@@ -2,7 +2,7 @@
 //
 // The refinement loop of vdr_solve_mixed_device solves each correction
 // A d = r approximately; its operator only has to be good to a few digits
-// (the FP64 residual of the outer loop is the judge).  This store keeps the
+// (the FP64 residual of the outer loop decides).  This store keeps the
 // Jacobi-scaled, Dirichlet-projected operator
 //
 //     A^ = P A P D^-1     (D = the assembled diagonal, 1 on Dirichlet nodes)
