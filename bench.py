@@ -67,10 +67,13 @@ def args_parse(argv=None):
     ap.add_argument("--learn-steps", type=int, default=LEARN_STEPS)
     ap.add_argument("--learn-epochs", type=int, default=1)
     ap.add_argument("--case", default=None,
-                    choices=["apply", "block_apply", "block_apply_tc", "bicg", "mixed",
+                    choices=["build", "apply", "block_apply", "block_apply_tc", "bicg", "mixed",
                              "unet_train", "unet_forward"],
                     help="run one small fixed workload for a profiler "
                          "capture instead of the benchmark")
+    ap.add_argument("--build-mode", default="auto", choices=["auto", "recompute"],
+                    help="element geometry of --case build: the mesh's "
+                         "geometric factors or the Jacobians at every build")
     ap.add_argument("--cpu-iters", type=int, default=4,
                     help="BiCGStab iterations timed in the CPU sample")
     return ap.parse_args(argv)
@@ -917,6 +920,29 @@ def run_native(a):
     build_issue = (inst_per_elem * E / (t_build * 1e-3) / 1e9
                    if inst_per_elem else None)
 
+    # ---- the build that evaluates the Jacobians from the coordinates at
+    # every step (no geometric factors), and the one-time cost of forming
+    # the factors (the first build after they were dropped) ----
+    geo_state, geo_bytes = s.geometry_status()
+    s.set_build_mode("recompute")
+    t_build_rc_s, _, _, _ = timed_steps(s, stream, b, x, aH, aM, cf, rM, lambda: None)
+    s.set_build_mode("auto")   # the factors were freed: the next build forms them
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.set_operator(aH, aM)
+    g0.record(stream)
+    s.assemble_rhs_device(b, cf, rM, None)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    build_modes = {
+        "geometric_factors_ms": t_build, "recompute_ms": t_build_rc_s * 1e3,
+        "first_build_with_factor_setup_ms": g0.elapsed_time(g1),
+        "geometry_bytes": geo_bytes, "geometry_state": geo_state,
+        "what": "element build + diag + RHS per step: from the mesh's "
+                "geometric factors (J^-1, detJ per Gauss point and the "
+                "unit-diffusivity stiffness, formed once per handle; the "
+                "headline step) vs evaluating the Jacobians from the "
+                "coordinates at every step"}
+
     # ---- the same step with the pure FP64 element-matrix store ----
     s64 = vdr.Solver(prob, vdr.Options(apply_mode="stored",
                                        matrix_storage="fp64",
@@ -1125,6 +1151,7 @@ def run_native(a):
                                             "per clock at the median SM "
                                             "clock of the timed region" % n_sm,
                                "instructions_from": "profiles/" + BUILD_PROFILE},
+            "build_modes": build_modes,
             "fp64_store": fp64_store,
             "apply_tuning": tuning,
             "scatter_variants": scatter_variants,
@@ -1199,6 +1226,8 @@ def summary_keys(line, step_s, solve_s):
         "apply_per_sm": g(line, "apply_tuning", "apply_blocks_per_sm"),
         "half_per_sm": g(line, "apply_tuning", "half_blocks_per_sm"),
         "build_ms": _r(g(line, "breakdown_ms", "element_matrices_and_rhs")),
+        "build_recompute_ms": _r(g(line, "build_modes", "recompute_ms")),
+        "build_first_ms": _r(g(line, "build_modes", "first_build_with_factor_setup_ms")),
         "time_loop_later_s": _r(g(line, "time_loop", "later_step_s")),
         "time_loop_mixed_later_s": _r(g(line, "time_loop", "mixed", "later_step_s")),
     }
@@ -1220,7 +1249,16 @@ def run_case(a):
     P = vdr.problems
     prob = P.rotation_shear(a.nex, a.ney, a.nez, seed=1002)
     dt = COURANT / max(a.nex, a.ney, a.nez)
-    if a.case == "apply":
+    if a.case == "build":
+        # element build + diag + RHS, as in the theta step (three builds)
+        s = vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=2.0, aM=3.0 / dt)
+        s.set_build_mode(a.build_mode)
+        b = torch.zeros(prob.mesh.nnode, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for _ in range(3):
+            s.set_operator(2.0, 3.0 / dt)
+            s.assemble_rhs_device(b, 3.0, 3.0 / dt, None)
+    elif a.case == "apply":
         s = vdr.Solver(prob, vdr.Options(apply_mode="stored"), aH=2.0, aM=3.0 / dt)
         x = torch.randn(prob.mesh.nnode, dtype=torch.float64, device="cuda")
         y = torch.zeros_like(x)

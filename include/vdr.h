@@ -135,6 +135,25 @@ int vdr_set_dirichlet(vdr_handle *h, const int *bc);
  * reference's theta-scheme: (2, 3/dt) (przest3d, :691-716). */
 int vdr_set_operator(vdr_handle *h, double aH, double aM);
 
+/* How the element build (el3d's per-element loop, vanadis_full_DR_OpenMP_
+ * timing.for:431-610) gets the element geometry.  AUTO: the mesh's
+ * geometric factors -- J^-1 and detJ at the 8 Gauss points and the
+ * unit-diffusivity stiffness int gradN_i . gradN_j, 928 bytes per element --
+ * are formed on the GPU once per handle (at the first build; a handle's
+ * coordinates never change) and every later build forms the element
+ * matrices from them and the current fields.  RECOMPUTE: every build
+ * evaluates the Jacobians from the coordinates.  AUTO falls back to
+ * RECOMPUTE where there is no device memory for the factors, where a factor
+ * lies outside the double-float window, and for Robin elements with a
+ * nonzero Robin coefficient.  Results agree to double-float rounding
+ * (~1e-15 relative).  Setting the mode marks the operator stale. */
+#define VDR_BUILD_AUTO 0
+#define VDR_BUILD_RECOMPUTE 1
+int vdr_set_build_mode(vdr_handle *h, int mode);
+/* *cached = 1 when the geometric factors are held (bytes of device memory
+ * in *bytes), 0 when not (yet) formed, -1 when they cannot be used. */
+int vdr_geometry_status(vdr_handle *h, int *cached, long long *bytes);
+
 /* y = P A P x (transpose = 0) or y = P A^T P x, host arrays of length N. */
 int vdr_apply(vdr_handle *h, const double *x, double *y, int transpose);
 int vdr_apply_device(vdr_handle *h, const double *d_x, double *d_y,

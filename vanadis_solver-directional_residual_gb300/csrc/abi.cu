@@ -118,6 +118,51 @@ int check_handle(vdr_handle *H) {
   return VDR_OK;
 }
 
+void free_geometry(Handle &h) {
+  dfree(h.geo.Ji);
+  dfree(h.geo.Dj);
+  dfree(h.geo.K);
+  h.geo = GeoFactors{};
+}
+
+// The mesh's geometric factors for the double-float build, formed at the
+// first build that can use them (h.flag allocated).  *use = false where the
+// build evaluates the Jacobians itself: VDR_BUILD_RECOMPUTE, no device memory
+// for the factors, a factor outside the pair window.
+int ensure_geometry(Handle &h, bool *use) {
+  *use = false;
+  if (h.build_mode == VDR_BUILD_RECOMPUTE || h.geo_state < 0) return VDR_OK;
+  if (h.geo_state > 0) {
+    *use = true;
+    return VDR_OK;
+  }
+  const size_t E = (size_t)std::max(h.E, 1);
+  if (cudaMalloc(&h.geo.Ji, sizeof(float2) * 72 * E) ||
+      cudaMalloc(&h.geo.Dj, sizeof(float2) * 8 * E) ||
+      cudaMalloc(&h.geo.K, sizeof(float2) * 36 * E)) {
+    cudaGetLastError();  // no room for them: not an error
+    free_geometry(h);
+    h.geo_state = -1;
+    return VDR_OK;
+  }
+  cudaError_t e;
+  int bad = 0;
+  if ((e = cudaMemsetAsync(h.flag, 0, sizeof(int), h.stream)) ||
+      (e = launch_geo_factors(op_args(h), h.geo, h.flag, h.stream)) ||
+      (e = cudaMemcpyAsync(&bad, h.flag, sizeof(int), cudaMemcpyDeviceToHost,
+                           h.stream)) ||
+      (e = cudaStreamSynchronize(h.stream)))
+    return cuda_fail(e, "geometric factors");
+  if (bad) {
+    free_geometry(h);
+    h.geo_state = -1;
+    return VDR_OK;
+  }
+  h.geo_state = 1;
+  *use = true;
+  return VDR_OK;
+}
+
 // Builds the stored element matrices and the Jacobi diagonal if they are
 // stale; when `rhs` is given, the right-hand side is assembled in the same
 // element pass (or alone, if the operator is already valid).
@@ -178,6 +223,18 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
       if (h.want_phi) {
         if ((e = dalloc(&h.phi, (size_t)h.E * 8))) return cuda_fail(e, "alloc phi");
         ba.phi = h.phi;
+      }
+    }
+    // from the mesh's geometric factors unless the rows are FP64 or a
+    // Robin term is on
+    if (!h.exact_build && !(h.robin && h.robin_alpha != 0.0)) {
+      bool geo = false;
+      const int gst = ensure_geometry(h, &geo);
+      if (gst) return gst;
+      if (geo) {
+        ba.gJi = h.geo.Ji;
+        ba.gDj = h.geo.Dj;
+        ba.gK = h.geo.K;
       }
     }
     if ((e = cudaMemsetAsync(h.flag, 0, sizeof(int), h.stream)))
@@ -336,6 +393,7 @@ void free_handle(Handle &h) {
   if (h.bk_graph) cudaGraphExecDestroy(h.bk_graph);
   dfree(h.gcr_work); dfree(h.stage_d); dfree(h.drs); dfree(h.work32);
   dfree(h.Mhi); dfree(h.Mlo); dfree(h.Fvec); dfree(h.rhs_tmp); dfree(h.massw);
+  free_geometry(h);
   if (h.graph32) cudaGraphExecDestroy(h.graph32);
   if (h.gcr_graph) cudaGraphExecDestroy(h.gcr_graph);
   dfree(h.seg_d); dfree(h.seg_i); dfree(h.seg_ticket); dfree(h.seg_of_elem);
@@ -934,6 +992,35 @@ int vdr_apply_block_accumulate_device(vdr_handle *H, int K, const void *X,
                                       void *Y, int precision) {
   return apply_block(H, K, X, Y, precision, false,
                      "vdr_apply_block_accumulate_device");
+}
+
+int vdr_set_build_mode(vdr_handle *H, int mode) {
+  int st = check_handle(H);
+  if (st) return st;
+  if (mode != VDR_BUILD_AUTO && mode != VDR_BUILD_RECOMPUTE) {
+    set_error("vdr_set_build_mode: unknown mode");
+    return VDR_BAD_ARGUMENT;
+  }
+  Handle &h = H->h;
+  if (h.build_mode != mode) {
+    h.build_mode = mode;
+    if (mode == VDR_BUILD_RECOMPUTE) {
+      free_geometry(h);
+      if (h.geo_state > 0) h.geo_state = 0;
+    }
+    invalidate(h);
+  }
+  return VDR_OK;
+}
+
+int vdr_geometry_status(vdr_handle *H, int *cached, long long *bytes) {
+  int st = check_handle(H);
+  if (st) return st;
+  const Handle &h = H->h;
+  if (cached) *cached = h.geo_state;
+  if (bytes)
+    *bytes = h.geo_state > 0 ? (long long)sizeof(float2) * GEO_PAIRS * h.E : 0;
+  return VDR_OK;
 }
 
 int vdr_set_mixed_operator(vdr_handle *H, int mode) {

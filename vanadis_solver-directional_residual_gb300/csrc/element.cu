@@ -400,22 +400,12 @@ __global__ void __launch_bounds__(256) elem_dr_scalars_kernel(OpArgs a,
 //     and node instead of 5, one accumulator row instead of two).
 // Any value outside the pairs' safe window sets bit 2 of the flag and the
 // host redoes the build with FP64 rows (elem_build_kernel<double>).
-struct BuildSmemDF {
-  Df2 g[ROWS_EPB][8][5][8];  // per element, point q, node j: dNj/dx, dNj/dy,
-                             // dNj/dz, v.gradNj + P Nj, Wj
-  Df2 d[ROWS_EPB][8][2];     // detJ, lambda*detJ
-  Df2 fw[ROWS_EPB][4][8];    // face-3 points: W
-  Df2 fd[ROWS_EPB][4];       // alpha*detJs
-  Df2 rel[ROWS_EPB][24];     // node k's (x, y, z) - node 1's at [3k..3k+2]
-  Df2 told[ROWS_EPB][8];     // T_old at the nodes times 2^-shift
-  Df2 tab[8][4][8];          // N, dN/dxi, dN/deta, dN/dzeta at the 8 points
-  Df2 ftab[4][8];            // N at the 4 face-3 points
-};
-
-template <bool SPLIT>
-__global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArgs ba) {
-  __shared__ BuildSmemDF sm;
-  for (int t = threadIdx.x; t < 12; t += blockDim.x) {
+// The shape tables of the double-float kernels: N and its reference
+// derivatives at the 8 Gauss points and, when ftab is given, N at the 4
+// face-3 points; once per block, ending with __syncthreads.
+__device__ __forceinline__ void fill_df_tables(Df2 (&tab)[8][4][8], Df2 (*ftab)[8]) {
+  const int npts = ftab ? 12 : 8;
+  for (int t = threadIdx.x; t < npts; t += blockDim.x) {
     double xi, eta, zeta;
     if (t < 8) {
       xi = gauss_coord<double>(t, 0);
@@ -431,18 +421,229 @@ __global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArg
     shape_at<double>(xi, eta, zeta, n, d0, d1, d2);
     if (t >= 8) {
 #pragma unroll
-      for (int i = 0; i < 8; i++) sm.ftab[t - 8][i] = df_from_double(n[i]);
+      for (int i = 0; i < 8; i++) ftab[t - 8][i] = df_from_double(n[i]);
       continue;
     }
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-      sm.tab[t][0][i] = df_from_double(n[i]);
-      sm.tab[t][1][i] = df_from_double(d0[i]);
-      sm.tab[t][2][i] = df_from_double(d1[i]);
-      sm.tab[t][3][i] = df_from_double(d2[i]);
+      tab[t][0][i] = df_from_double(n[i]);
+      tab[t][1][i] = df_from_double(d0[i]);
+      tab[t][2][i] = df_from_double(d1[i]);
+      tab[t][3][i] = df_from_double(d2[i]);
     }
   }
   __syncthreads();
+}
+
+// One Gauss point in double-float: J from the element's node coordinates
+// relative to local node 1 (rel[3k..3k+2], node 1 itself at the origin) and
+// the reference derivatives t0..t2 of the 8 shape functions at the point;
+// returns detJ as a pair, detj as FP64 and di[3a+b] = (J^-1)_{ab} =
+// d xi_a / d x_b.  A detJ outside 2^-60..2^60 (zero, inf and NaN included)
+// sets range_bad.
+__device__ __forceinline__ Df2 df_inverse_jacobian(const Df2 *rel, const Df2 *t0,
+                                                   const Df2 *t1, const Df2 *t2,
+                                                   Df2 (&di)[9], double &detj,
+                                                   bool &range_bad) {
+  DfAcc J[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) J[k] = DfAcc{0.0f, 0.0f};
+#pragma unroll 1
+  for (int k = 1; k < 8; k++) {  // local node 1 is the origin
+    const Df2 rx = rel[3 * k], ry = rel[3 * k + 1], rz = rel[3 * k + 2];
+    df_acc(J[0], rx, t0[k]);
+    df_acc(J[1], rx, t1[k]);
+    df_acc(J[2], rx, t2[k]);
+    df_acc(J[3], ry, t0[k]);
+    df_acc(J[4], ry, t1[k]);
+    df_acc(J[5], ry, t2[k]);
+    df_acc(J[6], rz, t0[k]);
+    df_acc(J[7], rz, t1[k]);
+    df_acc(J[8], rz, t2[k]);
+  }
+  const Df2 j11 = df_norm(J[0]), j12 = df_norm(J[1]), j13 = df_norm(J[2]);
+  const Df2 j21 = df_norm(J[3]), j22 = df_norm(J[4]), j23 = df_norm(J[5]);
+  const Df2 j31 = df_norm(J[6]), j32 = df_norm(J[7]), j33 = df_norm(J[8]);
+  const Df2 c11 = df_sub(df_mul(j22, j33), df_mul(j23, j32));
+  const Df2 c12 = df_sub(df_mul(j21, j33), df_mul(j23, j31));
+  const Df2 c13 = df_sub(df_mul(j21, j32), df_mul(j22, j31));
+  const Df2 detp =
+      df_add(df_sub(df_mul(j11, c11), df_mul(j12, c12)), df_mul(j13, c13));
+  detj = df_to_double(detp.h, detp.l);
+  {
+    const int ed = df_exp(detj);  // zero, subnormal, inf, NaN included
+    if (ed < 1023 - 60 || ed > 1023 + 60) range_bad = true;
+  }
+  const Df2 r = df_rcp(detp);
+  di[0] = df_mul(r, c11);
+  di[1] = df_mul(r, df_sub(df_mul(j13, j32), df_mul(j12, j33)));
+  di[2] = df_mul(r, df_sub(df_mul(j12, j23), df_mul(j13, j22)));
+  di[3] = df_neg(df_mul(r, c12));
+  di[4] = df_mul(r, df_sub(df_mul(j11, j33), df_mul(j13, j31)));
+  di[5] = df_mul(r, df_sub(df_mul(j13, j21), df_mul(j11, j23)));
+  di[6] = df_mul(r, c13);
+  di[7] = df_mul(r, df_sub(df_mul(j12, j31), df_mul(j11, j32)));
+  di[8] = df_mul(r, df_sub(df_mul(j11, j22), df_mul(j12, j21)));
+  return detp;
+}
+
+// The streamline parameter tau at one Gauss point of the double-float
+// builds, di = J^-1 at the point: OT from the per-element value; GP and VF
+// from h = 2/|J^-1 e| (zero for |J^-1 e| <= 1e-14), Pe = h kpe and
+// tau = h khalf beta(Pe) with the element's scalars of
+// elem_dr_scalars_kernel.
+__device__ __forceinline__ double df_point_tau(const OpArgs &a, const double *drs, long p,
+                                               const Df2 (&di)[9]) {
+  const long E = a.E;
+  if (a.variant == DR_OT) return __ldg(drs + p);
+  const Df2 exd = df_from_double(__ldg(drs + p));
+  const Df2 eyd = df_from_double(__ldg(drs + E + p));
+  const Df2 ezd = df_from_double(__ldg(drs + 2 * E + p));
+  DfAcc gxa{0.0f, 0.0f}, gya{0.0f, 0.0f}, gza{0.0f, 0.0f};
+  df_acc(gxa, di[0], exd);
+  df_acc(gxa, di[1], eyd);
+  df_acc(gxa, di[2], ezd);
+  df_acc(gya, di[3], exd);
+  df_acc(gya, di[4], eyd);
+  df_acc(gya, di[5], ezd);
+  df_acc(gza, di[6], exd);
+  df_acc(gza, di[7], eyd);
+  df_acc(gza, di[8], ezd);
+  const Df2 gx = df_norm(gxa), gy = df_norm(gya), gz = df_norm(gza);
+  DfAcc n2{0.0f, 0.0f};
+  df_acc(n2, gx, gx);
+  df_acc(n2, gy, gy);
+  df_acc(n2, gz, gz);
+  const double gn2 = df_to_double(n2.s, n2.c);
+  const double h = (gn2 > 1.0e-28) ? 2.0 * rsqrt(gn2) : 0.0;
+  const double pe = h * __ldg(drs + 3 * E + p);
+  double tau = 0.0;
+  if (pe > 1.0e-12) {
+    const double beta = (a.variant == DR_VF) ? beta_safe<double>(pe) : beta_exp(pe);
+    tau = h * __ldg(drs + 4 * E + p) * beta;
+  }
+  return tau;
+}
+
+// Lane i's output of the double-float builds, from its accumulated rows:
+// accH = A_e row i (!SPLIT) or H row i (SPLIT, with accM = M row i),
+// fw = int W_i dOmega, vol = the element volume.  Writes the element-matrix
+// store (double-float pairs, or FP64 rows), diag += A_ii, the M store, phi,
+// f and b += cf f_i - ((H - rM M) T_old)_i as the BuildArgs ask; told is the
+// element's T_old at the nodes scaled by 2^-tshift.
+template <bool SPLIT>
+__device__ __forceinline__ void df_rows_out(const OpArgs &a, const BuildArgs &ba, long p,
+                                            int i, int ci, DfAcc (&accH)[8],
+                                            DfAcc (&accM)[SPLIT ? 8 : 1], const DfAcc &fw,
+                                            double vol, Df2 aHd, Df2 aMd, Df2 nrMd,
+                                            const Df2 *told, int tshift) {
+  const long E = a.E;
+  if (ba.Ahi && !ba.A64) {
+    // double-float store: A_e row = aH H + aM M formed in double-float,
+    // stored as its (hi, lo) pair; the store window is checked on hi
+    // (FP32 biased exponent 27..247 = FP64 exponent -100..120)
+    Df2 rowd[8];
+    bool bad = false;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      if constexpr (SPLIT) {
+        DfAcc acc{0.0f, 0.0f};
+        df_acc(acc, aHd, df_norm(accH[j]));
+        df_acc(acc, aMd, df_norm(accM[j % (SPLIT ? 8 : 1)]));
+        rowd[j] = df_norm(acc);
+      } else {
+        rowd[j] = df_norm(accH[j]);
+      }
+      const unsigned eb = (__float_as_uint(rowd[j].h) >> 23) & 0xffu;
+      if (rowd[j].h != 0.0f && (eb < 27u || eb > 247u)) bad = true;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      ba.Ahi[(size_t)(2 * i + h) * E + p] =
+          make_float4(rowd[4 * h].h, rowd[4 * h + 1].h, rowd[4 * h + 2].h, rowd[4 * h + 3].h);
+      ba.Alo[(size_t)(2 * i + h) * E + p] =
+          make_float4(rowd[4 * h].l, rowd[4 * h + 1].l, rowd[4 * h + 2].l, rowd[4 * h + 3].l);
+    }
+    if (bad) atomicOr(ba.bad, 1);  // store window (bit 1)
+    if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, df_to_double(rowd[i].h, rowd[i].l));
+  }
+  if (!ba.Ahi && (ba.A64 || ba.diag)) {
+    double row[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      row[j] = SPLIT ? ba.aH * df_to_double(accH[j].s, accH[j].c) +
+                           ba.aM * df_to_double(accM[j % (SPLIT ? 8 : 1)].s,
+                                                accM[j % (SPLIT ? 8 : 1)].c)
+                     : df_to_double(accH[j].s, accH[j].c);
+    if (ba.A64) {
+#pragma unroll
+      for (int jj = 0; jj < 4; jj++)
+        ba.A64[(size_t)(4 * i + jj) * E + p] = make_double2(row[2 * jj], row[2 * jj + 1]);
+    }
+    if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, row[i]);
+  }
+  if constexpr (SPLIT) {
+    if (ba.Mhi) {
+      // M row as its own double-float store (window as for A: bit 3)
+      Df2 rowm[8];
+      bool badm = false;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        rowm[j] = df_norm(accM[j % (SPLIT ? 8 : 1)]);
+        const unsigned eb = (__float_as_uint(rowm[j].h) >> 23) & 0xffu;
+        if (rowm[j].h != 0.0f && (eb < 27u || eb > 247u)) badm = true;
+      }
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        ba.Mhi[(size_t)(2 * i + h) * E + p] =
+            make_float4(rowm[4 * h].h, rowm[4 * h + 1].h, rowm[4 * h + 2].h, rowm[4 * h + 3].h);
+        ba.Mlo[(size_t)(2 * i + h) * E + p] =
+            make_float4(rowm[4 * h].l, rowm[4 * h + 1].l, rowm[4 * h + 2].l, rowm[4 * h + 3].l);
+      }
+      if (badm) atomicOr(ba.bad, 4);
+    }
+  }
+  if (ba.phi) ba.phi[(size_t)i * E + p] = df_to_double(fw.s, fw.c) / vol;
+  if (ba.f && ci >= 0) {
+    const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
+    atomicAdd(ba.f + ci, (qe / vol) * df_to_double(fw.s, fw.c));
+  }
+  if (ba.b && ci >= 0) {
+    const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
+    double val = ba.cf * ((qe / vol) * df_to_double(fw.s, fw.c));
+    if (SPLIT && ba.told) {
+      // (H - rM M) T_old in double-float on the scaled T_old, scaled back
+      DfAcc ft{0.0f, 0.0f};
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        DfAcc rowj = accH[j];
+        df_acc(rowj, nrMd, df_norm(accM[j % (SPLIT ? 8 : 1)]));
+        df_acc(ft, df_norm(rowj), told[j]);
+      }
+      double f = df_to_double(ft.s, ft.c);
+      if (!df_scale(f, tshift)) f = ldexp(f, tshift);
+      val -= f;
+    }
+    atomicAdd(ba.b + ci, val);
+  }
+}
+
+struct BuildSmemDF {
+  Df2 g[ROWS_EPB][8][5][8];  // per element, point q, node j: dNj/dx, dNj/dy,
+                             // dNj/dz, v.gradNj + P Nj, Wj
+  Df2 d[ROWS_EPB][8][2];     // detJ, lambda*detJ
+  Df2 fw[ROWS_EPB][4][8];    // face-3 points: W
+  Df2 fd[ROWS_EPB][4];       // alpha*detJs
+  Df2 rel[ROWS_EPB][24];     // node k's (x, y, z) - node 1's at [3k..3k+2]
+  Df2 told[ROWS_EPB][8];     // T_old at the nodes times 2^-shift
+  Df2 tab[8][4][8];          // N, dN/dxi, dN/deta, dN/dzeta at the 8 points
+  Df2 ftab[4][8];            // N at the 4 face-3 points
+};
+
+template <bool SPLIT>
+__global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArgs ba) {
+  __shared__ BuildSmemDF sm;
+  fill_df_tables(sm.tab, sm.ftab);
   const int lane8 = threadIdx.x & 7;
   const int le = threadIdx.x >> 3;
   const long E = a.E;
@@ -489,79 +690,13 @@ __global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArg
     // ---- lane q = Gauss point q
     const Df2 *tn = sm.tab[lane8][0], *t0 = sm.tab[lane8][1],
               *t1 = sm.tab[lane8][2], *t2 = sm.tab[lane8][3];
-    DfAcc J[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) J[k] = DfAcc{0.0f, 0.0f};
-#pragma unroll 1
-    for (int k = 1; k < 8; k++) {  // local node 1 is the origin
-      const Df2 rx = sm.rel[le][3 * k], ry = sm.rel[le][3 * k + 1],
-                rz = sm.rel[le][3 * k + 2];
-      df_acc(J[0], rx, t0[k]);
-      df_acc(J[1], rx, t1[k]);
-      df_acc(J[2], rx, t2[k]);
-      df_acc(J[3], ry, t0[k]);
-      df_acc(J[4], ry, t1[k]);
-      df_acc(J[5], ry, t2[k]);
-      df_acc(J[6], rz, t0[k]);
-      df_acc(J[7], rz, t1[k]);
-      df_acc(J[8], rz, t2[k]);
-    }
-    const Df2 j11 = df_norm(J[0]), j12 = df_norm(J[1]), j13 = df_norm(J[2]);
-    const Df2 j21 = df_norm(J[3]), j22 = df_norm(J[4]), j23 = df_norm(J[5]);
-    const Df2 j31 = df_norm(J[6]), j32 = df_norm(J[7]), j33 = df_norm(J[8]);
-    const Df2 c11 = df_sub(df_mul(j22, j33), df_mul(j23, j32));
-    const Df2 c12 = df_sub(df_mul(j21, j33), df_mul(j23, j31));
-    const Df2 c13 = df_sub(df_mul(j21, j32), df_mul(j22, j31));
-    const Df2 detp =
-        df_add(df_sub(df_mul(j11, c11), df_mul(j12, c12)), df_mul(j13, c13));
-    const double detj = df_to_double(detp.h, detp.l);
-    {
-      const int ed = df_exp(detj);  // zero, subnormal, inf, NaN included
-      if (ed < 1023 - 60 || ed > 1023 + 60) range_bad = true;
-    }
-    const Df2 r = df_rcp(detp);
-    const Df2 di11 = df_mul(r, c11);
-    const Df2 di12 = df_mul(r, df_sub(df_mul(j13, j32), df_mul(j12, j33)));
-    const Df2 di13 = df_mul(r, df_sub(df_mul(j12, j23), df_mul(j13, j22)));
-    const Df2 di21 = df_neg(df_mul(r, c12));
-    const Df2 di22 = df_mul(r, df_sub(df_mul(j11, j33), df_mul(j13, j31)));
-    const Df2 di23 = df_mul(r, df_sub(df_mul(j13, j21), df_mul(j11, j23)));
-    const Df2 di31 = df_mul(r, c13);
-    const Df2 di32 = df_mul(r, df_sub(df_mul(j12, j31), df_mul(j11, j32)));
-    const Df2 di33 = df_mul(r, df_sub(df_mul(j11, j22), df_mul(j12, j21)));
-    double tau;
-    if (a.variant == DR_OT) {
-      tau = __ldg(ba.drs + p);
-    } else {
-      // h = 2/|J^-1 e| (zero for |J^-1 e| <= 1e-14), Pe = h kpe,
-      // tau = h khalf beta(Pe)
-      const Df2 exd = df_from_double(__ldg(ba.drs + p));
-      const Df2 eyd = df_from_double(__ldg(ba.drs + E + p));
-      const Df2 ezd = df_from_double(__ldg(ba.drs + 2 * E + p));
-      DfAcc gxa{0.0f, 0.0f}, gya{0.0f, 0.0f}, gza{0.0f, 0.0f};
-      df_acc(gxa, di11, exd);
-      df_acc(gxa, di12, eyd);
-      df_acc(gxa, di13, ezd);
-      df_acc(gya, di21, exd);
-      df_acc(gya, di22, eyd);
-      df_acc(gya, di23, ezd);
-      df_acc(gza, di31, exd);
-      df_acc(gza, di32, eyd);
-      df_acc(gza, di33, ezd);
-      const Df2 gx = df_norm(gxa), gy = df_norm(gya), gz = df_norm(gza);
-      DfAcc n2{0.0f, 0.0f};
-      df_acc(n2, gx, gx);
-      df_acc(n2, gy, gy);
-      df_acc(n2, gz, gz);
-      const double gn2 = df_to_double(n2.s, n2.c);
-      const double h = (gn2 > 1.0e-28) ? 2.0 * rsqrt(gn2) : 0.0;
-      const double pe = h * __ldg(ba.drs + 3 * E + p);
-      tau = 0.0;
-      if (pe > 1.0e-12) {
-        const double beta = (a.variant == DR_VF) ? beta_safe<double>(pe) : beta_exp(pe);
-        tau = h * __ldg(ba.drs + 4 * E + p) * beta;
-      }
-    }
+    Df2 di[9];
+    double detj;
+    const Df2 detp = df_inverse_jacobian(sm.rel[le], t0, t1, t2, di, detj, range_bad);
+    const Df2 di11 = di[0], di12 = di[1], di13 = di[2];
+    const Df2 di21 = di[3], di22 = di[4], di23 = di[5];
+    const Df2 di31 = di[6], di32 = di[7], di33 = di[8];
+    const double tau = df_point_tau(a, ba.drs, p, di);
     const Df2 vxd = df_from_double_chk(vx, range_bad);
     const Df2 vyd = df_from_double_chk(vy, range_bad);
     const Df2 vzd = df_from_double_chk(vz, range_bad);
@@ -670,98 +805,246 @@ __global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArg
       }
     }
     if (!valid) continue;
-    const int ci = ck;  // row i's node
-    if (ba.Ahi && !ba.A64) {
-      // double-float store: A_e row = aH H + aM M formed in double-float,
-      // stored as its (hi, lo) pair; the store window is checked on hi
-      // (FP32 biased exponent 27..247 = FP64 exponent -100..120)
-      Df2 rowd[8];
-      bool bad = false;
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        if constexpr (SPLIT) {
-          DfAcc acc{0.0f, 0.0f};
-          df_acc(acc, aHd, df_norm(accH[j]));
-          df_acc(acc, aMd, df_norm(accM[j % (SPLIT ? 8 : 1)]));
-          rowd[j] = df_norm(acc);
-        } else {
-          rowd[j] = df_norm(accH[j]);
-        }
-        const unsigned eb = (__float_as_uint(rowd[j].h) >> 23) & 0xffu;
-        if (rowd[j].h != 0.0f && (eb < 27u || eb > 247u)) bad = true;
-      }
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        ba.Ahi[(size_t)(2 * i + h) * E + p] =
-            make_float4(rowd[4 * h].h, rowd[4 * h + 1].h, rowd[4 * h + 2].h, rowd[4 * h + 3].h);
-        ba.Alo[(size_t)(2 * i + h) * E + p] =
-            make_float4(rowd[4 * h].l, rowd[4 * h + 1].l, rowd[4 * h + 2].l, rowd[4 * h + 3].l);
-      }
-      if (bad) atomicOr(ba.bad, 1);  // store window (bit 1)
-      if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, df_to_double(rowd[i].h, rowd[i].l));
-    }
-    if (!ba.Ahi && (ba.A64 || ba.diag)) {
-      double row[8];
-#pragma unroll
-      for (int j = 0; j < 8; j++)
-        row[j] = SPLIT ? ba.aH * df_to_double(accH[j].s, accH[j].c) +
-                             ba.aM * df_to_double(accM[j % (SPLIT ? 8 : 1)].s,
-                                                  accM[j % (SPLIT ? 8 : 1)].c)
-                       : df_to_double(accH[j].s, accH[j].c);
-      if (ba.A64) {
-#pragma unroll
-        for (int jj = 0; jj < 4; jj++)
-          ba.A64[(size_t)(4 * i + jj) * E + p] = make_double2(row[2 * jj], row[2 * jj + 1]);
-      }
-      if (ba.diag && ci >= 0) atomicAdd(ba.diag + ci, row[i]);
-    }
-    if constexpr (SPLIT) {
-      if (ba.Mhi) {
-        // M row as its own double-float store (window as for A: bit 3)
-        Df2 rowm[8];
-        bool badm = false;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          rowm[j] = df_norm(accM[j % (SPLIT ? 8 : 1)]);
-          const unsigned eb = (__float_as_uint(rowm[j].h) >> 23) & 0xffu;
-          if (rowm[j].h != 0.0f && (eb < 27u || eb > 247u)) badm = true;
-        }
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          ba.Mhi[(size_t)(2 * i + h) * E + p] =
-              make_float4(rowm[4 * h].h, rowm[4 * h + 1].h, rowm[4 * h + 2].h, rowm[4 * h + 3].h);
-          ba.Mlo[(size_t)(2 * i + h) * E + p] =
-              make_float4(rowm[4 * h].l, rowm[4 * h + 1].l, rowm[4 * h + 2].l, rowm[4 * h + 3].l);
-        }
-        if (badm) atomicOr(ba.bad, 4);
-      }
-    }
-    if (ba.phi) ba.phi[(size_t)i * E + p] = df_to_double(fw.s, fw.c) / vol;
-    if (ba.f && ci >= 0) {
-      const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
-      atomicAdd(ba.f + ci, (qe / vol) * df_to_double(fw.s, fw.c));
-    }
-    if (ba.b && ci >= 0) {
-      const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
-      double val = ba.cf * ((qe / vol) * df_to_double(fw.s, fw.c));
-      if (SPLIT && ba.told) {
-        // (H - rM M) T_old in double-float on the scaled T_old, scaled back
-        DfAcc ft{0.0f, 0.0f};
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          DfAcc rowj = accH[j];
-          df_acc(rowj, nrMd, df_norm(accM[j % (SPLIT ? 8 : 1)]));
-          df_acc(ft, df_norm(rowj), sm.told[le][j]);
-        }
-        double f = df_to_double(ft.s, ft.c);
-        if (!df_scale(f, tshift)) f = ldexp(f, tshift);
-        val -= f;
-      }
-      atomicAdd(ba.b + ci, val);
-    }
+    df_rows_out<SPLIT>(a, ba, p, i, ck, accH, accM, fw, vol, aHd, aMd, nrMd, sm.told[le],
+                       tshift);
   }
   // Any out-of-window value: the host redoes this build with the FP64 rows
   // (bit 2 of the flag).
+  if (range_bad) atomicOr(ba.bad, 2);
+}
+
+// ---- geometric factors of the double-float build, once per mesh
+struct GeoSmem {
+  Df2 g[ROWS_EPB][8][3][8];  // per element, point q, node j: dNj/dx, dNj/dy, dNj/dz
+  Df2 dj[ROWS_EPB][8];       // detJ at point q
+  Df2 rel[ROWS_EPB][24];     // node k's (x, y, z) - node 1's at [3k..3k+2]
+  Df2 tab[8][4][8];          // N, dN/dxi, dN/deta, dN/dzeta at the 8 points
+};
+
+// Per element on 8 lanes: lane q forms J^-1 and detJ at Gauss point q
+// (the same double-float evaluation as elem_build_df_kernel) and the
+// physical gradients of the 8 shape functions there; lane i then forms
+// K_ij = sum_q detJ_q gradN_i . gradN_j for j >= i.
+__global__ void __launch_bounds__(64) geo_factors_kernel(OpArgs a, GeoFactors g, int *bad) {
+  __shared__ GeoSmem sm;
+  fill_df_tables(sm.tab, nullptr);
+  const int lane8 = threadIdx.x & 7;
+  const int le = threadIdx.x >> 3;
+  const long E = a.E;
+  bool range_bad = false;
+  for (long base = (long)blockIdx.x * ROWS_EPB; base < E;
+       base += (long)gridDim.x * ROWS_EPB) {
+    const long pe = base + le;
+    const bool valid = pe < E;
+    const long p = valid ? pe : E - 1;
+    __syncwarp();  // the previous element's shared data has been read
+    // ---- lane k = node k
+    const int nk = __ldg(a.conn + (size_t)lane8 * E + p) & NODE_BITS;
+    const double xk = __ldg(a.xx + nk), yk = __ldg(a.yy + nk), zk = __ldg(a.zz + nk);
+    const double x0 = __shfl_sync(FULL, xk, 0, 8);
+    const double y0 = __shfl_sync(FULL, yk, 0, 8);
+    const double z0 = __shfl_sync(FULL, zk, 0, 8);
+    sm.rel[le][3 * lane8] = df_from_double_chk(xk - x0, range_bad);
+    sm.rel[le][3 * lane8 + 1] = df_from_double_chk(yk - y0, range_bad);
+    sm.rel[le][3 * lane8 + 2] = df_from_double_chk(zk - z0, range_bad);
+    __syncwarp();
+    // ---- lane q = Gauss point q
+    const int q = lane8;
+    const Df2 *t0 = sm.tab[q][1], *t1 = sm.tab[q][2], *t2 = sm.tab[q][3];
+    Df2 di[9];
+    double detj;
+    const Df2 detp = df_inverse_jacobian(sm.rel[le], t0, t1, t2, di, detj, range_bad);
+    if (valid) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) g.Ji[(size_t)(9 * q + k) * E + p] = make_float2(di[k].h, di[k].l);
+      g.Dj[(size_t)q * E + p] = make_float2(detp.h, detp.l);
+    }
+#pragma unroll 2
+    for (int j = 0; j < 8; j++) {
+      DfAcc ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
+      df_acc(ax, di[0], t0[j]);
+      df_acc(ax, di[3], t1[j]);
+      df_acc(ax, di[6], t2[j]);
+      df_acc(ay, di[1], t0[j]);
+      df_acc(ay, di[4], t1[j]);
+      df_acc(ay, di[7], t2[j]);
+      df_acc(az, di[2], t0[j]);
+      df_acc(az, di[5], t1[j]);
+      df_acc(az, di[8], t2[j]);
+      sm.g[le][q][0][j] = df_norm(ax);
+      sm.g[le][q][1][j] = df_norm(ay);
+      sm.g[le][q][2][j] = df_norm(az);
+    }
+    sm.dj[le][q] = detp;
+    __syncwarp();
+    // ---- lane i = row i of K (the upper triangle is stored)
+    const int i = lane8;
+    DfAcc acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[j] = DfAcc{0.0f, 0.0f};
+#pragma unroll 1
+    for (int r = 0; r < 8; r++) {
+      const Df2 dj = sm.dj[le][r];
+      const Df2 dgx = df_mul(dj, sm.g[le][r][0][i]);
+      const Df2 dgy = df_mul(dj, sm.g[le][r][1][i]);
+      const Df2 dgz = df_mul(dj, sm.g[le][r][2][i]);
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        df_acc(acc[j], dgx, sm.g[le][r][0][j]);
+        df_acc(acc[j], dgy, sm.g[le][r][1][j]);
+        df_acc(acc[j], dgz, sm.g[le][r][2][j]);
+      }
+    }
+    if (!valid) continue;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      if (j < i) continue;
+      const Df2 k = df_norm(acc[j]);
+      g.K[(size_t)(i * (15 - i) / 2 + j) * E + p] = make_float2(k.h, k.l);
+    }
+  }
+  if (range_bad) atomicOr(bad, 2);
+}
+
+struct GeoBuildSmem {
+  Df2 dw[ROWS_EPB][8][8];  // per element, point q, node j: detJ W_j
+  Df2 c[ROWS_EPB][8][8];   // SPLIT: v.gradN_j + P N_j; otherwise
+                           // aH v.gradN_j + (aH P + aM) N_j
+  Df2 told[ROWS_EPB][8];   // T_old at the nodes times 2^-shift
+  Df2 tab[8][4][8];        // N, dN/dxi, dN/deta, dN/dzeta at the 8 points
+};
+
+__device__ __forceinline__ Df2 ld_pair(const float2 *p) {
+  const float2 v = __ldg(p);
+  return Df2{v.x, v.y};
+}
+
+// The double-float build from the mesh's geometric factors.  With
+// a_j = v . gradN_j = (J^-1 v) . dN_j/dxi and W_j = N_j + tau a_j at each
+// Gauss point,
+//   H_ij = lambda K_ij + sum_q detJ W_i (a_j + P N_j),
+//   M_ij = sum_q detJ W_i N_j
+// (el3d's hma + hmav + cma and cman, vanadis_full_DR_OpenMP_timing.for:
+// 431-610, the diffusion term's geometry K formed once per mesh); no Robin
+// term (elements with a nonzero Robin coefficient take elem_build_df_kernel).
+// Per element on 8 lanes: lane q forms point q's tau, J^-1 v and, per node,
+// a_j and W_j (4 pair products); lane i accumulates row i, 1 + 8 pair
+// products per entry (SPLIT: H and M apart, 1 + 16), then writes as
+// elem_build_df_kernel does.  A value outside the pairs' safe window sets
+// bit 2 of the flag (the host redoes the build with FP64 rows).
+template <bool SPLIT>
+__global__ void __launch_bounds__(64, 8) elem_build_geo_kernel(OpArgs a, BuildArgs ba) {
+  __shared__ GeoBuildSmem sm;
+  fill_df_tables(sm.tab, nullptr);
+  const int lane8 = threadIdx.x & 7;
+  const int le = threadIdx.x >> 3;
+  const long E = a.E;
+  bool range_bad = false;
+  const Df2 aHd = df_from_double_chk(ba.aH, range_bad);
+  const Df2 aMd = df_from_double_chk(ba.aM, range_bad);
+  const Df2 nrMd = df_neg(df_from_double_chk(SPLIT ? ba.rM : 0.0, range_bad));
+  const bool need_rows = SPLIT || ba.Ahi || ba.A64 || ba.diag;
+  const double *V = a.f.vel;
+  for (long base = (long)blockIdx.x * ROWS_EPB; base < E;
+       base += (long)gridDim.x * ROWS_EPB) {
+    const long pe = base + le;
+    const bool valid = pe < E;
+    const long p = valid ? pe : E - 1;
+    __syncwarp();  // the previous element's shared data has been read
+    // ---- lane k = node k
+    const int ck = __ldg(a.conn + (size_t)lane8 * E + p);
+    int tshift = 0;
+    if (SPLIT && ba.told) {
+      const double tk = __ldg(ba.told + (ck & NODE_BITS));
+      int em = df_exp(tk);
+      em = max(em, __shfl_xor_sync(FULL, em, 1));
+      em = max(em, __shfl_xor_sync(FULL, em, 2));
+      em = max(em, __shfl_xor_sync(FULL, em, 4));
+      if (em == 0 && tk != 0.0) range_bad = true;  // all subnormal
+      tshift = em - 1023;
+      Df2 t;
+      df_split(tk, t.h, t.l, range_bad, tshift);  // inf/NaN: bad
+      sm.told[le][lane8] = t;
+    }
+    const double vx = __ldg(V + p), vy = __ldg(V + E + p), vz = __ldg(V + 2 * E + p);
+    const double lam = __ldg(a.f.lam + p);
+    const double pdec = a.f.pdec ? __ldg(a.f.pdec + p) : 0.0;
+    // ---- lane q = Gauss point q
+    const int q = lane8;
+    Df2 di[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) di[k] = ld_pair(ba.gJi + (size_t)(9 * q + k) * E + p);
+    const Df2 djq = ld_pair(ba.gDj + (size_t)q * E + p);
+    const double tau = df_point_tau(a, ba.drs, p, di);
+    const Df2 vxd = df_from_double_chk(vx, range_bad);
+    const Df2 vyd = df_from_double_chk(vy, range_bad);
+    const Df2 vzd = df_from_double_chk(vz, range_bad);
+    const Df2 pd = df_from_double_chk(pdec, range_bad);
+    const Df2 taud = df_from_double_chk(tau, range_bad);
+    Df2 w[3];  // J^-1 v
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      DfAcc acc{0.0f, 0.0f};
+      df_acc(acc, di[3 * r], vxd);
+      df_acc(acc, di[3 * r + 1], vyd);
+      df_acc(acc, di[3 * r + 2], vzd);
+      w[r] = df_norm(acc);
+    }
+    const Df2 cm = SPLIT ? pd : df_add(df_mul(aHd, pd), aMd);
+    const Df2 *tn = sm.tab[q][0], *t0 = sm.tab[q][1], *t1 = sm.tab[q][2], *t2 = sm.tab[q][3];
+#pragma unroll 2
+    for (int j = 0; j < 8; j++) {
+      DfAcc aa{0.0f, 0.0f};
+      df_acc(aa, w[0], t0[j]);
+      df_acc(aa, w[1], t1[j]);
+      df_acc(aa, w[2], t2[j]);
+      const Df2 av = df_norm(aa);
+      DfAcc aw{0.0f, 0.0f};
+      df_acc_add(aw, tn[j]);
+      df_acc(aw, taud, av);
+      sm.dw[le][q][j] = df_mul(djq, df_norm(aw));
+      DfAcc ac{0.0f, 0.0f};
+      if constexpr (SPLIT)
+        df_acc_add(ac, av);
+      else
+        df_acc(ac, aHd, av);
+      df_acc(ac, cm, tn[j]);
+      sm.c[le][q][j] = df_norm(ac);
+    }
+    const double vol = group8_sum<double>(df_to_double(djq.h, djq.l));
+    __syncwarp();
+    // ---- lane i = row i
+    const int i = lane8;
+    DfAcc accH[8], accM[SPLIT ? 8 : 1];
+#pragma unroll
+    for (int j = 0; j < 8; j++) accH[j] = DfAcc{0.0f, 0.0f};
+#pragma unroll
+    for (int j = 0; j < (SPLIT ? 8 : 1); j++) accM[j] = DfAcc{0.0f, 0.0f};
+    DfAcc fw{0.0f, 0.0f};
+    if (need_rows) {
+      const Df2 lamd = df_from_double_chk(lam, range_bad);
+      const Df2 lk = SPLIT ? lamd : df_mul(aHd, lamd);
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int t = (j >= i) ? i * (15 - i) / 2 + j : j * (15 - j) / 2 + i;
+        df_acc(accH[j], lk, ld_pair(ba.gK + (size_t)t * E + p));
+      }
+    }
+#pragma unroll 1
+    for (int r = 0; r < 8; r++) {
+      const Df2 dwi = sm.dw[le][r][i];
+      df_acc_add(fw, dwi);
+      if (!need_rows) continue;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        df_acc(accH[j], dwi, sm.c[le][r][j]);
+        if constexpr (SPLIT) df_acc(accM[j], dwi, sm.tab[r][0][j]);
+      }
+    }
+    if (!valid) continue;
+    df_rows_out<SPLIT>(a, ba, p, i, ck, accH, accM, fw, vol, aHd, aMd, nrMd, sm.told[le],
+                       tshift);
+  }
   if (range_bad) atomicOr(ba.bad, 2);
 }
 
@@ -1004,12 +1287,28 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
     });
     const int g2 = (int)std::min<long>(((long)a.E + 255) / 256, (long)device_sm_count() * 8);
     elem_dr_scalars_kernel<<<g2, 256, 0, s>>>(a, ba.drs);
-    if (ba.told || ba.Mhi)  // H and M apart
+    if (ba.gK) {  // from the mesh's geometric factors
+      if (ba.told || ba.Mhi)
+        elem_build_geo_kernel<true><<<grid, 64, 0, s>>>(a, ba);
+      else
+        elem_build_geo_kernel<false><<<grid, 64, 0, s>>>(a, ba);
+    } else if (ba.told || ba.Mhi) {  // H and M apart
       elem_build_df_kernel<true><<<grid, 64, 0, s>>>(a, ba);
-    else
+    } else {
       elem_build_df_kernel<false><<<grid, 64, 0, s>>>(a, ba);
+    }
     count_launches(1);
   }
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_geo_factors(const OpArgs &a, const GeoFactors &g, int *bad,
+                               cudaStream_t s) {
+  if (a.E <= 0) return cudaSuccess;
+  const long blocks_needed = ((long)a.E + ROWS_EPB - 1) / ROWS_EPB;
+  const int grid = (int)std::min<long>(blocks_needed, (long)device_sm_count() * 32);
+  geo_factors_kernel<<<grid, 64, 0, s>>>(a, g, bad);
   count_launches(1);
   return cudaGetLastError();
 }

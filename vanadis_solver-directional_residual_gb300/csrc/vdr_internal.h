@@ -131,6 +131,19 @@ constexpr int TUNE_TILES = 4;   // block apply: node tile (box height, column ha
                                 // (2,1) (4,2), and the tcgen05 box apply
 constexpr int TUNE_GRID_PER_SM[TUNE_GRIDS] = {2, 4, 8, 16, 32};
 
+// Geometric factors of the double-float build, formed once per mesh (a
+// handle's coordinates never change), double-float pairs (h, l), element
+// index fastest:
+//   Ji[(9 q + 3 a + b) E + p]  (J^-1)_{ab} = d xi_a / d x_b at Gauss point q
+//   Dj[q E + p]                detJ at Gauss point q
+//   K[t E + p]                 int gradN_i . gradN_j dOmega (unit
+//                              diffusivity), t = i (15 - i) / 2 + j, i <= j
+// 116 pairs = 928 bytes per element.
+constexpr int GEO_PAIRS = 72 + 8 + 36;
+struct GeoFactors {
+  float2 *Ji = nullptr, *Dj = nullptr, *K = nullptr;
+};
+
 struct Handle {
   int N = 0, E = 0;
   int nax = 0, nay = 0, naz = 0;  // > 0 when the mesh is the canonical structured numbering
@@ -153,6 +166,13 @@ struct Handle {
   bool apply_fp32 = false;  // operator applies use the FP32 operator
   int storage = VDR_STORE_DF;  // element-matrix store (resolved, never AUTO)
   bool exact_build = false;    // H/M rows in FP64 (values outside the pair window)
+  // the double-float build from the mesh's geometric factors, formed once
+  // (geo_state 1), or from the coordinates at every build (build_mode
+  // VDR_BUILD_RECOMPUTE, or geo_state -1: no room for them, a factor outside
+  // the pair window)
+  int build_mode = VDR_BUILD_AUTO;
+  int geo_state = 0;
+  GeoFactors geo;
 
   // geometry / topology (device, storage order)
   double *xx = nullptr, *yy = nullptr, *zz = nullptr;
@@ -305,11 +325,20 @@ struct BuildArgs {
   // time loop: M kept as its own double-float store, and f = sum_e f_e
   float4 *Mhi = nullptr, *Mlo = nullptr;
   double *f = nullptr;
+  // the mesh's geometric factors (element.cu, GeoFactors): given, the
+  // double-float build reads them instead of recomputing the Jacobians
+  const float2 *gJi = nullptr, *gDj = nullptr, *gK = nullptr;
 };
+
 
 // ---- launchers (element.cu) ----
 cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
                          cudaStream_t s);
+// The mesh's geometric factors into g (arrays of E * 72, E * 8, E * 36
+// pairs); sets bit 2 of *bad when a coordinate difference or detJ lies
+// outside the pairs' safe window (the factors are then not to be used).
+cudaError_t launch_geo_factors(const OpArgs &a, const GeoFactors &g, int *bad,
+                               cudaStream_t s);
 cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
                             const double *x, double *y, const int *skip,
                             const int *skip2, cudaStream_t s);

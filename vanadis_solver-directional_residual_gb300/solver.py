@@ -392,6 +392,27 @@ class Solver:
     # ---- many right-hand sides: node-major N x K device arrays ----
     BLOCK_PRECISION = {"fp64": 0, "tf32": 1, "tf32x3": 2}
 
+    def set_build_mode(self, mode="auto"):
+        """How the element build gets the element geometry: "auto" (the
+        mesh's geometric factors -- J^-1 and detJ at the Gauss points and
+        the unit-diffusivity stiffness, 928 bytes per element -- formed on
+        the GPU once and read by every later build) or "recompute" (the
+        Jacobians evaluated from the coordinates at every build).  Marks
+        the operator stale."""
+        L.check(self.lib.vdr_set_build_mode(
+            self.h, {"auto": 0, "recompute": 1}[mode]), "vdr_set_build_mode")
+
+    def geometry_status(self):
+        """(state, bytes): state 1 when the geometric factors are held (in
+        `bytes` of device memory), 0 when not formed yet, -1 when the build
+        cannot use them (no device memory, a factor outside the double-float
+        window)."""
+        st = ctypes.c_int(0)
+        nb = ctypes.c_longlong(0)
+        L.check(self.lib.vdr_geometry_status(self.h, ctypes.byref(st), ctypes.byref(nb)),
+                "vdr_geometry_status")
+        return st.value, nb.value
+
     def set_mixed_operator(self, mode="rounded"):
         """Inner operator of the mixed solve: "rounded" (the FP64 element
         matrices rounded to FP32), "recompute" (DR terms in FP32) or "half"
