@@ -153,6 +153,11 @@ int vdr_set_build_mode(vdr_handle *h, int mode);
 /* *cached = 1 when the geometric factors are held (bytes of device memory
  * in *bytes), 0 when not (yet) formed, -1 when they cannot be used. */
 int vdr_geometry_status(vdr_handle *h, int *cached, long long *bytes);
+/* Diagnostic of the element build's double-float beta(Pe) = coth(Pe) -
+ * 1/Pe (VF variant): beta[i] for the n host values pe[i] > 0, evaluated on
+ * the current device as the build evaluates it (pe split into a pair,
+ * result merged to FP64). */
+int vdr_diag_beta_vf(int n, const double *pe, double *beta);
 
 /* y = P A P x (transpose = 0) or y = P A^T P x, host arrays of length N. */
 int vdr_apply(vdr_handle *h, const double *x, double *y, int transpose);

@@ -36,6 +36,12 @@ def cases(vdr):
     p = P.rotation_shear(5, 4, 6, seed=26)
     p.pdec[:] = 0.3
     out["rotation_decay"] = p
+    # VF with the element Peclet number spread over 1e-4 .. 1e4 (diffusivity
+    # log-uniform over eight decades): every branch of the double-float
+    # beta(Pe) (series, exponential form, 1 - 1/Pe)
+    p = P.rotation_shear(8, 7, 6, seed=29)
+    p.lam[:] = 10.0 ** np.random.default_rng(30).uniform(-5.0, 3.0, p.lam.size)
+    out["vf_peclet_sweep"] = p
     # Robin faces present but a zero Robin coefficient: the cached build
     p = P.rotation_shear(4, 5, 3, seed=27)
     p.robin_alpha = 0.0
@@ -49,7 +55,7 @@ def problems(vdr):
 
 
 NAMES = ["const_adv_OT", "rotation_VF", "rotation_GP", "one_element",
-         "brick_axis", "rotation_decay", "robin_faces_alpha0"]
+         "brick_axis", "rotation_decay", "vf_peclet_sweep", "robin_faces_alpha0"]
 
 
 def oracle_system(oracle, prob, aH, aM, cf, rM, t_old):
@@ -161,3 +167,36 @@ def test_build_mode_argument_checked(vdr, gpu_lib, problems):
         with pytest.raises(KeyError):
             s.set_build_mode("sometimes")
         assert s.lib.vdr_set_build_mode(s.h, 7) == 4  # VDR_BAD_ARGUMENT
+
+
+def beta_exact(x):
+    """coth x - 1/x to ~40 digits (decimal arithmetic)."""
+    from decimal import Decimal, getcontext
+    getcontext().prec = 60
+    d = Decimal(x)
+    if d < Decimal("1e-3"):  # series, far below the rounding of the other form
+        y = d * d
+        return float(d / 3 - d * y / 45 + 2 * d * y * y / 945 - d * y ** 3 / 4725)
+    e = (2 * d).exp()
+    return float((e + 1) / (e - 1) - 1 / d)
+
+
+def test_double_float_beta_vf(vdr, gpu_lib):
+    """The build's beta(Pe) of the VF variant in double-float against the
+    exact function, across its three branches and their boundaries."""
+    import ctypes
+    xs = np.concatenate([np.logspace(-12, 4, 400),
+                         [0.4999999, 0.5, 0.5000001, 43.999, 44.0, 44.001,
+                          1e-3, 0.1, 1.0, 3.7, 709.0]])
+    got = np.zeros_like(xs)
+    lib = vdr.load_library()
+    D = ctypes.POINTER(ctypes.c_double)
+    st = lib.vdr_diag_beta_vf(int(xs.size), xs.ctypes.data_as(D), got.ctypes.data_as(D))
+    assert st == 0
+    ref = np.array([beta_exact(x) for x in xs])
+    rel = np.abs(got - ref) / np.abs(ref)
+    # largest just above 1/2, where 1 - 1/x and 2u/(1 - u) cancel by ~5
+    assert rel.max() < 2.5e-13, (xs[rel.argmax()], rel.max())
+    assert np.median(rel) < 1e-14
+    bad = np.array([0.0, -1.0])
+    assert lib.vdr_diag_beta_vf(2, bad.ctypes.data_as(D), got.ctypes.data_as(D)) == 4

@@ -81,6 +81,7 @@ SIGNATURES = {
     "vdr_diag_barrier_timeout": (_i, [_P]),
     "vdr_set_mixed_operator": (_i, [_P, _i]),
     "vdr_set_build_mode": (_i, [_P, _i]),
+    "vdr_diag_beta_vf": (_i, [_i, _D, _D]),
     "vdr_geometry_status": (_i, [_P, _I, ctypes.POINTER(ctypes.c_longlong)]),
     "vdr_apply_half_device": (_i, [_P, _P, _P]),
     "vdr_apply_block_device": (_i, [_P, _i, _P, _P, _i]),

@@ -1023,6 +1023,20 @@ int vdr_geometry_status(vdr_handle *H, int *cached, long long *bytes) {
   return VDR_OK;
 }
 
+int vdr_diag_beta_vf(int n, const double *pe, double *beta) {
+  if (n < 0 || (n > 0 && (!pe || !beta))) {
+    set_error("vdr_diag_beta_vf: bad arguments");
+    return VDR_BAD_ARGUMENT;
+  }
+  for (int i = 0; i < n; i++)
+    if (!(pe[i] > 0.0)) {
+      set_error("vdr_diag_beta_vf: pe must be positive");
+      return VDR_BAD_ARGUMENT;
+    }
+  cudaError_t e = diag_beta_vf(n, pe, beta);
+  return e ? cuda_fail(e, "vdr_diag_beta_vf") : VDR_OK;
+}
+
 int vdr_set_mixed_operator(vdr_handle *H, int mode) {
   int st = check_handle(H);
   if (st) return st;

@@ -487,15 +487,83 @@ __device__ __forceinline__ Df2 df_inverse_jacobian(const Df2 *rel, const Df2 *t0
   return detp;
 }
 
+// coth x - 1/x (beta of the VF variant, beta_safe) in double-float on the
+// FP32 pipe for a pair x > 0: below 1/2 the Taylor series of coth x - 1/x,
+// sum_n 2^2n B_2n x^(2n-1) / (2n)! (the Bernoulli-number expansion of coth,
+// ten terms: truncation below 2^-50 relative at x = 1/2); from 1/2 to 44,
+// 1 - 1/x + 2u/(1 - u) with u = e^(-2x): 2x = k ln 2 + r (Cody-Waite
+// reduction, ln 2 in three parts, the first of 16 bits so that k ln2_1 is
+// exact), e^(-r) from the degree-7 Taylor polynomial of e^s at s = -r/8
+// squared three times, then scaled by 2^-k; above 44 (u < 2^-126) 1 - 1/x.
+// Measured against the exact function: relative error ~1e-15 typically,
+// 1.2e-13 at most (just above 1/2, where 1 - 1/x and 2u/(1 - u) cancel).
+__device__ __constant__ float COTH_SERIES[10][2] = {
+    {0x1.555556p-2f, -0x1.555556p-27f},  {-0x1.6c16c2p-6f, 0x1.27d27ep-31f},
+    {0x1.1566acp-9f, -0x1.ff754cp-36f},  {-0x1.bbd77ap-13f, 0x1.99621ep-38f},
+    {0x1.66a8f2p-16f, 0x1.7ee1d8p-41f},  {-0x1.22805ep-19f, 0x1.377b30p-44f},
+    {0x1.d6db2cp-23f, 0x1.382458p-49f},  {-0x1.7da4e2p-26f, 0x1.0cd548p-55f},
+    {0x1.355872p-29f, -0x1.4d68b2p-56f}, {-0x1.f57d96p-33f, -0x1.19559ep-58f}};
+__device__ __constant__ float EXP_TAYLOR[8][2] = {  // 1/n!, n = 0..7
+    {1.0f, 0.0f},
+    {1.0f, 0.0f},
+    {0.5f, 0.0f},
+    {0x1.555556p-3f, -0x1.555556p-28f},
+    {0x1.555556p-5f, -0x1.555556p-30f},
+    {0x1.111112p-7f, -0x1.dddddep-32f},
+    {0x1.6c16c2p-10f, -0x1.27d27ep-35f},
+    {0x1.a01a02p-13f, -0x1.7f97fap-39f}};
+
+__device__ __forceinline__ Df2 df_beta_vf(Df2 x) {
+  const Df2 one{1.0f, 0.0f};
+  if (x.h < 0.5f) {
+    const Df2 y = df_mul(x, x);
+    Df2 p{COTH_SERIES[9][0], COTH_SERIES[9][1]};
+#pragma unroll
+    for (int n = 8; n >= 0; n--) p = df_add(df_mul(p, y), Df2{COTH_SERIES[n][0], COTH_SERIES[n][1]});
+    return df_mul(p, x);
+  }
+  const Df2 base = df_sub(one, df_rcp(x));
+  if (x.h > 44.0f) return base;
+  // 2x = k ln2 + r, |r| <= ln2 / 2
+  const Df2 y{2.0f * x.h, 2.0f * x.l};
+  const float k = rintf(y.h * 0x1.715476p+0f);
+  const float t1 = __fmaf_rn(-k, 0x1.62e4p-1f, y.h);  // exact
+  const float p2 = __fmul_rn(k, 0x1.7f7d1cp-20f);
+  const float e2 = __fmaf_rn(k, 0x1.7f7d1cp-20f, -p2);
+  Df2 r = df_add(Df2{t1, 0.0f}, Df2{-p2, -e2});
+  r = df_add(r, Df2{__fmaf_rn(-k, 0x1.ef357ap-45f, y.l), 0.0f});
+  // e^(-r) = (e^s)^8
+  const Df2 sx{-0.125f * r.h, -0.125f * r.l};
+  Df2 e{EXP_TAYLOR[7][0], EXP_TAYLOR[7][1]};
+#pragma unroll
+  for (int n = 6; n >= 0; n--) e = df_add(df_mul(e, sx), Df2{EXP_TAYLOR[n][0], EXP_TAYLOR[n][1]});
+  e = df_mul(e, e);
+  e = df_mul(e, e);
+  e = df_mul(e, e);
+  const int ki = (int)k;
+  const float sc = ki < 127 ? __int_as_float((127 - ki) << 23) : 0.0f;  // 2^-k
+  const Df2 u{e.h * sc, e.l * sc};
+  const Df2 t = df_mul(Df2{2.0f * u.h, 2.0f * u.l}, df_rcp(df_sub(one, u)));
+  return df_add(base, t);
+}
+
+__global__ void beta_vf_kernel(int n, const double *__restrict__ pe, double *__restrict__ beta) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Df2 b = df_beta_vf(df_from_double(pe[i]));
+  beta[i] = df_to_double(b.h, b.l);
+}
+
 // The streamline parameter tau at one Gauss point of the double-float
-// builds, di = J^-1 at the point: OT from the per-element value; GP and VF
-// from h = 2/|J^-1 e| (zero for |J^-1 e| <= 1e-14), Pe = h kpe and
+// builds as a pair, di = J^-1 at the point: OT from the per-element value;
+// GP and VF from h = 2/|J^-1 e| (zero for |J^-1 e| <= 1e-14), Pe = h kpe and
 // tau = h khalf beta(Pe) with the element's scalars of
-// elem_dr_scalars_kernel.
-__device__ __forceinline__ double df_point_tau(const OpArgs &a, const double *drs, long p,
-                                               const Df2 (&di)[9]) {
+// elem_dr_scalars_kernel, beta(Pe) in double-float for VF (df_beta_vf) and
+// in FP64 for GP (beta_exp, whose exp overflow the variant keeps).
+__device__ __forceinline__ Df2 df_point_tau(const OpArgs &a, const double *drs, long p,
+                                            const Df2 (&di)[9], bool &range_bad) {
   const long E = a.E;
-  if (a.variant == DR_OT) return __ldg(drs + p);
+  if (a.variant == DR_OT) return df_from_double_chk(__ldg(drs + p), range_bad);
   const Df2 exd = df_from_double(__ldg(drs + p));
   const Df2 eyd = df_from_double(__ldg(drs + E + p));
   const Df2 ezd = df_from_double(__ldg(drs + 2 * E + p));
@@ -517,12 +585,11 @@ __device__ __forceinline__ double df_point_tau(const OpArgs &a, const double *dr
   const double gn2 = df_to_double(n2.s, n2.c);
   const double h = (gn2 > 1.0e-28) ? 2.0 * rsqrt(gn2) : 0.0;
   const double pe = h * __ldg(drs + 3 * E + p);
-  double tau = 0.0;
-  if (pe > 1.0e-12) {
-    const double beta = (a.variant == DR_VF) ? beta_safe<double>(pe) : beta_exp(pe);
-    tau = h * __ldg(drs + 4 * E + p) * beta;
-  }
-  return tau;
+  if (!(pe > 1.0e-12)) return Df2{0.0f, 0.0f};
+  const double hk = h * __ldg(drs + 4 * E + p);
+  if (a.variant == DR_VF)
+    return df_mul(df_from_double_chk(hk, range_bad), df_beta_vf(df_from_double(fmin(pe, 1.0e30))));
+  return df_from_double_chk(hk * beta_exp(pe), range_bad);
 }
 
 // Lane i's output of the double-float builds, from its accumulated rows:
@@ -696,12 +763,11 @@ __global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArg
     const Df2 di11 = di[0], di12 = di[1], di13 = di[2];
     const Df2 di21 = di[3], di22 = di[4], di23 = di[5];
     const Df2 di31 = di[6], di32 = di[7], di33 = di[8];
-    const double tau = df_point_tau(a, ba.drs, p, di);
+    const Df2 taud = df_point_tau(a, ba.drs, p, di, range_bad);
     const Df2 vxd = df_from_double_chk(vx, range_bad);
     const Df2 vyd = df_from_double_chk(vy, range_bad);
     const Df2 vzd = df_from_double_chk(vz, range_bad);
     const Df2 pd = df_from_double_chk(pdec, range_bad);
-    const Df2 taud = df_from_double_chk(tau, range_bad);
 #pragma unroll 2
     for (int j = 0; j < 8; j++) {
       DfAcc ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
@@ -933,7 +999,7 @@ __device__ __forceinline__ Df2 ld_pair(const float2 *p) {
 // elem_build_df_kernel does.  A value outside the pairs' safe window sets
 // bit 2 of the flag (the host redoes the build with FP64 rows).
 template <bool SPLIT>
-__global__ void __launch_bounds__(64, 8) elem_build_geo_kernel(OpArgs a, BuildArgs ba) {
+__global__ void __launch_bounds__(64, SPLIT ? 12 : 16) elem_build_geo_kernel(OpArgs a, BuildArgs ba) {
   __shared__ GeoBuildSmem sm;
   fill_df_tables(sm.tab, nullptr);
   const int lane8 = threadIdx.x & 7;
@@ -975,12 +1041,11 @@ __global__ void __launch_bounds__(64, 8) elem_build_geo_kernel(OpArgs a, BuildAr
 #pragma unroll
     for (int k = 0; k < 9; k++) di[k] = ld_pair(ba.gJi + (size_t)(9 * q + k) * E + p);
     const Df2 djq = ld_pair(ba.gDj + (size_t)q * E + p);
-    const double tau = df_point_tau(a, ba.drs, p, di);
+    const Df2 taud = df_point_tau(a, ba.drs, p, di, range_bad);
     const Df2 vxd = df_from_double_chk(vx, range_bad);
     const Df2 vyd = df_from_double_chk(vy, range_bad);
     const Df2 vzd = df_from_double_chk(vz, range_bad);
     const Df2 pd = df_from_double_chk(pdec, range_bad);
-    const Df2 taud = df_from_double_chk(tau, range_bad);
     Df2 w[3];  // J^-1 v
 #pragma unroll
     for (int r = 0; r < 3; r++) {
@@ -1278,11 +1343,16 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
     elem_build_kernel<double><<<grid, 64, 0, s>>>(a, ba);
   else {
     if (!ba.drs) return cudaErrorInvalidValue;
-    static std::once_flag carveout;  // 8 blocks of 27.5 KB need the full carveout
+    static std::once_flag carveout;  // 8 blocks of 27.5 KB need the full carveout,
     std::call_once(carveout, [] {
       cudaFuncSetAttribute(elem_build_df_kernel<true>,
                            cudaFuncAttributePreferredSharedMemoryCarveout, 100);
       cudaFuncSetAttribute(elem_build_df_kernel<false>,
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      // 12 / 16 blocks of 10.5 KB
+      cudaFuncSetAttribute(elem_build_geo_kernel<true>,
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      cudaFuncSetAttribute(elem_build_geo_kernel<false>,
                            cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     });
     const int g2 = (int)std::min<long>(((long)a.E + 255) / 256, (long)device_sm_count() * 8);
@@ -1301,6 +1371,21 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
   }
   count_launches(1);
   return cudaGetLastError();
+}
+
+cudaError_t diag_beta_vf(int n, const double *pe, double *beta) {
+  if (n <= 0) return cudaSuccess;
+  double *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(double) * 2 * (size_t)n);
+  if (e) return e;
+  if (!(e = cudaMemcpy(d, pe, sizeof(double) * n, cudaMemcpyHostToDevice))) {
+    beta_vf_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n);
+    count_launches(1);
+    if (!(e = cudaGetLastError()))
+      e = cudaMemcpy(beta, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(d);
+  return e;
 }
 
 cudaError_t launch_geo_factors(const OpArgs &a, const GeoFactors &g, int *bad,

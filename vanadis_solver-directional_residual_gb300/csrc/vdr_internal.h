@@ -339,6 +339,8 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
 // outside the pairs' safe window (the factors are then not to be used).
 cudaError_t launch_geo_factors(const OpArgs &a, const GeoFactors &g, int *bad,
                                cudaStream_t s);
+// The build's double-float beta of the VF variant on n host values.
+cudaError_t diag_beta_vf(int n, const double *pe, double *beta);
 cudaError_t launch_mf_apply(const OpArgs &a, bool fp32, bool transpose,
                             const double *x, double *y, const int *skip,
                             const int *skip2, cudaStream_t s);
