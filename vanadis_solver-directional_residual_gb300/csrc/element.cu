@@ -973,16 +973,29 @@ __global__ void __launch_bounds__(64) geo_factors_kernel(OpArgs a, GeoFactors g,
 }
 
 struct GeoBuildSmem {
-  Df2 dw[ROWS_EPB][8][8];  // per element, point q, node j: detJ W_j
-  Df2 c[ROWS_EPB][8][8];   // SPLIT: v.gradN_j + P N_j; otherwise
-                           // aH v.gradN_j + (aH P + aM) N_j
-  Df2 told[ROWS_EPB][8];   // T_old at the nodes times 2^-shift
-  Df2 tab[8][4][8];        // N, dN/dxi, dN/deta, dN/dzeta at the 8 points
+  // per element, point q, node j: detJ W_j and c_j (SPLIT: v.gradN_j + P N_j;
+  // otherwise aH v.gradN_j + (aH P + aM) N_j), read by the row lanes two
+  // nodes per 16-byte load
+  __align__(16) Df2 dw[ROWS_EPB][8][8];
+  __align__(16) Df2 c[ROWS_EPB][8][8];
+  __align__(16) Df2 told[ROWS_EPB][8];  // T_old at the nodes times 2^-shift
+  __align__(16) float4 qt[8][8][2];     // point q, node j: (N, dN/dxi), (dN/deta, dN/dzeta)
+  __align__(16) Df2 nt[8][8];           // N_j at point q
 };
 
 __device__ __forceinline__ Df2 ld_pair(const float2 *p) {
   const float2 v = __ldg(p);
   return Df2{v.x, v.y};
+}
+
+// Two consecutive pairs (16-byte aligned) from shared memory.
+__device__ __forceinline__ void lds_pairs(const Df2 *p, Df2 &a, Df2 &b) {
+  const float4 v = *reinterpret_cast<const float4 *>(p);
+  a = Df2{v.x, v.y};
+  b = Df2{v.z, v.w};
+}
+__device__ __forceinline__ void sts_pairs(Df2 *p, Df2 a, Df2 b) {
+  *reinterpret_cast<float4 *>(p) = make_float4(a.h, a.l, b.h, b.l);
 }
 
 // The double-float build from the mesh's geometric factors.  With
@@ -1001,7 +1014,21 @@ __device__ __forceinline__ Df2 ld_pair(const float2 *p) {
 template <bool SPLIT>
 __global__ void __launch_bounds__(64, SPLIT ? 12 : 16) elem_build_geo_kernel(OpArgs a, BuildArgs ba) {
   __shared__ GeoBuildSmem sm;
-  fill_df_tables(sm.tab, nullptr);
+  if (threadIdx.x < 8) {
+    const int t = threadIdx.x;
+    double n[8], d0[8], d1[8], d2[8];
+    shape_at<double>(gauss_coord<double>(t, 0), gauss_coord<double>(t, 1),
+                     gauss_coord<double>(t, 2), n, d0, d1, d2);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const Df2 N = df_from_double(n[j]), a0 = df_from_double(d0[j]);
+      const Df2 a1 = df_from_double(d1[j]), a2 = df_from_double(d2[j]);
+      sm.qt[t][j][0] = make_float4(N.h, N.l, a0.h, a0.l);
+      sm.qt[t][j][1] = make_float4(a1.h, a1.l, a2.h, a2.l);
+      sm.nt[t][j] = N;
+    }
+  }
+  __syncthreads();
   const int lane8 = threadIdx.x & 7;
   const int le = threadIdx.x >> 3;
   const long E = a.E;
@@ -1056,25 +1083,32 @@ __global__ void __launch_bounds__(64, SPLIT ? 12 : 16) elem_build_geo_kernel(OpA
       w[r] = df_norm(acc);
     }
     const Df2 cm = SPLIT ? pd : df_add(df_mul(aHd, pd), aMd);
-    const Df2 *tn = sm.tab[q][0], *t0 = sm.tab[q][1], *t1 = sm.tab[q][2], *t2 = sm.tab[q][3];
-#pragma unroll 2
-    for (int j = 0; j < 8; j++) {
-      DfAcc aa{0.0f, 0.0f};
-      df_acc(aa, w[0], t0[j]);
-      df_acc(aa, w[1], t1[j]);
-      df_acc(aa, w[2], t2[j]);
-      const Df2 av = df_norm(aa);
-      DfAcc aw{0.0f, 0.0f};
-      df_acc_add(aw, tn[j]);
-      df_acc(aw, taud, av);
-      sm.dw[le][q][j] = df_mul(djq, df_norm(aw));
-      DfAcc ac{0.0f, 0.0f};
-      if constexpr (SPLIT)
-        df_acc_add(ac, av);
-      else
-        df_acc(ac, aHd, av);
-      df_acc(ac, cm, tn[j]);
-      sm.c[le][q][j] = df_norm(ac);
+#pragma unroll 1
+    for (int j = 0; j < 8; j += 2) {
+      Df2 dwv[2], cv[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const float4 u0 = sm.qt[q][j + h][0], u1 = sm.qt[q][j + h][1];
+        const Df2 N{u0.x, u0.y};
+        DfAcc aa{0.0f, 0.0f};
+        df_acc(aa, w[0], Df2{u0.z, u0.w});
+        df_acc(aa, w[1], Df2{u1.x, u1.y});
+        df_acc(aa, w[2], Df2{u1.z, u1.w});
+        const Df2 av = df_norm(aa);
+        DfAcc aw{0.0f, 0.0f};
+        df_acc_add(aw, N);
+        df_acc(aw, taud, av);
+        dwv[h] = df_mul(djq, df_norm(aw));
+        DfAcc ac{0.0f, 0.0f};
+        if constexpr (SPLIT)
+          df_acc_add(ac, av);
+        else
+          df_acc(ac, aHd, av);
+        df_acc(ac, cm, N);
+        cv[h] = df_norm(ac);
+      }
+      sts_pairs(&sm.dw[le][q][j], dwv[0], dwv[1]);
+      sts_pairs(&sm.c[le][q][j], cv[0], cv[1]);
     }
     const double vol = group8_sum<double>(df_to_double(djq.h, djq.l));
     __syncwarp();
@@ -1101,9 +1135,17 @@ __global__ void __launch_bounds__(64, SPLIT ? 12 : 16) elem_build_geo_kernel(OpA
       df_acc_add(fw, dwi);
       if (!need_rows) continue;
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        df_acc(accH[j], dwi, sm.c[le][r][j]);
-        if constexpr (SPLIT) df_acc(accM[j], dwi, sm.tab[r][0][j]);
+      for (int j = 0; j < 8; j += 2) {
+        Df2 c0, c1;
+        lds_pairs(&sm.c[le][r][j], c0, c1);
+        df_acc(accH[j], dwi, c0);
+        df_acc(accH[j + 1], dwi, c1);
+        if constexpr (SPLIT) {
+          Df2 n0, n1;
+          lds_pairs(&sm.nt[r][j], n0, n1);
+          df_acc(accM[j], dwi, n0);
+          df_acc(accM[j + 1], dwi, n1);
+        }
       }
     }
     if (!valid) continue;
