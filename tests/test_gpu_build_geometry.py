@@ -78,7 +78,15 @@ def build_all(vdr, prob, mode, store, aH, aM, cf, rM, t_old):
         d = s.diag()
         b2 = s.assemble_rhs(cf, rM, t_old)  # RHS alone, operator valid
         status = s.geometry_status()
-    return bb, b, d, b2, status
+        # a rebuild is four launches (per-element scalars, build, Dirichlet
+        # fix of the diagonal, element masks): no redo with FP64 rows (a
+        # value outside the pair window, such as a Gaussian source's far
+        # tail, must not send the build there)
+        s.set_operator(aH, aM)
+        n0 = vdr.kernel_launch_count()
+        s.assemble_rhs(cf, rM, t_old)
+        launches = vdr.kernel_launch_count() - n0
+    return bb, b, d, b2, status, launches
 
 
 @pytest.mark.parametrize("store", ["df", "fp64"])
@@ -94,7 +102,8 @@ def test_cached_build_matches_recompute_and_oracle(vdr, oracle, gpu_lib, problem
     bb_ref, b_ref, d_ref = oracle_system(oracle, prob, aH, aM, cf, rM, t_old)
     got = {mode: build_all(vdr, prob, mode, store, aH, aM, cf, rM, t_old)
            for mode in ("auto", "recompute")}
-    for mode, (bb, b, d, b2, status) in got.items():
+    for mode, (bb, b, d, b2, status, launches) in got.items():
+        assert launches == 4, (name, mode, launches)
         assert rel_l2(bb, bb_ref) < TOL, (name, mode)
         assert rel_l2(b, b_ref) < TOL, (name, mode)
         assert rel_l2(b2, b_ref) < TOL, (name, mode)
@@ -104,8 +113,12 @@ def test_cached_build_matches_recompute_and_oracle(vdr, oracle, gpu_lib, problem
     assert got["recompute"][4] == (0, 0)
     bb_a, bb_r = got["auto"][0], got["recompute"][0]
     scale = np.abs(bb_r).max()
-    assert np.abs(bb_a - bb_r).max() <= TOL_MODES * scale, name
-    assert rel_l2(got["auto"][1], got["recompute"][1]) < TOL_MODES
+    # GP's beta(Pe) is coth(Pe) - 1/Pe through exp in FP64 (the variant's
+    # own form), which magnifies its input's rounding by ~3/Pe^2 at small Pe:
+    # the two builds form Pe with different roundings
+    tol = 1e-12 if prob.variant == vdr.problems.DR_GP else TOL_MODES
+    assert np.abs(bb_a - bb_r).max() <= tol * scale, name
+    assert rel_l2(got["auto"][1], got["recompute"][1]) < tol
 
 
 def test_robin_term_takes_the_recompute_build(vdr, oracle, gpu_lib):

@@ -232,9 +232,12 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
       const int gst = ensure_geometry(h, &geo);
       if (gst) return gst;
       if (geo) {
+        if ((e = dalloc(&h.gsc, (size_t)h.E * 10)))
+          return cuda_fail(e, "alloc element scalars");
         ba.gJi = h.geo.Ji;
         ba.gDj = h.geo.Dj;
         ba.gK = h.geo.K;
+        ba.gsc = h.gsc;
       }
     }
     if ((e = cudaMemsetAsync(h.flag, 0, sizeof(int), h.stream)))
@@ -394,6 +397,7 @@ void free_handle(Handle &h) {
   dfree(h.gcr_work); dfree(h.stage_d); dfree(h.drs); dfree(h.work32);
   dfree(h.Mhi); dfree(h.Mlo); dfree(h.Fvec); dfree(h.rhs_tmp); dfree(h.massw);
   free_geometry(h);
+  dfree(h.gsc);
   if (h.graph32) cudaGraphExecDestroy(h.graph32);
   if (h.gcr_graph) cudaGraphExecDestroy(h.gcr_graph);
   dfree(h.seg_d); dfree(h.seg_i); dfree(h.seg_ticket); dfree(h.seg_of_elem);

@@ -594,7 +594,8 @@ __device__ __forceinline__ Df2 df_point_tau(const OpArgs &a, const double *drs, 
 
 // Lane i's output of the double-float builds, from its accumulated rows:
 // accH = A_e row i (!SPLIT) or H row i (SPLIT, with accM = M row i),
-// fw = int W_i dOmega, vol = the element volume.  Writes the element-matrix
+// fw = int W_i dOmega, qe = the element's source Q, vol = the element
+// volume.  Writes the element-matrix
 // store (double-float pairs, or FP64 rows), diag += A_ii, the M store, phi,
 // f and b += cf f_i - ((H - rM M) T_old)_i as the BuildArgs ask; told is the
 // element's T_old at the nodes scaled by 2^-tshift.
@@ -602,7 +603,7 @@ template <bool SPLIT>
 __device__ __forceinline__ void df_rows_out(const OpArgs &a, const BuildArgs &ba, long p,
                                             int i, int ci, DfAcc (&accH)[8],
                                             DfAcc (&accM)[SPLIT ? 8 : 1], const DfAcc &fw,
-                                            double vol, Df2 aHd, Df2 aMd, Df2 nrMd,
+                                            double qe, double vol, Df2 aHd, Df2 aMd, Df2 nrMd,
                                             const Df2 *told, int tshift) {
   const long E = a.E;
   if (ba.Ahi && !ba.A64) {
@@ -670,14 +671,11 @@ __device__ __forceinline__ void df_rows_out(const OpArgs &a, const BuildArgs &ba
       if (badm) atomicOr(ba.bad, 4);
     }
   }
-  if (ba.phi) ba.phi[(size_t)i * E + p] = df_to_double(fw.s, fw.c) / vol;
-  if (ba.f && ci >= 0) {
-    const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
-    atomicAdd(ba.f + ci, (qe / vol) * df_to_double(fw.s, fw.c));
-  }
+  const double fwd = df_to_double(fw.s, fw.c);
+  if (ba.phi) ba.phi[(size_t)i * E + p] = fwd / vol;
+  if (ba.f && ci >= 0) atomicAdd(ba.f + ci, (qe / vol) * fwd);
   if (ba.b && ci >= 0) {
-    const double qe = a.f.q ? __ldg(a.f.q + p) : 0.0;
-    double val = ba.cf * ((qe / vol) * df_to_double(fw.s, fw.c));
+    double val = ba.cf * ((qe / vol) * fwd);
     if (SPLIT && ba.told) {
       // (H - rM M) T_old in double-float on the scaled T_old, scaled back
       DfAcc ft{0.0f, 0.0f};
@@ -871,7 +869,8 @@ __global__ void __launch_bounds__(64, 8) elem_build_df_kernel(OpArgs a, BuildArg
       }
     }
     if (!valid) continue;
-    df_rows_out<SPLIT>(a, ba, p, i, ck, accH, accM, fw, vol, aHd, aMd, nrMd, sm.told[le],
+    const double qe = (a.f.q && (ba.f || ba.b)) ? __ldg(a.f.q + p) : 0.0;
+    df_rows_out<SPLIT>(a, ba, p, i, ck, accH, accM, fw, qe, vol, aHd, aMd, nrMd, sm.told[le],
                        tshift);
   }
   // Any out-of-window value: the host redoes this build with the FP64 rows
@@ -972,6 +971,123 @@ __global__ void __launch_bounds__(64) geo_factors_kernel(OpArgs a, GeoFactors g,
   if (range_bad) atomicOr(bad, 2);
 }
 
+__device__ __forceinline__ Df2 ld_pair(const float2 *p) {
+  const float2 v = __ldg(p);
+  return Df2{v.x, v.y};
+}
+
+// Per-element scalars of the geometric-factor build as double-float pairs,
+// one thread per element in FP64 (the operations of elem_dr_scalars_kernel):
+// sc[k E + p] for k = 0..2 velocity, 3 lambda, 4 decay rate; OT: 5 tau; GP
+// and VF: 5..7 e = v/|v|, 8 kpe = |v|/(2 lambda_s), 9 khalf = 0.5/|v| (kpe
+// and khalf zero where Pe is zero at every point).  A value outside the
+// pairs' safe window sets bit 2 of *bad (the source stays FP64: its
+// Gaussian tails reach far below that window).
+__global__ void __launch_bounds__(256) elem_geo_scalars_kernel(OpArgs a, float2 *__restrict__ sc,
+                                                               int *bad) {
+  const long E = a.E;
+  const double eps = 1.0e-14;
+  bool range_bad = false;
+  auto put = [&](int k, long p, double v, bool chk) {
+    const Df2 d = chk ? df_from_double_chk(v, range_bad) : df_from_double(v);
+    sc[(size_t)k * E + p] = make_float2(d.h, d.l);
+  };
+  for (long p = (long)blockIdx.x * blockDim.x + threadIdx.x; p < E;
+       p += (long)gridDim.x * blockDim.x) {
+    const double vx = __ldg(a.f.vel + p), vy = __ldg(a.f.vel + E + p),
+                 vz = __ldg(a.f.vel + 2 * E + p);
+    const double lam = __ldg(a.f.lam + p);
+    put(0, p, vx, true);
+    put(1, p, vy, true);
+    put(2, p, vz, true);
+    put(3, p, lam, true);
+    put(4, p, a.f.pdec ? __ldg(a.f.pdec + p) : 0.0, true);
+    const double vmag = sqrt(vx * vx + vy * vy + vz * vz);
+    if (a.variant == DR_OT) {
+      const int n0 = __ldg(a.conn + p) & NODE_BITS;
+      const int n1 = __ldg(a.conn + (size_t)1 * E + p) & NODE_BITS;
+      const int n3 = __ldg(a.conn + (size_t)3 * E + p) & NODE_BITS;
+      const int n4 = __ldg(a.conn + (size_t)4 * E + p) & NODE_BITS;
+      const double h = dr_h_axes<double>(
+          vx, vy, vz, vmag, fabs(__ldg(a.xx + n1) - __ldg(a.xx + n0)),
+          fabs(__ldg(a.yy + n3) - __ldg(a.yy + n0)),
+          fabs(__ldg(a.zz + n4) - __ldg(a.zz + n0)));
+      put(5, p, dr_tau_from<double>(DR_OT, h, vmag, lam), true);
+    } else {
+      double ex = 0.0, ey = 0.0, ez = 0.0, iv = 0.0;
+      if (vmag > eps) {
+        iv = 1.0 / vmag;
+        ex = vx * iv;
+        ey = vy * iv;
+        ez = vz * iv;
+      }
+      const double lams =
+          (a.variant == DR_VF) ? (lam * ex * ex + lam * ey * ey + lam * ez * ez) : lam;
+      const bool on = vmag > eps && lams > eps;
+      put(5, p, ex, false);
+      put(6, p, ey, false);
+      put(7, p, ez, false);
+      put(8, p, on ? vmag / (2.0 * lams) : 0.0, true);
+      put(9, p, on ? 0.5 * iv : 0.0, true);
+    }
+  }
+  if (range_bad) atomicOr(bad, 2);
+}
+
+// 1/sqrt(a) for a positive normal pair: the FP32 estimate refined once in
+// FP32 and once in double-float (Newton's y (3 - a y^2) / 2 with the
+// residual 1 - a y^2 formed from the exact square of y); relative error
+// ~2^-47.
+__device__ __forceinline__ Df2 df_rsqrt(Df2 a) {
+  float y = rsqrtf(a.h);
+  y = __fmul_rn(y, __fmaf_rn(-0.5f * a.h * y, y, 1.5f));
+  const float p = __fmul_rn(y, y);
+  const Df2 r = df_sub(Df2{1.0f, 0.0f}, df_mul(a, Df2{p, __fmaf_rn(y, y, -p)}));
+  const float c = __fmul_rn(0.5f * y, r.h);
+  const float s = __fadd_rn(y, c);
+  return Df2{s, __fsub_rn(c, __fsub_rn(s, y))};
+}
+
+// tau at one Gauss point from the pair scalars of elem_geo_scalars_kernel,
+// di = J^-1 at the point: as df_point_tau with h = 2/|J^-1 e|, Pe = h kpe
+// and h khalf in double-float.
+__device__ __forceinline__ Df2 df_point_tau_pairs(int variant, const float2 *sc, long E,
+                                                  long p, const Df2 (&di)[9],
+                                                  bool &range_bad) {
+  const Df2 zero{0.0f, 0.0f};
+  if (variant == DR_OT) return ld_pair(sc + 5 * E + p);
+  const Df2 ex = ld_pair(sc + 5 * E + p), ey = ld_pair(sc + 6 * E + p),
+            ez = ld_pair(sc + 7 * E + p);
+  DfAcc gxa{0.0f, 0.0f}, gya{0.0f, 0.0f}, gza{0.0f, 0.0f};
+  df_acc(gxa, di[0], ex);
+  df_acc(gxa, di[1], ey);
+  df_acc(gxa, di[2], ez);
+  df_acc(gya, di[3], ex);
+  df_acc(gya, di[4], ey);
+  df_acc(gya, di[5], ez);
+  df_acc(gza, di[6], ex);
+  df_acc(gza, di[7], ey);
+  df_acc(gza, di[8], ez);
+  const Df2 gx = df_norm(gxa), gy = df_norm(gya), gz = df_norm(gza);
+  DfAcc n2{0.0f, 0.0f};
+  df_acc(n2, gx, gx);
+  df_acc(n2, gy, gy);
+  df_acc(n2, gz, gz);
+  const Df2 g2 = df_norm(n2);
+  if (!(g2.h > 1.0e-28f)) return zero;  // h = 0
+  const Df2 rs = df_rsqrt(g2);
+  const Df2 h{2.0f * rs.h, 2.0f * rs.l};
+  Df2 pe = df_mul(h, ld_pair(sc + 8 * E + p));
+  if (!(pe.h > 1.0e-12f)) return zero;
+  const Df2 hk = df_mul(h, ld_pair(sc + 9 * E + p));
+  if (variant == DR_VF) {
+    if (!(pe.h < 1.0e30f)) pe = Df2{1.0e30f, 0.0f};  // beta = 1 - 1/Pe there
+    return df_mul(hk, df_beta_vf(pe));
+  }
+  return df_from_double_chk(df_to_double(hk.h, hk.l) * beta_exp(df_to_double(pe.h, pe.l)),
+                            range_bad);
+}
+
 struct GeoBuildSmem {
   // per element, point q, node j: detJ W_j and c_j (SPLIT: v.gradN_j + P N_j;
   // otherwise aH v.gradN_j + (aH P + aM) N_j), read by the row lanes two
@@ -982,11 +1098,6 @@ struct GeoBuildSmem {
   __align__(16) float4 qt[8][8][2];     // point q, node j: (N, dN/dxi), (dN/deta, dN/dzeta)
   __align__(16) Df2 nt[8][8];           // N_j at point q
 };
-
-__device__ __forceinline__ Df2 ld_pair(const float2 *p) {
-  const float2 v = __ldg(p);
-  return Df2{v.x, v.y};
-}
 
 // Two consecutive pairs (16-byte aligned) from shared memory.
 __device__ __forceinline__ void lds_pairs(const Df2 *p, Df2 &a, Df2 &b) {
@@ -1037,7 +1148,7 @@ __global__ void __launch_bounds__(64, SPLIT ? 12 : 16) elem_build_geo_kernel(OpA
   const Df2 aMd = df_from_double_chk(ba.aM, range_bad);
   const Df2 nrMd = df_neg(df_from_double_chk(SPLIT ? ba.rM : 0.0, range_bad));
   const bool need_rows = SPLIT || ba.Ahi || ba.A64 || ba.diag;
-  const double *V = a.f.vel;
+  const float2 *sc = ba.gsc;
   for (long base = (long)blockIdx.x * ROWS_EPB; base < E;
        base += (long)gridDim.x * ROWS_EPB) {
     const long pe = base + le;
@@ -1059,20 +1170,15 @@ __global__ void __launch_bounds__(64, SPLIT ? 12 : 16) elem_build_geo_kernel(OpA
       df_split(tk, t.h, t.l, range_bad, tshift);  // inf/NaN: bad
       sm.told[le][lane8] = t;
     }
-    const double vx = __ldg(V + p), vy = __ldg(V + E + p), vz = __ldg(V + 2 * E + p);
-    const double lam = __ldg(a.f.lam + p);
-    const double pdec = a.f.pdec ? __ldg(a.f.pdec + p) : 0.0;
+    const Df2 vxd = ld_pair(sc + p), vyd = ld_pair(sc + E + p), vzd = ld_pair(sc + 2 * E + p);
+    const Df2 pd = ld_pair(sc + 4 * E + p);
     // ---- lane q = Gauss point q
     const int q = lane8;
     Df2 di[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) di[k] = ld_pair(ba.gJi + (size_t)(9 * q + k) * E + p);
     const Df2 djq = ld_pair(ba.gDj + (size_t)q * E + p);
-    const Df2 taud = df_point_tau(a, ba.drs, p, di, range_bad);
-    const Df2 vxd = df_from_double_chk(vx, range_bad);
-    const Df2 vyd = df_from_double_chk(vy, range_bad);
-    const Df2 vzd = df_from_double_chk(vz, range_bad);
-    const Df2 pd = df_from_double_chk(pdec, range_bad);
+    const Df2 taud = df_point_tau_pairs(a.variant, sc, E, p, di, range_bad);
     Df2 w[3];  // J^-1 v
 #pragma unroll
     for (int r = 0; r < 3; r++) {
@@ -1110,7 +1216,12 @@ __global__ void __launch_bounds__(64, SPLIT ? 12 : 16) elem_build_geo_kernel(OpA
       sts_pairs(&sm.dw[le][q][j], dwv[0], dwv[1]);
       sts_pairs(&sm.c[le][q][j], cv[0], cv[1]);
     }
-    const double vol = group8_sum<double>(df_to_double(djq.h, djq.l));
+    // element volume as a pair (the same sum in every lane: TwoSum is exact
+    // in either order)
+    Df2 vol = djq;
+#pragma unroll
+    for (int m = 1; m < 8; m <<= 1)
+      vol = df_add(vol, Df2{__shfl_xor_sync(FULL, vol.h, m), __shfl_xor_sync(FULL, vol.l, m)});
     __syncwarp();
     // ---- lane i = row i
     const int i = lane8;
@@ -1121,7 +1232,7 @@ __global__ void __launch_bounds__(64, SPLIT ? 12 : 16) elem_build_geo_kernel(OpA
     for (int j = 0; j < (SPLIT ? 8 : 1); j++) accM[j] = DfAcc{0.0f, 0.0f};
     DfAcc fw{0.0f, 0.0f};
     if (need_rows) {
-      const Df2 lamd = df_from_double_chk(lam, range_bad);
+      const Df2 lamd = ld_pair(sc + 3 * E + p);
       const Df2 lk = SPLIT ? lamd : df_mul(aHd, lamd);
 #pragma unroll
       for (int j = 0; j < 8; j++) {
@@ -1149,7 +1260,9 @@ __global__ void __launch_bounds__(64, SPLIT ? 12 : 16) elem_build_geo_kernel(OpA
       }
     }
     if (!valid) continue;
-    df_rows_out<SPLIT>(a, ba, p, i, ck, accH, accM, fw, vol, aHd, aMd, nrMd, sm.told[le],
+    const double qe = (a.f.q && (ba.f || ba.b)) ? __ldg(a.f.q + p) : 0.0;
+    df_rows_out<SPLIT>(a, ba, p, i, ck, accH, accM, fw, qe, df_to_double(vol.h, vol.l), aHd,
+                       aMd, nrMd, sm.told[le],
                        tshift);
   }
   if (range_bad) atomicOr(ba.bad, 2);
@@ -1398,16 +1511,19 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
                            cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     });
     const int g2 = (int)std::min<long>(((long)a.E + 255) / 256, (long)device_sm_count() * 8);
-    elem_dr_scalars_kernel<<<g2, 256, 0, s>>>(a, ba.drs);
     if (ba.gK) {  // from the mesh's geometric factors
+      if (!ba.gsc) return cudaErrorInvalidValue;
+      elem_geo_scalars_kernel<<<g2, 256, 0, s>>>(a, ba.gsc, ba.bad);
       if (ba.told || ba.Mhi)
         elem_build_geo_kernel<true><<<grid, 64, 0, s>>>(a, ba);
       else
         elem_build_geo_kernel<false><<<grid, 64, 0, s>>>(a, ba);
-    } else if (ba.told || ba.Mhi) {  // H and M apart
-      elem_build_df_kernel<true><<<grid, 64, 0, s>>>(a, ba);
     } else {
-      elem_build_df_kernel<false><<<grid, 64, 0, s>>>(a, ba);
+      elem_dr_scalars_kernel<<<g2, 256, 0, s>>>(a, ba.drs);
+      if (ba.told || ba.Mhi)  // H and M apart
+        elem_build_df_kernel<true><<<grid, 64, 0, s>>>(a, ba);
+      else
+        elem_build_df_kernel<false><<<grid, 64, 0, s>>>(a, ba);
     }
     count_launches(1);
   }

@@ -238,6 +238,7 @@ struct Handle {
   size_t h_stage_bytes = 0;
   double *stage_d = nullptr;  // [3E] device staging of uploaded fields
   double *drs = nullptr;      // [5E] per-element DR scalars of the build
+  float2 *gsc = nullptr;      // [10E] the same as pairs, with the fields (geometric-factor build)
   // time loop: the mass matrix M (double-float store) and the source vector
   // F = sum_e f_e of the current fields, so that later steps form their
   // right-hand side from two applies; rhs_tmp holds A T and M T
@@ -328,6 +329,7 @@ struct BuildArgs {
   // the mesh's geometric factors (element.cu, GeoFactors): given, the
   // double-float build reads them instead of recomputing the Jacobians
   const float2 *gJi = nullptr, *gDj = nullptr, *gK = nullptr;
+  float2 *gsc = nullptr;  // [10][E] per-element scalars of that build, as pairs
 };
 
 
