@@ -203,7 +203,7 @@ def profile_value(name, key):
 # double-float rows, FP64 for the DR scalars): its roofline is the SMs'
 # issue rate, 4 warp instructions per SM per clock, against the warp
 # instructions per element that ncu counted for the kernel.
-BUILD_PROFILE = "elem_build_df_rotation_shear_128x128x64.md"
+BUILD_PROFILE = "elem_build_geo_rotation_shear_128x128x64.md"
 ISSUE_PER_SM_CLOCK = 4.0
 
 
@@ -1143,9 +1143,10 @@ def run_native(a):
                                "unit": "G warp instructions/s",
                                "frac": (build_issue / issue_peak
                                         if build_issue else None),
-                               "kernel": "elem_build_df_kernel (element "
-                                         "matrices + diag + RHS; H/M rows "
-                                         "in double-float on the FP32 pipe)",
+                               "kernel": "elem_build_geo_kernel (element "
+                                         "matrices + diag + RHS from the "
+                                         "mesh's geometric factors; rows in "
+                                         "double-float on the FP32 pipe)",
                                "warp_instructions_per_element": inst_per_elem,
                                "peak_kind": "%d SMs x 4 warp instructions "
                                             "per clock at the median SM "
