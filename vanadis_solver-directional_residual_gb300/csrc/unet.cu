@@ -250,46 +250,76 @@ __global__ void __launch_bounds__(128) conv3_kernel(ConvArgs a) {
 // dW[tap][co][ci] += sum_v dY'[v][co] X[v + off(tap)][ci], an implicit GEMM
 // with M = output channels, N = input channels, K = voxels (16 per MMA),
 // X = [in1 | up(in2)].  dY' (the ReLU-masked output gradient) is first
-// written transposed in BF16, dyt[co][v], so that A fragments load as
-// pairs of consecutive voxels; B fragments are single loads of the shifted
-// inputs.  Grid: (voxel chunks, 27 taps, groups of NG input-channel
-// tiles); a block's chunk is a range of 16-voxel x-row segments, each warp
-// takes every fourth one, and adds its tile to dW with atomics.  db
-// accumulates in the centre-tap blocks.
+// written transposed in BF16, dyt[co][v] with rows of Vp = V rounded up to
+// 16 voxels (zero past V), so that A fragments load as aligned pairs of
+// consecutive voxels; B fragments come from the shifted inputs staged in
+// shared memory.  Grid: (voxel chunks, 27 taps, groups of NG input-channel
+// tiles); a block's chunk is a range of 16-voxel k-steps of the flat voxel
+// index, each warp takes every fourth one, and adds its tile to dW with
+// atomics.  db accumulates in the centre-tap blocks.
 struct WgArgs {
   const bf16 *in1, *in2;
-  const bf16 *dyt;  // [COUT][V]
+  const bf16 *dyt;  // [COUT][Vp]
   float *dw, *db;
   int W, H, D, Wc, Hc;
-  long V, chunk;
+  long V, Vp, chunk;
 };
 
 template <int C>
-__global__ void mask_transpose(const float *dy, const bf16 *y, bf16 *dyt, long V) {
+__global__ void mask_transpose(const float *dy, const bf16 *y, bf16 *dyt, long V, long Vp) {
   const long total = V * C;
   for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long)gridDim.x * blockDim.x) {
     const long v = idx / C;
     const int c = (int)(idx % C);
     const float d = __bfloat162float(y[idx]) > 0.f ? dy[idx] : 0.f;
-    dyt[(long)c * V + v] = __float2bfloat16_rn(d);
+    dyt[(long)c * Vp + v] = __float2bfloat16_rn(d);
   }
+  // the rows' tails past V (the buffer is shared by layers of other strides)
+  const long pad = Vp - V;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < pad * C;
+       idx += (long)gridDim.x * blockDim.x)
+    dyt[(idx / pad) * Vp + V + idx % pad] = __float2bfloat16_rn(0.f);
 }
 
+// Four 8x8 b16 matrices from shared memory, transposed (ldmatrix .trans):
+// lane l supplies the address of row l & 7 of matrix l >> 3.
+__device__ __forceinline__ void ldsm_x4_trans(const bf16 *p, uint32_t &r0, uint32_t &r1,
+                                              uint32_t &r2, uint32_t &r3) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(sa)
+               : "memory");
+}
+
+// Weight gradient of one tap: dW[tap][co][ci] = sum_v dY[co][v] X[v + off][ci]
+// as an MMA with K = voxels.  Per k-step (16 voxels of one x row) a warp
+// copies the 16 shifted voxels' channels of its n-tile group (NG units of 8
+// channels, 16 bytes each, channels-last rows) into a padded shared tile
+// and reads the B fragments from it with ldmatrix .trans; the next k-step's
+// rows are loaded while the current one is multiplied.  A fragments come
+// from the transposed, masked output gradient dyt[co][v].
 template <int CIN1, int CIN2, int COUT, int NG>
 __global__ void __launch_bounds__(128) conv3_wgrad_tc(WgArgs a) {
   constexpr int CIN = CIN1 + CIN2, MT = COUT / 16, NT = CIN / 8;
-  static_assert(COUT % 16 == 0 && CIN % 8 == 0, "shape");
+  static_assert(COUT % 16 == 0 && CIN % 8 == 0 && CIN1 % 8 == 0 && NG % 2 == 0, "shape");
+  // B tile per warp: 16 rows (voxels) x NG units, rows padded by one unit so
+  // that the 8 rows of one ldmatrix matrix fall on distinct banks
+  constexpr int RSTR = NG * 8 + 8;  // bf16 per row
+  constexpr int ITEMS = 16 * NG, PER_LANE = (ITEMS + 31) / 32;
+  __shared__ __align__(16) bf16 tile[4][16 * RSTR];
   const int tap = blockIdx.y;
   const int dz = tap / 9 - 1, dyy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
   const int ntile0 = blockIdx.z * NG;
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const int warp = threadIdx.x >> 5;
-  const long WH = (long)a.W * a.H;
-  // k-steps are 16-voxel segments of x rows: row = y + H z, segment s
-  // covers x in [16 s, 16 s + 16).
-  const int segs = (a.W + 15) >> 4;
-  const long nks = (long)a.H * a.D * segs;
+  bf16 *tw = tile[warp];
+  const int W = a.W, H = a.H, D = a.D;
+  const long WH = (long)W * H;
+  const long off = dx + (long)dyy * W + (long)dz * WH;  // the tap's voxel offset
+  // k-steps are 16 consecutive voxels of the flat index: vb = 16 ks
+  const long nks = (a.V + 15) >> 4;
   const long ks0 = (long)blockIdx.x * a.chunk;
   const long ks1 = nks < ks0 + a.chunk ? nks : ks0 + a.chunk;
   float acc[MT][NG][4];
@@ -300,72 +330,98 @@ __global__ void __launch_bounds__(128) conv3_wgrad_tc(WgArgs a) {
 #pragma unroll
       for (int q = 0; q < 4; q++) acc[mt][j][q] = 0.f;
   float dbs[MT][2] = {};
-  const int jv[4] = {2 * t, 2 * t + 1, 2 * t + 8, 2 * t + 9};
-  for (long ks = ks0 + warp; ks < ks1; ks += 4) {
-    const int row = (int)(ks / segs), seg = (int)(ks - (long)row * segs);
-    const int y = row % a.H, z = row / a.H, xs = seg << 4;
-    const long vb = (long)row * a.W + xs;
-    const int yn = y + dyy, zn = z + dz;
-    const bool rowok = yn >= 0 && yn < a.H && zn >= 0 && zn < a.D;
-    const long crow = (long)a.Wc * ((yn >> 1) + (long)a.Hc * (zn >> 1));
-    long nf[4], nc[4];
-    bool vin[4];
+  // (x, y, z) of the warp's next k-step's first voxel, advanced by 64
+  // voxels per step without divisions
+  long ks = ks0 + warp;
+  int x0 = 0, y0 = 0, z0 = 0;
+  if (ks < ks1) {
+    const long vb = ks << 4;
+    z0 = (int)(vb / WH);
+    const long rem = vb - (long)z0 * WH;
+    y0 = (int)(rem / W);
+    x0 = (int)(rem - (long)y0 * W);
+  }
+  // the B rows of a k-step: item idx = lane + 32 k is voxel idx / NG, unit
+  // idx % NG of the group (zero outside the volume and past CIN)
+  auto load_rows = [&](long vb, int xb, int yb, int zb, uint4 (&sv)[PER_LANE]) {
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int x = xs + jv[u];
-      vin[u] = x < a.W;
-      const int xn = x + dx;
-      const bool ok = rowok && vin[u] && xn >= 0 && xn < a.W;
-      nf[u] = ok ? vb + jv[u] + dx + (long)dyy * a.W + (long)dz * WH : -1;
-      nc[u] = ok ? (long)(xn >> 1) + crow : -1;
+    for (int k = 0; k < PER_LANE; k++) {
+      const int idx = lane + 32 * k;
+      const int r = idx / NG, u = idx % NG;
+      int x = xb + r, y = yb, z = zb;
+      while (x >= W) {  // W may be below 16 on small grids
+        x -= W;
+        if (++y >= H) {
+          y = 0;
+          ++z;
+        }
+      }
+      const int xn = x + dx, yn = y + dyy, zn = z + dz, ch = (ntile0 + u) * 8;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (idx < ITEMS && vb + r < a.V && xn >= 0 && xn < W && yn >= 0 && yn < H &&
+          zn >= 0 && zn < D && ch < CIN) {
+        if (ch < CIN1)
+          v = *reinterpret_cast<const uint4 *>(a.in1 + (vb + r + off) * CIN1 + ch);
+        else if (CIN2 > 0)
+          v = *reinterpret_cast<const uint4 *>(
+              a.in2 + ((long)(xn >> 1) + (long)a.Wc * ((yn >> 1) + (long)a.Hc * (zn >> 1))) *
+                          (CIN2 > 0 ? CIN2 : 1) +
+              (ch - CIN1));
+      }
+      sv[k] = v;
     }
-    // A fragments: dyt[co][v] for v = vb + (2t, 2t+1) and vb + (2t+8, 2t+9)
+  };
+  uint4 sv[PER_LANE];
+  if (ks < ks1) load_rows(ks << 4, x0, y0, z0, sv);
+  for (; ks < ks1; ks += 4) {
+    const long vb = ks << 4;
+    __syncwarp();  // the previous k-step's ldmatrix reads are done
+#pragma unroll
+    for (int k = 0; k < PER_LANE; k++) {
+      const int idx = lane + 32 * k;
+      if (idx < ITEMS)
+        *reinterpret_cast<uint4 *>(tw + (idx / NG) * RSTR + (idx % NG) * 8) = sv[k];
+    }
+    __syncwarp();
+    x0 += 64;
+    while (x0 >= W) {
+      x0 -= W;
+      if (++y0 >= H) {
+        y0 = 0;
+        ++z0;
+      }
+    }
+    if (ks + 4 < ks1) load_rows(vb + 64, x0, y0, z0, sv);  // in flight during the MMAs
+    // A fragments: dyt[co][v] for v = vb + (2t, 2t+1) and vb + (2t+8, 2t+9),
+    // aligned pairs (rows of Vp, a multiple of 16; zero past V)
     uint32_t af[MT][4];
 #pragma unroll
     for (int mt = 0; mt < MT; mt++)
 #pragma unroll
       for (int h = 0; h < 2; h++) {  // rows g, g+8
-        const long base = (long)(mt * 16 + g + 8 * h) * a.V;
-        const bf16 *rp = a.dyt + base + vb;
-        uint32_t lo, hi;
-        const bool even = !((base + vb) & 1);  // 4-byte aligned pairs
-        if (vin[1] && even) {
-          lo = ld2(rp + 2 * t);
-        } else {
-          lo = pack2(vin[0] ? __bfloat162float(rp[2 * t]) : 0.f,
-                     vin[1] ? __bfloat162float(rp[2 * t + 1]) : 0.f);
-        }
-        if (vin[3] && even) {
-          hi = ld2(rp + 2 * t + 8);
-        } else {
-          hi = pack2(vin[2] ? __bfloat162float(rp[2 * t + 8]) : 0.f,
-                     vin[3] ? __bfloat162float(rp[2 * t + 9]) : 0.f);
-        }
+        const bf16 *rp = a.dyt + (long)(mt * 16 + g + 8 * h) * a.Vp + vb;
+        const uint32_t lo = ld2(rp + 2 * t), hi = ld2(rp + 2 * t + 8);
         af[mt][h] = lo;      // a0 (row g) / a1 (row g+8): k = 2t, 2t+1
         af[mt][2 + h] = hi;  // a2 / a3: k = 2t+8, 2t+9
         if (tap == 13 && blockIdx.z == 0)
           dbs[mt][h] += bf_lo(lo) + bf_hi(lo) + bf_lo(hi) + bf_hi(hi);
       }
+    // B fragments of n-tiles (j, j+1): matrices (rows 0-7, j), (rows 8-15, j),
+    // (rows 0-7, j+1), (rows 8-15, j+1)
 #pragma unroll
-    for (int j = 0; j < NG; j++) {
-      const int nt = ntile0 + j;
-      if (nt >= NT) break;
-      const int ci = nt * 8 + g;
-      float xv[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        xv[u] = 0.f;
-        if (ci < CIN1) {
-          if (nf[u] >= 0) xv[u] = __bfloat162float(a.in1[nf[u] * CIN1 + ci]);
-        } else if (CIN2 > 0) {
-          if (nc[u] >= 0)
-            xv[u] = __bfloat162float(a.in2[nc[u] * (CIN2 > 0 ? CIN2 : 1) + (ci - CIN1)]);
-        }
-      }
-      const uint32_t b0 = pack2(xv[0], xv[1]), b1 = pack2(xv[2], xv[3]);
+    for (int j = 0; j < NG; j += 2) {
+      if (ntile0 + j >= NT) break;
+      const int m = lane >> 3;
+      uint32_t b0, b1, b2, b3;
+      ldsm_x4_trans(tw + ((m & 1) * 8 + (lane & 7)) * RSTR + (j + (m >> 1)) * 8, b0, b1, b2, b3);
 #pragma unroll
       for (int mt = 0; mt < MT; mt++)
         mma_bf16(acc[mt][j], af[mt][0], af[mt][1], af[mt][2], af[mt][3], b0, b1);
+      if (ntile0 + j + 1 < NT) {
+#pragma unroll
+        for (int mt = 0; mt < MT; mt++)
+          mma_bf16(acc[mt][j + 1], af[mt][0], af[mt][1], af[mt][2], af[mt][3], b2, b3);
+      }
     }
   }
   // D fragment: rows co = g (c0, c1), g+8 (c2, c3); cols ci = 2t, 2t+1
@@ -950,13 +1006,16 @@ cudaError_t conv_launch(const ConvArgs &a, cudaStream_t s) {
 template <int CIN1, int CIN2, int COUT>
 cudaError_t wgrad_launch(const Net &n, WgArgs a, const float *dy, const bf16 *y,
                          cudaStream_t s) {
-  constexpr int CIN = CIN1 + CIN2, NT = CIN / 8;
-  constexpr int NG = NT < 4 ? NT : 4;
+  constexpr int CIN = CIN1 + CIN2, NT = CIN / 8, MT = COUT / 16;
+  // n-tiles per block: groups of 6 where they divide the channels evenly
+  // (no zero-filled units staged), else up to 4; at most 16 accumulator tiles
+  constexpr int NG = (NT % 6 == 0 && MT * 6 <= 16) ? 6 : (NT < 4 ? NT : 4);
   constexpr int NGROUPS = (NT + NG - 1) / NG;
   // masked, transposed BF16 output gradient (scratch sized for the largest)
-  mask_transpose<COUT><<<grid_for(a.V * COUT, 256), 256, 0, s>>>(dy, y, n.dyt, a.V);
+  a.Vp = (a.V + 15) & ~15L;
+  mask_transpose<COUT><<<grid_for(a.V * COUT, 256), 256, 0, s>>>(dy, y, n.dyt, a.V, a.Vp);
   a.dyt = n.dyt;
-  const long nks = (long)a.H * a.D * ((a.W + 15) / 16);  // 16-voxel row segments
+  const long nks = (a.V + 15) / 16;  // 16-voxel k-steps
   const long target = std::max<long>(1, (long)device_sm_count() * 8 / (27 * NGROUPS));
   long chunk = (nks + target - 1) / target;
   chunk = std::max<long>(16, ((chunk + 3) / 4) * 4);
@@ -1409,7 +1468,8 @@ extern "C" int vdr_net_create(vdr_handle *H, unsigned long long seed, vdr_net **
         (e = nalloc(n, &n.rbuf, V0)) || (e = nalloc(n, &n.zbuf, V0)) ||
         (e = nalloc(n, &n.qbuf, V0)) || (e = nalloc(n, &n.pbuf, V0)) ||
         (e = nalloc(n, &n.gbuf, V0)) || (e = nalloc(n, &n.dc, V0)) ||
-        (e = nalloc(n, &n.dyt, std::max(V0 * 16, V1 * 32))) ||
+        (e = nalloc(n, &n.dyt, std::max(std::max(((V0 + 15) & ~15L) * 16, ((V1 + 15) & ~15L) * 32),
+                                         ((V2 + 15) & ~15L) * 64))) ||
         (e = nalloc(n, &n.scal, 8)) || (e = nalloc(n, &n.partials, 2L * n.red_grid)) ||
         (e = nalloc(n, &n.ticket, 1)) || (e = nalloc(n, &n.wtc, off)) ||
         (e = nalloc(n, &n.up0, V0 * 32)) || (e = nalloc(n, &n.up1, V1 * 64)) ||
