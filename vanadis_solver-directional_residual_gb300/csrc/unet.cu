@@ -250,36 +250,42 @@ __global__ void __launch_bounds__(128) conv3_kernel(ConvArgs a) {
 // dW[tap][co][ci] += sum_v dY'[v][co] X[v + off(tap)][ci], an implicit GEMM
 // with M = output channels, N = input channels, K = voxels (16 per MMA),
 // X = [in1 | up(in2)].  dY' (the ReLU-masked output gradient) is first
-// written transposed in BF16, dyt[co][v] with rows of Vp = V rounded up to
-// 16 voxels (zero past V), so that A fragments load as aligned pairs of
-// consecutive voxels; B fragments come from the shifted inputs staged in
-// shared memory.  Grid: (voxel chunks, 27 taps, groups of NG input-channel
-// tiles); a block's chunk is a range of 16-voxel k-steps of the flat voxel
-// index, each warp takes every fourth one, and adds its tile to dW with
-// atomics.  db accumulates in the centre-tap blocks.
+// written transposed in BF16, dyt[co][row][x] with x rows padded to Wp, a
+// multiple of 16 voxels (zero past W), so that A fragments load as aligned
+// pairs of consecutive voxels; B fragments come from the shifted inputs
+// staged in shared memory.  Grid: (voxel chunks, 9 (dy, dz) pairs, groups
+// of NG input-channel tiles); a block's chunk is a range of 16-voxel x-row
+// segments, each warp takes every fourth one, and the three x-taps of the
+// pair share its staging and its A fragments; the tiles go to dW with
+// atomics.  db accumulates in the centre-pair blocks.
 struct WgArgs {
   const bf16 *in1, *in2;
-  const bf16 *dyt;  // [COUT][Vp]
+  const bf16 *dyt;  // [COUT][H D][Wp]
   float *dw, *db;
-  int W, H, D, Wc, Hc;
-  long V, Vp, chunk;
+  int W, H, D, Wc, Hc, Wp;
+  long V, Vp, chunk;  // Vp = H D Wp
 };
 
 template <int C>
-__global__ void mask_transpose(const float *dy, const bf16 *y, bf16 *dyt, long V, long Vp) {
+__global__ void mask_transpose(const float *dy, const bf16 *y, bf16 *dyt, long V, int W,
+                               int Wp, long Vp) {
   const long total = V * C;
   for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long)gridDim.x * blockDim.x) {
     const long v = idx / C;
     const int c = (int)(idx % C);
+    const long row = v / W;
     const float d = __bfloat162float(y[idx]) > 0.f ? dy[idx] : 0.f;
-    dyt[(long)c * Vp + v] = __float2bfloat16_rn(d);
+    dyt[(long)c * Vp + row * Wp + (v - row * W)] = __float2bfloat16_rn(d);
   }
-  // the rows' tails past V (the buffer is shared by layers of other strides)
-  const long pad = Vp - V;
-  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < pad * C;
-       idx += (long)gridDim.x * blockDim.x)
-    dyt[(idx / pad) * Vp + V + idx % pad] = __float2bfloat16_rn(0.f);
+  // the rows' padding past W (the buffer is shared by layers of other shapes)
+  const int pad = Wp - W;
+  const long rows = Vp / Wp;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < (long)pad * rows * C;
+       idx += (long)gridDim.x * blockDim.x) {
+    const long cr = idx / pad;  // c * rows + row
+    dyt[cr * Wp + W + (idx - cr * pad)] = __float2bfloat16_rn(0.f);
+  }
 }
 
 // Four 8x8 b16 matrices from shared memory, transposed (ldmatrix .trans):
@@ -293,88 +299,84 @@ __device__ __forceinline__ void ldsm_x4_trans(const bf16 *p, uint32_t &r0, uint3
                : "memory");
 }
 
-// Weight gradient of one tap: dW[tap][co][ci] = sum_v dY[co][v] X[v + off][ci]
-// as an MMA with K = voxels.  Per k-step (16 voxels of one x row) a warp
-// copies the 16 shifted voxels' channels of its n-tile group (NG units of 8
-// channels, 16 bytes each, channels-last rows) into a padded shared tile
-// and reads the B fragments from it with ldmatrix .trans; the next k-step's
-// rows are loaded while the current one is multiplied.  A fragments come
-// from the transposed, masked output gradient dyt[co][v].
+// Weight gradient of the three x-taps of one (dy, dz) pair:
+// dW[tap][co][ci] = sum_v dY[co][v] X[v + off(tap)][ci] as MMAs with K =
+// voxels.  A k-step is a 16-voxel segment of one x row; per k-step a warp
+// copies the 18 voxels xs-1 .. xs+16 of the shifted row (zero outside the
+// volume), NG units of 8 channels each (16-byte loads of channels-last
+// rows), into a padded shared tile, and tap dx reads its B fragments from
+// tile rows 1 + dx .. 16 + dx with ldmatrix .trans: one staging and one set
+// of A fragments for three taps.  The next k-step's rows are loaded while
+// the current one multiplies.
 template <int CIN1, int CIN2, int COUT, int NG>
 __global__ void __launch_bounds__(128) conv3_wgrad_tc(WgArgs a) {
   constexpr int CIN = CIN1 + CIN2, MT = COUT / 16, NT = CIN / 8;
   static_assert(COUT % 16 == 0 && CIN % 8 == 0 && CIN1 % 8 == 0 && NG % 2 == 0, "shape");
-  // B tile per warp: 16 rows (voxels) x NG units, rows padded by one unit so
+  // B tile per warp: 18 rows (voxels) x NG units, rows padded by one unit so
   // that the 8 rows of one ldmatrix matrix fall on distinct banks
   constexpr int RSTR = NG * 8 + 8;  // bf16 per row
-  constexpr int ITEMS = 16 * NG, PER_LANE = (ITEMS + 31) / 32;
-  __shared__ __align__(16) bf16 tile[4][16 * RSTR];
-  const int tap = blockIdx.y;
-  const int dz = tap / 9 - 1, dyy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+  constexpr int TROWS = 18, ITEMS = TROWS * NG, PER_LANE = (ITEMS + 31) / 32;
+  __shared__ __align__(16) bf16 tile[4][TROWS * RSTR];
+  const int pair = blockIdx.y;  // 3 (dz + 1) + (dy + 1)
+  const int dyy = pair % 3 - 1, dz = pair / 3 - 1;
   const int ntile0 = blockIdx.z * NG;
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const int warp = threadIdx.x >> 5;
   bf16 *tw = tile[warp];
   const int W = a.W, H = a.H, D = a.D;
-  const long WH = (long)W * H;
-  const long off = dx + (long)dyy * W + (long)dz * WH;  // the tap's voxel offset
-  // k-steps are 16 consecutive voxels of the flat index: vb = 16 ks
-  const long nks = (a.V + 15) >> 4;
+  const int segs = a.Wp >> 4;  // 16-voxel segments per (padded) x row
+  const long nks = (long)H * D * segs;
   const long ks0 = (long)blockIdx.x * a.chunk;
   const long ks1 = nks < ks0 + a.chunk ? nks : ks0 + a.chunk;
-  float acc[MT][NG][4];
+  float acc[3][MT][NG][4];
 #pragma unroll
-  for (int mt = 0; mt < MT; mt++)
+  for (int tx = 0; tx < 3; tx++)
 #pragma unroll
-    for (int j = 0; j < NG; j++)
+    for (int mt = 0; mt < MT; mt++)
 #pragma unroll
-      for (int q = 0; q < 4; q++) acc[mt][j][q] = 0.f;
+      for (int j = 0; j < NG; j++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[tx][mt][j][q] = 0.f;
   float dbs[MT][2] = {};
-  // (x, y, z) of the warp's next k-step's first voxel, advanced by 64
-  // voxels per step without divisions
+  // the warp's k-step as (segment, y, z), advanced by 4 segments per step
+  // without divisions
   long ks = ks0 + warp;
-  int x0 = 0, y0 = 0, z0 = 0;
+  int seg = 0, y = 0, z = 0;
   if (ks < ks1) {
-    const long vb = ks << 4;
-    z0 = (int)(vb / WH);
-    const long rem = vb - (long)z0 * WH;
-    y0 = (int)(rem / W);
-    x0 = (int)(rem - (long)y0 * W);
+    const long row = ks / segs;
+    seg = (int)(ks - row * segs);
+    y = (int)(row % H);
+    z = (int)(row / H);
   }
-  // the B rows of a k-step: item idx = lane + 32 k is voxel idx / NG, unit
-  // idx % NG of the group (zero outside the volume and past CIN)
-  auto load_rows = [&](long vb, int xb, int yb, int zb, uint4 (&sv)[PER_LANE]) {
+  // the B rows of a k-step: item idx = lane + 32 k is tile row idx / NG
+  // (input x = 16 sg - 1 + row), unit idx % NG of the group (zero outside
+  // the volume and past CIN)
+  auto load_rows = [&](int sg, int yy, int zz, uint4 (&sv)[PER_LANE]) {
+    const int yn = yy + dyy, zn = zz + dz;
+    const bool rowok = yn >= 0 && yn < H && zn >= 0 && zn < D;
+    const long frow = (long)W * (yn + (long)H * zn);
+    const long crow = (long)a.Wc * ((yn >> 1) + (long)a.Hc * (zn >> 1));
 #pragma unroll
     for (int k = 0; k < PER_LANE; k++) {
       const int idx = lane + 32 * k;
       const int r = idx / NG, u = idx % NG;
-      int x = xb + r, y = yb, z = zb;
-      while (x >= W) {  // W may be below 16 on small grids
-        x -= W;
-        if (++y >= H) {
-          y = 0;
-          ++z;
-        }
-      }
-      const int xn = x + dx, yn = y + dyy, zn = z + dz, ch = (ntile0 + u) * 8;
+      const int x = (sg << 4) - 1 + r, ch = (ntile0 + u) * 8;
       uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (idx < ITEMS && vb + r < a.V && xn >= 0 && xn < W && yn >= 0 && yn < H &&
-          zn >= 0 && zn < D && ch < CIN) {
+      if (idx < ITEMS && rowok && x >= 0 && x < W && ch < CIN) {
         if (ch < CIN1)
-          v = *reinterpret_cast<const uint4 *>(a.in1 + (vb + r + off) * CIN1 + ch);
+          v = *reinterpret_cast<const uint4 *>(a.in1 + (frow + x) * CIN1 + ch);
         else if (CIN2 > 0)
           v = *reinterpret_cast<const uint4 *>(
-              a.in2 + ((long)(xn >> 1) + (long)a.Wc * ((yn >> 1) + (long)a.Hc * (zn >> 1))) *
-                          (CIN2 > 0 ? CIN2 : 1) +
-              (ch - CIN1));
+              a.in2 + ((long)(x >> 1) + crow) * (CIN2 > 0 ? CIN2 : 1) + (ch - CIN1));
       }
       sv[k] = v;
     }
   };
   uint4 sv[PER_LANE];
-  if (ks < ks1) load_rows(ks << 4, x0, y0, z0, sv);
+  if (ks < ks1) load_rows(seg, y, z, sv);
   for (; ks < ks1; ks += 4) {
-    const long vb = ks << 4;
+    // the k-step's first voxel in the padded gradient rows
+    const long vb = ((long)y + (long)H * z) * a.Wp + ((long)seg << 4);
     __syncwarp();  // the previous k-step's ldmatrix reads are done
 #pragma unroll
     for (int k = 0; k < PER_LANE; k++) {
@@ -383,17 +385,17 @@ __global__ void __launch_bounds__(128) conv3_wgrad_tc(WgArgs a) {
         *reinterpret_cast<uint4 *>(tw + (idx / NG) * RSTR + (idx % NG) * 8) = sv[k];
     }
     __syncwarp();
-    x0 += 64;
-    while (x0 >= W) {
-      x0 -= W;
-      if (++y0 >= H) {
-        y0 = 0;
-        ++z0;
+    seg += 4;
+    while (seg >= segs) {
+      seg -= segs;
+      if (++y >= H) {
+        y = 0;
+        ++z;
       }
     }
-    if (ks + 4 < ks1) load_rows(vb + 64, x0, y0, z0, sv);  // in flight during the MMAs
-    // A fragments: dyt[co][v] for v = vb + (2t, 2t+1) and vb + (2t+8, 2t+9),
-    // aligned pairs (rows of Vp, a multiple of 16; zero past V)
+    if (ks + 4 < ks1) load_rows(seg, y, z, sv);  // in flight during the MMAs
+    // A fragments: dyt[co][vb + (2t, 2t+1)] and [vb + (2t+8, 2t+9)], aligned
+    // pairs (zero in the rows' padding)
     uint32_t af[MT][4];
 #pragma unroll
     for (int mt = 0; mt < MT; mt++)
@@ -403,41 +405,48 @@ __global__ void __launch_bounds__(128) conv3_wgrad_tc(WgArgs a) {
         const uint32_t lo = ld2(rp + 2 * t), hi = ld2(rp + 2 * t + 8);
         af[mt][h] = lo;      // a0 (row g) / a1 (row g+8): k = 2t, 2t+1
         af[mt][2 + h] = hi;  // a2 / a3: k = 2t+8, 2t+9
-        if (tap == 13 && blockIdx.z == 0)
+        if (pair == 4 && blockIdx.z == 0)
           dbs[mt][h] += bf_lo(lo) + bf_hi(lo) + bf_lo(hi) + bf_hi(hi);
       }
-    // B fragments of n-tiles (j, j+1): matrices (rows 0-7, j), (rows 8-15, j),
-    // (rows 0-7, j+1), (rows 8-15, j+1)
+    // tap dx = tx - 1: B rows tx .. tx + 15; matrices (rows 0-7, j),
+    // (rows 8-15, j), (rows 0-7, j+1), (rows 8-15, j+1)
 #pragma unroll
-    for (int j = 0; j < NG; j += 2) {
-      if (ntile0 + j >= NT) break;
-      const int m = lane >> 3;
-      uint32_t b0, b1, b2, b3;
-      ldsm_x4_trans(tw + ((m & 1) * 8 + (lane & 7)) * RSTR + (j + (m >> 1)) * 8, b0, b1, b2, b3);
+    for (int tx = 0; tx < 3; tx++)
 #pragma unroll
-      for (int mt = 0; mt < MT; mt++)
-        mma_bf16(acc[mt][j], af[mt][0], af[mt][1], af[mt][2], af[mt][3], b0, b1);
-      if (ntile0 + j + 1 < NT) {
+      for (int j = 0; j < NG; j += 2) {
+        if (ntile0 + j >= NT) break;
+        const int m = lane >> 3;
+        uint32_t b0, b1, b2, b3;
+        ldsm_x4_trans(tw + ((m & 1) * 8 + (lane & 7) + tx) * RSTR + (j + (m >> 1)) * 8, b0, b1,
+                      b2, b3);
 #pragma unroll
         for (int mt = 0; mt < MT; mt++)
-          mma_bf16(acc[mt][j + 1], af[mt][0], af[mt][1], af[mt][2], af[mt][3], b2, b3);
+          mma_bf16(acc[tx][mt][j], af[mt][0], af[mt][1], af[mt][2], af[mt][3], b0, b1);
+        if (ntile0 + j + 1 < NT) {
+#pragma unroll
+          for (int mt = 0; mt < MT; mt++)
+            mma_bf16(acc[tx][mt][j + 1], af[mt][0], af[mt][1], af[mt][2], af[mt][3], b2, b3);
+        }
       }
-    }
   }
-  // D fragment: rows co = g (c0, c1), g+8 (c2, c3); cols ci = 2t, 2t+1
+  // D fragments: rows co = g (c0, c1), g+8 (c2, c3); cols ci = 2t, 2t+1
 #pragma unroll
-  for (int mt = 0; mt < MT; mt++)
+  for (int tx = 0; tx < 3; tx++) {
+    const int tap = 3 * pair + tx;
 #pragma unroll
-    for (int j = 0; j < NG; j++) {
-      const int nt = ntile0 + j;
-      if (nt >= NT) break;
+    for (int mt = 0; mt < MT; mt++)
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int co = mt * 16 + g + 8 * (q >> 1), ci = nt * 8 + 2 * t + (q & 1);
-        atomicAdd(a.dw + ((size_t)tap * COUT + co) * CIN + ci, acc[mt][j][q]);
+      for (int j = 0; j < NG; j++) {
+        const int nt = ntile0 + j;
+        if (nt >= NT) break;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int co = mt * 16 + g + 8 * (q >> 1), ci = nt * 8 + 2 * t + (q & 1);
+          atomicAdd(a.dw + ((size_t)tap * COUT + co) * CIN + ci, acc[tx][mt][j][q]);
+        }
       }
-    }
-  if (tap == 13 && blockIdx.z == 0) {
+  }
+  if (pair == 4 && blockIdx.z == 0) {
 #pragma unroll
     for (int mt = 0; mt < MT; mt++)
 #pragma unroll
@@ -455,6 +464,8 @@ struct Dims {
   int W, H, D;
   long V;
 };
+// Voxels of a level's transposed output gradient with x rows padded to 16.
+inline long padded_rows(const Dims &f) { return (long)f.H * f.D * ((f.W + 15) & ~15); }
 __host__ __device__ inline Dims coarse_of(const Dims &f) {
   Dims c;
   c.W = (f.W + 1) / 2;
@@ -1007,21 +1018,25 @@ template <int CIN1, int CIN2, int COUT>
 cudaError_t wgrad_launch(const Net &n, WgArgs a, const float *dy, const bf16 *y,
                          cudaStream_t s) {
   constexpr int CIN = CIN1 + CIN2, NT = CIN / 8, MT = COUT / 16;
-  // n-tiles per block: groups of 6 where they divide the channels evenly
-  // (no zero-filled units staged), else up to 4; at most 16 accumulator tiles
-  constexpr int NG = (NT % 6 == 0 && MT * 6 <= 16) ? 6 : (NT < 4 ? NT : 4);
+  // n-tiles per block (3 taps x MT x NG accumulator tiles, at most 24):
+  // groups of 6 where they divide the channels evenly (no zero-filled units
+  // staged), else 4 where they divide, else 2
+  constexpr int NG = (MT == 1 && NT % 6 == 0) ? 6 : (MT <= 2 && NT % 4 == 0) ? 4 : 2;
   constexpr int NGROUPS = (NT + NG - 1) / NG;
-  // masked, transposed BF16 output gradient (scratch sized for the largest)
-  a.Vp = (a.V + 15) & ~15L;
-  mask_transpose<COUT><<<grid_for(a.V * COUT, 256), 256, 0, s>>>(dy, y, n.dyt, a.V, a.Vp);
+  // masked, transposed BF16 output gradient with x rows padded to 16 voxels
+  // (scratch sized for the largest layer)
+  a.Wp = (a.W + 15) & ~15;
+  a.Vp = (long)a.H * a.D * a.Wp;
+  mask_transpose<COUT><<<grid_for(a.V * COUT, 256), 256, 0, s>>>(dy, y, n.dyt, a.V, a.W, a.Wp,
+                                                                 a.Vp);
   a.dyt = n.dyt;
-  const long nks = (a.V + 15) / 16;  // 16-voxel k-steps
-  const long target = std::max<long>(1, (long)device_sm_count() * 8 / (27 * NGROUPS));
+  const long nks = (long)a.H * a.D * (a.Wp / 16);  // 16-voxel x-row segments
+  const long target = std::max<long>(1, (long)device_sm_count() * 8 / (9 * NGROUPS));
   long chunk = (nks + target - 1) / target;
   chunk = std::max<long>(16, ((chunk + 3) / 4) * 4);
   a.chunk = chunk;
   const long nchunk = (nks + chunk - 1) / chunk;
-  conv3_wgrad_tc<CIN1, CIN2, COUT, NG><<<dim3((unsigned)nchunk, 27, NGROUPS), 128, 0, s>>>(a);
+  conv3_wgrad_tc<CIN1, CIN2, COUT, NG><<<dim3((unsigned)nchunk, 9, NGROUPS), 128, 0, s>>>(a);
   count_launches(2);
   return cudaGetLastError();
 }
@@ -1468,8 +1483,9 @@ extern "C" int vdr_net_create(vdr_handle *H, unsigned long long seed, vdr_net **
         (e = nalloc(n, &n.rbuf, V0)) || (e = nalloc(n, &n.zbuf, V0)) ||
         (e = nalloc(n, &n.qbuf, V0)) || (e = nalloc(n, &n.pbuf, V0)) ||
         (e = nalloc(n, &n.gbuf, V0)) || (e = nalloc(n, &n.dc, V0)) ||
-        (e = nalloc(n, &n.dyt, std::max(std::max(((V0 + 15) & ~15L) * 16, ((V1 + 15) & ~15L) * 32),
-                                         ((V2 + 15) & ~15L) * 64))) ||
+        (e = nalloc(n, &n.dyt, std::max(std::max(padded_rows(n.d[0]) * 16,
+                                                  padded_rows(n.d[1]) * 32),
+                                         padded_rows(n.d[2]) * 64))) ||
         (e = nalloc(n, &n.scal, 8)) || (e = nalloc(n, &n.partials, 2L * n.red_grid)) ||
         (e = nalloc(n, &n.ticket, 1)) || (e = nalloc(n, &n.wtc, off)) ||
         (e = nalloc(n, &n.up0, V0 * 32)) || (e = nalloc(n, &n.up1, V1 * 64)) ||
