@@ -105,7 +105,8 @@ def workload_config(a, prob):
         "elements": prob.mesh.nelem, "nodes": prob.mesh.nnode,
         "dirichlet_nodes": int(prob.bc.sum()),
         "apply": "stored element matrices, double-float pairs (built on GPU "
-                 "each step)",
+                 "each step from the fields and the mesh's geometric factors, "
+                 "which the handle forms once)",
         "scatter": a.scatter, "solver": "bicgstab", "precision": "fp64",
         "l2": "inputs larger than L2 (element matrices 4.3 GB per apply)",
     }
