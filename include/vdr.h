@@ -143,9 +143,9 @@ int vdr_set_operator(vdr_handle *h, double aH, double aM);
  * coordinates never change) and every later build forms the element
  * matrices from them and the current fields.  RECOMPUTE: every build
  * evaluates the Jacobians from the coordinates.  AUTO falls back to
- * RECOMPUTE where there is no device memory for the factors, where a factor
- * lies outside the double-float window, and for Robin elements with a
- * nonzero Robin coefficient.  Results agree to double-float rounding
+ * RECOMPUTE where the factors would take more than half of the free device
+ * memory, where a factor lies outside the double-float window, and for
+ * Robin elements with a nonzero Robin coefficient.  Results agree to double-float rounding
  * (~1e-15 relative).  Setting the mode marks the operator stale. */
 #define VDR_BUILD_AUTO 0
 #define VDR_BUILD_RECOMPUTE 1

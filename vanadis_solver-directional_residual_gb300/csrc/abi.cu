@@ -137,6 +137,15 @@ int ensure_geometry(Handle &h, bool *use) {
     return VDR_OK;
   }
   const size_t E = (size_t)std::max(h.E, 1);
+  // only where they leave at least half of the free device memory to the
+  // rest of the work
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess ||
+      sizeof(float2) * GEO_PAIRS * E > free_b / 2) {
+    cudaGetLastError();
+    h.geo_state = -1;
+    return VDR_OK;
+  }
   if (cudaMalloc(&h.geo.Ji, sizeof(float2) * 72 * E) ||
       cudaMalloc(&h.geo.Dj, sizeof(float2) * 8 * E) ||
       cudaMalloc(&h.geo.K, sizeof(float2) * 36 * E)) {
