@@ -145,8 +145,9 @@ int vdr_set_operator(vdr_handle *h, double aH, double aM);
  * evaluates the Jacobians from the coordinates.  AUTO falls back to
  * RECOMPUTE where the factors would take more than half of the free device
  * memory, where a factor lies outside the double-float window, and for
- * Robin elements with a nonzero Robin coefficient.  Results agree to double-float rounding
- * (~1e-15 relative).  Setting the mode marks the operator stale. */
+ * Robin elements with a nonzero Robin coefficient.  Results agree to
+ * double-float rounding (~1e-15 relative).  Setting the mode marks the
+ * operator stale. */
 #define VDR_BUILD_AUTO 0
 #define VDR_BUILD_RECOMPUTE 1
 int vdr_set_build_mode(vdr_handle *h, int mode);
