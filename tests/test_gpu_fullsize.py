@@ -2,6 +2,9 @@
 theta step (8,388,608 elements, 8,520,321 nodes; the bench's step), against
 the oracle assembled and solved on all host cores.
 
+* element matrices of the step's build (from the mesh's geometric factors)
+  and of the build that evaluates the Jacobians from the coordinates,
+  against the oracle's BB: 1e-12 relative L2, 1e-13 between the two;
 * operator apply and its transpose: GPU vs the oracle's colour-parallel
   matvec_0 / mttvec_0 on the oracle's BB, 1e-12 relative L2, with the
   atomic scatter and with the colour-by-colour scatter;
@@ -49,6 +52,20 @@ def full(vdr, oracle):
     yield {"prob": prob, "aH": aH, "aM": aM, "bb": bb, "b": b, "d": d,
            "colors": colors, "nt": nt, "s": s}
     s.close()
+
+
+def test_fullsize_element_matrices_both_builds(gpu_lib, full):
+    s = full["s"]
+    bb_geo = s.element_matrices()
+    assert s.geometry_status()[0] == 1
+    assert rel_l2(bb_geo, full["bb"]) < 1e-12
+    s.set_build_mode("recompute")
+    try:
+        bb_rc = s.element_matrices()
+    finally:
+        s.set_build_mode("auto")
+    assert rel_l2(bb_rc, full["bb"]) < 1e-12
+    assert rel_l2(bb_geo, bb_rc) < 1e-13
 
 
 def test_fullsize_apply_parity(oracle, gpu_lib, full):
