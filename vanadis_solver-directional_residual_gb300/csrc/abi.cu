@@ -195,10 +195,6 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
     BuildArgs ba;
     ba.exact_fp64 = h.exact_build;
     ba.bad = h.flag;
-    if (!h.exact_build) {
-      if ((e = dalloc(&h.drs, (size_t)h.E * 5))) return cuda_fail(e, "alloc DR scalars");
-      ba.drs = h.drs;
-    }
     if (rhs) {
       ba.cf = rhs->cf;
       ba.rM = rhs->rM;
@@ -235,11 +231,13 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
       }
     }
     // from the mesh's geometric factors unless the rows are FP64 or a
-    // Robin term is on
-    if (!h.exact_build && !(h.robin && h.robin_alpha != 0.0)) {
+    // Robin term is on; each double-float build has its per-element scalars
+    if (!h.exact_build) {
       bool geo = false;
-      const int gst = ensure_geometry(h, &geo);
-      if (gst) return gst;
+      if (!(h.robin && h.robin_alpha != 0.0)) {
+        const int gst = ensure_geometry(h, &geo);
+        if (gst) return gst;
+      }
       if (geo) {
         if ((e = dalloc(&h.gsc, (size_t)h.E * 10)))
           return cuda_fail(e, "alloc element scalars");
@@ -247,6 +245,9 @@ int build_operator(Handle &h, const BuildArgs *rhs) {
         ba.gDj = h.geo.Dj;
         ba.gK = h.geo.K;
         ba.gsc = h.gsc;
+      } else {
+        if ((e = dalloc(&h.drs, (size_t)h.E * 5))) return cuda_fail(e, "alloc DR scalars");
+        ba.drs = h.drs;
       }
     }
     if ((e = cudaMemsetAsync(h.flag, 0, sizeof(int), h.stream)))

@@ -1497,7 +1497,7 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
   else if (ba.exact_fp64)
     elem_build_kernel<double><<<grid, 64, 0, s>>>(a, ba);
   else {
-    if (!ba.drs) return cudaErrorInvalidValue;
+    if (ba.gK ? !ba.gsc : !ba.drs) return cudaErrorInvalidValue;
     static std::once_flag carveout;  // 8 blocks of 27.5 KB need the full carveout,
     std::call_once(carveout, [] {
       cudaFuncSetAttribute(elem_build_df_kernel<true>,
@@ -1512,7 +1512,6 @@ cudaError_t launch_build(const OpArgs &a, const BuildArgs &ba, bool fp32,
     });
     const int g2 = (int)std::min<long>(((long)a.E + 255) / 256, (long)device_sm_count() * 8);
     if (ba.gK) {  // from the mesh's geometric factors
-      if (!ba.gsc) return cudaErrorInvalidValue;
       elem_geo_scalars_kernel<<<g2, 256, 0, s>>>(a, ba.gsc, ba.bad);
       if (ba.told || ba.Mhi)
         elem_build_geo_kernel<true><<<grid, 64, 0, s>>>(a, ba);
