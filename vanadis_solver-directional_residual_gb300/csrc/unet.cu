@@ -266,25 +266,39 @@ struct WgArgs {
   long V, Vp, chunk;  // Vp = H D Wp
 };
 
+// dyt[c][row][x] = dY[v][c] where Y[v][c] > 0 (the ReLU's derivative), v =
+// row W + x; zero in the rows' padding x in [W, Wp) (the buffer is shared
+// by layers of other shapes).  One block per x row, one thread per padded
+// voxel: its C channels in 16-byte loads, and per channel a coalesced store
+// across the row.
 template <int C>
-__global__ void mask_transpose(const float *dy, const bf16 *y, bf16 *dyt, long V, int W,
-                               int Wp, long Vp) {
-  const long total = V * C;
-  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long)gridDim.x * blockDim.x) {
-    const long v = idx / C;
-    const int c = (int)(idx % C);
-    const long row = v / W;
-    const float d = __bfloat162float(y[idx]) > 0.f ? dy[idx] : 0.f;
-    dyt[(long)c * Vp + row * Wp + (v - row * W)] = __float2bfloat16_rn(d);
-  }
-  // the rows' padding past W (the buffer is shared by layers of other shapes)
-  const int pad = Wp - W;
-  const long rows = Vp / Wp;
-  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < (long)pad * rows * C;
-       idx += (long)gridDim.x * blockDim.x) {
-    const long cr = idx / pad;  // c * rows + row
-    dyt[cr * Wp + W + (idx - cr * pad)] = __float2bfloat16_rn(0.f);
+__global__ void mask_transpose(const float *__restrict__ dy, const bf16 *__restrict__ y,
+                               bf16 *__restrict__ dyt, int W, int Wp, long Vp) {
+  static_assert(C % 8 == 0, "channels");
+  const long row = blockIdx.x;
+  for (int x = threadIdx.x; x < Wp; x += blockDim.x) {
+    bf16 *out = dyt + row * Wp + x;
+    if (x >= W) {
+#pragma unroll
+      for (int c = 0; c < C; c++) out[(long)c * Vp] = __float2bfloat16_rn(0.f);
+      continue;
+    }
+    const long v = row * W + x;
+    const float4 *dp = reinterpret_cast<const float4 *>(dy + v * C);
+    const uint4 *yp = reinterpret_cast<const uint4 *>(y + v * C);
+#pragma unroll
+    for (int c8 = 0; c8 < C / 8; c8++) {
+      const uint4 ym = yp[c8];
+      const float4 d0 = dp[2 * c8], d1 = dp[2 * c8 + 1];
+      const uint32_t yw[4] = {ym.x, ym.y, ym.z, ym.w};
+      const float dv[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const uint32_t h16 = (k & 1) ? (yw[k >> 1] >> 16) : (yw[k >> 1] & 0xffffu);
+        out[(long)(8 * c8 + k) * Vp] =
+            __float2bfloat16_rn(__uint_as_float(h16 << 16) > 0.f ? dv[k] : 0.f);
+      }
+    }
   }
 }
 
@@ -1027,8 +1041,7 @@ cudaError_t wgrad_launch(const Net &n, WgArgs a, const float *dy, const bf16 *y,
   // (scratch sized for the largest layer)
   a.Wp = (a.W + 15) & ~15;
   a.Vp = (long)a.H * a.D * a.Wp;
-  mask_transpose<COUT><<<grid_for(a.V * COUT, 256), 256, 0, s>>>(dy, y, n.dyt, a.V, a.W, a.Wp,
-                                                                 a.Vp);
+  mask_transpose<COUT><<<(unsigned)((long)a.H * a.D), 128, 0, s>>>(dy, y, n.dyt, a.W, a.Wp, a.Vp);
   a.dyt = n.dyt;
   const long nks = (long)a.H * a.D * (a.Wp / 16);  // 16-voxel x-row segments
   const long target = std::max<long>(1, (long)device_sm_count() * 8 / (9 * NGROUPS));
