@@ -20,10 +20,12 @@
 //
 // Kernels:
 //   conv3_kernel   implicit GEMM on the tensor cores (mma.sync m16n8k16
-//                  BF16, FP32 accumulate): M = 16 voxels per m-tile, N =
-//                  output channels, K = 27 taps x input channels.  The
+//                  BF16, FP32 accumulate): M = 16-voxel x-row segments, N =
+//                  output channels, K = 27 taps x input channels, the A
+//                  operand staged per (dy, dz) row in shared memory and read
+//                  by ldmatrix for the three x-taps.  The
 //                  nearest upsampling and concatenation of the decoder
-//                  inputs are fused into the operand gather.  The same
+//                  inputs are fused into the operand staging.  The same
 //                  kernel computes the backward data pass (flipped,
 //                  transposed weights; FP32 gradient input with the ReLU
 //                  mask of the layer output fused into the gather).
@@ -129,121 +131,156 @@ struct ConvArgs {
   const int *skip, *skip2;
 };
 
-// Tap t = (dz+1)*9 + (dy+1)*3 + (dx+1).
-template <int CIN1, int CIN2, int COUT, int MT, bool F32IN, bool F32OUT>
+// Four 8x8 b16 matrices from shared memory (ldmatrix): lane l supplies the
+// address of row l & 7 of matrix l >> 3.
+__device__ __forceinline__ void ldsm_x4(const bf16 *p, uint32_t &r0, uint32_t &r1,
+                                        uint32_t &r2, uint32_t &r3) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(sa)
+               : "memory");
+}
+
+// 3x3x3 convolution by x-row segments: out[v][co] = bias + sum over taps
+// t = (dz+1)*9 + (dy+1)*3 + (dx+1) of W[t][co][.] . X[v + off(t)][.],
+// X = [in1 (zero where mask1 <= 0) | up(in2)].  A warp takes MS segments of
+// 16 voxels of x rows (MS m-tiles); for each (dy, dz) pair it copies the 18
+// voxels xs-1 .. xs+16 of the shifted row of each segment into a padded
+// shared tile once (BF16; FP32 inputs converted; zero outside the volume),
+// and the three x-taps read their A fragments from tile rows dx+1 .. dx+16
+// with ldmatrix; the weight fragments (L1-resident) serve all MS m-tiles.
+template <int CIN1, int CIN2, int COUT, int MS, bool F32IN, bool F32OUT>
 __global__ void __launch_bounds__(128) conv3_kernel(ConvArgs a) {
   if (skipped(a.skip, a.skip2)) return;
-  constexpr int CIN = CIN1 + CIN2, KC = CIN / 16, KC1 = CIN1 / 16, NT = COUT / 8;
+  constexpr int CIN = CIN1 + CIN2, KC = CIN / 16, NT = COUT / 8;
   static_assert(CIN1 % 16 == 0 && CIN2 % 16 == 0 && COUT % 8 == 0, "shape");
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long row0 = warp * (16L * MT);
-  if (row0 >= a.V) return;
-  const long WH = (long)a.W * a.H;
-  int vx[MT][2], vy[MT][2], vz[MT][2];
-  long vr[MT][2];
+  constexpr int RSTR = CIN + 8;  // bf16 per tile row (16 bytes of padding)
+  constexpr int UNITS = CIN / 8, ITEMS = MS * 18 * UNITS, PER_LANE = (ITEMS + 31) / 32;
+  __shared__ __align__(16) bf16 tile[4][MS * 18 * RSTR];
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, warp = threadIdx.x >> 5;
+  bf16 *tw = tile[warp];
+  const int W = a.W, H = a.H, D = a.D;
+  const int segs = (W + 15) >> 4;
+  const long nseg = (long)H * D * segs;
+  const long ngroup = (nseg + MS - 1) / MS;
+  for (long gi = (long)blockIdx.x * 4 + warp; gi < ngroup; gi += (long)gridDim.x * 4) {
+    // segment m of the group: flat segment MS gi + m = (row, xs)
+    long rowm[MS];
+    int xsm[MS], ym[MS], zm[MS];
+    bool segok[MS];
 #pragma unroll
-  for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const long r = row0 + mt * 16 + g + 8 * h;
-      vr[mt][h] = r < a.V ? r : -1;
-      const long rr = r < a.V ? r : 0;
-      vx[mt][h] = (int)(rr % a.W);
-      vy[mt][h] = (int)((rr / a.W) % a.H);
-      vz[mt][h] = (int)(rr / WH);
+    for (int m = 0; m < MS; m++) {
+      const long sg = MS * gi + m;
+      segok[m] = sg < nseg;
+      const long sgc = segok[m] ? sg : 0;
+      rowm[m] = sgc / segs;
+      xsm[m] = (int)(sgc - rowm[m] * segs) << 4;
+      ym[m] = (int)(rowm[m] % H);
+      zm[m] = (int)(rowm[m] / H);
     }
-  float acc[MT][NT][4];
+    float acc[MS][NT][4];
 #pragma unroll
-  for (int mt = 0; mt < MT; mt++)
+    for (int m = 0; m < MS; m++)
 #pragma unroll
-    for (int nt = 0; nt < NT; nt++)
+      for (int nt = 0; nt < NT; nt++)
 #pragma unroll
-      for (int q = 0; q < 4; q++) acc[mt][nt][q] = 0.f;
-
-  for (int tap = 0; tap < 27; tap++) {
-    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-    long nf[MT][2], nc[MT][2];
+        for (int q = 0; q < 4; q++) acc[m][nt][q] = 0.f;
+#pragma unroll 1
+    for (int pair = 0; pair < 9; pair++) {
+      const int dyy = pair % 3 - 1, dz = pair / 3 - 1;
+      __syncwarp();  // the previous pair's ldmatrix reads are done
 #pragma unroll
-    for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int x = vx[mt][h] + dx, y = vy[mt][h] + dy, z = vz[mt][h] + dz;
-        const bool ok = vr[mt][h] >= 0 && x >= 0 && x < a.W && y >= 0 &&
-                        y < a.H && z >= 0 && z < a.D;
-        nf[mt][h] = ok ? vr[mt][h] + dx + (long)dy * a.W + (long)dz * WH : -1;
-        nc[mt][h] = ok ? (long)(x >> 1) + (long)a.Wc * ((y >> 1) + (long)a.Hc * (z >> 1))
-                       : -1;
-      }
-    const bf16 *wt = a.w + (size_t)tap * COUT * CIN;
-#pragma unroll
-    for (int kc = 0; kc < KC; kc++) {
-      uint32_t bfr[NT][2];
-#pragma unroll
-      for (int nt = 0; nt < NT; nt++) {
-        const bf16 *wp = wt + (size_t)(nt * 8 + g) * CIN + kc * 16 + 2 * t;
-        bfr[nt][0] = ld2(wp);
-        bfr[nt][1] = ld2(wp + 8);
-      }
-#pragma unroll
-      for (int mt = 0; mt < MT; mt++) {
-        uint32_t lo[2], hi[2];
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          lo[h] = hi[h] = 0u;
-          if (kc < KC1) {
-            const long n = nf[mt][h];
-            if (n >= 0) {
-              const long i = n * CIN1 + kc * 16 + 2 * t;
-              lo[h] = ld_pair<F32IN>(a.in1, i);
-              hi[h] = ld_pair<F32IN>(a.in1, i + 8);
-              if (a.mask1) {
-                lo[h] = apply_mask(lo[h], ld2(a.mask1 + i));
-                hi[h] = apply_mask(hi[h], ld2(a.mask1 + i + 8));
-              }
+      for (int k = 0; k < PER_LANE; k++) {
+        const int idx = lane + 32 * k;
+        if (idx >= ITEMS) break;
+        const int m = idx / (18 * UNITS), rem = idx - m * 18 * UNITS;
+        const int r = rem / UNITS, ch = (rem - r * UNITS) * 8;
+        const int x = xsm[m] - 1 + r, yn = ym[m] + dyy, zn = zm[m] + dz;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (segok[m] && x >= 0 && x < W && yn >= 0 && yn < H && zn >= 0 && zn < D) {
+          if (ch < CIN1) {
+            const long i = ((long)W * (yn + (long)H * zn) + x) * CIN1 + ch;
+            if (F32IN) {
+              const float4 f0 = *reinterpret_cast<const float4 *>(static_cast<const float *>(a.in1) + i);
+              const float4 f1 =
+                  *reinterpret_cast<const float4 *>(static_cast<const float *>(a.in1) + i + 4);
+              v = make_uint4(pack2(f0.x, f0.y), pack2(f0.z, f0.w), pack2(f1.x, f1.y),
+                             pack2(f1.z, f1.w));
+            } else {
+              v = *reinterpret_cast<const uint4 *>(static_cast<const bf16 *>(a.in1) + i);
+            }
+            if (a.mask1) {
+              const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask1 + i);
+              v = make_uint4(apply_mask(v.x, mk.x), apply_mask(v.y, mk.y),
+                             apply_mask(v.z, mk.z), apply_mask(v.w, mk.w));
             }
           } else if (CIN2 > 0) {
-            const long n = nc[mt][h];
-            if (n >= 0) {
-              const long i = n * (CIN2 > 0 ? CIN2 : 1) + (kc - KC1) * 16 + 2 * t;
-              lo[h] = ld2(a.in2 + i);
-              hi[h] = ld2(a.in2 + i + 8);
-            }
+            v = *reinterpret_cast<const uint4 *>(
+                a.in2 +
+                ((long)(x >> 1) + (long)a.Wc * ((yn >> 1) + (long)a.Hc * (zn >> 1))) *
+                    (CIN2 > 0 ? CIN2 : 1) +
+                (ch - CIN1));
           }
         }
+        *reinterpret_cast<uint4 *>(tw + (m * 18 + r) * RSTR + ch) = v;
+      }
+      __syncwarp();
 #pragma unroll
-        for (int nt = 0; nt < NT; nt++)
-          mma_bf16(acc[mt][nt], lo[0], lo[1], hi[0], hi[1], bfr[nt][0], bfr[nt][1]);
+      for (int tx = 0; tx < 3; tx++) {
+        const bf16 *wt = a.w + (size_t)(3 * pair + tx) * COUT * CIN;
+        const int mi = lane >> 3;  // ldmatrix matrix of this lane's address
+#pragma unroll
+        for (int kc = 0; kc < KC; kc++) {
+          uint32_t bfr[NT][2];
+#pragma unroll
+          for (int nt = 0; nt < NT; nt++) {
+            const bf16 *wp = wt + (size_t)(nt * 8 + g) * CIN + kc * 16 + 2 * t;
+            bfr[nt][0] = ld2(wp);
+            bfr[nt][1] = ld2(wp + 8);
+          }
+#pragma unroll
+          for (int m = 0; m < MS; m++) {
+            uint32_t a0, a1, a2, a3;
+            ldsm_x4(tw + (m * 18 + tx + (mi & 1) * 8 + (lane & 7)) * RSTR + kc * 16 + (mi >> 1) * 8,
+                    a0, a1, a2, a3);
+#pragma unroll
+            for (int nt = 0; nt < NT; nt++)
+              mma_bf16(acc[m][nt], a0, a1, a2, a3, bfr[nt][0], bfr[nt][1]);
+          }
+        }
       }
     }
+    // D fragments: rows g, g + 8 (voxels xs + g, xs + g + 8), cols co = 8 nt + 2t, +1
+#pragma unroll
+    for (int m = 0; m < MS; m++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int x = xsm[m] + g + 8 * h;
+        if (!segok[m] || x >= W) continue;
+        const long r = rowm[m] * W + x;
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++) {
+          const int co = nt * 8 + 2 * t;
+          float v0 = acc[m][nt][2 * h], v1 = acc[m][nt][2 * h + 1];
+          if (a.bias) {
+            v0 += a.bias[co];
+            v1 += a.bias[co + 1];
+          }
+          if (a.relu) {
+            v0 = fmaxf(v0, 0.f);
+            v1 = fmaxf(v1, 0.f);
+          }
+          if (F32OUT) {
+            *reinterpret_cast<float2 *>(static_cast<float *>(a.out) + r * COUT + co) =
+                make_float2(v0, v1);
+          } else {
+            *reinterpret_cast<uint32_t *>(static_cast<bf16 *>(a.out) + r * COUT + co) =
+                pack2(v0, v1);
+          }
+        }
+      }
   }
-#pragma unroll
-  for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const long r = vr[mt][h];
-      if (r < 0) continue;
-#pragma unroll
-      for (int nt = 0; nt < NT; nt++) {
-        const int co = nt * 8 + 2 * t;
-        float v0 = acc[mt][nt][2 * h], v1 = acc[mt][nt][2 * h + 1];
-        if (a.bias) {
-          v0 += a.bias[co];
-          v1 += a.bias[co + 1];
-        }
-        if (a.relu) {
-          v0 = fmaxf(v0, 0.f);
-          v1 = fmaxf(v1, 0.f);
-        }
-        if (F32OUT) {
-          *reinterpret_cast<float2 *>(static_cast<float *>(a.out) + r * COUT + co) =
-              make_float2(v0, v1);
-        } else {
-          *reinterpret_cast<uint32_t *>(static_cast<bf16 *>(a.out) + r * COUT + co) =
-              pack2(v0, v1);
-        }
-      }
-    }
 }
 
 // Weight and bias gradients of one 3x3x3 layer on the tensor cores:
@@ -1020,10 +1057,13 @@ struct HostRng {
 
 template <int CIN1, int CIN2, int COUT, bool F32IN, bool F32OUT>
 cudaError_t conv_launch(const ConvArgs &a, cudaStream_t s) {
-  constexpr int MT = COUT >= 64 ? 1 : 2;
-  const long warps = (a.V + 16 * MT - 1) / (16 * MT);
-  const long blocks = (warps + 3) / 4;
-  conv3_kernel<CIN1, CIN2, COUT, MT, F32IN, F32OUT><<<(unsigned)blocks, 128, 0, s>>>(a);
+  // segments (m-tiles) per warp: two where the accumulators and the
+  // staged rows of both fit the registers
+  constexpr int MS = (COUT >= 64 || CIN1 + CIN2 >= 96) ? 1 : 2;
+  const long nseg = (long)a.H * a.D * ((a.W + 15) / 16);
+  const long warps = (nseg + MS - 1) / MS;
+  const long blocks = std::min<long>((warps + 3) / 4, (long)device_sm_count() * 16);
+  conv3_kernel<CIN1, CIN2, COUT, MS, F32IN, F32OUT><<<(unsigned)blocks, 128, 0, s>>>(a);
   count_launches(1);
   return cudaGetLastError();
 }
