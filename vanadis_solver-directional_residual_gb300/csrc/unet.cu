@@ -145,27 +145,35 @@ __device__ __forceinline__ void ldsm_x4(const bf16 *p, uint32_t &r0, uint32_t &r
 // 3x3x3 convolution by x-row segments: out[v][co] = bias + sum over taps
 // t = (dz+1)*9 + (dy+1)*3 + (dx+1) of W[t][co][.] . X[v + off(t)][.],
 // X = [in1 (zero where mask1 <= 0) | up(in2)].  A warp takes MS segments of
-// 16 voxels of x rows (MS m-tiles); for each (dy, dz) pair it copies the 18
-// voxels xs-1 .. xs+16 of the shifted row of each segment into a padded
-// shared tile once (BF16; FP32 inputs converted; zero outside the volume),
-// and the three x-taps read their A fragments from tile rows dx+1 .. dx+16
-// with ldmatrix; the weight fragments (L1-resident) serve all MS m-tiles.
+// 16 voxels of x rows (MS m-tiles), the block's four warps four such groups
+// together.  For each (dy, dz) pair each warp copies the 18 voxels
+// xs-1 .. xs+16 of the shifted row of each of its segments into a padded
+// shared tile (BF16; FP32 inputs converted; zero outside the volume), and
+// the three x-taps read their A fragments from tile rows dx+1 .. dx+16 with
+// ldmatrix.  With one m-tile per warp (the wide layers) the block also
+// copies the pair's three taps of weights into shared memory and the B
+// fragments come from there by ldmatrix; with two, the m-tiles share 32-bit
+// weight loads through L1 (measured faster for those layers).
 template <int CIN1, int CIN2, int COUT, int MS, bool F32IN, bool F32OUT>
 __global__ void __launch_bounds__(128) conv3_kernel(ConvArgs a) {
   if (skipped(a.skip, a.skip2)) return;
   constexpr int CIN = CIN1 + CIN2, KC = CIN / 16, NT = COUT / 8;
-  static_assert(CIN1 % 16 == 0 && CIN2 % 16 == 0 && COUT % 8 == 0, "shape");
-  constexpr int RSTR = CIN + 8;  // bf16 per tile row (16 bytes of padding)
+  static_assert(CIN1 % 16 == 0 && CIN2 % 16 == 0 && COUT % 16 == 0, "shape");
+  constexpr int RSTR = CIN + 8;  // bf16 per tile / weight row (16 bytes of padding)
   constexpr int UNITS = CIN / 8, ITEMS = MS * 18 * UNITS, PER_LANE = (ITEMS + 31) / 32;
+  constexpr bool WSM = MS == 1;              // weights staged in shared memory
+  constexpr int WUNITS = 3 * COUT * UNITS;  // 16-byte units of a pair's weights
   __shared__ __align__(16) bf16 tile[4][MS * 18 * RSTR];
+  __shared__ __align__(16) bf16 wsm[WSM ? 3 * COUT * RSTR : 8];  // [tx][co][ci]
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, warp = threadIdx.x >> 5;
   bf16 *tw = tile[warp];
   const int W = a.W, H = a.H, D = a.D;
   const int segs = (W + 15) >> 4;
   const long nseg = (long)H * D * segs;
   const long ngroup = (nseg + MS - 1) / MS;
-  for (long gi = (long)blockIdx.x * 4 + warp; gi < ngroup; gi += (long)gridDim.x * 4) {
-    // segment m of the group: flat segment MS gi + m = (row, xs)
+  for (long bgi = blockIdx.x; bgi * 4 < ngroup; bgi += gridDim.x) {
+    // segment m of this warp's group: flat segment MS gi + m = (row, xs)
+    const long gi = bgi * 4 + warp;
     long rowm[MS];
     int xsm[MS], ym[MS], zm[MS];
     bool segok[MS];
@@ -189,7 +197,17 @@ __global__ void __launch_bounds__(128) conv3_kernel(ConvArgs a) {
 #pragma unroll 1
     for (int pair = 0; pair < 9; pair++) {
       const int dyy = pair % 3 - 1, dz = pair / 3 - 1;
-      __syncwarp();  // the previous pair's ldmatrix reads are done
+      if constexpr (WSM) {
+        __syncthreads();  // every warp has read the previous pair's weights and tile
+        const bf16 *wsrc = a.w + (size_t)3 * pair * COUT * CIN;  // taps 3 pair .. + 2
+        for (int u = threadIdx.x; u < WUNITS; u += blockDim.x) {
+          const int rowc = u / UNITS, c8 = (u - rowc * UNITS) * 8;  // row = tx COUT + co
+          *reinterpret_cast<uint4 *>(wsm + rowc * RSTR + c8) =
+              *reinterpret_cast<const uint4 *>(wsrc + (size_t)rowc * CIN + c8);
+        }
+      } else {
+        __syncwarp();  // the previous pair's ldmatrix reads of the tile are done
+      }
 #pragma unroll
       for (int k = 0; k < PER_LANE; k++) {
         const int idx = lane + 32 * k;
@@ -225,19 +243,31 @@ __global__ void __launch_bounds__(128) conv3_kernel(ConvArgs a) {
         }
         *reinterpret_cast<uint4 *>(tw + (m * 18 + r) * RSTR + ch) = v;
       }
-      __syncwarp();
+      if constexpr (WSM)
+        __syncthreads();  // the weights and this warp's tile are in place
+      else
+        __syncwarp();
+      const int mi = lane >> 3;  // ldmatrix matrix of this lane's address
 #pragma unroll
       for (int tx = 0; tx < 3; tx++) {
-        const bf16 *wt = a.w + (size_t)(3 * pair + tx) * COUT * CIN;
-        const int mi = lane >> 3;  // ldmatrix matrix of this lane's address
 #pragma unroll
         for (int kc = 0; kc < KC; kc++) {
+          // B: matrices (n-tile nt, k 0-7), (nt, k 8-15), (nt+1, k 0-7), (nt+1, k 8-15)
           uint32_t bfr[NT][2];
+          if constexpr (WSM) {
 #pragma unroll
-          for (int nt = 0; nt < NT; nt++) {
-            const bf16 *wp = wt + (size_t)(nt * 8 + g) * CIN + kc * 16 + 2 * t;
-            bfr[nt][0] = ld2(wp);
-            bfr[nt][1] = ld2(wp + 8);
+            for (int nt = 0; nt < NT; nt += 2)
+              ldsm_x4(wsm + (tx * COUT + (nt + (mi >> 1)) * 8 + (lane & 7)) * RSTR + kc * 16 +
+                          (mi & 1) * 8,
+                      bfr[nt][0], bfr[nt][1], bfr[nt + 1][0], bfr[nt + 1][1]);
+          } else {
+            const bf16 *wt = a.w + (size_t)(3 * pair + tx) * COUT * CIN;
+#pragma unroll
+            for (int nt = 0; nt < NT; nt++) {
+              const bf16 *wp = wt + (size_t)(nt * 8 + g) * CIN + kc * 16 + 2 * t;
+              bfr[nt][0] = ld2(wp);
+              bfr[nt][1] = ld2(wp + 8);
+            }
           }
 #pragma unroll
           for (int m = 0; m < MS; m++) {
@@ -1061,8 +1091,8 @@ cudaError_t conv_launch(const ConvArgs &a, cudaStream_t s) {
   // staged rows of both fit the registers
   constexpr int MS = (COUT >= 64 || CIN1 + CIN2 >= 96) ? 1 : 2;
   const long nseg = (long)a.H * a.D * ((a.W + 15) / 16);
-  const long warps = (nseg + MS - 1) / MS;
-  const long blocks = std::min<long>((warps + 3) / 4, (long)device_sm_count() * 16);
+  const long groups = (nseg + MS - 1) / MS;
+  const long blocks = std::min<long>((groups + 3) / 4, (long)device_sm_count() * 16);
   conv3_kernel<CIN1, CIN2, COUT, MS, F32IN, F32OUT><<<(unsigned)blocks, 128, 0, s>>>(a);
   count_launches(1);
   return cudaGetLastError();
