@@ -23,14 +23,18 @@
 //                  BF16, FP32 accumulate): M = 16-voxel x-row segments, N =
 //                  output channels, K = 27 taps x input channels, the A
 //                  operand staged per (dy, dz) row in shared memory and read
-//                  by ldmatrix for the three x-taps.  The
-//                  nearest upsampling and concatenation of the decoder
-//                  inputs are fused into the operand staging.  The same
-//                  kernel computes the backward data pass (flipped,
-//                  transposed weights; FP32 gradient input with the ReLU
-//                  mask of the layer output fused into the gather).
-//   conv3_wgrad    weight and bias gradients, FP32 (shared-memory tiles of
-//                  32 voxels per tap).
+//                  by ldmatrix for the three x-taps (the wide layers' weights
+//                  staged the same way).  The nearest upsampling and
+//                  concatenation of the decoder inputs are fused into the
+//                  operand staging.  The same kernel computes the backward
+//                  data pass (flipped, transposed weights; FP32 gradient
+//                  input with the ReLU mask of the layer output fused into
+//                  the staging).
+//   conv3_wgrad_tc weight and bias gradients on mma.sync, K = voxels: per
+//                  (dy, dz) pair an 18-voxel row segment of the inputs
+//                  staged in shared memory serves the three x-taps (B by
+//                  ldmatrix.trans), the masked output gradient transposed
+//                  into x rows padded to 16 voxels (A); FP32 atomics.
 //   conv3_tc_kernel (conv_tc.cuh) the forward convolutions on the fifth-
 //                  generation tensor cores: tcgen05.mma from TMA-staged
 //                  halo slabs into tensor memory (VDR_NET_CONV_TCGEN05,
