@@ -92,8 +92,10 @@ def expected_c(base, value):
     """The C (type, pointer depth) a Fortran dummy argument passes."""
     if base == "c_ptr":
         return ("vdr_handle", 1 if value else 2)
+    # (the header parser keeps the first word of a type: "long long" -> "long")
     c = {"c_double": "double", "c_int": "int", "c_long": "long",
-         "c_char": "char", "vdr_options": "vdr_options"}[base]
+         "c_long_long": "long", "c_char": "char",
+         "vdr_options": "vdr_options"}[base]
     return (c, 0 if value else 1)
 
 

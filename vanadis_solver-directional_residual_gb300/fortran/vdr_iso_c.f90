@@ -29,6 +29,7 @@ module vdr_iso_c
   integer(c_int), parameter :: VDR_STORE_AUTO = 0, VDR_STORE_FP64 = 1, &
        VDR_STORE_DF = 2
   integer(c_int), parameter :: VDR_PRECISION_FP64 = 0, VDR_PRECISION_MIXED = 1
+  integer(c_int), parameter :: VDR_BUILD_AUTO = 0, VDR_BUILD_RECOMPUTE = 1
 
   type, bind(c) :: vdr_options
      integer(c_int) :: dr_variant, scatter, apply_mode, solver
@@ -83,6 +84,22 @@ module vdr_iso_c
        type(c_ptr), value :: h
        real(c_double), value :: ah, am
      end function vdr_set_operator
+
+     ! element geometry of the build: the mesh's geometric factors formed
+     ! once (VDR_BUILD_AUTO) or the Jacobians at every build
+     integer(c_int) function vdr_set_build_mode(h, mode) bind(c, name="vdr_set_build_mode")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), value :: mode
+     end function vdr_set_build_mode
+
+     integer(c_int) function vdr_geometry_status(h, cached, bytes) &
+          bind(c, name="vdr_geometry_status")
+       import :: c_int, c_long_long, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), intent(out) :: cached
+       integer(c_long_long), intent(out) :: bytes
+     end function vdr_geometry_status
 
      integer(c_int) function vdr_apply(h, x, y, transpose) bind(c, name="vdr_apply")
        import :: c_int, c_double, c_ptr
